@@ -1,0 +1,239 @@
+"""ctypes front end of the CPU oracle (oracle/mvr_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()`` and by
+the ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` -- as the checker and
+the timed CPU restatement, never by the product library.
+
+Every function mirrors a reference routine (cited in mvr_oracle.c); arrays are
+numpy, C-contiguous ``[z][y][x]`` (x fastest), shapes passed as ``(x, y, z)`` sizes.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "mvr_oracle.c")
+_LIB = os.path.join(_HERE, "liboracle.so")
+
+PSF_OPTIMIZATION_II, PSF_OPTIMIZATION_I, PSF_EFFICIENT_BAYESIAN, PSF_INDEPENDENT = 0, 1, 2, 3
+EXT_ZERO, EXT_MIRROR_SINGLE, EXT_VALUE = 0, 1, 2
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so with gcc (OpenMP, no FMA contraction)."""
+    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(_SRC):
+        cmd = ["gcc", "-O2", "-std=gnu11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+               "-o", _LIB, _SRC, "-lm"]
+        subprocess.run(cmd, check=True)
+    return _LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB)
+        P = C.c_void_p
+        L.orc_fft1d.argtypes = [P, C.c_int, C.c_int]
+        L.orc_mirror_single.argtypes = [C.c_long, C.c_long]
+        L.orc_mirror_single.restype = C.c_long
+        L.orc_convolve.argtypes = [P, P, C.c_int, C.c_double, P, P, P]
+        L.orc_block_seq.argtypes = [P, P, P, P, P, P, P, P, P, C.c_double, C.c_float, C.c_float,
+                                    C.c_int, P]
+        L.orc_block_mul.argtypes = [P, P, C.c_int, P, P, P, P, P, P, P, C.c_double, C.c_float, P,
+                                    C.c_int, P]
+        L.orc_norm_to_sum1.argtypes = [P, C.c_long, C.c_int]
+        L.orc_invert_kernel.argtypes = [P, P, P]
+        L.orc_psf_init.argtypes = [C.c_int, P, P, C.c_int, C.c_int, P]
+        L.orc_divide_into_blocks.argtypes = [P, P, P, P, C.c_int]
+        L.orc_divide_into_blocks.restype = C.c_int
+        L.orc_sort_blocks.argtypes = [P, C.c_int]
+        L.orc_sort_blocks.restype = C.c_int
+        L.orc_normalize_weights.argtypes = [C.c_int, P, C.c_long, C.c_double, C.c_int, C.c_float,
+                                            C.c_float, P]
+        L.orc_psi_init_avg.argtypes = [C.c_int, P, C.c_long, P, P]
+        L.orc_psi_init_avg.restype = C.c_double
+        L.orc_decon_run.argtypes = [C.c_int, P, P, P, P, P, P, P, P, C.c_int, C.c_int, C.c_double,
+                                    C.c_float, P, C.c_int, C.c_int, P, P, P]
+        L.orc_decon_run.restype = C.c_int
+        L.orc_num_threads.restype = C.c_int
+        L.orc_set_num_threads.argtypes = [C.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def _dims(a):
+    """(x, y, z) sizes of a [z][y][x] array."""
+    return np.array([a.shape[2], a.shape[1], a.shape[0]], dtype=np.int32)
+
+
+def _ptr_array(arrs):
+    return (C.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+
+
+def set_threads(n: int) -> None:
+    lib().orc_set_num_threads(int(n))
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()
+
+
+def fft1d(x: np.ndarray, inverse: bool = False) -> np.ndarray:
+    d = np.empty(2 * len(x), dtype=np.float64)
+    d[0::2] = x.real
+    d[1::2] = x.imag
+    lib().orc_fft1d(_p(d), len(x), int(inverse))
+    return d[0::2] + 1j * d[1::2]
+
+
+def mirror_single(i: int, n: int) -> int:
+    return lib().orc_mirror_single(i, n)
+
+
+def convolve(block: np.ndarray, kernel: np.ndarray, ext: int, ext_value: float = 0.0) -> np.ndarray:
+    block = np.ascontiguousarray(block, dtype=np.float32)
+    kernel = np.ascontiguousarray(kernel, dtype=np.float32)
+    out = np.empty(block.shape, dtype=np.float64)
+    lib().orc_convolve(_p(block), _p(_dims(block)), ext, ext_value, _p(kernel), _p(_dims(kernel)),
+                       _p(out))
+    return out
+
+
+def block_seq(psi, img, w, k1, k2, lam, min_value, max_intensity, fp64=False):
+    """ComputeBlockSeqThreadCPU.runIteration on one block; returns (psi', (sum, max))."""
+    img = np.ascontiguousarray(img, dtype=np.float32)
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    k1 = np.ascontiguousarray(k1, dtype=np.float32)
+    k2 = np.ascontiguousarray(k2, dtype=np.float32)
+    st = np.zeros(2, dtype=np.float64)
+    if fp64:
+        p64 = np.array(psi, dtype=np.float64, order="C")
+        lib().orc_block_seq(None, _p(p64), _p(img), _p(w), _p(_dims(img)), _p(k1), _p(_dims(k1)),
+                            _p(k2), _p(_dims(k2)), lam, min_value, max_intensity, 1, _p(st))
+        return p64, (st[0], st[1])
+    p32 = np.array(psi, dtype=np.float32, order="C")
+    lib().orc_block_seq(_p(p32), None, _p(img), _p(w), _p(_dims(img)), _p(k1), _p(_dims(k1)),
+                        _p(k2), _p(_dims(k2)), lam, min_value, max_intensity, 0, _p(st))
+    return p32, (st[0], st[1])
+
+
+def block_mul(psi, imgs, ws, k1s, k2s, lam, min_value, max_intensities, fp64=False):
+    """ComputeBlockMulThreadCPU.runIteration on one block; returns (psi', (sum, max))."""
+    nv = len(imgs)
+    imgs = [np.ascontiguousarray(a, dtype=np.float32) for a in imgs]
+    ws = [np.ascontiguousarray(a, dtype=np.float32) for a in ws]
+    k1s = [np.ascontiguousarray(a, dtype=np.float32) for a in k1s]
+    k2s = [np.ascontiguousarray(a, dtype=np.float32) for a in k2s]
+    k1d = np.concatenate([_dims(k) for k in k1s]).astype(np.int32)
+    k2d = np.concatenate([_dims(k) for k in k2s]).astype(np.int32)
+    mx = np.asarray(max_intensities, dtype=np.float32)
+    st = np.zeros(2, dtype=np.float64)
+    args = (nv, _ptr_array(imgs), _ptr_array(ws), _p(_dims(imgs[0])), _ptr_array(k1s), _p(k1d),
+            _ptr_array(k2s), _p(k2d), lam, min_value, _p(mx))
+    if fp64:
+        p64 = np.array(psi, dtype=np.float64, order="C")
+        lib().orc_block_mul(None, _p(p64), *args, 1, _p(st))
+        return p64, (st[0], st[1])
+    p32 = np.array(psi, dtype=np.float32, order="C")
+    lib().orc_block_mul(_p(p32), None, *args, 0, _p(st))
+    return p32, (st[0], st[1])
+
+
+def norm_to_sum1(k: np.ndarray, T: int) -> np.ndarray:
+    k = np.array(k, dtype=np.float32, order="C")
+    lib().orc_norm_to_sum1(_p(k), k.size, T)
+    return k
+
+
+def invert_kernel(k: np.ndarray) -> np.ndarray:
+    k = np.ascontiguousarray(k, dtype=np.float32)
+    out = np.empty_like(k)
+    lib().orc_invert_kernel(_p(k), _p(_dims(k)), _p(out))
+    return out
+
+
+def psf_init(kernels, psf_type: int, T: int):
+    """DeconViewPSF.init for all views in order; returns (kernel1 list, kernel2 list)."""
+    k1 = [np.array(k, dtype=np.float32, order="C") for k in kernels]
+    k2 = [np.empty_like(k) for k in k1]
+    kd = np.concatenate([_dims(k) for k in k1]).astype(np.int32)
+    lib().orc_psf_init(len(k1), _ptr_array(k1), _p(kd), psf_type, T, _ptr_array(k2))
+    return k1, k2
+
+
+def divide_into_blocks(img_size, kernel2_size, block_size):
+    """Blocks as dicts (offset, eff_offset, eff_size, eff_local), each (x, y, z)."""
+    a = np.asarray(img_size, dtype=np.int64)
+    k = np.asarray(kernel2_size, dtype=np.int64)
+    b = np.asarray(block_size, dtype=np.int64)
+    n = lib().orc_divide_into_blocks(_p(a), _p(k), _p(b), None, 0)
+    if n < 0:
+        return None
+    out = np.zeros((n, 12), dtype=np.int64)
+    lib().orc_divide_into_blocks(_p(a), _p(k), _p(b), _p(out), n)
+    return [dict(offset=tuple(r[0:3]), eff_offset=tuple(r[3:6]), eff_size=tuple(r[6:9]),
+                 eff_local=tuple(r[9:12])) for r in out]
+
+
+def sort_dim(num_blocks, min_required: int = 1) -> int:
+    nb = np.asarray(num_blocks, dtype=np.int64)
+    return lib().orc_sort_blocks(_p(nb), min_required)
+
+
+def normalize_weights(raw, osem=1.0, smooth=False, max_diff_range=0.1, scaling_range=0.05):
+    raw = [np.ascontiguousarray(r, dtype=np.float32) for r in raw]
+    out = [np.empty_like(r) for r in raw]
+    lib().orc_normalize_weights(len(raw), _ptr_array(raw), raw[0].size, osem, int(smooth),
+                                max_diff_range, scaling_range, _ptr_array(out))
+    return out
+
+
+def psi_init_avg(imgs):
+    imgs = [np.ascontiguousarray(r, dtype=np.float32) for r in imgs]
+    psi = np.empty_like(imgs[0])
+    mx = np.zeros(len(imgs), dtype=np.float32)
+    avg = lib().orc_psi_init_avg(len(imgs), _ptr_array(imgs), imgs[0].size, _p(psi), _p(mx))
+    return psi, mx, avg
+
+
+def decon_run(psi, imgs, ws, k1s, k2s, block_size, iters, mul=False, lam=0.0, min_value=1e-4,
+              max_intensities=None, filter_blocks=True, fp64=False):
+    """MultiViewDeconvolution{Seq,Mul}.runIterations with the reference's block order.
+
+    Returns (psi, stats[n_steps, 2])."""
+    nv = len(imgs)
+    D = np.array([psi.shape[2], psi.shape[1], psi.shape[0]], dtype=np.int64)
+    imgs = [np.ascontiguousarray(a, dtype=np.float32) for a in imgs]
+    ws = [np.ascontiguousarray(a, dtype=np.float32) for a in ws]
+    k1s = [np.ascontiguousarray(a, dtype=np.float32) for a in k1s]
+    k2s = [np.ascontiguousarray(a, dtype=np.float32) for a in k2s]
+    k1d = np.concatenate([_dims(k) for k in k1s]).astype(np.int32)
+    k2d = np.concatenate([_dims(k) for k in k2s]).astype(np.int32)
+    b = np.asarray(block_size, dtype=np.int32)
+    mx = np.asarray(max_intensities, dtype=np.float32)
+    nsteps = iters * (1 if mul else nv)
+    st = np.zeros((nsteps, 2), dtype=np.float64)
+    if fp64:
+        p64 = np.array(psi, dtype=np.float64, order="C")
+        p32 = None
+    else:
+        p32 = np.array(psi, dtype=np.float32, order="C")
+        p64 = None
+    rc = lib().orc_decon_run(nv, _p(D), _ptr_array(imgs), _ptr_array(ws), _ptr_array(k1s), _p(k1d),
+                             _ptr_array(k2s), _p(k2d), _p(b), iters, int(mul), lam, min_value, _p(mx),
+                             int(filter_blocks), int(fp64), _p(p32), _p(p64), _p(st))
+    if rc != 0:
+        raise ValueError("block size smaller than the doubled kernel")
+    return (p64 if fp64 else p32), st

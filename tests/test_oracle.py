@@ -1,0 +1,209 @@
+"""The CPU oracle against the golden fixtures (independent numpy restatement),
+direct spatial convolution and analytic known-answer cases."""
+import itertools
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 7, 8, 12, 13, 31, 96, 97, 124, 156, 192, 222, 252])
+def test_fft1d_matches_numpy(n):
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    ref = np.fft.fft(x)
+    assert np.abs(O.fft1d(x) - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+    assert np.abs(O.fft1d(x, inverse=True) - np.fft.ifft(x) * n).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+
+
+def test_mirror_single_ramp():
+    # imglib2 extendMirrorSingle: border voxel not repeated, period 2n-2
+    n = 5
+    got = [O.mirror_single(i, n) for i in range(-9, 14)]
+    exp = [1, 0, 1, 2, 3, 4, 3, 2, 1, 0, 1, 2, 3, 4, 3, 2, 1, 0, 1, 2, 3, 4, 3]
+    assert got == exp
+    assert O.mirror_single(-3, 1) == 0
+
+
+def _direct(blk, k, ext, val):
+    bz, by, bx = blk.shape
+    kz, ky, kx = k.shape
+    out = np.zeros(blk.shape)
+    for z, y, x in itertools.product(range(bz), range(by), range(bx)):
+        s = 0.0
+        for tz, ty, tx in itertools.product(range(kz), range(ky), range(kx)):
+            g = (z - (tz - kz // 2), y - (ty - ky // 2), x - (tx - kx // 2))
+            if 0 <= g[0] < bz and 0 <= g[1] < by and 0 <= g[2] < bx:
+                v = blk[g]
+            elif ext == O.EXT_MIRROR_SINGLE:
+                v = blk[O.mirror_single(g[0], bz), O.mirror_single(g[1], by), O.mirror_single(g[2], bx)]
+            elif ext == O.EXT_VALUE:
+                v = val
+            else:
+                v = 0.0
+            s += v * k[tz, ty, tx]
+        out[z, y, x] = s
+    return out
+
+
+@pytest.mark.parametrize("ext", [O.EXT_ZERO, O.EXT_MIRROR_SINGLE, O.EXT_VALUE])
+def test_convolution_vs_direct(ext):
+    rng = np.random.default_rng(3)
+    blk = rng.random((4, 5, 6)).astype(np.float32)
+    k = rng.random((3, 4, 5)).astype(np.float32)  # even size along y
+    got = O.convolve(blk, k, ext, 1.0)
+    ref = _direct(blk.astype(np.float64), k.astype(np.float64), ext, 1.0)
+    assert np.abs(got - ref).max() < 1e-12
+
+
+def test_convolution_golden():
+    g = np.load(os.path.join(G, "conv_cases.npz"))
+    for name, k, ext in [("mirror_odd", "k_odd", 1), ("value_odd", "k_odd", 2), ("zero_odd", "k_odd", 0),
+                         ("mirror_even", "k_even", 1), ("value_even", "k_even", 2)]:
+        assert np.abs(O.convolve(g["block"], g[k], ext, 1.0) - g[name]).max() < 1e-10, name
+
+
+def test_block_seq_golden():
+    b = np.load(os.path.join(G, "block_cases.npz"))
+    out, st = O.block_seq(b["psi"], b["img0"], b["w0"], b["k1_0"], b["k2_0"], float(b["lam"]), 1e-4,
+                          float(b["max"][0]))
+    assert np.array_equal(out, b["seq_out"])  # float-faithful path is bit-exact
+    assert np.allclose(st, b["seq_stats"], rtol=1e-12)
+    out, st = O.block_seq(b["psi"], b["img0"], b["w0"], b["k1_0"], b["k2_0"], float(b["lam"]), 1e-4,
+                          float(b["max"][0]), fp64=True)
+    assert rel_l2(out, b["seq_out64"]) < 1e-12
+    assert np.allclose(st, b["seq_stats64"], rtol=1e-10)
+
+
+def test_block_mul_golden():
+    b = np.load(os.path.join(G, "block_cases.npz"))
+    args = ([b["img0"], b["img1"]], [b["w0"], b["w1"]], [b["k1_0"], b["k1_1"]], [b["k2_0"], b["k2_1"]],
+            float(b["lam"]), 1e-4, b["max"])
+    out, st = O.block_mul(b["psi"], *args)
+    assert np.array_equal(out, b["mul_out"])
+    assert np.allclose(st, b["mul_stats"], rtol=1e-12)
+    out, st = O.block_mul(b["psi"], *args, fp64=True)
+    assert rel_l2(out, b["mul_out64"]) < 1e-12
+
+
+@pytest.mark.parametrize("psf_type", [0, 1, 2, 3])
+def test_psf_init_golden(psf_type):
+    p = np.load(os.path.join(G, "psf_cases.npz"))
+    k1, k2 = O.psf_init([p["raw0"], p["raw1"], p["raw2"]], psf_type, 4)
+    for v in range(3):
+        assert np.array_equal(k1[v], p[f"t{psf_type}_k1_{v}"])
+        ref = p[f"t{psf_type}_k2_{v}"]
+        assert np.abs(k2[v] - ref).max() <= 1e-6 * np.abs(ref).max()
+
+
+def test_invert_even_quirk():
+    p = np.load(os.path.join(G, "psf_cases.npz"))
+    assert np.array_equal(O.invert_kernel(p["even"]), p["even_inv"])
+    odd = np.arange(3 * 5 * 7, dtype=np.float32).reshape(7, 5, 3)
+    assert np.array_equal(O.invert_kernel(odd), odd[::-1, ::-1, ::-1])
+
+
+def test_norm_to_sum1_double_counts_first_portion():
+    k = np.ones(100, dtype=np.float32)
+    # T = 4: first portion = 25 voxels counted twice -> sum 125
+    assert np.allclose(O.norm_to_sum1(k, 4), 1.0 / 125.0)
+    assert np.allclose(O.norm_to_sum1(k, 0), 1.0 / 100.0)
+
+
+def test_weights_and_psi_init_golden():
+    v = np.load(os.path.join(G, "volume_cases.npz"))
+    ws = O.normalize_weights([v["raw_w0"], v["raw_w1"]])
+    assert np.array_equal(ws[0], v["w0"]) and np.array_equal(ws[1], v["w1"])
+    psi, mx, avg = O.psi_init_avg([v["img0"], v["img1"]])
+    assert abs(avg - float(v["avg"])) < 1e-9 * abs(avg)
+    assert np.array_equal(mx, v["max"])
+    assert np.all(psi == np.float32(avg))
+
+
+def test_block_geometry():
+    # 256^3, k = 31x31x61 -> doubled 61x61x121, block 192^3 -> effective 132x132x72, 2x2x4 blocks
+    bl = O.divide_into_blocks((256, 256, 256), (61, 61, 121), (192, 192, 192))
+    assert len(bl) == 16
+    assert bl[0]["eff_size"] == (132, 132, 72) and bl[0]["offset"] == (-30, -30, -60)
+    assert bl[-1]["eff_offset"] == (132, 132, 216) and bl[-1]["eff_size"] == (124, 124, 40)
+    assert O.divide_into_blocks((10, 10, 10), (11, 3, 3), (10, 10, 10)) is None
+    # fewest blocks per slab: products (8, 8, 4) -> slabs along z
+    assert O.sort_dim((2, 2, 4), 1) == 2
+    # equal products keep the last dimension (HashMap overwrite)
+    assert O.sort_dim((2, 2, 2), 1) == 2
+    assert O.sort_dim((3, 1, 1), 1) == 0
+
+
+@pytest.mark.parametrize("mul,key,bs,lam", [(False, "seq", (28, 28, 28), None), (True, "mul", (28, 28, 28), None),
+                                            (False, "one", (48, 44, 48), 0.0)])
+def test_volume_runs_golden(mul, key, bs, lam):
+    v = np.load(os.path.join(G, "volume_cases.npz"))
+    lam = float(v["lam"]) if lam is None else lam
+    out, st = O.decon_run(v["psi0"], [v["img0"], v["img1"]], [v["w0"], v["w1"]], [v["k1_0"], v["k1_1"]],
+                          [v["k2_0"], v["k2_1"]], bs, 2, mul=mul, lam=lam, max_intensities=v["max"])
+    assert np.array_equal(out, v[key + "_psi"])
+    assert np.allclose(st, v[key + "_stats"], rtol=1e-10)
+
+
+def test_volume_fp64_golden():
+    v = np.load(os.path.join(G, "volume_cases.npz"))
+    out, _ = O.decon_run(v["psi0"], [v["img0"], v["img1"]], [v["w0"], v["w1"]], [v["k1_0"], v["k1_1"]],
+                         [v["k2_0"], v["k2_1"]], (28, 28, 28), 2, lam=float(v["lam"]),
+                         max_intensities=v["max"], fp64=True)
+    assert rel_l2(out, v["seq_psi64"]) < 1e-12
+
+
+def test_kat_delta_psf_identity():
+    # delta PSF: both convolutions are the identity, so psi' = img where img > 0 (lambda 0, w 1)
+    rng = np.random.default_rng(5)
+    img = rng.uniform(1, 50, (6, 7, 8)).astype(np.float32)
+    img[0, 0, :3] = 0
+    psi = rng.uniform(1, 50, img.shape).astype(np.float32)
+    d = np.ones((1, 1, 1), np.float32)
+    out, _ = O.block_seq(psi, img, np.ones_like(img), d, d, 0.0, 1e-4, 100.0)
+    m = img > 0
+    assert np.allclose(out[m], img[m], rtol=4e-6)  # float rounding of psi + (next - psi) * w
+    assert np.array_equal(out[~m], psi[~m])  # ratio 1 outside the data
+
+
+def test_kat_constant_fixed_point():
+    c = 37.0
+    img = np.full((10, 12, 14), c, np.float32)
+    k = np.random.default_rng(1).random((3, 5, 5)).astype(np.float32)
+    k /= k.sum()
+    k2 = O.invert_kernel(k)
+    out, _ = O.block_seq(img.copy(), img, np.ones_like(img), k, k2, 0.0, 1e-4, c)
+    assert np.abs(out - c).max() < 1e-4
+
+
+def test_kat_guards():
+    # psi * conv2 <= 0 -> minValue; w = 0 keeps psi; NaN never escapes
+    psi = np.full((3, 3, 3), 5.0, np.float32)
+    img = np.zeros_like(psi)  # ratio 1 everywhere -> conv2 = 1
+    d = np.ones((1, 1, 1), np.float32)
+    w = np.ones_like(psi)
+    w[0] = 0
+    out, st = O.block_seq(psi, img, w, d, d, 0.0, 1e-4, 10.0)
+    assert np.array_equal(out, psi)
+    assert st == (0.0, 0.0)
+    neg = np.full_like(psi, -1.0)
+    out, st = O.block_seq(neg, img, np.ones_like(psi), d, d, 0.0, 1e-4, 10.0)
+    assert np.all(out == np.float32(1e-4))
+
+
+def test_seq_equals_mul_for_one_view():
+    b = np.load(os.path.join(G, "block_cases.npz"))
+    a, sa = O.block_seq(b["psi"], b["img0"], b["w0"], b["k1_0"], b["k2_0"], 0.0, 1e-4, float(b["max"][0]))
+    m, sm = O.block_mul(b["psi"], [b["img0"]], [b["w0"]], [b["k1_0"]], [b["k2_0"]], 0.0, 1e-4, [b["max"][0]])
+    assert np.array_equal(a, m)
+    assert np.allclose(sa, sm)
