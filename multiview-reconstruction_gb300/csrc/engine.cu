@@ -1,0 +1,463 @@
+// Host side of the block iteration (see engine.cuh).
+#include "engine.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+namespace mvr {
+
+namespace {
+constexpr int kThreads = 256;
+constexpr int kRadices[] = {8, 4, 2, 3, 5, 7, 11, 13};
+constexpr size_t kRowSmemTarget = 48 * 1024;
+constexpr size_t kColSmemTarget = 72 * 1024;
+constexpr size_t kSmemMax = 227 * 1024;
+}  // namespace
+
+bool fft_friendly(long long n)
+{
+    if (n < 1) return false;
+    for (int r : {2, 3, 5, 7, 11, 13})
+        while (n % r == 0) n /= r;
+    return n == 1;
+}
+
+long long next_friendly_even(long long n)
+{
+    long long m = std::max<long long>(2, n);
+    if (m & 1) ++m;
+    while (!fft_friendly(m)) m += 2;
+    return m;
+}
+
+FftDesc make_desc(int n)
+{
+    FftDesc d{};
+    d.n = n;
+    d.ns = 0;
+    int m = n;
+    for (int r : kRadices)
+        while (m % r == 0 && d.ns < kMaxStages) {
+            d.radix[d.ns++] = r;
+            m /= r;
+        }
+    return d;
+}
+
+template <typename T>
+int Engine<T>::fail(int code, const std::string &msg)
+{
+    err_ = msg;
+    return code;
+}
+
+template <typename T>
+int Engine<T>::cuda_check(cudaError_t e, const char *what)
+{
+    if (e == cudaSuccess) return OK;
+    err_ = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? ERR_OOM : ERR_CUDA;
+}
+
+#define MVR_TRY(expr)                      \
+    do {                                   \
+        int rc__ = (expr);                 \
+        if (rc__ != OK) return rc__;       \
+    } while (0)
+#define MVR_CUDA(expr) MVR_TRY(cuda_check((expr), #expr))
+#define MVR_LAUNCHED(name) MVR_TRY(cuda_check(cudaGetLastError(), name))
+
+namespace {
+template <typename V>
+V *dev_twiddles_impl(int n, cudaStream_t s, std::string &err)
+{
+    typedef typename Re<V>::t T;
+    std::vector<V> h(n);
+    for (int k = 0; k < n; ++k) {
+        // exp(-2 pi i k / n), exact angle reduction by symmetry before the libm call
+        const double a = -2.0 * M_PI * (double)k / (double)n;
+        h[k].x = (T)std::cos(a);
+        h[k].y = (T)std::sin(a);
+    }
+    V *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, sizeof(V) * (size_t)n);
+    if (e != cudaSuccess) { err = cudaGetErrorString(e); return nullptr; }
+    e = cudaMemcpyAsync(d, h.data(), sizeof(V) * (size_t)n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) { err = cudaGetErrorString(e); cudaFree(d); return nullptr; }
+    return d;
+}
+
+template <typename T>
+void set_smem_limits()
+{
+    // allow every instantiation to use up to the opt-in maximum; launches size it exactly
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const int m = (int)kSmemMax;
+        cudaFuncSetAttribute(k_rows_fwd<T, SrcMirror<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_rows_fwd<T, SrcMirror<float>>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_rows_fwd<T, SrcZero<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_rows_fwd<T, SrcKernel>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_cols<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_cols<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_cols<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_rows_ratio<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_rows_update<T, EPI_SEQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_rows_update<T, EPI_MUL_FIRST>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_rows_update<T, EPI_MUL_ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_rows_update<T, EPI_MUL_FINAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        cudaFuncSetAttribute(k_rows_update<T, EPI_STORE>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    });
+}
+}  // namespace
+
+template <typename T>
+Engine<T>::~Engine()
+{
+    if (device_ >= 0) cudaSetDevice(device_);
+    cudaFree(S0_);
+    cudaFree(S1_);
+    cudaFree(prod_);
+    cudaFree(partials_);
+    cudaFree(kbuf_);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+template <typename T>
+int Engine<T>::init(int device, int boundary, double lambda, float min_value)
+{
+    int n = 0;
+    MVR_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(ERR_ARG, "device ordinal out of range");
+    device_ = device;
+    boundary_ = boundary;
+    lambda_ = lambda;
+    min_value_ = min_value;
+    MVR_CUDA(cudaSetDevice(device));
+    MVR_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    set_smem_limits<T>();
+    return OK;
+}
+
+template <typename T>
+int Engine<T>::reserve(long long Pc, long long nvox_block, long long rows)
+{
+    if (Pc > Scap_) {
+        cudaFree(S0_);
+        cudaFree(S1_);
+        S0_ = S1_ = nullptr;
+        Scap_ = 0;
+        MVR_CUDA(cudaMalloc(&S0_, sizeof(V) * (size_t)Pc));
+        MVR_CUDA(cudaMalloc(&S1_, sizeof(V) * (size_t)Pc));
+        Scap_ = Pc;
+    }
+    if (nvox_block > prodcap_) {
+        cudaFree(prod_);
+        prod_ = nullptr;
+        prodcap_ = 0;
+        MVR_CUDA(cudaMalloc(&prod_, sizeof(double) * (size_t)nvox_block));
+        prodcap_ = nvox_block;
+    }
+    if (rows > partcap_) {
+        cudaFree(partials_);
+        partials_ = nullptr;
+        partcap_ = 0;
+        MVR_CUDA(cudaMalloc(&partials_, sizeof(double) * 2 * (size_t)rows));
+        partcap_ = rows;
+    }
+    return OK;
+}
+
+template <typename T>
+void Engine<T>::free_plan(Plan<T> &pl)
+{
+    cudaFree(pl.twx);
+    cudaFree(pl.twy);
+    cudaFree(pl.twz);
+    cudaFree(pl.k1h);
+    cudaFree(pl.k2h);
+    pl.twx = pl.twy = pl.twz = pl.k1h = pl.k2h = nullptr;
+}
+
+template <typename T>
+int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int kd1[3], const float *k2,
+                         const int kd2[3], bool k_on_device)
+{
+    if (stream_ == nullptr) return fail(ERR_STATE, "engine not initialised");
+    for (int d = 0; d < 3; ++d) {
+        if (b[d] < 1 || kd1[d] < 1) return fail(ERR_ARG, "block and kernel sizes must be >= 1");
+        if (k2 && kd2[d] != kd1[d]) return fail(ERR_ARG, "kernel1 and kernel2 must have the same size");
+        if (kd1[d] > b[d] && boundary_ == BOUNDARY_CIRCULAR)
+            return fail(ERR_ARG, "kernel larger than the block under circular boundary");
+    }
+    free_plan(pl);
+    for (int d = 0; d < 3; ++d) {
+        pl.b[d] = b[d];
+        pl.kd[d] = kd1[d];
+        if (boundary_ == BOUNDARY_CIRCULAR) {
+            pl.P[d] = b[d];
+            pl.L[d] = 0;
+            if (!fft_friendly(b[d]) || (d == 0 && (b[d] & 1)))
+                return fail(ERR_UNSUPPORTED, "circular boundary needs block sizes with prime factors <= 13 (even along x)");
+        } else {
+            pl.P[d] = (int)next_friendly_even(b[d] + kd1[d] - 1);
+            pl.L[d] = kd1[d] - 1 - kd1[d] / 2;
+        }
+    }
+    if (pl.P[0] > 4096 || pl.P[1] > 2048 || pl.P[2] > 2048)
+        return fail(ERR_UNSUPPORTED, "FFT domain larger than 4096 x 2048 x 2048");
+    pl.Hx = pl.P[0] / 2 + 1;
+    pl.Pc = (long long)pl.Hx * pl.P[1] * pl.P[2];
+    pl.dx = make_desc(pl.P[0] / 2);
+    pl.dy = make_desc(pl.P[1]);
+    pl.dz = make_desc(pl.P[2]);
+    std::string e;
+    pl.twx = dev_twiddles_impl<V>(pl.P[0], stream_, e);
+    pl.twy = dev_twiddles_impl<V>(pl.P[1], stream_, e);
+    pl.twz = dev_twiddles_impl<V>(pl.P[2], stream_, e);
+    if (!pl.twx || !pl.twy || !pl.twz) return fail(ERR_CUDA, "twiddle upload: " + e);
+    // launch shapes
+    const int m = pl.P[0] / 2;
+    const size_t per_row = 2 * sizeof(V) * (size_t)(m + 1);
+    const size_t tws = sizeof(V) * (size_t)pl.P[0];
+    int RP = 16;
+    while (RP > 1 && tws + RP * per_row > kRowSmemTarget) RP >>= 1;
+    if (tws + RP * per_row > kSmemMax) return fail(ERR_UNSUPPORTED, "row too long for shared memory");
+    pl.RP = RP;
+    pl.smem_row = tws + RP * per_row;
+    auto col_np = [&](int n, int &NP, size_t &smem) -> bool {
+        NP = 16;
+        while (NP > 1 && sizeof(V) * (size_t)n * (1 + 2 * NP) > kColSmemTarget) NP >>= 1;
+        smem = sizeof(V) * (size_t)n * (1 + 2 * NP);
+        return smem <= kSmemMax;
+    };
+    if (!col_np(pl.P[1], pl.NPy, pl.smem_coly) || !col_np(pl.P[2], pl.NPz, pl.smem_colz))
+        return fail(ERR_UNSUPPORTED, "column too long for shared memory");
+    const long long nrows = (long long)pl.P[1] * pl.P[2];
+    MVR_TRY(reserve(pl.Pc, (long long)b[0] * b[1] * b[2], (nrows + pl.RP - 1) / pl.RP));
+    // kernel spectra, scaled by 1 / (Px Py Pz) so that the inverse needs no scaling
+    MVR_CUDA(cudaMalloc(&pl.k1h, sizeof(V) * (size_t)pl.Pc));
+    if (k2) MVR_CUDA(cudaMalloc(&pl.k2h, sizeof(V) * (size_t)pl.Pc));
+    const long long kn = (long long)kd1[0] * kd1[1] * kd1[2];
+    if (!k_on_device && kn > kcap_) {
+        cudaFree(kbuf_);
+        kbuf_ = nullptr;
+        kcap_ = 0;
+        MVR_CUDA(cudaMalloc(&kbuf_, sizeof(float) * (size_t)kn));
+        kcap_ = kn;
+    }
+    BlockMap bm{};
+    for (int d = 0; d < 3; ++d) {
+        bm.P[d] = pl.P[d];
+        bm.b[d] = pl.P[d];
+        bm.D[d] = pl.P[d];
+    }
+    const double scale = 1.0 / ((double)pl.P[0] * pl.P[1] * pl.P[2]);
+    for (int which = 0; which < (k2 ? 2 : 1); ++which) {
+        const float *kh = which == 0 ? k1 : k2;
+        const float *kdev = kh;
+        if (!k_on_device) {
+            MVR_CUDA(cudaMemcpyAsync(kbuf_, kh, sizeof(float) * (size_t)kn, cudaMemcpyHostToDevice, stream_));
+            kdev = kbuf_;
+        }
+        SrcKernel src{kdev, {kd1[0], kd1[1], kd1[2]}, scale};
+        const unsigned grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
+        k_rows_fwd<T, SrcKernel><<<grid, kThreads, pl.smem_row, stream_>>>(src, S0_, bm, pl.dx, pl.twx, pl.RP);
+        MVR_LAUNCHED("k_rows_fwd(kernel)");
+        MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
+        MVR_TRY(launch_cols(pl, 2, 0, S0_, which == 0 ? pl.k1h : pl.k2h, nullptr));
+    }
+    MVR_CUDA(cudaStreamSynchronize(stream_));
+    return OK;
+}
+
+template <typename T>
+int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh)
+{
+    const int Hx = pl.Hx;
+    long long estride, ostride;
+    int nother, NP;
+    size_t smem;
+    const FftDesc *d;
+    if (axis == 1) {
+        estride = Hx;
+        ostride = (long long)pl.P[1] * Hx;
+        nother = pl.P[2];
+        NP = pl.NPy;
+        smem = pl.smem_coly;
+        d = &pl.dy;
+    } else {
+        estride = (long long)pl.P[1] * Hx;
+        ostride = Hx;
+        nother = pl.P[1];
+        NP = pl.NPz;
+        smem = pl.smem_colz;
+        d = &pl.dz;
+    }
+    const V *tw = axis == 1 ? pl.twy : pl.twz;
+    dim3 grid((unsigned)((Hx + NP - 1) / NP), (unsigned)nother);
+    if (mode == 0) k_cols<T, 0><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
+    else if (mode == 1) k_cols<T, 1><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
+    else k_cols<T, 2><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
+    MVR_LAUNCHED("k_cols");
+    return OK;
+}
+
+template <typename T>
+BlockMap Engine<T>::block_map(const Plan<T> &pl, const BlockPlace &bp) const
+{
+    BlockMap bm{};
+    for (int d = 0; d < 3; ++d) {
+        bm.P[d] = pl.P[d];
+        bm.b[d] = pl.b[d];
+        bm.L[d] = pl.L[d];
+        bm.off[d] = bp.off[d];
+        bm.D[d] = bp.D[d];
+        bm.wlo[d] = bp.wlo[d];
+        bm.whi[d] = bp.whi[d];
+        bm.ooff[d] = bp.ooff[d];
+        bm.OD[d] = bp.OD[d];
+    }
+    return bm;
+}
+
+template <typename T>
+int Engine<T>::launch_fwd_mirror(const Plan<T> &pl, const BlockMap &bm, const T *src, V *S)
+{
+    const long long nrows = (long long)pl.P[1] * pl.P[2];
+    const unsigned grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
+    k_rows_fwd<T, SrcMirror<T>><<<grid, kThreads, pl.smem_row, stream_>>>(SrcMirror<T>{src}, S, bm, pl.dx, pl.twx,
+                                                                           pl.RP);
+    MVR_LAUNCHED("k_rows_fwd");
+    return OK;
+}
+
+template <typename T>
+int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace &bp, const float *img, const float *w, float maxI,
+                       double *stats_dev)
+{
+    if (!pl.k1h || !pl.k2h) return fail(ERR_STATE, "kernels not set for this view");
+    const BlockMap bm = block_map(pl, bp);
+    const long long nrows = (long long)pl.P[1] * pl.P[2];
+    const unsigned grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
+    MVR_TRY(launch_fwd_mirror(pl, bm, reinterpret_cast<const T *>(bp.psi_src), S0_));
+    MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
+    MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h));
+    MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr));
+    k_rows_ratio<T><<<grid, kThreads, pl.smem_row, stream_>>>(S0_, img, bm, pl.dx, pl.twx, pl.RP);
+    MVR_LAUNCHED("k_rows_ratio");
+    MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
+    MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k2h));
+    MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr));
+    UpdateArgs ua{};
+    ua.psi_src = bp.psi_src;
+    ua.psi_dst = bp.psi_dst;
+    ua.weight[0] = w;
+    ua.nviews = 1;
+    ua.lambda = lambda_;
+    ua.minI = min_value_;
+    ua.maxI = maxI;
+    ua.partials = partials_;
+    k_rows_update<T, EPI_SEQ><<<grid, kThreads, pl.smem_row, stream_>>>(S0_, ua, bm, pl.dx, pl.twx, pl.RP);
+    MVR_LAUNCHED("k_rows_update");
+    if (stats_dev) {
+        k_reduce_stats<double><<<1, 1024, 0, stream_>>>(partials_, (int)grid, stats_dev);
+        MVR_LAUNCHED("k_reduce_stats");
+    }
+    return OK;
+}
+
+template <typename T>
+int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace &bp, const float *const *imgs,
+                       const float *const *ws, float maxI, double *stats_dev)
+{
+    const int nv = (int)pls.size();
+    if (nv < 1 || nv > kMaxViews) return fail(ERR_ARG, "number of views must be 1..16");
+    UpdateArgs ua{};
+    ua.psi_src = bp.psi_src;
+    ua.psi_dst = bp.psi_dst;
+    for (int v = 0; v < nv; ++v) ua.weight[v] = ws[v];
+    ua.nviews = nv;
+    ua.prod = prod_;
+    ua.lambda = lambda_;
+    ua.minI = min_value_;
+    ua.maxI = maxI;
+    ua.partials = partials_;
+    const Plan<T> *prev = nullptr;
+    unsigned grid = 0;
+    for (int v = 0; v < nv; ++v) {
+        const Plan<T> &pl = *pls[v];
+        if (!pl.k1h || !pl.k2h) return fail(ERR_STATE, "kernels not set for a view");
+        const BlockMap bm = block_map(pl, bp);
+        const long long nrows = (long long)pl.P[1] * pl.P[2];
+        grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
+        if (!prev || std::memcmp(prev->P, pl.P, sizeof(pl.P)) != 0 || std::memcmp(prev->L, pl.L, sizeof(pl.L)) != 0) {
+            // FFT of psi along x and y, shared by every view with this domain
+            MVR_TRY(launch_fwd_mirror(pl, bm, reinterpret_cast<const T *>(bp.psi_src), S0_));
+            MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
+        }
+        prev = &pl;
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S1_, pl.k1h));
+        MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr));
+        k_rows_ratio<T><<<grid, kThreads, pl.smem_row, stream_>>>(S1_, imgs[v], bm, pl.dx, pl.twx, pl.RP);
+        MVR_LAUNCHED("k_rows_ratio");
+        MVR_TRY(launch_cols(pl, 1, 0, S1_, S1_, nullptr));
+        MVR_TRY(launch_cols(pl, 2, 2, S1_, S1_, pl.k2h));
+        MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr));
+        if (v == nv - 1) {
+            ua.nviews = nv;
+            k_rows_update<T, EPI_MUL_FINAL><<<grid, kThreads, pl.smem_row, stream_>>>(S1_, ua, bm, pl.dx, pl.twx,
+                                                                                      pl.RP);
+        } else if (v == 0) {
+            k_rows_update<T, EPI_MUL_FIRST><<<grid, kThreads, pl.smem_row, stream_>>>(S1_, ua, bm, pl.dx, pl.twx, pl.RP);
+        } else {
+            k_rows_update<T, EPI_MUL_ACC><<<grid, kThreads, pl.smem_row, stream_>>>(S1_, ua, bm, pl.dx, pl.twx, pl.RP);
+        }
+        MVR_LAUNCHED("k_rows_update(mul)");
+    }
+    if (stats_dev) {
+        k_reduce_stats<double><<<1, 1024, 0, stream_>>>(partials_, (int)grid, stats_dev);
+        MVR_LAUNCHED("k_reduce_stats");
+    }
+    return OK;
+}
+
+template <typename T>
+int Engine<T>::convolve(const Plan<T> &pl, const T *blk, int src_kind, float *out)
+{
+    BlockMap bm{};
+    for (int d = 0; d < 3; ++d) {
+        bm.P[d] = pl.P[d];
+        bm.b[d] = pl.b[d];
+        bm.L[d] = pl.L[d];
+        bm.D[d] = pl.b[d];
+        bm.OD[d] = pl.b[d];
+        bm.whi[d] = pl.b[d];
+    }
+    const long long nrows = (long long)pl.P[1] * pl.P[2];
+    const unsigned grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
+    if (src_kind == SRC_ZERO)
+        k_rows_fwd<T, SrcZero<T>><<<grid, kThreads, pl.smem_row, stream_>>>(SrcZero<T>{blk}, S0_, bm, pl.dx, pl.twx, pl.RP);
+    else
+        k_rows_fwd<T, SrcMirror<T>><<<grid, kThreads, pl.smem_row, stream_>>>(SrcMirror<T>{blk}, S0_, bm, pl.dx, pl.twx,
+                                                                               pl.RP);
+    MVR_LAUNCHED("k_rows_fwd(conv)");
+    MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
+    MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h));
+    MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr));
+    UpdateArgs ua{};
+    ua.store = out;
+    ua.partials = partials_;
+    k_rows_update<T, EPI_STORE><<<grid, kThreads, pl.smem_row, stream_>>>(S0_, ua, bm, pl.dx, pl.twx, pl.RP);
+    MVR_LAUNCHED("k_rows_update(store)");
+    return OK;
+}
+
+template class Engine<float>;
+template class Engine<double>;
+
+}  // namespace mvr

@@ -1,0 +1,107 @@
+// Host side of the block iteration: FFT plans, kernel spectra, scratch and the
+// per-block Seq / Mul pipelines.  One Engine belongs to one device and one stream.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace mvr {
+
+enum Status { OK = 0, ERR_ARG = 1, ERR_CUDA = 2, ERR_OOM = 3, ERR_UNSUPPORTED = 4, ERR_STATE = 5 };
+enum Boundary { BOUNDARY_REFERENCE = 0, BOUNDARY_CIRCULAR = 1 };
+enum SrcKind { SRC_MIRROR = 0, SRC_ZERO = 1 };
+
+bool fft_friendly(long long n);
+long long next_friendly_even(long long n);
+FftDesc make_desc(int n);
+
+// FFT domain of one (block size, kernel size) pair and the spectra of its kernels.
+template <typename T>
+struct Plan {
+    typedef typename Cx<T>::t V;
+    int b[3] = {0, 0, 0};
+    int kd[3] = {0, 0, 0};
+    int P[3] = {0, 0, 0};
+    int L[3] = {0, 0, 0};
+    int Hx = 0;
+    long long Pc = 0;
+    FftDesc dx{}, dy{}, dz{};
+    V *twx = nullptr, *twy = nullptr, *twz = nullptr;
+    V *k1h = nullptr, *k2h = nullptr;
+    int RP = 1, NPy = 1, NPz = 1;
+    size_t smem_row = 0, smem_coly = 0, smem_colz = 0;
+};
+
+// Where the block's output goes (volume driver) or the block itself (block API).
+struct BlockPlace {
+    const void *psi_src = nullptr;  // T volume (mirror-single read)
+    long long D[3] = {0, 0, 0};     // its dims
+    long long off[3] = {0, 0, 0};   // block offset
+    void *psi_dst = nullptr;        // T output volume
+    long long OD[3] = {0, 0, 0};
+    long long ooff[3] = {0, 0, 0};  // volume coordinate of block-local origin in the output
+    int wlo[3] = {0, 0, 0}, whi[3] = {0, 0, 0};
+};
+
+template <typename T>
+class Engine {
+public:
+    typedef typename Cx<T>::t V;
+    Engine() = default;
+    ~Engine();
+    Engine(const Engine &) = delete;
+    Engine &operator=(const Engine &) = delete;
+
+    // Binds the engine to a device and creates its stream.
+    int init(int device, int boundary, double lambda, float min_value);
+    // Plan for (block b, kernel kd); k1/k2 are host arrays (k2 may be null). Kernel
+    // spectra are computed on the device.
+    int make_plan(Plan<T> &pl, const int b[3], const float *k1, const int kd1[3], const float *k2,
+                  const int kd2[3], bool k_on_device = false);
+    void free_plan(Plan<T> &pl);
+
+    // One sequential iteration (ComputeBlockSeqThread.runIteration) of view plan pl.
+    int run_seq(const Plan<T> &pl, const BlockPlace &bp, const float *img, const float *w, float maxI,
+                double *stats_dev);
+    // One multiplicative iteration over views (ComputeBlockMulThread.runIteration).
+    int run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace &bp, const float *const *imgs,
+                const float *const *ws, float maxI, double *stats_dev);
+    // Linear convolution of a T block (mirror or zero extension) with pl's k1, result
+    // to a float block of the same size.
+    int convolve(const Plan<T> &pl, const T *blk, int src_kind, float *out);
+
+    cudaStream_t stream() const { return stream_; }
+    int device() const { return device_; }
+    const std::string &error() const { return err_; }
+    int fail(int code, const std::string &msg);
+    int cuda_check(cudaError_t e, const char *what);
+    int reserve(long long Pc, long long nvox_block, long long rows);
+
+private:
+    int launch_fwd_mirror(const Plan<T> &pl, const BlockMap &bm, const T *src, V *S);
+    int launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh);
+    BlockMap block_map(const Plan<T> &pl, const BlockPlace &bp) const;
+
+    int device_ = -1;
+    int boundary_ = BOUNDARY_REFERENCE;
+    double lambda_ = 0.0;
+    float min_value_ = 1e-4f;
+    cudaStream_t stream_ = nullptr;
+    V *S0_ = nullptr, *S1_ = nullptr;
+    long long Scap_ = 0;
+    double *prod_ = nullptr;
+    long long prodcap_ = 0;
+    double *partials_ = nullptr;
+    long long partcap_ = 0;
+    float *kbuf_ = nullptr;
+    long long kcap_ = 0;
+    std::string err_;
+};
+
+extern template class Engine<float>;
+extern template class Engine<double>;
+
+}  // namespace mvr

@@ -1,0 +1,470 @@
+// Pass kernels of one block iteration.  The spectrum of a block lives in HBM as
+// complex [Pz][Py][Hx], Hx = Px/2 + 1 (half spectrum along x).  One iteration of one
+// view on one block is:
+//
+//   k_rows_fwd      extract psi (mirror-single, from the volume) + R2C along x
+//   k_cols   Y fwd
+//   k_cols   Z fwd -> x K1^ -> Z inv      (spectral multiply fused between the passes)
+//   k_cols   Y inv
+//   k_rows_ratio    C2R along x -> conv1 -> quotient img/conv1 -> R2C along x
+//   k_cols   Y fwd
+//   k_cols   Z fwd -> x K2^ -> Z inv
+//   k_cols   Y inv
+//   k_rows_update   C2R along x -> conv2 -> multiplicative update, FP64 stats,
+//                   effective region written to the output volume
+//
+// Reference semantics (cited relative to src/main/java/ of the reference):
+//   quotient   net/preibisch/mvrecon/process/deconvolution/iteration/sequential/DeconvolutionMethods.java:71-74
+//   update     .../DeconvolutionMethods.java:320-358 (Seq), 370-419 (Mul), tikhonov 421
+//   extension  .../ComputeBlockSeqThreadCPU.java:171-209 (mirror-single for conv1, 1 for conv2)
+//   extract    net/preibisch/mvrecon/process/deconvolution/MultiViewDeconvolutionSeq.java:115
+//              (Views.extendMirrorSingle(psi)), img/weight zero-extended (:122-123)
+#pragma once
+#include "fft_device.cuh"
+
+namespace mvr {
+
+constexpr int kMaxViews = 16;
+
+// Where a block sits: FFT domain, block, volume, and the region written back.
+struct BlockMap {
+    int P[3];            // FFT domain (x, y, z)
+    int b[3];            // block size
+    int L[3];            // wrapped left extension: domain index j >= P-L is block coordinate j-P
+    long long off[3];    // block offset in volume coordinates (may be negative)
+    long long D[3];      // volume dims
+    int wlo[3], whi[3];  // block-local region written to the output volume [lo, hi)
+    long long ooff[3];   // volume coordinate of block-local (0,0,0) in the output volume
+    long long OD[3];     // output volume dims
+};
+
+__device__ __forceinline__ int ext_e(int j, int P, int L) { return j >= P - L ? j - P : j; }
+
+__device__ __forceinline__ long long mirror1(long long i, long long n)
+{
+    if (n <= 1) return 0;
+    const long long p = 2 * n - 2;
+    i %= p;
+    if (i < 0) i += p;
+    return i >= n ? p - i : i;
+}
+
+// Volume index of block coordinate (bx, by, bz) under mirror-single on the volume.
+struct MirrorRow {
+    long long base;  // (gz * D1 + gy) * D0
+};
+__device__ __forceinline__ MirrorRow mirror_row(const BlockMap &m, int y, int z)
+{
+    const int ey = ext_e(y, m.P[1], m.L[1]), ez = ext_e(z, m.P[2], m.L[2]);
+    const long long by = mirror1(ey, m.b[1]), bz = mirror1(ez, m.b[2]);
+    const long long gy = mirror1(m.off[1] + by, m.D[1]), gz = mirror1(m.off[2] + bz, m.D[2]);
+    MirrorRow r;
+    r.base = (gz * m.D[1] + gy) * m.D[0];
+    return r;
+}
+__device__ __forceinline__ long long mirror_x(const BlockMap &m, int x)
+{
+    const int ex = ext_e(x, m.P[0], m.L[0]);
+    return mirror1(m.off[0] + mirror1(ex, m.b[0]), m.D[0]);
+}
+
+// Zero-extended access to img / weight volumes for block voxels.
+struct ZeroRow {
+    long long base;  // -1 when the row lies outside the volume
+};
+__device__ __forceinline__ ZeroRow zero_row(const BlockMap &m, int by, int bz)
+{
+    const long long gy = m.off[1] + by, gz = m.off[2] + bz;
+    ZeroRow r;
+    r.base = (gy < 0 || gy >= m.D[1] || gz < 0 || gz >= m.D[2]) ? -1 : (gz * m.D[1] + gy) * m.D[0];
+    return r;
+}
+__device__ __forceinline__ float zero_at(const float *__restrict__ v, const BlockMap &m, ZeroRow r, int bx)
+{
+    const long long gx = m.off[0] + bx;
+    if (r.base < 0 || gx < 0 || gx >= m.D[0]) return 0.0f;
+    return __ldg(v + r.base + gx);
+}
+
+// ---- row sources for the forward pass ----------------------------------------------
+template <typename TS>
+struct SrcMirror {  // psi (or any volume) under the block's mirror mapping
+    const TS *vol;
+    typedef MirrorRow Row;
+    __device__ __forceinline__ Row row(const BlockMap &m, int y, int z) const { return mirror_row(m, y, z); }
+    template <typename T>
+    __device__ __forceinline__ T at(const Row &r, const BlockMap &m, int x) const { return (T)vol[r.base + mirror_x(m, x)]; }
+};
+
+template <typename TS>
+struct SrcZero {  // a block buffer [b] with zero outside it (FFTConvolution with extendZero)
+    const TS *blk;
+    struct Row { long long base; };
+    __device__ __forceinline__ Row row(const BlockMap &m, int y, int z) const
+    {
+        const int ey = ext_e(y, m.P[1], m.L[1]), ez = ext_e(z, m.P[2], m.L[2]);
+        Row r;
+        r.base = (ey >= 0 && ey < m.b[1] && ez >= 0 && ez < m.b[2]) ? ((long long)ez * m.b[1] + ey) * m.b[0] : -1;
+        return r;
+    }
+    template <typename T>
+    __device__ __forceinline__ T at(const Row &r, const BlockMap &m, int x) const
+    {
+        const int ex = ext_e(x, m.P[0], m.L[0]);
+        if (r.base < 0 || ex < 0 || ex >= m.b[0]) return (T)0;
+        return (T)blk[r.base + ex];
+    }
+};
+
+struct SrcKernel {  // kernel placed with its centre (k/2) at the origin, wrapped, scaled
+    const float *k;
+    int kd[3];
+    double scale;
+    struct Row { long long base; };
+    __device__ __forceinline__ Row row(const BlockMap &m, int y, int z) const
+    {
+        const int ty = (y + kd[1] / 2) % m.P[1], tz = (z + kd[2] / 2) % m.P[2];
+        Row r;
+        r.base = (ty < kd[1] && tz < kd[2]) ? ((long long)tz * kd[1] + ty) * kd[0] : -1;
+        return r;
+    }
+    template <typename T>
+    __device__ __forceinline__ T at(const Row &r, const BlockMap &m, int x) const
+    {
+        const int tx = (x + kd[0] / 2) % m.P[0];
+        if (r.base < 0 || tx >= kd[0]) return (T)0;
+        return (T)((double)k[r.base + tx] * scale);
+    }
+};
+
+// ---- shared helpers of the row kernels ----------------------------------------------
+template <typename V>
+__device__ __forceinline__ void load_twiddles(V *tw, const V *__restrict__ twg, int n)
+{
+    for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = twg[i];
+}
+
+// Z (m-point FFT of packed rows) -> half spectrum X[0..m], stored to S rows.
+template <typename V>
+__device__ __forceinline__ void r2c_post_store(const V *Z, int ps, V *__restrict__ S, long long row0, int nr, int m,
+                                               const V *tw)
+{
+    typedef typename Re<V>::t T;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int r = warp; r < nr; r += nw) {
+        const V *z = Z + r * ps;
+        V *out = S + (row0 + r) * (long long)(m + 1);
+        for (int k = lane; k <= m; k += 32) {
+            const V zk = z[k == m ? 0 : k];
+            const V zc = cconj(z[k == 0 ? 0 : m - k]);
+            const V e = cscale(cadd(zk, zc), (T)0.5);
+            const V dd = cscale(csub(zk, zc), (T)0.5);
+            const V o = cx<V>(dd.y, -dd.x);  // -i * dd
+            out[k] = cadd(e, cmul(tw[k], o));
+        }
+    }
+}
+
+// S rows -> packed Z' for the inverse m-point FFT (yields Px * x after it).
+template <typename V>
+__device__ __forceinline__ void c2r_pre_load(const V *__restrict__ S, V *A, int ps, long long row0, int nr, int m,
+                                             const V *tw)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int r = warp; r < nr; r += nw) {
+        const V *in = S + (row0 + r) * (long long)(m + 1);
+        V *a = A + r * ps;
+        for (int k = lane; k < m; k += 32) {
+            const V xk = in[k];
+            const V xc = cconj(in[m - k]);
+            const V e = cadd(xk, xc);
+            const V o = cmul(csub(xk, xc), cconj(tw[k]));
+            a[k] = cx<V>(e.x - o.y, e.y + o.x);  // e + i*o
+        }
+    }
+}
+
+// ---- forward row pass with a fused source -------------------------------------------
+template <typename T, class Src>
+__global__ void __launch_bounds__(256) k_rows_fwd(Src src, typename Cx<T>::t *__restrict__ S, BlockMap bm, FftDesc d,
+                                                  const typename Cx<T>::t *__restrict__ twg, int RP)
+{
+    typedef typename Cx<T>::t V;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Px = bm.P[0], m = Px >> 1, ps = m + 1;
+    V *tw = reinterpret_cast<V *>(smem_raw);
+    V *A = tw + Px;
+    V *B = A + RP * ps;
+    const long long nrows = (long long)bm.P[1] * bm.P[2];
+    const long long row0 = (long long)blockIdx.x * RP;
+    const int nr = (int)min((long long)RP, nrows - row0);
+    load_twiddles(tw, twg, Px);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int r = warp; r < nr; r += nw) {
+        const long long row = row0 + r;
+        const int y = (int)(row % bm.P[1]), z = (int)(row / bm.P[1]);
+        const typename Src::Row R = src.row(bm, y, z);
+        for (int q = lane; q < m; q += 32)
+            A[r * ps + q] = cx<V>(src.template at<T>(R, bm, 2 * q), src.template at<T>(R, bm, 2 * q + 1));
+    }
+    __syncthreads();
+    V *Z = fft_run<false, false>(A, B, nr, ps, 1, d, tw, 2);
+    r2c_post_store(Z, ps, S, row0, nr, m, tw);
+}
+
+// ---- column passes (y or z axis) ----------------------------------------------------
+// MODE 0: forward, 1: inverse, 2: forward, multiply by Kh, inverse.
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256) k_cols(const typename Cx<T>::t *src, typename Cx<T>::t *dst,
+                                              const typename Cx<T>::t *__restrict__ Kh, int Hx, long long estride,
+                                              long long ostride, int NP, FftDesc d,
+                                              const typename Cx<T>::t *__restrict__ twg)
+{
+    typedef typename Cx<T>::t V;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = d.n;
+    V *tw = reinterpret_cast<V *>(smem_raw);
+    V *A = tw + n;
+    V *B = A + n * NP;
+    load_twiddles(tw, twg, n);
+    const int x0 = blockIdx.x * NP;
+    const long long base = (long long)blockIdx.y * ostride + x0;
+    const int np = min(NP, Hx - x0);
+    const int tot = n * NP;
+    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+        const int p = t % NP, i = t / NP;
+        A[t] = p < np ? src[base + i * estride + p] : cx<V>((T)0, (T)0);
+    }
+    __syncthreads();
+    V *R = fft_run<MODE == 1, true>(A, B, NP, 1, NP, d, tw, 1);
+    if (MODE == 2) {
+        for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+            const int p = t % NP, i = t / NP;
+            if (p < np) R[t] = cmul(R[t], __ldg(&Kh[base + i * estride + p]));
+        }
+        __syncthreads();
+        R = fft_run<true, true>(R, R == A ? B : A, NP, 1, NP, d, tw, 1);
+    }
+    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+        const int p = t % NP, i = t / NP;
+        if (p < np) dst[base + i * estride + p] = R[t];
+    }
+}
+
+// ---- pointwise rules ------------------------------------------------------------------
+// DeconvolutionMethods.java:71-74: img > 0 ? img / blurred : 1 (float division).
+__device__ __forceinline__ float quotient(float img, float blurred) { return img > 0.0f ? __fdiv_rn(img, blurred) : 1.0f; }
+__device__ __forceinline__ double quotient(float img, double blurred) { return img > 0.0f ? (double)img / blurred : 1.0; }
+
+// tikhonov (DeconvolutionMethods.java:421), double, no contraction
+__device__ __forceinline__ double tikhonov(double v, double lambda)
+{
+    return __ddiv_rn(__dsub_rn(__dsqrt_rn(__dadd_rn(1.0, __dmul_rn(__dmul_rn(2.0, lambda), v))), 1.0), lambda);
+}
+
+// computeNextValue (DeconvolutionMethods.java:320-358) in float, as Java evaluates it.
+__device__ __forceinline__ float next_value(float last, float integral, float weight, double lambda, float minI,
+                                            float maxI)
+{
+    const float value = __fmul_rn(last, integral);
+    float adjusted;
+    if (value > 0.0f) adjusted = lambda > 0 ? __fmul_rn((float)tikhonov((double)__fdiv_rn(value, maxI), lambda), maxI) : value;
+    else adjusted = minI;
+    const float next = isnan(adjusted) ? minI : (minI >= adjusted ? minI : adjusted);
+    return __fadd_rn(last, __fmul_rn(__fsub_rn(next, last), weight));
+}
+// The same rule in double (FP64 run).
+__device__ __forceinline__ double next_value(double last, double integral, double weight, double lambda, double minI,
+                                             double maxI)
+{
+    const double value = __dmul_rn(last, integral);
+    double adjusted;
+    if (value > 0.0) adjusted = lambda > 0 ? __dmul_rn(tikhonov(__ddiv_rn(value, maxI), lambda), maxI) : value;
+    else adjusted = minI;
+    const double next = isnan(adjusted) ? minI : (minI >= adjusted ? minI : adjusted);
+    return __dadd_rn(last, __dmul_rn(__dsub_rn(next, last), weight));
+}
+
+// ---- C2R -> quotient -> R2C (conv1 of one view, then the input of conv2) -------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_rows_ratio(typename Cx<T>::t *__restrict__ S, const float *__restrict__ img,
+                                                    BlockMap bm, FftDesc d, const typename Cx<T>::t *__restrict__ twg,
+                                                    int RP)
+{
+    typedef typename Cx<T>::t V;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int Px = bm.P[0], m = Px >> 1, ps = m + 1;
+    V *tw = reinterpret_cast<V *>(smem_raw);
+    V *A = tw + Px;
+    V *B = A + RP * ps;
+    const long long nrows = (long long)bm.P[1] * bm.P[2];
+    const long long row0 = (long long)blockIdx.x * RP;
+    const int nr = (int)min((long long)RP, nrows - row0);
+    load_twiddles(tw, twg, Px);
+    __syncthreads();
+    c2r_pre_load(S, A, ps, row0, nr, m, tw);
+    __syncthreads();
+    V *Z = fft_run<true, false>(A, B, nr, ps, 1, d, tw, 2);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int r = warp; r < nr; r += nw) {
+        const long long row = row0 + r;
+        const int y = (int)(row % bm.P[1]), z = (int)(row / bm.P[1]);
+        const int ey = ext_e(y, bm.P[1], bm.L[1]), ez = ext_e(z, bm.P[2], bm.L[2]);
+        const bool rin = ey >= 0 && ey < bm.b[1] && ez >= 0 && ez < bm.b[2];
+        const ZeroRow zr = rin ? zero_row(bm, ey, ez) : ZeroRow{-1};
+        V *zz = Z + r * ps;
+        for (int q = lane; q < m; q += 32) {
+            V c = zz[q];  // conv1 at x = 2q, 2q+1 (kernel spectrum carries 1/(Px Py Pz))
+            T out[2] = {c.x, c.y};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int ex = ext_e(2 * q + h, Px, bm.L[0]);
+                T ratio = (T)1;  // value-1 extension of the quotient outside the block
+                if (rin && ex >= 0 && ex < bm.b[0]) ratio = (T)quotient(zero_at(img, bm, zr, ex), out[h]);
+                out[h] = ratio;
+            }
+            zz[q] = cx<V>(out[0], out[1]);
+        }
+    }
+    __syncthreads();
+    V *Z2 = fft_run<false, false>(Z, Z == A ? B : A, nr, ps, 1, d, tw, 2);
+    r2c_post_store(Z2, ps, S, row0, nr, m, tw);
+}
+
+// ---- C2R -> update -------------------------------------------------------------------
+enum { EPI_SEQ = 0, EPI_MUL_FIRST = 1, EPI_MUL_ACC = 2, EPI_MUL_FINAL = 3, EPI_STORE = 4 };
+
+struct UpdateArgs {
+    const void *psi_src;  // T volume, read under the mirror mapping
+    void *psi_dst;        // T output volume (write region only)
+    const float *weight[kMaxViews];
+    int nviews;
+    double *prod;         // Mul: running product over views, block layout [bz][by][bx]
+    float *store;         // EPI_STORE: conv result, block layout
+    double lambda;
+    float minI;
+    float maxI;
+    double *partials;     // per CTA {sum, max}
+};
+
+template <typename T, int EPI>
+__global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restrict__ S, UpdateArgs ua, BlockMap bm,
+                                                     FftDesc d, const typename Cx<T>::t *__restrict__ twg, int RP)
+{
+    typedef typename Cx<T>::t V;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double red_s[32], red_m[32];
+    const int Px = bm.P[0], m = Px >> 1, ps = m + 1;
+    V *tw = reinterpret_cast<V *>(smem_raw);
+    V *A = tw + Px;
+    V *B = A + RP * ps;
+    const long long nrows = (long long)bm.P[1] * bm.P[2];
+    const long long row0 = (long long)blockIdx.x * RP;
+    const int nr = (int)min((long long)RP, nrows - row0);
+    load_twiddles(tw, twg, Px);
+    __syncthreads();
+    c2r_pre_load(S, A, ps, row0, nr, m, tw);
+    __syncthreads();
+    V *Z = fft_run<true, false>(A, B, nr, ps, 1, d, tw, 2);
+    const T *psrc = reinterpret_cast<const T *>(ua.psi_src);
+    T *pdst = reinterpret_cast<T *>(ua.psi_dst);
+    double lsum = 0.0, lmax = -1.0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int r = warp; r < nr; r += nw) {
+        const long long row = row0 + r;
+        const int y = (int)(row % bm.P[1]), z = (int)(row / bm.P[1]);
+        if (y >= bm.b[1] || z >= bm.b[2]) continue;  // extension rows carry no block voxels
+        const ZeroRow zr = zero_row(bm, y, z);
+        const MirrorRow mr = mirror_row(bm, y, z);
+        const bool wrow = y >= bm.wlo[1] && y < bm.whi[1] && z >= bm.wlo[2] && z < bm.whi[2];
+        const long long orow = ((bm.ooff[2] + z) * bm.OD[1] + (bm.ooff[1] + y)) * bm.OD[0] + bm.ooff[0];
+        const long long brow = ((long long)z * bm.b[1] + y) * bm.b[0];
+        const V *zz = Z + r * ps;
+        for (int q = lane; q < m; q += 32) {
+            const V c = zz[q];
+            const T cv[2] = {c.x, c.y};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int x = 2 * q + h;
+                if (x >= bm.b[0]) continue;
+                const T integral = cv[h];
+                if (EPI == EPI_STORE) {
+                    ua.store[brow + x] = (float)integral;
+                    continue;
+                }
+                if (EPI == EPI_MUL_FIRST) { ua.prod[brow + x] = (double)integral; continue; }
+                if (EPI == EPI_MUL_ACC) { ua.prod[brow + x] *= (double)integral; continue; }
+                const T last = psrc[mr.base + mirror_x(bm, x)];
+                T next;
+                if (EPI == EPI_SEQ) {
+                    const float w = zero_at(ua.weight[0], bm, zr, x);
+                    next = next_value(last, integral, (T)w, ua.lambda, (T)ua.minI, (T)ua.maxI);
+                } else {  // EPI_MUL_FINAL: DeconvolutionMethods.computeNextValueMul 370-419
+                    double prod = (ua.nviews == 1 ? 1.0 : ua.prod[brow + x]) * (double)integral;
+                    double sumW = 0.0;
+                    for (int v = 0; v < ua.nviews; ++v) sumW += (double)zero_at(ua.weight[v], bm, zr, x);
+                    prod = pow(prod, 1.0 / ua.nviews);
+                    sumW = sumW < 1.0 ? sumW : 1.0;
+                    next = next_value(last, (T)prod, (T)sumW, ua.lambda, (T)ua.minI, (T)ua.maxI);
+                }
+                const T ch = next - last;  // signed change (DeconvolutionMethods.java:308)
+                lsum += (double)ch;
+                lmax = fmax(lmax, (double)ch);
+                if (wrow && x >= bm.wlo[0] && x < bm.whi[0]) pdst[orow + x] = next;
+            }
+        }
+    }
+    if (EPI == EPI_SEQ || EPI == EPI_MUL_FINAL) {
+        // deterministic block reduction -> partials[blockIdx.x]
+        for (int o = 16; o > 0; o >>= 1) {
+            lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+            lmax = fmax(lmax, __shfl_down_sync(0xffffffffu, lmax, o));
+        }
+        if (lane == 0) { red_s[warp] = lsum; red_m[warp] = lmax; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0, mx = -1.0;
+            for (int w = 0; w < nw; ++w) { s += red_s[w]; mx = fmax(mx, red_m[w]); }
+            ua.partials[2 * blockIdx.x] = s;
+            ua.partials[2 * blockIdx.x + 1] = mx;
+        }
+    }
+}
+
+// Sum / max of per-CTA partials in a fixed order (one CTA), into out[0..1].
+template <typename D>
+__global__ void k_reduce_stats(const D *__restrict__ partials, int n, D *out)
+{
+    __shared__ double s_s[1024], s_m[1024];
+    double s = 0.0, mx = -1.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) { s += partials[2 * i]; mx = fmax(mx, partials[2 * i + 1]); }
+    s_s[threadIdx.x] = s;
+    s_m[threadIdx.x] = mx;
+    __syncthreads();
+    for (int h = blockDim.x >> 1; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            s_s[threadIdx.x] += s_s[threadIdx.x + h];
+            s_m[threadIdx.x] = fmax(s_m[threadIdx.x], s_m[threadIdx.x + h]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { out[0] = s_s[0]; out[1] = s_m[0]; }
+}
+
+// Copy the effective region of a block from one volume to another (paste,
+// Block.java:357-403).
+template <typename T>
+__global__ void k_paste(const T *__restrict__ src, T *__restrict__ dst, long long D0, long long D1, long long ox,
+                        long long oy, long long oz, int sx, int sy, int sz)
+{
+    const long long n = (long long)sx * sy * sz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % sx);
+        const long long t = i / sx;
+        const int y = (int)(t % sy), z = (int)(t / sy);
+        const long long g = ((oz + z) * D1 + (oy + y)) * D0 + (ox + x);
+        dst[g] = src[g];
+    }
+}
+
+}  // namespace mvr

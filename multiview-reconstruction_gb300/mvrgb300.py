@@ -1,0 +1,217 @@
+"""Python mirror of the reference's per-block plugin surface over the C ABI
+(include/mvr_gb300.h), loaded with ctypes from the in-tree libmvrgb300.so.
+
+Reference interfaces (paths relative to src/main/java/ of PreibischLab/multiview-reconstruction,
+MV = net/preibisch/mvrecon/process/deconvolution):
+
+* ``ComputeBlockThreadFactory.create`` (MV/iteration/ComputeBlockThreadFactory.java:25-29)
+  -> :class:`BlockWorker`
+* ``ComputeBlockSeqThread.runIteration`` (MV/iteration/sequential/ComputeBlockSeqThread.java:54-61)
+  -> :meth:`BlockWorker.run_iteration`
+* ``ComputeBlockMulThread.runIteration`` (MV/iteration/mul/ComputeBlockMulThread.java:56-62)
+  -> :meth:`BlockWorker.run_iteration_mul`
+* ``ComputeBlockThread.IterationStatistics`` (MV/iteration/ComputeBlockThread.java:64-68)
+  -> :class:`IterationStatistics`
+
+There is no CPU fallback: loading fails with an exception when the library was not
+built, and every call raises :class:`MvrError` on a non-zero status.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libmvrgb300.so")
+
+OK, ERR_ARG, ERR_CUDA, ERR_OOM, ERR_UNSUPPORTED, ERR_STATE = 0, 1, 2, 3, 4, 5
+BOUNDARY_REFERENCE, BOUNDARY_CIRCULAR = 0, 1
+PSF_OPTIMIZATION_II, PSF_OPTIMIZATION_I, PSF_EFFICIENT_BAYESIAN, PSF_INDEPENDENT = 0, 1, 2, 3
+
+# every symbol include/mvr_gb300.h declares
+EXPORTS = [
+    "mvr_block_create", "mvr_block_destroy", "mvr_block_last_error", "mvr_block_set_kernels",
+    "mvr_block_run_seq", "mvr_block_run_mul", "mvr_block_run_seq_device", "mvr_block_synchronize",
+    "convolution3DfftCUDA", "convolution3DfftCUDAInPlace", "getNumDevicesCUDA", "getNameDeviceCUDA",
+    "getMemDeviceCUDA", "getFreeMemDeviceCUDA", "getCUDAcomputeCapabilityMajorVersion",
+    "getCUDAcomputeCapabilityMinorVersion", "mvr_free",
+]
+
+
+class MvrError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class _BlockParams(C.Structure):
+    _fields_ = [("block_size", C.c_int * 3), ("min_value", C.c_float), ("lambda_", C.c_float),
+                ("num_views", C.c_int), ("boundary", C.c_int), ("device", C.c_int)]
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Loads libmvrgb300.so (raises if it was not built: there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} not built; run __graft_entry__.build()")
+    L = C.CDLL(LIB_PATH)
+    P = C.c_void_p
+    L.mvr_block_create.argtypes = [C.POINTER(_BlockParams), C.POINTER(P)]
+    L.mvr_block_destroy.argtypes = [P]
+    L.mvr_block_destroy.restype = None
+    L.mvr_block_last_error.argtypes = [P]
+    L.mvr_block_last_error.restype = C.c_char_p
+    L.mvr_block_set_kernels.argtypes = [P, C.c_int, P, P, P]
+    L.mvr_block_run_seq.argtypes = [P, C.c_int, P, P, P, C.c_float, P]
+    L.mvr_block_run_mul.argtypes = [P, P, P, P, P, P]
+    L.mvr_block_run_seq_device.argtypes = [P, C.c_int, P, P, P, C.c_float, P]
+    L.mvr_block_synchronize.argtypes = [P]
+    L.convolution3DfftCUDAInPlace.argtypes = [P, P, P, P, C.c_int]
+    L.convolution3DfftCUDAInPlace.restype = None
+    L.convolution3DfftCUDA.argtypes = [P, P, P, P, C.c_int]
+    L.convolution3DfftCUDA.restype = C.POINTER(C.c_float)
+    L.mvr_free.argtypes = [P]
+    L.mvr_free.restype = None
+    L.getNumDevicesCUDA.restype = C.c_int
+    L.getNameDeviceCUDA.argtypes = [C.c_int, C.c_char_p]
+    L.getNameDeviceCUDA.restype = None
+    L.getMemDeviceCUDA.argtypes = [C.c_int]
+    L.getMemDeviceCUDA.restype = C.c_longlong
+    L.getFreeMemDeviceCUDA.argtypes = [C.c_int]
+    L.getFreeMemDeviceCUDA.restype = C.c_longlong
+    L.getCUDAcomputeCapabilityMajorVersion.argtypes = [C.c_int]
+    L.getCUDAcomputeCapabilityMinorVersion.argtypes = [C.c_int]
+    _lib = L
+    return L
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _size_xyz(a: np.ndarray):
+    return (C.c_int * 3)(a.shape[2], a.shape[1], a.shape[0])
+
+
+@dataclass
+class IterationStatistics:
+    """ComputeBlockThread.IterationStatistics: signed sum and max of the change."""
+    sum_change: float = 0.0
+    max_change: float = -1.0
+
+
+class BlockWorker:
+    """One block worker (ComputeBlockSeqThread / ComputeBlockMulThread) on one GPU.
+
+    ``block_size`` is (x, y, z); arrays are float32 [z][y][x]."""
+
+    def __init__(self, block_size, min_value: float = 1e-4, lam: float = 0.0, num_views: int = 1,
+                 boundary: int = BOUNDARY_REFERENCE, device: int = 0):
+        self._lib = load()
+        prm = _BlockParams((C.c_int * 3)(*block_size), min_value, lam, num_views, boundary, device)
+        h = C.c_void_p()
+        rc = self._lib.mvr_block_create(C.byref(prm), C.byref(h))
+        if rc != OK:
+            raise MvrError(rc, self._lib.mvr_block_last_error(None).decode())
+        self._h = h
+        self.block_size = tuple(block_size)
+        self.min_value = min_value
+        self.num_views = num_views
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mvr_block_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != OK:
+            raise MvrError(rc, self._lib.mvr_block_last_error(self._h).decode())
+
+    @property
+    def shape(self):
+        return (self.block_size[2], self.block_size[1], self.block_size[0])
+
+    def set_kernels(self, view: int, kernel1, kernel2):
+        k1, k2 = _f32(kernel1), _f32(kernel2)
+        if k1.shape != k2.shape:
+            raise ValueError("kernel1 and kernel2 must have the same shape")
+        self._check(self._lib.mvr_block_set_kernels(self._h, view, _p(k1), _p(k2), _size_xyz(k1)))
+
+    def run_iteration(self, view: int, psi_block, img_block, weight_block, max_intensity: float):
+        """ComputeBlockSeqThread.runIteration; psi_block (float32) is updated in place."""
+        if psi_block.dtype != np.float32 or not psi_block.flags.c_contiguous or psi_block.shape != self.shape:
+            raise ValueError("psi_block must be a C-contiguous float32 array of the block shape")
+        img, w = _f32(img_block), _f32(weight_block)
+        if img.shape != self.shape or w.shape != self.shape:
+            raise ValueError("img/weight blocks must have the block shape")
+        st = np.zeros(2, dtype=np.float64)
+        self._check(self._lib.mvr_block_run_seq(self._h, view, _p(psi_block), _p(img), _p(w),
+                                                float(max_intensity), _p(st)))
+        return IterationStatistics(float(st[0]), float(st[1]))
+
+    def run_iteration_mul(self, psi_block, img_blocks, weight_blocks, max_intensities):
+        """ComputeBlockMulThread.runIteration over all views; psi_block updated in place."""
+        if psi_block.dtype != np.float32 or not psi_block.flags.c_contiguous or psi_block.shape != self.shape:
+            raise ValueError("psi_block must be a C-contiguous float32 array of the block shape")
+        imgs = [_f32(a) for a in img_blocks]
+        ws = [_f32(a) for a in weight_blocks]
+        if len(imgs) != self.num_views or len(ws) != self.num_views:
+            raise ValueError("one image and one weight block per view")
+        ip = (C.c_void_p * self.num_views)(*[a.ctypes.data for a in imgs])
+        wp = (C.c_void_p * self.num_views)(*[a.ctypes.data for a in ws])
+        mx = np.asarray(max_intensities, dtype=np.float32)
+        st = np.zeros(2, dtype=np.float64)
+        self._check(self._lib.mvr_block_run_mul(self._h, _p(psi_block), ip, wp, _p(mx), _p(st)))
+        return IterationStatistics(float(st[0]), float(st[1]))
+
+    def run_iteration_device(self, view: int, psi_ptr: int, img_ptr: int, w_ptr: int, max_intensity: float,
+                             stats_ptr: int = 0):
+        """Queues one iteration on device buffers (raw device addresses)."""
+        self._check(self._lib.mvr_block_run_seq_device(self._h, view, C.c_void_p(psi_ptr), C.c_void_p(img_ptr),
+                                                       C.c_void_p(w_ptr), float(max_intensity),
+                                                       C.c_void_p(stats_ptr) if stats_ptr else None))
+
+    def synchronize(self):
+        self._check(self._lib.mvr_block_synchronize(self._h))
+
+
+def convolution3d_fft_cuda_in_place(im, kernel, device: int = 0) -> np.ndarray:
+    """The reference's JNA call CUDAFourierConvolution.convolution3DfftCUDAInPlace with
+    reversed dims; returns the convolved copy of ``im``."""
+    L = load()
+    a = np.array(im, dtype=np.float32, order="C")
+    k = _f32(kernel)
+    imdim = (C.c_int * 3)(*a.shape)  # reversed: {z, y, x}
+    kdim = (C.c_int * 3)(*k.shape)
+    L.convolution3DfftCUDAInPlace(_p(a), imdim, _p(k), kdim, device)
+    return a
+
+
+def device_info(device: int = 0) -> dict:
+    L = load()
+    name = C.create_string_buffer(256)
+    L.getNameDeviceCUDA(device, name)
+    return dict(count=L.getNumDevicesCUDA(), name=name.value.decode(), mem=L.getMemDeviceCUDA(device),
+                free=L.getFreeMemDeviceCUDA(device), major=L.getCUDAcomputeCapabilityMajorVersion(device),
+                minor=L.getCUDAcomputeCapabilityMinorVersion(device))
