@@ -1,0 +1,376 @@
+#!/usr/bin/env python3
+"""Throughput of the multiview Bayesian (RL-type) deconvolution iteration on GB300.
+
+Workload (the reference's 4-view case): 4 views of 256^3 float32, PSFs 31x31x61
+Gaussian-plus-side-lobes rotated 0/45/90/135 degrees about y, Optimization-I compound
+kernels, cosine-blended weights normalised with the reference's hard rule, psi from
+PsiInitAvgPrecise, Tikhonov lambda 0.006, compute blocks 192^3 (16 per view).
+Synthetic seeded data stands in for the reference's microscopy datasets.
+
+A step is one full iteration (all 4 views, all blocks) over the whole volume.
+Metric: voxel-iterations/s = 256^3 * steps / seconds.
+
+  value  device-resident inputs, CUDA events on the library's stream around K steps
+  e2e    the public C ABI with pinned host buffers: every step uploads the 4 images,
+         4 raw weights and psi, runs one iteration and reads psi back
+  --impl reference  the CPU restatement of the reference block iteration (oracle/,
+         all host threads) on a bounded sample of the same workload
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "multiview-reconstruction_gb300")
+for _p in (PKG, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+DIMS = (256, 256, 256)
+VIEWS = 4
+BLOCK = (192, 192, 192)
+PSF = (31, 31, 61)
+LAMBDA = 0.006
+METRIC = "voxel-iterations/s (4 views)"
+UNIT = "voxel-iterations/s"
+NVOX = DIMS[0] * DIMS[1] * DIMS[2]
+VIEW_BLOCKS_PER_ITER = 16 * VIEWS  # 2 x 2 x 4 blocks of 192^3 per view
+
+
+def workload_config(boundary):
+    return {"workload": "4 views 256^3 float32, PSF 31x31x61 Optimization-I, blocks 192^3, Seq (OSEM-like)",
+            "views": VIEWS, "dims": list(DIMS), "block": list(BLOCK), "psf": list(PSF), "lambda": LAMBDA,
+            "iterations_per_step": 1, "boundary": boundary,
+            "l2": "inputs larger than L2 (4 images + 4 weights + psi = 576 MiB)",
+            "data": "seeded synthetic beads + ellipsoid, Poisson, background 10"}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_data():
+    import synthetic
+
+    return synthetic.config_256()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons while the timed region runs."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        try:
+            rows = [l.strip().split(",") for l in open(self.path) if l.strip()]
+        except Exception:
+            rows = []
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_block_sample(ds, k1s, k2s, mx, n_blocks):
+    """Times the oracle (reference-faithful CPU block iteration) on n_blocks view-blocks
+    of the workload; returns (seconds per view-block, threads)."""
+    import oracle
+
+    D = DIMS
+    kk = tuple(2 * k - 1 for k in PSF)
+    blocks = oracle.divide_into_blocks(D, kk, BLOCK)
+    times = []
+    for i in range(n_blocks):
+        v = i % VIEWS
+        bl = blocks[(5 + i) % len(blocks)]
+        off = bl["offset"]
+        idx = [np.arange(off[d], off[d] + BLOCK[d]) for d in range(3)]
+        psi = np.full((BLOCK[2], BLOCK[1], BLOCK[0]), 50.0, np.float32)
+        img = np.zeros_like(psi)
+        w = np.zeros_like(psi)
+        ok = [(idx[d] >= 0) & (idx[d] < D[d]) for d in range(3)]
+        sub = np.ix_(idx[2][ok[2]], idx[1][ok[1]], idx[0][ok[0]])
+        dst = np.ix_(np.nonzero(ok[2])[0], np.nonzero(ok[1])[0], np.nonzero(ok[0])[0])
+        img[dst] = ds.images[v][sub]
+        w[dst] = ds.weights[v][sub]
+        t0 = time.perf_counter()
+        oracle.block_seq(psi, img, w, k1s[v], k2s[v], LAMBDA, 1e-4, float(mx[v]))
+        times.append(time.perf_counter() - t0)
+    return float(np.mean(times)), oracle.num_threads()
+
+
+def prepare_reference_inputs(ds):
+    import oracle
+
+    k1s, k2s = oracle.psf_init(ds.psfs, oracle.PSF_OPTIMIZATION_I, 0)
+    ws = oracle.normalize_weights(ds.weights)
+    _, mx, _ = oracle.psi_init_avg(ds.images)
+    ds.weights = ws
+    return k1s, k2s, mx
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    import oracle
+
+    oracle.build()
+    ds = make_data()
+    k1s, k2s, mx = prepare_reference_inputs(ds)
+    threads = oracle.num_threads()
+    for _ in range(args.warmup):
+        cpu_block_sample(ds, k1s, k2s, mx, 1)
+    t0 = time.perf_counter()
+    per_vb = []
+    for _ in range(args.steps):
+        t, _ = cpu_block_sample(ds, k1s, k2s, mx, 1)
+        per_vb.append(t)
+    wall = time.perf_counter() - t0
+    t_vb = float(np.mean(per_vb))
+    value = NVOX / (t_vb * VIEW_BLOCKS_PER_ITER)
+    sample = (f"1 view-block (192^3, reference boundary, FFT domain 222x222x252) per step, "
+              f"extrapolated to the {VIEW_BLOCKS_PER_ITER} view-blocks of one 256^3 iteration")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_vb * VIEW_BLOCKS_PER_ITER,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config("reference (mirror-single / value-1 extension)"),
+            "wall_s": wall,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, ws, rank, local):
+    import torch
+
+    import mvrgb300 as M
+
+    torch.cuda.set_device(local)
+    dev = local
+    ds = make_data()
+    shape = (DIMS[2], DIMS[1], DIMS[0])
+    boundary = M.BOUNDARY_CIRCULAR if args.boundary == "circular" else M.BOUNDARY_REFERENCE
+    d_img = [torch.from_numpy(a).to(f"cuda:{dev}") for a in ds.images]
+    d_w = [torch.from_numpy(a).to(f"cuda:{dev}") for a in ds.weights]
+    dec = M.Deconvolution(DIMS, VIEWS, BLOCK, mul=False, psf_type=M.PSF_OPTIMIZATION_I, psf_norm_threads=0,
+                          lam=LAMBDA, boundary=boundary, precision=M.PRECISION_FP32, weight_norm=M.WEIGHTS_HARD,
+                          device=dev)
+    for v in range(VIEWS):
+        dec.set_view_device(v, d_img[v].data_ptr(), d_w[v].data_ptr(), ds.psfs[v])
+    dec.prepare()
+    stream = torch.cuda.ExternalStream(dec.stream_ptr(), device=f"cuda:{dev}")
+    for _ in range(args.warmup):
+        dec.run_iterations(1)
+    dec.synchronize()
+
+    # ---- value: device-resident, K steps bracketed by barrier + synchronize ----
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier(ws)
+    torch.cuda.synchronize()
+    launches0 = dec.launch_count()
+    with ClockSampler(dev) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            dec.run_iterations(1)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        dec.synchronize()
+    launches = dec.launch_count() - launches0
+    ms = e0.elapsed_time(e1)
+    barrier(ws)
+    ms = max_over_ranks(ms, ws)
+    clocks = clk.summary()
+    value = ws * NVOX * args.steps / (ms / 1e3)
+
+    # ---- roofline: per-kernel CUDA events on the library stream, same workload ----
+    dec.set_profiling(True)
+    prof_steps = max(1, min(args.steps, 3))
+    for _ in range(prof_steps):
+        dec.run_iterations(1)
+    prof = dec.profile()
+    dec.set_profiling(False)
+    total_ms = sum(v[0] for v in prof.values()) or 1.0
+    dom = max(prof.items(), key=lambda kv: kv[1][0])
+    dname, (dms, dlaunch, dbytes) = dom
+    peak, peak_kind = load_peaks()
+    achieved = (dbytes / dlaunch) / (dms / dlaunch / 1e3) / 1e9 if dlaunch else 0.0
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(dname)
+    kernels = {k: {"share": v[0] / total_ms, "launches": v[1],
+                   "gbs": (v[2] / (v[0] / 1e3) / 1e9) if v[0] > 0 else None} for k, v in prof.items() if v[1]}
+    path_bytes = sum(v[2] for v in prof.values())
+    roofline = {"bound": "hbm", "kernel": dname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
+                "traffic": traffic, "bytes_per_launch": dbytes / max(1, dlaunch),
+                "path_achieved": path_bytes / (total_ms / 1e3) / 1e9, "kernels": kernels}
+
+    # ---- e2e: public C ABI with pinned host buffers, copies inside the timed region ----
+    h_img = [torch.from_numpy(a).pin_memory() for a in ds.images]
+    h_w = [torch.from_numpy(a).pin_memory() for a in ds.weights]
+    h_psi = torch.empty(shape, dtype=torch.float32).pin_memory()
+    h_psi.copy_(torch.from_numpy(dec.get_psi()))
+    e2e_dec = M.Deconvolution(DIMS, VIEWS, BLOCK, mul=False, psf_type=M.PSF_OPTIMIZATION_I, psf_norm_threads=0,
+                              lam=LAMBDA, boundary=boundary, precision=M.PRECISION_FP32, weight_norm=M.WEIGHTS_HARD,
+                              device=dev)
+    for v in range(VIEWS):
+        e2e_dec.set_view(v, h_img[v].numpy(), h_w[v].numpy(), ds.psfs[v])
+    e2e_dec.prepare()
+    out = h_psi.numpy()
+    e2e_steps = max(1, min(args.steps, 10))
+    for _ in range(min(2, args.warmup)):
+        for v in range(VIEWS):
+            e2e_dec.update_images(v, h_img[v].numpy(), h_w[v].numpy())
+        e2e_dec.set_psi(out)
+        e2e_dec.run_iterations(1)
+        e2e_dec.get_psi(out)
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for v in range(VIEWS):
+            e2e_dec.update_images(v, h_img[v].numpy(), h_w[v].numpy())
+        e2e_dec.set_psi(out)
+        e2e_dec.run_iterations(1)
+        e2e_dec.get_psi(out)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
+    e2e_value = ws * NVOX * e2e_steps / e2e_s
+    h2d = VIEWS * 2 * NVOX * 4 + NVOX * 4
+    d2h = NVOX * 4
+    e2e_dec.close()
+
+    # ---- CPU baseline: the oracle on a bounded sample (rank 0, N = 1 only) ----
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        import oracle
+
+        oracle.build()
+        k1s, k2s, mx = prepare_reference_inputs(ds)
+        t_vb, threads = cpu_block_sample(ds, k1s, k2s, mx, args.cpu_blocks)
+        cpu = {"value": NVOX / (t_vb * VIEW_BLOCKS_PER_ITER), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_blocks} view-block(s) of 192^3 (reference boundary, FFT domain "
+                         f"222x222x252), extrapolated to the {VIEW_BLOCKS_PER_ITER} view-blocks of one iteration"}
+    dec.close()
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": workload_config(args.boundary), "clocks": clocks, "gpu_launches": launches,
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                        "steps": e2e_steps},
+                "roofline": roofline, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--boundary", choices=["circular", "reference"], default="circular")
+    ap.add_argument("--cpu-blocks", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_gb300(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -105,6 +105,91 @@ MVR_API int mvr_block_run_seq_device(mvr_block *h, int view, float *psi_block, c
 /* Waits for the work queued on the handle's stream. */
 MVR_API int mvr_block_synchronize(mvr_block *h);
 
+/* ---- whole-volume deconvolution (device resident) ---------------------------------
+ * MultiViewDeconvolutionSeq / MultiViewDeconvolutionMul with their set-up:
+ *   MV/deconvolution/MultiViewDeconvolution.java:90-200 (constructor, runIterations)
+ *   MV/deconvolution/MultiViewDeconvolutionSeq.java:57-180, MultiViewDeconvolutionMul.java:116-245
+ *   MV/deconvolution/DeconView.java:118-184 (block grid with the doubled kernel 2k-1)
+ *   MV/deconvolution/DeconViews.java:44-71 + DeconViewPSF.java:119-254 (PSF preparation)
+ *   MV/deconvolution/normalization/NormalizingRandomAccess.java:76-109 (weights)
+ *   MV/deconvolution/init/PsiInitAvgPrecise.java:52-110 (psi initialisation, max per view)
+ * Images, weights and psi stay on the device between calls.  Sizes are {x, y, z}. */
+#define MVR_PSF_OPTIMIZATION_II 0
+#define MVR_PSF_OPTIMIZATION_I 1
+#define MVR_PSF_EFFICIENT_BAYESIAN 2
+#define MVR_PSF_INDEPENDENT 3
+
+#define MVR_PRECISION_FP32 0
+#define MVR_PRECISION_FP64 1
+
+#define MVR_WEIGHTS_AS_GIVEN 0 /* weights are used as passed */
+#define MVR_WEIGHTS_HARD 1     /* NormalizingRandomAccess hardWeights */
+#define MVR_WEIGHTS_SMOOTH 2   /* NormalizingRandomAccess smoothWeights */
+
+typedef struct mvr_decon_params {
+    int dims[3];          /* volume size {x, y, z} */
+    int num_views;        /* 1..16 */
+    int block_size[3];    /* compute block size (DeconView blockSize) */
+    int mul;              /* 0: sequential (OSEM-like), 1: multiplicative */
+    int psf_type;         /* MVR_PSF_* (DeconViewPSF.PSFTYPE) */
+    int psf_norm_threads; /* thread count T of AdjustInput.sumImg: the first of T portions is
+                             counted twice in the PSF sum as in the reference; 0 = plain sum */
+    float lambda;         /* Tikhonov lambda, 0 = off */
+    float min_value;      /* psi floor, reference 1e-4 */
+    int boundary;         /* MVR_BOUNDARY_* */
+    int precision;        /* MVR_PRECISION_*: FP64 runs every stage in double */
+    int filter_blocks;    /* drop blocks whose weight is all zero (DeconView.filterBlocksForContent) */
+    int weight_norm;      /* MVR_WEIGHTS_* */
+    float osem_speedup;   /* OSEM speed-up of the weight normalisation (1 = none) */
+    float max_diff_range; /* smoothWeights parameters (reference 0.1, 0.05) */
+    float scaling_range;
+    int device;           /* CUDA device ordinal */
+} mvr_decon_params;
+
+typedef struct mvr_decon mvr_decon;
+
+MVR_API int mvr_decon_create(const mvr_decon_params *params, mvr_decon **out);
+MVR_API void mvr_decon_destroy(mvr_decon *h);
+MVR_API const char *mvr_decon_last_error(const mvr_decon *h);
+/* DeconView(image, weight, psf): host arrays, copied to the device. */
+MVR_API int mvr_decon_set_view(mvr_decon *h, int view, const float *img, const float *weight, const float *psf,
+                               const int psf_size[3]);
+/* The same with device-resident image and weight (borrowed, not copied; they must
+ * outlive the handle). */
+MVR_API int mvr_decon_set_view_device(mvr_decon *h, int view, const float *img, const float *weight,
+                                      const float *psf, const int psf_size[3]);
+/* Replaces a view's image and raw weight (host) without redoing the PSF preparation. */
+MVR_API int mvr_decon_update_images(mvr_decon *h, int view, const float *img, const float *weight);
+/* DeconViews + DeconViewPSF.init, weight normalisation, block grids, PsiInitAvgPrecise. */
+MVR_API int mvr_decon_prepare(mvr_decon *h);
+/* PsiInitFromRAI: replace psi (host or device float volume). */
+MVR_API int mvr_decon_set_psi(mvr_decon *h, const float *psi);
+MVR_API int mvr_decon_set_psi_device(mvr_decon *h, const float *psi);
+MVR_API int mvr_decon_get_psi(mvr_decon *h, float *psi);
+/* runIterations: `iterations` more iterations.  stats (or NULL) receives per iteration
+ * and view-step {sumChange, maxChange} (Seq: num_views steps, Mul: 1 step). */
+MVR_API int mvr_decon_run(mvr_decon *h, int iterations, double *stats);
+/* Prepared kernel1 / kernel2 of a view (DeconViewPSF.getKernel1/getKernel2). */
+MVR_API int mvr_decon_get_kernels(mvr_decon *h, int view, float *kernel1, float *kernel2);
+/* Maximum intensity per view (PsiInit.getMax). */
+MVR_API int mvr_decon_get_max(mvr_decon *h, float *max_per_view);
+/* Normalised weight of a view (host copy). */
+MVR_API int mvr_decon_get_weights(mvr_decon *h, int view, float *weight);
+/* Device address of psi (float for FP32, double for FP64), valid until the next run. */
+MVR_API const void *mvr_decon_psi_device(const mvr_decon *h);
+MVR_API int mvr_decon_synchronize(mvr_decon *h);
+/* The cudaStream_t (as void *) all of the handle's work is queued on. */
+MVR_API void *mvr_decon_stream(mvr_decon *h);
+/* Number of kernel launches the handle has queued so far. */
+MVR_API long long mvr_decon_launch_count(const mvr_decon *h);
+/* Per-kernel-family timing with CUDA events on the handle's stream (off by default). */
+#define MVR_KERNEL_KINDS 8
+MVR_API int mvr_decon_set_profiling(mvr_decon *h, int on);
+/* Accumulated {ms, launches, algorithmic bytes} per family (MVR_KERNEL_KINDS entries each);
+ * synchronises the stream. */
+MVR_API int mvr_decon_get_profile(mvr_decon *h, double *ms, long long *launches, double *bytes);
+MVR_API const char *mvr_kernel_name(int kind);
+
 /* ---- the reference's JNA library (CUDAFourierConvolution / CUDAStandardFunctions) ----
  * Exported under the reference's own symbol names so that the unchanged
  * ComputeBlockSeqThreadCUDA can load this library.  Dimensions arrive reversed

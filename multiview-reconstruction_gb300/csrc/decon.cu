@@ -1,0 +1,1062 @@
+// Device-resident whole-volume deconvolution: the GB300 counterpart of
+// MultiViewDeconvolution{Seq,Mul} with DeconViews / DeconViewPSF.init, the block
+// grid (BlockGeneratorFixedSizePrecise, BlockSorter, DeconView.filterBlocksForContent),
+// weight normalisation (NormalizingRandomAccess) and PsiInitAvgPrecise.
+//
+// Reference files (relative to src/main/java/net/preibisch/mvrecon/process/):
+//   deconvolution/MultiViewDeconvolutionSeq.java:57-180, MultiViewDeconvolutionMul.java:116-245
+//   deconvolution/DeconViewPSF.java:119-284, deconvolution/normalization/AdjustInput.java:52-122,
+//   deconvolution/util/Mirror.java:55-132, cuda/BlockGeneratorFixedSizePrecise.java:59-131,
+//   cuda/BlockSorter.java:55-143, deconvolution/DeconView.java:118-274,
+//   deconvolution/normalization/NormalizingRandomAccess.java:76-214,
+//   deconvolution/init/PsiInitAvgPrecise.java:52-110
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/mvr_gb300.h"
+#include "engine.cuh"
+
+namespace mvr {
+
+// ---- small device kernels -----------------------------------------------------------
+namespace {
+
+// sum over all and over the first `first` elements (AdjustInput.sumImg 115-119), FP64,
+// one CTA in a fixed order
+__global__ void k_sum_first(const float *__restrict__ k, long long n, long long first, double *out)
+{
+    __shared__ double sa[256], sf[256];
+    double a = 0.0, f = 0.0;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        const double v = (double)k[i];
+        a += v;
+        if (i < first) f += v;
+    }
+    sa[threadIdx.x] = a;
+    sf[threadIdx.x] = f;
+    __syncthreads();
+    for (int h = blockDim.x >> 1; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            sa[threadIdx.x] += sa[threadIdx.x + h];
+            sf[threadIdx.x] += sf[threadIdx.x + h];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = sa[0];
+        out[1] = sf[0];
+    }
+}
+
+__global__ void k_div(float *k, long long n, const double *sums, int quirk)
+{
+    const double s = sums[0] + (quirk ? sums[1] : 0.0);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        k[i] = (float)((double)k[i] / s);
+}
+
+// out[z][y][x] = in[pz[z]][py[y]][px[x]]
+__global__ void k_gather(const float *__restrict__ in, float *__restrict__ out, int kx, int ky, int kz,
+                         const int *__restrict__ perm)
+{
+    const long long n = (long long)kx * ky * kz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % kx);
+        const long long t = i / kx;
+        const int y = (int)(t % ky), z = (int)(t / ky);
+        const int sx = perm[x], sy = perm[kx + y], sz = perm[kx + ky + z];
+        out[i] = in[((long long)sz * ky + sy) * kx + sx];
+    }
+}
+
+__global__ void k_mul_into(float *tmp, const float *__restrict__ o, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        tmp[i] = __fmul_rn(o[i], tmp[i]);
+}
+
+// DeconViewPSF.pow 276-284: value^power by repeated float multiplication
+__global__ void k_pow_views(const float *__restrict__ k, float *e, long long n, int power)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float r = k[i];
+        for (int j = 1; j < power; ++j) r = __fmul_rn(r, k[i]);
+        e[i] = r;
+    }
+}
+
+struct WeightPtrs {
+    const float *raw[kMaxViews];
+    float *out[kMaxViews];
+};
+
+// NormalizingRandomAccess.get 76-109 (hardWeights 211-214, smoothWeights 183-200)
+__global__ void k_normalize_weights(WeightPtrs wp, int nv, long long n, double osem, int smooth, float maxDiffRange,
+                                    float scalingRange)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double sumW = 0.0;
+        float my[kMaxViews];
+        for (int v = 0; v < nv; ++v) {
+            const double val = fmin(1.0, (double)wp.raw[v][i]);
+            my[v] = (float)val;
+            sumW += val;
+        }
+        for (int v = 0; v < nv; ++v) {
+            double r;
+            if (smooth) {
+                float s;
+                if (sumW <= 0) s = 0.0f;
+                else {
+                    const float ideal = (float)((double)my[v] / sumW);
+                    const float diff = __fsub_rn(my[v], ideal);
+                    float y = __fmul_rn(__fsub_rn(maxDiffRange, fabsf(diff)), __fdiv_rn(1.0f, maxDiffRange));
+                    y = y > 0.0f ? y : 0.0f;
+                    const float scale = __fmul_rn(__fmul_rn(y, my[v]), scalingRange);
+                    s = __fsub_rn(fminf(my[v], ideal), scale);
+                }
+                r = s;
+            } else if (sumW > 1) r = (float)((double)my[v] / sumW);
+            else r = my[v];
+            const double m = r * osem;
+            wp.out[v][i] = (float)(m < 1.0 ? m : 1.0);
+        }
+    }
+}
+
+struct ImgPtrs {
+    const float *img[kMaxViews];
+};
+
+// PsiInitAvgPreciseThread.compatibleLoop 127-160, per-CTA partials
+__global__ void k_psi_avg_partials(ImgPtrs ip, int nv, long long n, double *psum, long long *pcnt, float *pmax)
+{
+    __shared__ double ss[256];
+    __shared__ long long sc[256];
+    __shared__ float sm[256];
+    double s = 0.0;
+    long long c = 0;
+    float mx[kMaxViews];
+    for (int v = 0; v < nv; ++v) mx[v] = 0.0f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        double sum = 0.0;
+        int cnt = 0;
+        for (int v = 0; v < nv; ++v) {
+            const float x = ip.img[v][i];
+            if (x > 0.0f) {
+                mx[v] = fmaxf(mx[v], x);
+                sum += x;
+                ++cnt;
+            }
+        }
+        if (cnt > 0) {
+            s += sum / cnt;
+            ++c;
+        }
+    }
+    ss[threadIdx.x] = s;
+    sc[threadIdx.x] = c;
+    __syncthreads();
+    for (int h = blockDim.x >> 1; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            ss[threadIdx.x] += ss[threadIdx.x + h];
+            sc[threadIdx.x] += sc[threadIdx.x + h];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        psum[blockIdx.x] = ss[0];
+        pcnt[blockIdx.x] = sc[0];
+    }
+    for (int v = 0; v < nv; ++v) {
+        sm[threadIdx.x] = mx[v];
+        __syncthreads();
+        for (int h = blockDim.x >> 1; h > 0; h >>= 1) {
+            if (threadIdx.x < h) sm[threadIdx.x] = fmaxf(sm[threadIdx.x], sm[threadIdx.x + h]);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) pmax[blockIdx.x * kMaxViews + v] = sm[0];
+        __syncthreads();
+    }
+}
+
+__global__ void k_psi_avg_final(const double *psum, const long long *pcnt, const float *pmax, int nparts, int nv,
+                                double *avg_out, float *max_out)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s = 0.0;
+    long long c = 0;
+    for (int i = 0; i < nparts; ++i) {
+        s += psum[i];
+        c += pcnt[i];
+    }
+    double avg = s / (double)c;
+    if (isnan(avg)) avg = 1.0;
+    *avg_out = avg;
+    for (int v = 0; v < nv; ++v) {
+        float m = 0.0f;
+        for (int i = 0; i < nparts; ++i) m = fmaxf(m, pmax[i * kMaxViews + v]);
+        max_out[v] = m;
+    }
+}
+
+template <typename T>
+__global__ void k_fill_avg(T *psi, long long n, const double *avg)
+{
+    const T v = (T)(float)(*avg);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        psi[i] = v;
+}
+
+template <typename A, typename B>
+__global__ void k_convert(const A *__restrict__ in, B *__restrict__ out, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (B)in[i];
+}
+
+// any non-zero weight inside the block's box (zero outside the volume)
+__global__ void k_block_content(const float *__restrict__ w, long long D0, long long D1, long long D2, long long ox,
+                                long long oy, long long oz, int bx, int by, int bz, int *flag)
+{
+    const long long n = (long long)bx * by * bz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long x = ox + i % bx;
+        const long long t = i / bx;
+        const long long y = oy + t % by, z = oz + t / by;
+        if (x < 0 || y < 0 || z < 0 || x >= D0 || y >= D1 || z >= D2) continue;
+        if (w[(z * D1 + y) * D0 + x] != 0.0f) {
+            *flag = 1;
+            return;
+        }
+    }
+}
+
+int grid_for(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152 * 16)); }
+
+}  // namespace
+
+// ---- host helpers ---------------------------------------------------------------------
+struct BlockDesc {
+    long long off[3];
+    long long eoff[3];
+    int esize[3];
+    int eloc[3];
+    int batch;
+};
+
+// BlockGeneratorFixedSizePrecise.divideIntoBlocks + BlockSorter slab dimension; the
+// doubled kernel kk = 2k-1 (DeconView 155-157).  Returns false when the block is
+// smaller than the doubled kernel.
+static bool divide_blocks(const long long D[3], const int kk[3], const int b[3], std::vector<BlockDesc> &out,
+                          int &sort_dim)
+{
+    long long eff[3], nb[3];
+    for (int d = 0; d < 3; ++d) {
+        eff[d] = b[d] - kk[d] + 1;
+        if (eff[d] <= 0) return false;
+        nb[d] = D[d] / eff[d] + (D[d] % eff[d] != 0);
+    }
+    // BlockSorter: product of the other dims' counts; equal products keep the last dim
+    long long sz[3];
+    for (int d = 0; d < 3; ++d) {
+        sz[d] = 1;
+        for (int e = 0; e < 3; ++e)
+            if (e != d) sz[d] *= nb[e];
+    }
+    long long srt[3] = {sz[0], sz[1], sz[2]};
+    std::sort(srt, srt + 3);
+    sort_dim = 2;
+    for (int i = 0; i < 3; ++i) {
+        if (srt[i] >= 1 || i == 2) {
+            for (int d = 0; d < 3; ++d)
+                if (sz[d] == srt[i]) sort_dim = d;  // last d with this product
+            break;
+        }
+    }
+    out.clear();
+    for (long long z = 0; z < nb[2]; ++z)
+        for (long long y = 0; y < nb[1]; ++y)
+            for (long long x = 0; x < nb[0]; ++x) {
+                const long long cb[3] = {x, y, z};
+                BlockDesc bd{};
+                for (int d = 0; d < 3; ++d) {
+                    bd.eoff[d] = cb[d] * eff[d];
+                    long long es = eff[d];
+                    if (bd.eoff[d] + es > D[d]) es = D[d] - bd.eoff[d];
+                    bd.esize[d] = (int)es;
+                    bd.off[d] = bd.eoff[d] - kk[d] / 2;
+                    bd.eloc[d] = kk[d] / 2;
+                }
+                bd.batch = (int)cb[sort_dim];
+                out.push_back(bd);
+            }
+    return true;
+}
+
+// permutation of Mirror.mirror along one axis: swaps p <= n/2 with n-1-p in order
+static std::vector<int> mirror_perm(int n)
+{
+    std::vector<int> p(n);
+    for (int i = 0; i < n; ++i) p[i] = i;
+    for (int i = 0; i < n; ++i)
+        if (i <= n / 2) std::swap(p[i], p[n - 1 - i]);
+    return p;
+}
+
+// FusionTools.divideIntoPortions 1287-1329: length of the first portion for T threads
+static long long first_portion(long long size, int T)
+{
+    if (size == 0 || T <= 0) return 0;
+    long long np = size <= T ? size : std::max<long long>(T, size / (64LL * 64 * 64));
+    long long chunk = size / np;
+    while (chunk == 0) {
+        --np;
+        chunk = size / np;
+    }
+    return np == 1 ? size : chunk;
+}
+
+class DeconBase {
+public:
+    virtual ~DeconBase() = default;
+    virtual int set_images(int v, const float *img, const float *w, bool on_device) = 0;
+    virtual int set_psf(int v, const float *psf, const int dims[3]) = 0;
+    virtual int prepare() = 0;
+    virtual int set_psi(const float *psi, bool on_device) = 0;
+    virtual int get_psi(float *psi) = 0;
+    virtual int run(int iterations, double *stats) = 0;
+    virtual int get_kernels(int v, float *k1, float *k2) = 0;
+    virtual int get_max(float *mx) = 0;
+    virtual int get_weights(int v, float *w) = 0;
+    virtual const void *psi_device() const = 0;
+    virtual int synchronize() = 0;
+    virtual int num_steps() const = 0;
+    virtual const std::string &error() const = 0;
+    virtual void *stream() = 0;
+    virtual long long launches() const = 0;
+    virtual void set_profiling(bool on) = 0;
+    virtual int profile(KernelProfile &out) = 0;
+};
+
+template <typename T>
+class Decon : public DeconBase {
+public:
+    explicit Decon(const mvr_decon_params &p) : p_(p) {}
+    ~Decon() override;
+    int init();
+    int set_images(int v, const float *img, const float *w, bool on_device) override;
+    int set_psf(int v, const float *psf, const int dims[3]) override;
+    int prepare() override;
+    int set_psi(const float *psi, bool on_device) override;
+    int get_psi(float *psi) override;
+    int run(int iterations, double *stats) override;
+    int get_kernels(int v, float *k1, float *k2) override;
+    int get_max(float *mx) override;
+    int get_weights(int v, float *w) override;
+    const void *psi_device() const override { return psi_; }
+    int synchronize() override;
+    int num_steps() const override { return p_.mul ? 1 : p_.num_views; }
+    const std::string &error() const override { return err_; }
+    void *stream() override { return (void *)engine_.stream(); }
+    long long launches() const override { return engine_.launches(); }
+    void set_profiling(bool on) override { engine_.set_profiling(on); }
+    int profile(KernelProfile &out) override { return eng(engine_.profile_collect(out)); }
+
+private:
+    struct View {
+        float *img = nullptr, *w = nullptr, *w_raw = nullptr;
+        bool own_img = false, own_w = false;
+        std::vector<float> psf;
+        int kd[3] = {0, 0, 0};
+        float *k1 = nullptr, *k2 = nullptr;  // device, prepared kernels
+        Plan<T> plan;
+    };
+    int fail(int c, const std::string &m)
+    {
+        err_ = m;
+        return c;
+    }
+    int cuda(cudaError_t e, const char *what)
+    {
+        if (e == cudaSuccess) return MVR_OK;
+        err_ = std::string(what) + ": " + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? MVR_ERR_OOM : MVR_ERR_CUDA;
+    }
+    int eng(int rc)
+    {
+        if (rc != MVR_OK) err_ = engine_.error();
+        return rc;
+    }
+    int norm_to_sum1(float *k, long long n);
+    int invert(const float *in, float *out, const int kd[3]);
+    int conv_zero(const float *in, const int id[3], const float *k, const int kd[3], float *out);
+    int psf_init();
+    int run_step(int s, double *stats_slot);
+
+    mvr_decon_params p_;
+    Engine<T> engine_;
+    std::vector<View> views_;
+    long long n_ = 0;
+    T *psi_ = nullptr, *stage_ = nullptr;
+    std::vector<std::vector<BlockDesc>> blocks_;  // per step
+    std::vector<int> sort_dim_;
+    std::vector<int> jacobi_;
+    std::vector<float> max_;
+    double *d_scratch_ = nullptr;  // reductions
+    int *d_perm_ = nullptr;
+    int *d_flag_ = nullptr;
+    double *d_stats_ = nullptr;
+    long long stats_cap_ = 0;
+    bool prepared_ = false;
+    std::string err_;
+};
+
+#define D_TRY(expr)                   \
+    do {                              \
+        int rc__ = (expr);            \
+        if (rc__ != MVR_OK) return rc__; \
+    } while (0)
+#define D_CUDA(expr) D_TRY(cuda((expr), #expr))
+
+template <typename T>
+Decon<T>::~Decon()
+{
+    cudaSetDevice(p_.device);
+    for (auto &v : views_) {
+        if (v.own_img) cudaFree(v.img);
+        if (v.own_w) cudaFree(v.w_raw);
+        if (v.w != v.w_raw) cudaFree(v.w);
+        cudaFree(v.k1);
+        cudaFree(v.k2);
+        engine_.free_plan(v.plan);
+    }
+    cudaFree(psi_);
+    cudaFree(stage_);
+    cudaFree(d_scratch_);
+    cudaFree(d_perm_);
+    cudaFree(d_flag_);
+    cudaFree(d_stats_);
+}
+
+template <typename T>
+int Decon<T>::init()
+{
+    for (int d = 0; d < 3; ++d)
+        if (p_.dims[d] < 1 || p_.block_size[d] < 1) return fail(MVR_ERR_ARG, "dims and block_size must be >= 1");
+    if (p_.num_views < 1 || p_.num_views > kMaxViews) return fail(MVR_ERR_ARG, "num_views must be 1..16");
+    if (p_.psf_type < 0 || p_.psf_type > 3) return fail(MVR_ERR_ARG, "unknown psf_type");
+    if (p_.boundary != MVR_BOUNDARY_REFERENCE && p_.boundary != MVR_BOUNDARY_CIRCULAR)
+        return fail(MVR_ERR_ARG, "unknown boundary");
+    D_TRY(eng(engine_.init(p_.device, p_.boundary, (double)p_.lambda, p_.min_value)));
+    n_ = (long long)p_.dims[0] * p_.dims[1] * p_.dims[2];
+    views_.resize(p_.num_views);
+    D_CUDA(cudaMalloc(&psi_, sizeof(T) * (size_t)n_));
+    D_CUDA(cudaMalloc(&stage_, sizeof(T) * (size_t)n_));
+    D_CUDA(cudaMalloc(&d_scratch_, sizeof(double) * 2 * 4096 + sizeof(long long) * 4096 + sizeof(float) * 4096 * kMaxViews));
+    D_CUDA(cudaMalloc(&d_flag_, sizeof(int)));
+    return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::set_images(int v, const float *img, const float *w, bool on_device)
+{
+    if (v < 0 || v >= p_.num_views) return fail(MVR_ERR_ARG, "view out of range");
+    if (!img || !w) return fail(MVR_ERR_ARG, "image and weight must not be NULL");
+    D_CUDA(cudaSetDevice(p_.device));
+    View &vw = views_[v];
+    cudaStream_t s = engine_.stream();
+    if (on_device) {
+        if (vw.own_img) cudaFree(vw.img);
+        if (vw.own_w) cudaFree(vw.w_raw);
+        vw.img = const_cast<float *>(img);
+        vw.w_raw = const_cast<float *>(w);
+        vw.own_img = vw.own_w = false;
+    } else {
+        if (!vw.own_img) {
+            vw.img = nullptr;
+            D_CUDA(cudaMalloc(&vw.img, sizeof(float) * (size_t)n_));
+            vw.own_img = true;
+        }
+        if (!vw.own_w) {
+            vw.w_raw = nullptr;
+            D_CUDA(cudaMalloc(&vw.w_raw, sizeof(float) * (size_t)n_));
+            vw.own_w = true;
+        }
+        D_CUDA(cudaMemcpyAsync(vw.img, img, sizeof(float) * (size_t)n_, cudaMemcpyHostToDevice, s));
+        D_CUDA(cudaMemcpyAsync(vw.w_raw, w, sizeof(float) * (size_t)n_, cudaMemcpyHostToDevice, s));
+    }
+    if (p_.weight_norm == MVR_WEIGHTS_AS_GIVEN) {
+        if (vw.w != vw.w_raw && vw.w) cudaFree(vw.w);
+        vw.w = vw.w_raw;
+    } else if (prepared_) {
+        // weights depend on all views: renormalise with the new raw weights
+        WeightPtrs wp{};
+        for (int u = 0; u < p_.num_views; ++u) {
+            wp.raw[u] = views_[u].w_raw;
+            wp.out[u] = views_[u].w;
+        }
+        k_normalize_weights<<<grid_for(n_), 256, 0, s>>>(wp, p_.num_views, n_, (double)p_.osem_speedup,
+                                                        p_.weight_norm == MVR_WEIGHTS_SMOOTH, p_.max_diff_range,
+                                                        p_.scaling_range);
+        D_CUDA(cudaGetLastError());
+    }
+    return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::set_psf(int v, const float *psf, const int dims[3])
+{
+    if (v < 0 || v >= p_.num_views) return fail(MVR_ERR_ARG, "view out of range");
+    if (!psf || !dims || dims[0] < 1 || dims[1] < 1 || dims[2] < 1) return fail(MVR_ERR_ARG, "bad psf");
+    View &vw = views_[v];
+    const long long kn = (long long)dims[0] * dims[1] * dims[2];
+    vw.psf.assign(psf, psf + kn);
+    std::memcpy(vw.kd, dims, sizeof(vw.kd));
+    prepared_ = false;
+    return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::norm_to_sum1(float *k, long long n)
+{
+    const long long first = p_.psf_norm_threads > 0 ? first_portion(n, p_.psf_norm_threads) : 0;
+    cudaStream_t s = engine_.stream();
+    k_sum_first<<<1, 256, 0, s>>>(k, n, first, d_scratch_);
+    D_CUDA(cudaGetLastError());
+    k_div<<<grid_for(n), 256, 0, s>>>(k, n, d_scratch_, p_.psf_norm_threads > 0);
+    D_CUDA(cudaGetLastError());
+    return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::invert(const float *in, float *out, const int kd[3])
+{
+    std::vector<int> perm;
+    for (int d = 0; d < 3; ++d) {
+        std::vector<int> p = mirror_perm(kd[d]);
+        perm.insert(perm.end(), p.begin(), p.end());
+    }
+    cudaFree(d_perm_);
+    d_perm_ = nullptr;
+    D_CUDA(cudaMalloc(&d_perm_, sizeof(int) * perm.size()));
+    cudaStream_t s = engine_.stream();
+    D_CUDA(cudaMemcpyAsync(d_perm_, perm.data(), sizeof(int) * perm.size(), cudaMemcpyHostToDevice, s));
+    const long long n = (long long)kd[0] * kd[1] * kd[2];
+    k_gather<<<grid_for(n), 256, 0, s>>>(in, out, kd[0], kd[1], kd[2], d_perm_);
+    D_CUDA(cudaGetLastError());
+    D_CUDA(cudaStreamSynchronize(s));  // perm buffer is reused
+    return MVR_OK;
+}
+
+// FFTConvolution(extendZero(in), in, extendZero(k), k, out): linear, zero extension,
+// output over `in`, rounded to float.
+template <typename T>
+int Decon<T>::conv_zero(const float *in, const int id[3], const float *k, const int kd[3], float *out)
+{
+    Engine<float> e;
+    D_TRY(e.init(p_.device, BOUNDARY_REFERENCE, 0.0, 0.0f) == MVR_OK ? MVR_OK : fail(MVR_ERR_CUDA, e.error()));
+    D_CUDA(cudaStreamSynchronize(engine_.stream()));
+    Plan<float> pl;
+    int rc = e.make_plan(pl, id, k, kd, nullptr, nullptr, true);
+    if (rc == MVR_OK) rc = e.convolve(pl, in, SRC_ZERO, out);
+    if (rc == MVR_OK) rc = e.cuda_check(cudaStreamSynchronize(e.stream()), "conv_zero");
+    if (rc != MVR_OK) err_ = e.error();
+    e.free_plan(pl);
+    return rc;
+}
+
+// DeconViewPSF.init 119-254 for all views in order.
+template <typename T>
+int Decon<T>::psf_init()
+{
+    const int nv = p_.num_views;
+    cudaStream_t s = engine_.stream();
+    for (auto &vw : views_) {
+        const long long kn = (long long)vw.kd[0] * vw.kd[1] * vw.kd[2];
+        cudaFree(vw.k1);
+        cudaFree(vw.k2);
+        vw.k1 = vw.k2 = nullptr;
+        D_CUDA(cudaMalloc(&vw.k1, sizeof(float) * (size_t)kn));
+        D_CUDA(cudaMalloc(&vw.k2, sizeof(float) * (size_t)kn));
+        D_CUDA(cudaMemcpyAsync(vw.k1, vw.psf.data(), sizeof(float) * (size_t)kn, cudaMemcpyHostToDevice, s));
+    }
+    for (int v = 0; v < nv; ++v) {
+        View &vw = views_[v];
+        const long long n = (long long)vw.kd[0] * vw.kd[1] * vw.kd[2];
+        D_TRY(norm_to_sum1(vw.k1, n));
+        if (nv == 1 || p_.psf_type == MVR_PSF_INDEPENDENT) {
+            D_TRY(invert(vw.k1, vw.k2, vw.kd));
+            continue;
+        }
+        float *tmp = nullptr, *a = nullptr, *b = nullptr, *c = nullptr;
+        D_CUDA(cudaMalloc(&tmp, sizeof(float) * (size_t)n));
+        D_CUDA(cudaMalloc(&a, sizeof(float) * (size_t)n));
+        D_CUDA(cudaMalloc(&b, sizeof(float) * (size_t)n));
+        int rc = MVR_OK;
+        if (p_.psf_type == MVR_PSF_EFFICIENT_BAYESIAN) {
+            rc = invert(vw.k1, tmp, vw.kd);
+            for (int w = 0; w < nv && rc == MVR_OK; ++w) {
+                if (w == v) continue;
+                View &ww = views_[w];
+                const long long nw = (long long)ww.kd[0] * ww.kd[1] * ww.kd[2];
+                c = nullptr;
+                if (cudaMalloc(&c, sizeof(float) * (size_t)nw) != cudaSuccess) { rc = fail(MVR_ERR_OOM, "psf scratch"); break; }
+                rc = invert(vw.k1, a, vw.kd);
+                if (rc == MVR_OK) rc = conv_zero(a, vw.kd, ww.k1, ww.kd, b);
+                if (rc == MVR_OK) rc = invert(ww.k1, c, ww.kd);
+                if (rc == MVR_OK) rc = conv_zero(b, vw.kd, c, ww.kd, a);
+                if (rc == MVR_OK) {
+                    k_mul_into<<<grid_for(n), 256, 0, s>>>(tmp, a, n);
+                    rc = cuda(cudaGetLastError(), "k_mul_into");
+                }
+                cudaStreamSynchronize(s);
+                cudaFree(c);
+            }
+            if (rc == MVR_OK) rc = norm_to_sum1(tmp, n);
+            if (rc == MVR_OK) rc = cuda(cudaMemcpyAsync(vw.k2, tmp, sizeof(float) * (size_t)n, cudaMemcpyDeviceToDevice, s), "copy");
+        } else if (p_.psf_type == MVR_PSF_OPTIMIZATION_I) {
+            rc = cuda(cudaMemcpyAsync(tmp, vw.k1, sizeof(float) * (size_t)n, cudaMemcpyDeviceToDevice, s), "copy");
+            for (int w = 0; w < nv && rc == MVR_OK; ++w) {
+                if (w == v) continue;
+                View &ww = views_[w];
+                const long long nw = (long long)ww.kd[0] * ww.kd[1] * ww.kd[2];
+                c = nullptr;
+                if (cudaMalloc(&c, sizeof(float) * (size_t)nw) != cudaSuccess) { rc = fail(MVR_ERR_OOM, "psf scratch"); break; }
+                rc = invert(ww.k1, c, ww.kd);
+                if (rc == MVR_OK) rc = conv_zero(vw.k1, vw.kd, c, ww.kd, a);
+                if (rc == MVR_OK) {
+                    k_mul_into<<<grid_for(n), 256, 0, s>>>(tmp, a, n);
+                    rc = cuda(cudaGetLastError(), "k_mul_into");
+                }
+                cudaStreamSynchronize(s);
+                cudaFree(c);
+            }
+            if (rc == MVR_OK) rc = norm_to_sum1(tmp, n);
+            if (rc == MVR_OK) rc = invert(tmp, vw.k2, vw.kd);
+        } else {  // OPTIMIZATION_II
+            k_pow_views<<<grid_for(n), 256, 0, s>>>(vw.k1, tmp, n, nv);
+            rc = cuda(cudaGetLastError(), "k_pow_views");
+            if (rc == MVR_OK) rc = norm_to_sum1(tmp, n);
+            if (rc == MVR_OK) rc = invert(tmp, vw.k2, vw.kd);
+        }
+        cudaStreamSynchronize(s);
+        cudaFree(tmp);
+        cudaFree(a);
+        cudaFree(b);
+        D_TRY(rc);
+    }
+    return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::prepare()
+{
+    D_CUDA(cudaSetDevice(p_.device));
+    cudaStream_t s = engine_.stream();
+    const int nv = p_.num_views;
+    for (int v = 0; v < nv; ++v) {
+        if (!views_[v].img || !views_[v].w_raw) return fail(MVR_ERR_STATE, "images/weights missing for a view");
+        if (views_[v].psf.empty()) return fail(MVR_ERR_STATE, "psf missing for a view");
+    }
+    if (p_.mul) {
+        for (int v = 1; v < nv; ++v)
+            if (std::memcmp(views_[v].kd, views_[0].kd, sizeof(views_[0].kd)) != 0)
+                return fail(MVR_ERR_ARG, "multiplicative mode needs one block grid: equal PSF sizes "
+                                         "(MultiViewDeconvolutionMul.testBlockIntegrity)");
+    }
+    // weights
+    if (p_.weight_norm != MVR_WEIGHTS_AS_GIVEN) {
+        WeightPtrs wp{};
+        for (int v = 0; v < nv; ++v) {
+            if (views_[v].w == nullptr || views_[v].w == views_[v].w_raw) {
+                views_[v].w = nullptr;
+                D_CUDA(cudaMalloc(&views_[v].w, sizeof(float) * (size_t)n_));
+            }
+            wp.raw[v] = views_[v].w_raw;
+            wp.out[v] = views_[v].w;
+        }
+        k_normalize_weights<<<grid_for(n_), 256, 0, s>>>(wp, nv, n_, (double)p_.osem_speedup,
+                                                        p_.weight_norm == MVR_WEIGHTS_SMOOTH, p_.max_diff_range,
+                                                        p_.scaling_range);
+        D_CUDA(cudaGetLastError());
+    } else {
+        for (auto &vw : views_) vw.w = vw.w_raw;
+    }
+    // PSFs and their spectra for this block size
+    D_TRY(psf_init());
+    for (auto &vw : views_) D_TRY(eng(engine_.make_plan(vw.plan, p_.block_size, vw.k1, vw.kd, vw.k2, vw.kd, true)));
+    // block grids per step
+    const long long D[3] = {p_.dims[0], p_.dims[1], p_.dims[2]};
+    const int steps = num_steps();
+    blocks_.assign(steps, {});
+    sort_dim_.assign(steps, 2);
+    jacobi_.assign(steps, 1);
+    for (int st = 0; st < steps; ++st) {
+        const View &vw = views_[st];
+        int kk[3];
+        for (int d = 0; d < 3; ++d) kk[d] = 2 * vw.kd[d] - 1;
+        std::vector<BlockDesc> all;
+        if (!divide_blocks(D, kk, p_.block_size, all, sort_dim_[st]))
+            return fail(MVR_ERR_ARG, "block size smaller than the doubled kernel (2k-1)");
+        const float *wcheck = views_[st].w;  // Mul: view 0's grid and weight
+        for (auto &bd : all) {
+            int keep = 1;
+            if (p_.filter_blocks) {
+                D_CUDA(cudaMemsetAsync(d_flag_, 0, sizeof(int), s));
+                const long long bn = (long long)p_.block_size[0] * p_.block_size[1] * p_.block_size[2];
+                k_block_content<<<grid_for(bn), 256, 0, s>>>(wcheck, D[0], D[1], D[2], bd.off[0], bd.off[1], bd.off[2],
+                                                            p_.block_size[0], p_.block_size[1], p_.block_size[2], d_flag_);
+                D_CUDA(cudaGetLastError());
+                D_CUDA(cudaMemcpyAsync(&keep, d_flag_, sizeof(int), cudaMemcpyDeviceToHost, s));
+                D_CUDA(cudaStreamSynchronize(s));
+            }
+            if (keep) blocks_[st].push_back(bd);
+        }
+        // every block of a batch reads psi before the step when the slab's effective
+        // size >= k-1 (deferred write-back, MultiViewDeconvolutionSeq 79-162)
+        const int sd = sort_dim_[st];
+        const long long eff = p_.block_size[sd] - kk[sd] + 1;
+        jacobi_[st] = (eff >= vw.kd[sd] - 1 && blocks_[st].size() == all.size()) ? 1 : 0;
+    }
+    // psi init: PsiInitAvgPrecise (average over views with data) and max per view
+    {
+        ImgPtrs ip{};
+        for (int v = 0; v < nv; ++v) ip.img[v] = views_[v].img;
+        const int parts = 1024;
+        double *psum = d_scratch_;
+        long long *pcnt = reinterpret_cast<long long *>(d_scratch_ + 2 * 4096);
+        float *pmax = reinterpret_cast<float *>(pcnt + 4096);
+        k_psi_avg_partials<<<parts, 256, 0, s>>>(ip, nv, n_, psum, pcnt, pmax);
+        D_CUDA(cudaGetLastError());
+        double *avg = d_scratch_ + 4096;
+        float *mx = reinterpret_cast<float *>(d_scratch_ + 4097);
+        k_psi_avg_final<<<1, 1, 0, s>>>(psum, pcnt, pmax, parts, nv, avg, mx);
+        D_CUDA(cudaGetLastError());
+        k_fill_avg<T><<<grid_for(n_), 256, 0, s>>>(psi_, n_, avg);
+        D_CUDA(cudaGetLastError());
+        max_.assign(nv, 0.0f);
+        D_CUDA(cudaMemcpyAsync(max_.data(), mx, sizeof(float) * nv, cudaMemcpyDeviceToHost, s));
+    }
+    D_CUDA(cudaStreamSynchronize(s));
+    prepared_ = true;
+    return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::set_psi(const float *psi, bool on_device)
+{
+    if (!psi) return fail(MVR_ERR_ARG, "psi must not be NULL");
+    D_CUDA(cudaSetDevice(p_.device));
+    cudaStream_t s = engine_.stream();
+    if (sizeof(T) == sizeof(float)) {
+        D_CUDA(cudaMemcpyAsync(psi_, psi, sizeof(float) * (size_t)n_,
+                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+        return MVR_OK;
+    }
+    const float *src = psi;
+    if (!on_device) {
+        float *tmp = reinterpret_cast<float *>(stage_);
+        D_CUDA(cudaMemcpyAsync(tmp, psi, sizeof(float) * (size_t)n_, cudaMemcpyHostToDevice, s));
+        float *hold = nullptr;
+        D_CUDA(cudaMalloc(&hold, sizeof(float) * (size_t)n_));
+        D_CUDA(cudaMemcpyAsync(hold, tmp, sizeof(float) * (size_t)n_, cudaMemcpyDeviceToDevice, s));
+        k_convert<float, T><<<grid_for(n_), 256, 0, s>>>(hold, psi_, n_);
+        D_CUDA(cudaGetLastError());
+        D_CUDA(cudaStreamSynchronize(s));
+        cudaFree(hold);
+        return MVR_OK;
+    }
+    k_convert<float, T><<<grid_for(n_), 256, 0, s>>>(src, psi_, n_);
+    D_CUDA(cudaGetLastError());
+    return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::get_psi(float *psi)
+{
+    if (!psi) return fail(MVR_ERR_ARG, "psi must not be NULL");
+    D_CUDA(cudaSetDevice(p_.device));
+    cudaStream_t s = engine_.stream();
+    if (sizeof(T) == sizeof(float)) {
+        D_CUDA(cudaMemcpyAsync(psi, psi_, sizeof(float) * (size_t)n_, cudaMemcpyDeviceToHost, s));
+    } else {
+        float *tmp = reinterpret_cast<float *>(stage_);
+        k_convert<T, float><<<grid_for(n_), 256, 0, s>>>(psi_, tmp, n_);
+        D_CUDA(cudaGetLastError());
+        D_CUDA(cudaMemcpyAsync(psi, tmp, sizeof(float) * (size_t)n_, cudaMemcpyDeviceToHost, s));
+    }
+    D_CUDA(cudaStreamSynchronize(s));
+    return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::get_kernels(int v, float *k1, float *k2)
+{
+    if (v < 0 || v >= p_.num_views || !prepared_) return fail(MVR_ERR_STATE, "not prepared or view out of range");
+    const View &vw = views_[v];
+    const size_t kn = (size_t)vw.kd[0] * vw.kd[1] * vw.kd[2];
+    cudaStream_t s = engine_.stream();
+    if (k1) D_CUDA(cudaMemcpyAsync(k1, vw.k1, sizeof(float) * kn, cudaMemcpyDeviceToHost, s));
+    if (k2) D_CUDA(cudaMemcpyAsync(k2, vw.k2, sizeof(float) * kn, cudaMemcpyDeviceToHost, s));
+    D_CUDA(cudaStreamSynchronize(s));
+    return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::get_max(float *mx)
+{
+    if (!prepared_ || !mx) return fail(MVR_ERR_STATE, "not prepared");
+    std::memcpy(mx, max_.data(), sizeof(float) * max_.size());
+    return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::get_weights(int v, float *w)
+{
+    if (v < 0 || v >= p_.num_views || !prepared_ || !w) return fail(MVR_ERR_STATE, "not prepared or view out of range");
+    cudaStream_t s = engine_.stream();
+    D_CUDA(cudaMemcpyAsync(w, views_[v].w, sizeof(float) * (size_t)n_, cudaMemcpyDeviceToHost, s));
+    D_CUDA(cudaStreamSynchronize(s));
+    return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::synchronize()
+{
+    D_CUDA(cudaSetDevice(p_.device));
+    D_CUDA(cudaStreamSynchronize(engine_.stream()));
+    return MVR_OK;
+}
+
+// One view-step (Seq) or one iteration (Mul): blocks in slab batches.
+template <typename T>
+int Decon<T>::run_step(int st, double *stats_slot)
+{
+    cudaStream_t s = engine_.stream();
+    const std::vector<BlockDesc> &bl = blocks_[st];
+    const long long D[3] = {p_.dims[0], p_.dims[1], p_.dims[2]};
+    int nb = 0;
+    for (const auto &b : bl) nb = std::max(nb, b.batch + 1);
+    const bool jac = jacobi_[st] != 0;
+    auto place = [&](const BlockDesc &b) {
+        BlockPlace bp;
+        bp.psi_src = psi_;
+        bp.psi_dst = stage_;
+        for (int d = 0; d < 3; ++d) {
+            bp.D[d] = D[d];
+            bp.off[d] = b.off[d];
+            bp.OD[d] = D[d];
+            bp.ooff[d] = b.off[d];
+            bp.wlo[d] = b.eloc[d];
+            bp.whi[d] = b.eloc[d] + b.esize[d];
+        }
+        return bp;
+    };
+    auto paste = [&](const BlockDesc &b) -> int {
+        const long long nvx = (long long)b.esize[0] * b.esize[1] * b.esize[2];
+        D_TRY(eng(engine_.prof_begin(KK_PASTE, 2.0 * sizeof(T) * (double)nvx)));
+        k_paste<T><<<grid_for(nvx), 256, 0, s>>>(stage_, psi_, D[0], D[1], b.eoff[0], b.eoff[1], b.eoff[2], b.esize[0],
+                                                 b.esize[1], b.esize[2]);
+        D_TRY(cuda(cudaGetLastError(), "k_paste"));
+        return eng(engine_.prof_end());
+    };
+    int slot = 0;
+    std::vector<const BlockDesc *> prev;
+    for (int j = 0; j < nb; ++j) {
+        std::vector<const BlockDesc *> cur;
+        for (const auto &b : bl)
+            if (b.batch == j) cur.push_back(&b);
+        for (const BlockDesc *b : cur) {
+            const BlockPlace bp = place(*b);
+            double *sd = stats_slot ? stats_slot + 2 * (slot++) : nullptr;
+            if (!p_.mul) {
+                const View &vw = views_[st];
+                D_TRY(eng(engine_.run_seq(vw.plan, bp, vw.img, vw.w, max_[st], sd)));
+            } else {
+                std::vector<const Plan<T> *> pls;
+                std::vector<const float *> imgs, ws;
+                double miv = 0.0;
+                for (auto &vw : views_) {
+                    pls.push_back(&vw.plan);
+                    imgs.push_back(vw.img);
+                    ws.push_back(vw.w);
+                }
+                for (float m : max_) miv += m;
+                miv /= (double)max_.size();
+                D_TRY(eng(engine_.run_mul(pls, bp, imgs.data(), ws.data(), (float)miv, sd)));
+            }
+        }
+        if (!jac) {
+            for (const BlockDesc *b : prev) D_TRY(paste(*b));
+            prev = cur;
+        }
+    }
+    if (jac) std::swap(psi_, stage_);
+    else
+        for (const BlockDesc *b : prev) D_TRY(paste(*b));
+    return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::run(int iterations, double *stats)
+{
+    if (!prepared_) return fail(MVR_ERR_STATE, "mvr_decon_prepare was not called");
+    if (iterations < 0) return fail(MVR_ERR_ARG, "iterations must be >= 0");
+    D_CUDA(cudaSetDevice(p_.device));
+    const int steps = num_steps();
+    size_t maxb = 1;
+    for (auto &b : blocks_) maxb = std::max(maxb, b.size());
+    const long long need = (long long)steps * (long long)maxb * 2;
+    if (stats && need > stats_cap_) {
+        cudaFree(d_stats_);
+        d_stats_ = nullptr;
+        stats_cap_ = 0;
+        D_CUDA(cudaMalloc(&d_stats_, sizeof(double) * (size_t)need));
+        stats_cap_ = need;
+    }
+    std::vector<double> hs;
+    for (int it = 0; it < iterations; ++it) {
+        for (int st = 0; st < steps; ++st) D_TRY(run_step(st, stats ? d_stats_ + (size_t)st * maxb * 2 : nullptr));
+        if (stats) {
+            hs.resize((size_t)need);
+            D_CUDA(cudaMemcpyAsync(hs.data(), d_stats_, sizeof(double) * (size_t)need, cudaMemcpyDeviceToHost,
+                                   engine_.stream()));
+            D_CUDA(cudaStreamSynchronize(engine_.stream()));
+            for (int st = 0; st < steps; ++st) {
+                double sum = 0.0, mx = -1.0;
+                for (size_t b = 0; b < blocks_[st].size(); ++b) {
+                    sum += hs[((size_t)st * maxb + b) * 2];
+                    mx = std::max(mx, hs[((size_t)st * maxb + b) * 2 + 1]);
+                }
+                stats[((size_t)it * steps + st) * 2] = sum;
+                stats[((size_t)it * steps + st) * 2 + 1] = mx;
+            }
+        }
+    }
+    return MVR_OK;
+}
+
+template class Decon<float>;
+template class Decon<double>;
+
+}  // namespace mvr
+
+// ---- C ABI ---------------------------------------------------------------------------
+struct mvr_decon {
+    std::unique_ptr<mvr::DeconBase> impl;
+};
+
+namespace {
+thread_local std::string g_decon_create_error;
+}
+
+extern "C" int mvr_decon_create(const mvr_decon_params *p, mvr_decon **out)
+{
+    if (!out) return MVR_ERR_ARG;
+    *out = nullptr;
+    if (!p) {
+        g_decon_create_error = "params is NULL";
+        return MVR_ERR_ARG;
+    }
+    std::unique_ptr<mvr_decon> h(new mvr_decon());
+    int rc;
+    if (p->precision == MVR_PRECISION_FP64) {
+        auto *d = new mvr::Decon<double>(*p);
+        h->impl.reset(d);
+        rc = d->init();
+    } else if (p->precision == MVR_PRECISION_FP32) {
+        auto *d = new mvr::Decon<float>(*p);
+        h->impl.reset(d);
+        rc = d->init();
+    } else {
+        g_decon_create_error = "unknown precision";
+        return MVR_ERR_ARG;
+    }
+    if (rc != MVR_OK) {
+        g_decon_create_error = h->impl->error();
+        return rc;
+    }
+    *out = h.release();
+    return MVR_OK;
+}
+
+extern "C" void mvr_decon_destroy(mvr_decon *h) { delete h; }
+
+extern "C" const char *mvr_decon_last_error(const mvr_decon *h)
+{
+    return h ? h->impl->error().c_str() : g_decon_create_error.c_str();
+}
+
+extern "C" int mvr_decon_set_view(mvr_decon *h, int view, const float *img, const float *weight, const float *psf,
+                                  const int psf_size[3])
+{
+    if (!h) return MVR_ERR_ARG;
+    int rc = h->impl->set_images(view, img, weight, false);
+    return rc != MVR_OK ? rc : h->impl->set_psf(view, psf, psf_size);
+}
+
+extern "C" int mvr_decon_set_view_device(mvr_decon *h, int view, const float *img, const float *weight,
+                                         const float *psf, const int psf_size[3])
+{
+    if (!h) return MVR_ERR_ARG;
+    int rc = h->impl->set_images(view, img, weight, true);
+    return rc != MVR_OK ? rc : h->impl->set_psf(view, psf, psf_size);
+}
+
+extern "C" int mvr_decon_update_images(mvr_decon *h, int view, const float *img, const float *weight)
+{
+    return h ? h->impl->set_images(view, img, weight, false) : MVR_ERR_ARG;
+}
+
+extern "C" int mvr_decon_prepare(mvr_decon *h) { return h ? h->impl->prepare() : MVR_ERR_ARG; }
+extern "C" int mvr_decon_set_psi(mvr_decon *h, const float *psi) { return h ? h->impl->set_psi(psi, false) : MVR_ERR_ARG; }
+extern "C" int mvr_decon_set_psi_device(mvr_decon *h, const float *psi)
+{
+    return h ? h->impl->set_psi(psi, true) : MVR_ERR_ARG;
+}
+extern "C" int mvr_decon_get_psi(mvr_decon *h, float *psi) { return h ? h->impl->get_psi(psi) : MVR_ERR_ARG; }
+extern "C" int mvr_decon_run(mvr_decon *h, int iterations, double *stats)
+{
+    return h ? h->impl->run(iterations, stats) : MVR_ERR_ARG;
+}
+extern "C" int mvr_decon_get_kernels(mvr_decon *h, int view, float *k1, float *k2)
+{
+    return h ? h->impl->get_kernels(view, k1, k2) : MVR_ERR_ARG;
+}
+extern "C" int mvr_decon_get_max(mvr_decon *h, float *mx) { return h ? h->impl->get_max(mx) : MVR_ERR_ARG; }
+extern "C" int mvr_decon_get_weights(mvr_decon *h, int view, float *w)
+{
+    return h ? h->impl->get_weights(view, w) : MVR_ERR_ARG;
+}
+extern "C" const void *mvr_decon_psi_device(const mvr_decon *h) { return h ? h->impl->psi_device() : nullptr; }
+extern "C" int mvr_decon_synchronize(mvr_decon *h) { return h ? h->impl->synchronize() : MVR_ERR_ARG; }
+
+extern "C" void *mvr_decon_stream(mvr_decon *h) { return h ? h->impl->stream() : nullptr; }
+extern "C" long long mvr_decon_launch_count(const mvr_decon *h) { return h ? h->impl->launches() : -1; }
+extern "C" int mvr_decon_set_profiling(mvr_decon *h, int on)
+{
+    if (!h) return MVR_ERR_ARG;
+    h->impl->set_profiling(on != 0);
+    return MVR_OK;
+}
+extern "C" int mvr_decon_get_profile(mvr_decon *h, double *ms, long long *launches, double *bytes)
+{
+    if (!h) return MVR_ERR_ARG;
+    mvr::KernelProfile p{};
+    const int rc = h->impl->profile(p);
+    if (rc != MVR_OK) return rc;
+    for (int k = 0; k < mvr::KK_COUNT; ++k) {
+        if (ms) ms[k] = p.ms[k];
+        if (launches) launches[k] = p.launches[k];
+        if (bytes) bytes[k] = p.bytes[k];
+    }
+    return MVR_OK;
+}
+extern "C" const char *mvr_kernel_name(int kind) { return mvr::kernel_kind_name(kind); }

@@ -17,6 +17,13 @@ constexpr size_t kColSmemTarget = 72 * 1024;
 constexpr size_t kSmemMax = 227 * 1024;
 }  // namespace
 
+const char *kernel_kind_name(int k)
+{
+    static const char *names[KK_COUNT] = {"rows_fwd_extract", "cols_y_fwd", "cols_y_inv", "cols_z_fwd_mul_inv",
+                                          "rows_c2r_ratio_r2c", "rows_c2r_update", "reduce_stats", "paste"};
+    return (k >= 0 && k < KK_COUNT) ? names[k] : "?";
+}
+
 bool fft_friendly(long long n)
 {
     if (n < 1) return false;
@@ -124,7 +131,57 @@ Engine<T>::~Engine()
     cudaFree(prod_);
     cudaFree(partials_);
     cudaFree(kbuf_);
+    for (auto &p : pending_) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    for (auto e : event_pool_) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
+}
+
+template <typename T>
+int Engine<T>::prof_begin(int kind, double bytes)
+{
+    ++launches_;
+    if (!prof_on_) return OK;
+    Pending p{kind, bytes, nullptr, nullptr};
+    for (cudaEvent_t *e : {&p.a, &p.b}) {
+        if (!event_pool_.empty()) {
+            *e = event_pool_.back();
+            event_pool_.pop_back();
+        } else {
+            MVR_CUDA(cudaEventCreate(e));
+        }
+    }
+    MVR_CUDA(cudaEventRecord(p.a, stream_));
+    pending_.push_back(p);
+    return OK;
+}
+
+template <typename T>
+int Engine<T>::prof_end()
+{
+    if (!prof_on_ || pending_.empty()) return OK;
+    MVR_CUDA(cudaEventRecord(pending_.back().b, stream_));
+    return OK;
+}
+
+template <typename T>
+int Engine<T>::profile_collect(KernelProfile &out)
+{
+    MVR_CUDA(cudaStreamSynchronize(stream_));
+    for (auto &p : pending_) {
+        float ms = 0.0f;
+        MVR_CUDA(cudaEventElapsedTime(&ms, p.a, p.b));
+        acc_.ms[p.kind] += ms;
+        acc_.launches[p.kind] += 1;
+        acc_.bytes[p.kind] += p.bytes;
+        event_pool_.push_back(p.a);
+        event_pool_.push_back(p.b);
+    }
+    pending_.clear();
+    out = acc_;
+    return OK;
 }
 
 template <typename T>
@@ -300,11 +357,14 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
     }
     const V *tw = axis == 1 ? pl.twy : pl.twz;
     dim3 grid((unsigned)((Hx + NP - 1) / NP), (unsigned)nother);
+    const double cb = (double)sizeof(V) * (double)pl.Pc;
+    const int kind = mode == 2 ? KK_COLS_ZMUL : (mode == 1 ? KK_COLS_INV : KK_COLS_FWD);
+    MVR_TRY(prof_begin(kind, mode == 2 ? 3.0 * cb : 2.0 * cb));
     if (mode == 0) k_cols<T, 0><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
     else if (mode == 1) k_cols<T, 1><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
     else k_cols<T, 2><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
     MVR_LAUNCHED("k_cols");
-    return OK;
+    return prof_end();
 }
 
 template <typename T>
@@ -330,10 +390,12 @@ int Engine<T>::launch_fwd_mirror(const Plan<T> &pl, const BlockMap &bm, const T 
 {
     const long long nrows = (long long)pl.P[1] * pl.P[2];
     const unsigned grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
+    const double nb = (double)pl.b[0] * pl.b[1] * pl.b[2];
+    MVR_TRY(prof_begin(KK_ROWS_FWD, sizeof(T) * nb + sizeof(V) * (double)pl.Pc));
     k_rows_fwd<T, SrcMirror<T>><<<grid, kThreads, pl.smem_row, stream_>>>(SrcMirror<T>{src}, S, bm, pl.dx, pl.twx,
                                                                            pl.RP);
     MVR_LAUNCHED("k_rows_fwd");
-    return OK;
+    return prof_end();
 }
 
 template <typename T>
@@ -348,8 +410,12 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace &bp, const float *img
     MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
     MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h));
     MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr));
+    const double nb = (double)pl.b[0] * pl.b[1] * pl.b[2];
+    const double sb = (double)sizeof(V) * (double)pl.Pc;
+    MVR_TRY(prof_begin(KK_ROWS_RATIO, 2.0 * sb + 4.0 * nb));
     k_rows_ratio<T><<<grid, kThreads, pl.smem_row, stream_>>>(S0_, img, bm, pl.dx, pl.twx, pl.RP);
     MVR_LAUNCHED("k_rows_ratio");
+    MVR_TRY(prof_end());
     MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
     MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k2h));
     MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr));
@@ -362,11 +428,16 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace &bp, const float *img
     ua.minI = min_value_;
     ua.maxI = maxI;
     ua.partials = partials_;
+    const double neff = (double)(bp.whi[0] - bp.wlo[0]) * (bp.whi[1] - bp.wlo[1]) * (bp.whi[2] - bp.wlo[2]);
+    MVR_TRY(prof_begin(KK_ROWS_UPDATE, sb + (sizeof(T) + 4.0) * nb + sizeof(T) * neff));
     k_rows_update<T, EPI_SEQ><<<grid, kThreads, pl.smem_row, stream_>>>(S0_, ua, bm, pl.dx, pl.twx, pl.RP);
     MVR_LAUNCHED("k_rows_update");
+    MVR_TRY(prof_end());
     if (stats_dev) {
+        MVR_TRY(prof_begin(KK_REDUCE, 16.0 * grid));
         k_reduce_stats<double><<<1, 1024, 0, stream_>>>(partials_, (int)grid, stats_dev);
         MVR_LAUNCHED("k_reduce_stats");
+        MVR_TRY(prof_end());
     }
     return OK;
 }
@@ -403,11 +474,18 @@ int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace
         prev = &pl;
         MVR_TRY(launch_cols(pl, 2, 2, S0_, S1_, pl.k1h));
         MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr));
+        const double nb = (double)pl.b[0] * pl.b[1] * pl.b[2];
+        const double sb = (double)sizeof(V) * (double)pl.Pc;
+        MVR_TRY(prof_begin(KK_ROWS_RATIO, 2.0 * sb + 4.0 * nb));
         k_rows_ratio<T><<<grid, kThreads, pl.smem_row, stream_>>>(S1_, imgs[v], bm, pl.dx, pl.twx, pl.RP);
         MVR_LAUNCHED("k_rows_ratio");
+        MVR_TRY(prof_end());
         MVR_TRY(launch_cols(pl, 1, 0, S1_, S1_, nullptr));
         MVR_TRY(launch_cols(pl, 2, 2, S1_, S1_, pl.k2h));
         MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr));
+        const double neff = (double)(bp.whi[0] - bp.wlo[0]) * (bp.whi[1] - bp.wlo[1]) * (bp.whi[2] - bp.wlo[2]);
+        MVR_TRY(prof_begin(KK_ROWS_UPDATE, v == nv - 1 ? sb + (sizeof(T) + 12.0 + 4.0 * nv) * nb + sizeof(T) * neff
+                                                        : sb + (v == 0 ? 8.0 : 16.0) * nb));
         if (v == nv - 1) {
             ua.nviews = nv;
             k_rows_update<T, EPI_MUL_FINAL><<<grid, kThreads, pl.smem_row, stream_>>>(S1_, ua, bm, pl.dx, pl.twx,
@@ -418,10 +496,13 @@ int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace
             k_rows_update<T, EPI_MUL_ACC><<<grid, kThreads, pl.smem_row, stream_>>>(S1_, ua, bm, pl.dx, pl.twx, pl.RP);
         }
         MVR_LAUNCHED("k_rows_update(mul)");
+        MVR_TRY(prof_end());
     }
     if (stats_dev) {
+        MVR_TRY(prof_begin(KK_REDUCE, 16.0 * grid));
         k_reduce_stats<double><<<1, 1024, 0, stream_>>>(partials_, (int)grid, stats_dev);
         MVR_LAUNCHED("k_reduce_stats");
+        MVR_TRY(prof_end());
     }
     return OK;
 }

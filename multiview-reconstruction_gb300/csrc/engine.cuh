@@ -14,6 +14,26 @@ enum Status { OK = 0, ERR_ARG = 1, ERR_CUDA = 2, ERR_OOM = 3, ERR_UNSUPPORTED = 
 enum Boundary { BOUNDARY_REFERENCE = 0, BOUNDARY_CIRCULAR = 1 };
 enum SrcKind { SRC_MIRROR = 0, SRC_ZERO = 1 };
 
+// Kernel families timed by the optional profiler (CUDA events on the engine stream).
+enum KernelKind {
+    KK_ROWS_FWD = 0,   // extract + R2C along x
+    KK_COLS_FWD,       // y forward
+    KK_COLS_INV,       // y inverse
+    KK_COLS_ZMUL,      // z forward, spectral multiply, z inverse
+    KK_ROWS_RATIO,     // C2R, quotient, R2C
+    KK_ROWS_UPDATE,    // C2R, update, stats partials
+    KK_REDUCE,         // stats reduction
+    KK_PASTE,          // effective-region copy
+    KK_COUNT
+};
+const char *kernel_kind_name(int k);
+
+struct KernelProfile {
+    double ms[KK_COUNT];
+    long long launches[KK_COUNT];
+    double bytes[KK_COUNT];  // algorithmic bytes moved by those launches
+};
+
 bool fft_friendly(long long n);
 long long next_friendly_even(long long n);
 FftDesc make_desc(int n);
@@ -74,6 +94,13 @@ public:
     int convolve(const Plan<T> &pl, const T *blk, int src_kind, float *out);
 
     cudaStream_t stream() const { return stream_; }
+    // launch accounting: every kernel launch of the engine (and of its owner through
+    // count_launch) is counted; with profiling on, each is bracketed by CUDA events
+    long long launches() const { return launches_; }
+    void set_profiling(bool on) { prof_on_ = on; }
+    int prof_begin(int kind, double bytes);
+    int prof_end();
+    int profile_collect(KernelProfile &out);  // synchronises, then adds the pending times
     int device() const { return device_; }
     const std::string &error() const { return err_; }
     int fail(int code, const std::string &msg);
@@ -99,6 +126,16 @@ private:
     float *kbuf_ = nullptr;
     long long kcap_ = 0;
     std::string err_;
+    long long launches_ = 0;
+    bool prof_on_ = false;
+    struct Pending {
+        int kind;
+        double bytes;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pending> pending_;
+    std::vector<cudaEvent_t> event_pool_;
+    KernelProfile acc_{};
 };
 
 extern template class Engine<float>;

@@ -28,6 +28,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libmvrgb300.so")
 
 OK, ERR_ARG, ERR_CUDA, ERR_OOM, ERR_UNSUPPORTED, ERR_STATE = 0, 1, 2, 3, 4, 5
+PRECISION_FP32, PRECISION_FP64 = 0, 1
+WEIGHTS_AS_GIVEN, WEIGHTS_HARD, WEIGHTS_SMOOTH = 0, 1, 2
+KERNEL_KINDS = 8
 BOUNDARY_REFERENCE, BOUNDARY_CIRCULAR = 0, 1
 PSF_OPTIMIZATION_II, PSF_OPTIMIZATION_I, PSF_EFFICIENT_BAYESIAN, PSF_INDEPENDENT = 0, 1, 2, 3
 
@@ -35,6 +38,12 @@ PSF_OPTIMIZATION_II, PSF_OPTIMIZATION_I, PSF_EFFICIENT_BAYESIAN, PSF_INDEPENDENT
 EXPORTS = [
     "mvr_block_create", "mvr_block_destroy", "mvr_block_last_error", "mvr_block_set_kernels",
     "mvr_block_run_seq", "mvr_block_run_mul", "mvr_block_run_seq_device", "mvr_block_synchronize",
+    "mvr_decon_create", "mvr_decon_destroy", "mvr_decon_last_error", "mvr_decon_set_view",
+    "mvr_decon_set_view_device", "mvr_decon_update_images", "mvr_decon_prepare", "mvr_decon_set_psi",
+    "mvr_decon_set_psi_device", "mvr_decon_get_psi", "mvr_decon_run", "mvr_decon_get_kernels",
+    "mvr_decon_get_max", "mvr_decon_get_weights", "mvr_decon_psi_device", "mvr_decon_synchronize",
+    "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
+    "mvr_kernel_name",
     "convolution3DfftCUDA", "convolution3DfftCUDAInPlace", "getNumDevicesCUDA", "getNameDeviceCUDA",
     "getMemDeviceCUDA", "getFreeMemDeviceCUDA", "getCUDAcomputeCapabilityMajorVersion",
     "getCUDAcomputeCapabilityMinorVersion", "mvr_free",
@@ -50,6 +59,14 @@ class MvrError(RuntimeError):
 class _BlockParams(C.Structure):
     _fields_ = [("block_size", C.c_int * 3), ("min_value", C.c_float), ("lambda_", C.c_float),
                 ("num_views", C.c_int), ("boundary", C.c_int), ("device", C.c_int)]
+
+
+class _DeconParams(C.Structure):
+    _fields_ = [("dims", C.c_int * 3), ("num_views", C.c_int), ("block_size", C.c_int * 3), ("mul", C.c_int),
+                ("psf_type", C.c_int), ("psf_norm_threads", C.c_int), ("lambda_", C.c_float),
+                ("min_value", C.c_float), ("boundary", C.c_int), ("precision", C.c_int),
+                ("filter_blocks", C.c_int), ("weight_norm", C.c_int), ("osem_speedup", C.c_float),
+                ("max_diff_range", C.c_float), ("scaling_range", C.c_float), ("device", C.c_int)]
 
 
 _lib = None
@@ -89,6 +106,33 @@ def load() -> C.CDLL:
     L.getFreeMemDeviceCUDA.restype = C.c_longlong
     L.getCUDAcomputeCapabilityMajorVersion.argtypes = [C.c_int]
     L.getCUDAcomputeCapabilityMinorVersion.argtypes = [C.c_int]
+    L.mvr_decon_create.argtypes = [C.POINTER(_DeconParams), C.POINTER(P)]
+    L.mvr_decon_destroy.argtypes = [P]
+    L.mvr_decon_destroy.restype = None
+    L.mvr_decon_last_error.argtypes = [P]
+    L.mvr_decon_last_error.restype = C.c_char_p
+    L.mvr_decon_set_view.argtypes = [P, C.c_int, P, P, P, P]
+    L.mvr_decon_set_view_device.argtypes = [P, C.c_int, P, P, P, P]
+    L.mvr_decon_update_images.argtypes = [P, C.c_int, P, P]
+    L.mvr_decon_prepare.argtypes = [P]
+    L.mvr_decon_set_psi.argtypes = [P, P]
+    L.mvr_decon_set_psi_device.argtypes = [P, P]
+    L.mvr_decon_get_psi.argtypes = [P, P]
+    L.mvr_decon_run.argtypes = [P, C.c_int, P]
+    L.mvr_decon_get_kernels.argtypes = [P, C.c_int, P, P]
+    L.mvr_decon_get_max.argtypes = [P, P]
+    L.mvr_decon_get_weights.argtypes = [P, C.c_int, P]
+    L.mvr_decon_psi_device.argtypes = [P]
+    L.mvr_decon_psi_device.restype = C.c_void_p
+    L.mvr_decon_synchronize.argtypes = [P]
+    L.mvr_decon_stream.argtypes = [P]
+    L.mvr_decon_stream.restype = C.c_void_p
+    L.mvr_decon_launch_count.argtypes = [P]
+    L.mvr_decon_launch_count.restype = C.c_longlong
+    L.mvr_decon_set_profiling.argtypes = [P, C.c_int]
+    L.mvr_decon_get_profile.argtypes = [P, P, P, P]
+    L.mvr_kernel_name.argtypes = [C.c_int]
+    L.mvr_kernel_name.restype = C.c_char_p
     _lib = L
     return L
 
@@ -194,6 +238,131 @@ class BlockWorker:
 
     def synchronize(self):
         self._check(self._lib.mvr_block_synchronize(self._h))
+
+
+class Deconvolution:
+    """Device-resident MultiViewDeconvolutionSeq / MultiViewDeconvolutionMul
+    (MultiViewDeconvolution.java:90-200) with DeconViews/DeconViewPSF.init, the block grid,
+    weight normalisation and PsiInitAvgPrecise.  Volumes are float32 [z][y][x]; sizes (x, y, z)."""
+
+    def __init__(self, dims, num_views, block_size, mul=False, psf_type=PSF_OPTIMIZATION_I,
+                 psf_norm_threads=0, lam=0.006, min_value=1e-4, boundary=BOUNDARY_REFERENCE,
+                 precision=PRECISION_FP32, filter_blocks=True, weight_norm=WEIGHTS_AS_GIVEN, osem_speedup=1.0,
+                 max_diff_range=0.1, scaling_range=0.05, device=0):
+        self._lib = load()
+        prm = _DeconParams((C.c_int * 3)(*dims), num_views, (C.c_int * 3)(*block_size), int(mul), psf_type,
+                           psf_norm_threads, lam, min_value, boundary, precision, int(filter_blocks), weight_norm,
+                           osem_speedup, max_diff_range, scaling_range, device)
+        h = C.c_void_p()
+        rc = self._lib.mvr_decon_create(C.byref(prm), C.byref(h))
+        if rc != OK:
+            raise MvrError(rc, self._lib.mvr_decon_last_error(None).decode())
+        self._h = h
+        self.dims = tuple(dims)
+        self.num_views = num_views
+        self.mul = bool(mul)
+        self._keep = {}
+
+    @property
+    def shape(self):
+        return (self.dims[2], self.dims[1], self.dims[0])
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mvr_decon_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != OK:
+            raise MvrError(rc, self._lib.mvr_decon_last_error(self._h).decode())
+
+    def set_view(self, view, img, weight, psf):
+        img, w, k = _f32(img), _f32(weight), _f32(psf)
+        if img.shape != self.shape or w.shape != self.shape:
+            raise ValueError("image/weight must have the volume shape")
+        self._check(self._lib.mvr_decon_set_view(self._h, view, _p(img), _p(w), _p(k), _size_xyz(k)))
+
+    def set_view_device(self, view, img_ptr: int, weight_ptr: int, psf):
+        k = _f32(psf)
+        self._check(self._lib.mvr_decon_set_view_device(self._h, view, C.c_void_p(img_ptr), C.c_void_p(weight_ptr),
+                                                        _p(k), _size_xyz(k)))
+
+    def update_images(self, view, img, weight):
+        img, w = _f32(img), _f32(weight)
+        self._check(self._lib.mvr_decon_update_images(self._h, view, _p(img), _p(w)))
+
+    def prepare(self):
+        self._check(self._lib.mvr_decon_prepare(self._h))
+
+    def set_psi(self, psi):
+        psi = _f32(psi)
+        self._check(self._lib.mvr_decon_set_psi(self._h, _p(psi)))
+
+    def set_psi_device(self, ptr: int):
+        self._check(self._lib.mvr_decon_set_psi_device(self._h, C.c_void_p(ptr)))
+
+    def get_psi(self, out=None):
+        if out is None:
+            out = np.empty(self.shape, dtype=np.float32)
+        self._check(self._lib.mvr_decon_get_psi(self._h, _p(out)))
+        return out
+
+    def run_iterations(self, n: int, stats: bool = False):
+        """runIterations; returns per (iteration, view-step) [sumChange, maxChange] if asked."""
+        steps = 1 if self.mul else self.num_views
+        st = np.zeros((n * steps, 2), dtype=np.float64) if stats else None
+        self._check(self._lib.mvr_decon_run(self._h, n, _p(st) if stats else None))
+        return st
+
+    def kernels(self, view, shape):
+        k1 = np.empty(shape, dtype=np.float32)
+        k2 = np.empty(shape, dtype=np.float32)
+        self._check(self._lib.mvr_decon_get_kernels(self._h, view, _p(k1), _p(k2)))
+        return k1, k2
+
+    def max_intensities(self):
+        m = np.zeros(self.num_views, dtype=np.float32)
+        self._check(self._lib.mvr_decon_get_max(self._h, _p(m)))
+        return m
+
+    def weights(self, view):
+        w = np.empty(self.shape, dtype=np.float32)
+        self._check(self._lib.mvr_decon_get_weights(self._h, view, _p(w)))
+        return w
+
+    def psi_device_ptr(self) -> int:
+        return int(self._lib.mvr_decon_psi_device(self._h) or 0)
+
+    def synchronize(self):
+        self._check(self._lib.mvr_decon_synchronize(self._h))
+
+    def stream_ptr(self) -> int:
+        """cudaStream_t of the handle (for torch.cuda.ExternalStream / events)."""
+        return int(self._lib.mvr_decon_stream(self._h) or 0)
+
+    def launch_count(self) -> int:
+        return int(self._lib.mvr_decon_launch_count(self._h))
+
+    def set_profiling(self, on: bool):
+        self._check(self._lib.mvr_decon_set_profiling(self._h, int(on)))
+
+    def profile(self):
+        """{kernel family: (ms, launches, algorithmic bytes)} accumulated while profiling."""
+        n = KERNEL_KINDS
+        ms = np.zeros(n, np.float64)
+        la = np.zeros(n, np.int64)
+        by = np.zeros(n, np.float64)
+        self._check(self._lib.mvr_decon_get_profile(self._h, _p(ms), _p(la), _p(by)))
+        return {self._lib.mvr_kernel_name(k).decode(): (float(ms[k]), int(la[k]), float(by[k])) for k in range(n)}
 
 
 def convolution3d_fft_cuda_in_place(im, kernel, device: int = 0) -> np.ndarray:
