@@ -190,6 +190,30 @@ MVR_API int mvr_decon_set_profiling(mvr_decon *h, int on);
 MVR_API int mvr_decon_get_profile(mvr_decon *h, double *ms, long long *launches, double *bytes);
 MVR_API const char *mvr_kernel_name(int kind);
 
+/* ---- convolution without device allocation ------------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot call
+ * cudaMalloc -- code running inside another framework's CUDA context whose caching
+ * allocator owns the device memory, or latency-critical paths that cannot take the
+ * implicit device synchronisation of cudaMalloc / cudaFree.
+ *
+ * The same convolution as convolution3DfftCUDA (linear, zero extension, output over
+ * the image; sizes here are {x, y, z}, not reversed), but every intermediate lives in
+ * one fixed device array compiled into the library (16 MiB + 24 KiB, held by every
+ * GPU that loads the library until the process exits).  img, kernel and out are
+ * device pointers supplied by the caller; the work is queued on `stream` (a
+ * cudaStream_t, NULL = legacy default stream) and the call does not wait for it.
+ * Limits: the FFT domain (img + kernel - 1 per axis, rounded up to an even size with
+ * prime factors <= 13) must be <= 1024 per axis and (x/2 + 1) * y * z <= 1048576;
+ * larger sizes return MVR_ERR_UNSUPPORTED with the reason in err.
+ * The first call on a device resolves the array's device address (and loads the
+ * module); make that first call before any stream capture.  All calls share the one
+ * array and it keeps the last call's contents (every value is written before it is
+ * read, nothing needs clearing); calls whose work overlaps on the GPU -- from
+ * different streams or threads -- race on it.  It calls no cudaMalloc, cudaFree or
+ * other allocating routine.  err (may be NULL) receives a message on failure. */
+MVR_API int mvr_convolve_static(const float *img, const int img_size[3], const float *kernel,
+                                const int kernel_size[3], float *out, void *stream, char *err, int err_len);
+
 /* ---- the reference's JNA library (CUDAFourierConvolution / CUDAStandardFunctions) ----
  * Exported under the reference's own symbol names so that the unchanged
  * ComputeBlockSeqThreadCUDA can load this library.  Dimensions arrive reversed

@@ -43,7 +43,7 @@ EXPORTS = [
     "mvr_decon_set_psi_device", "mvr_decon_get_psi", "mvr_decon_run", "mvr_decon_get_kernels",
     "mvr_decon_get_max", "mvr_decon_get_weights", "mvr_decon_psi_device", "mvr_decon_synchronize",
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
-    "mvr_kernel_name",
+    "mvr_kernel_name", "mvr_convolve_static",
     "convolution3DfftCUDA", "convolution3DfftCUDAInPlace", "getNumDevicesCUDA", "getNameDeviceCUDA",
     "getMemDeviceCUDA", "getFreeMemDeviceCUDA", "getCUDAcomputeCapabilityMajorVersion",
     "getCUDAcomputeCapabilityMinorVersion", "mvr_free",
@@ -133,6 +133,7 @@ def load() -> C.CDLL:
     L.mvr_decon_get_profile.argtypes = [P, P, P, P]
     L.mvr_kernel_name.argtypes = [C.c_int]
     L.mvr_kernel_name.restype = C.c_char_p
+    L.mvr_convolve_static.argtypes = [P, P, P, P, P, P, C.c_char_p, C.c_int]
     _lib = L
     return L
 
@@ -375,6 +376,18 @@ def convolution3d_fft_cuda_in_place(im, kernel, device: int = 0) -> np.ndarray:
     kdim = (C.c_int * 3)(*k.shape)
     L.convolution3DfftCUDAInPlace(_p(a), imdim, _p(k), kdim, device)
     return a
+
+
+def convolve_static(img_ptr: int, img_size, kernel_ptr: int, kernel_size, out_ptr: int, stream: int = 0):
+    """mvr_convolve_static on device buffers (raw addresses, sizes (x, y, z)); queued on
+    `stream` without waiting.  Raises MvrError with the library's message on failure."""
+    L = load()
+    err = C.create_string_buffer(256)
+    rc = L.mvr_convolve_static(C.c_void_p(img_ptr), (C.c_int * 3)(*img_size), C.c_void_p(kernel_ptr),
+                               (C.c_int * 3)(*kernel_size), C.c_void_p(out_ptr), C.c_void_p(stream) if stream else None,
+                               err, len(err))
+    if rc != OK:
+        raise MvrError(rc, err.value.decode())
 
 
 def device_info(device: int = 0) -> dict:
