@@ -96,34 +96,32 @@ struct WeightPtrs {
     float *out[kMaxViews];
 };
 
-// NormalizingRandomAccess.get 76-109 (hardWeights 211-214, smoothWeights 183-200)
+// NormalizingRandomAccess.get 76-109 (hardWeights 211-214, smoothWeights 183-200).
+// The raw weights are read twice (sum, then per view) instead of being held in a
+// per-thread array, which would live in local memory.
 __global__ void k_normalize_weights(WeightPtrs wp, int nv, long long n, double osem, int smooth, float maxDiffRange,
                                     float scalingRange)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         double sumW = 0.0;
-        float my[kMaxViews];
+        for (int v = 0; v < nv; ++v) sumW += fmin(1.0, (double)wp.raw[v][i]);
         for (int v = 0; v < nv; ++v) {
-            const double val = fmin(1.0, (double)wp.raw[v][i]);
-            my[v] = (float)val;
-            sumW += val;
-        }
-        for (int v = 0; v < nv; ++v) {
+            const float my = (float)fmin(1.0, (double)wp.raw[v][i]);
             double r;
             if (smooth) {
                 float s;
                 if (sumW <= 0) s = 0.0f;
                 else {
-                    const float ideal = (float)((double)my[v] / sumW);
-                    const float diff = __fsub_rn(my[v], ideal);
+                    const float ideal = (float)((double)my / sumW);
+                    const float diff = __fsub_rn(my, ideal);
                     float y = __fmul_rn(__fsub_rn(maxDiffRange, fabsf(diff)), __fdiv_rn(1.0f, maxDiffRange));
                     y = y > 0.0f ? y : 0.0f;
-                    const float scale = __fmul_rn(__fmul_rn(y, my[v]), scalingRange);
-                    s = __fsub_rn(fminf(my[v], ideal), scale);
+                    const float scale = __fmul_rn(__fmul_rn(y, my), scalingRange);
+                    s = __fsub_rn(fminf(my, ideal), scale);
                 }
                 r = s;
-            } else if (sumW > 1) r = (float)((double)my[v] / sumW);
-            else r = my[v];
+            } else if (sumW > 1) r = (float)((double)my / sumW);
+            else r = my;
             const double m = r * osem;
             wp.out[v][i] = (float)(m < 1.0 ? m : 1.0);
         }
@@ -399,6 +397,8 @@ private:
     int conv_zero(const float *in, const int id[3], const float *k, const int kd[3], float *out);
     int psf_init();
     int run_step(int s, double *stats_slot);
+    int normalize_weights();
+    bool weights_dirty_ = false;
 
     mvr_decon_params p_;
     Engine<T> engine_;
@@ -496,16 +496,7 @@ int Decon<T>::set_images(int v, const float *img, const float *w, bool on_device
         if (vw.w != vw.w_raw && vw.w) cudaFree(vw.w);
         vw.w = vw.w_raw;
     } else if (prepared_) {
-        // weights depend on all views: renormalise with the new raw weights
-        WeightPtrs wp{};
-        for (int u = 0; u < p_.num_views; ++u) {
-            wp.raw[u] = views_[u].w_raw;
-            wp.out[u] = views_[u].w;
-        }
-        k_normalize_weights<<<grid_for(n_), 256, 0, s>>>(wp, p_.num_views, n_, (double)p_.osem_speedup,
-                                                        p_.weight_norm == MVR_WEIGHTS_SMOOTH, p_.max_diff_range,
-                                                        p_.scaling_range);
-        D_CUDA(cudaGetLastError());
+        weights_dirty_ = true;  // weights depend on all views: renormalised before the next use
     }
     return MVR_OK;
 }
@@ -673,19 +664,13 @@ int Decon<T>::prepare()
     }
     // weights
     if (p_.weight_norm != MVR_WEIGHTS_AS_GIVEN) {
-        WeightPtrs wp{};
         for (int v = 0; v < nv; ++v) {
             if (views_[v].w == nullptr || views_[v].w == views_[v].w_raw) {
                 views_[v].w = nullptr;
                 D_CUDA(cudaMalloc(&views_[v].w, sizeof(float) * (size_t)n_));
             }
-            wp.raw[v] = views_[v].w_raw;
-            wp.out[v] = views_[v].w;
         }
-        k_normalize_weights<<<grid_for(n_), 256, 0, s>>>(wp, nv, n_, (double)p_.osem_speedup,
-                                                        p_.weight_norm == MVR_WEIGHTS_SMOOTH, p_.max_diff_range,
-                                                        p_.scaling_range);
-        D_CUDA(cudaGetLastError());
+        D_TRY(normalize_weights());
     } else {
         for (auto &vw : views_) vw.w = vw.w_raw;
     }
@@ -746,6 +731,22 @@ int Decon<T>::prepare()
     }
     D_CUDA(cudaStreamSynchronize(s));
     prepared_ = true;
+    return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::normalize_weights()
+{
+    WeightPtrs wp{};
+    for (int v = 0; v < p_.num_views; ++v) {
+        wp.raw[v] = views_[v].w_raw;
+        wp.out[v] = views_[v].w;
+    }
+    k_normalize_weights<<<grid_for(n_), 256, 0, engine_.stream()>>>(wp, p_.num_views, n_, (double)p_.osem_speedup,
+                                                                   p_.weight_norm == MVR_WEIGHTS_SMOOTH,
+                                                                   p_.max_diff_range, p_.scaling_range);
+    D_CUDA(cudaGetLastError());
+    weights_dirty_ = false;
     return MVR_OK;
 }
 
@@ -821,6 +822,7 @@ template <typename T>
 int Decon<T>::get_weights(int v, float *w)
 {
     if (v < 0 || v >= p_.num_views || !prepared_ || !w) return fail(MVR_ERR_STATE, "not prepared or view out of range");
+    if (weights_dirty_) D_TRY(normalize_weights());
     cudaStream_t s = engine_.stream();
     D_CUDA(cudaMemcpyAsync(w, views_[v].w, sizeof(float) * (size_t)n_, cudaMemcpyDeviceToHost, s));
     D_CUDA(cudaStreamSynchronize(s));
@@ -910,6 +912,7 @@ int Decon<T>::run(int iterations, double *stats)
     if (!prepared_) return fail(MVR_ERR_STATE, "mvr_decon_prepare was not called");
     if (iterations < 0) return fail(MVR_ERR_ARG, "iterations must be >= 0");
     D_CUDA(cudaSetDevice(p_.device));
+    if (weights_dirty_) D_TRY(normalize_weights());
     const int steps = num_steps();
     size_t maxb = 1;
     for (auto &b : blocks_) maxb = std::max(maxb, b.size());

@@ -46,11 +46,22 @@ FftDesc make_desc(int n)
     d.n = n;
     d.ns = 0;
     int m = n;
+    // powers of two first: Ns stays a power of two up to the first odd radix
     for (int r : kRadices)
         while (m % r == 0 && d.ns < kMaxStages) {
             d.radix[d.ns++] = r;
             m /= r;
         }
+    int Ns = 1;
+    for (int s = 0; s < d.ns; ++s) {
+        const int R = d.radix[s];
+        d.Ns[s] = Ns;
+        d.twstep[s] = n / (Ns * R);
+        d.ns_magic[s] = (unsigned)((0x100000000ULL + Ns - 1) / Ns);
+        const unsigned nb = (unsigned)(n / R);
+        d.nb_magic[s] = (unsigned)((0x100000000ULL + nb - 1) / nb);
+        Ns *= R;
+    }
     return d;
 }
 
@@ -313,6 +324,7 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
         bm.b[d] = pl.P[d];
         bm.D[d] = pl.P[d];
     }
+    bm.fast_x = block_fast_x(bm);
     const double scale = 1.0 / ((double)pl.P[0] * pl.P[1] * pl.P[2]);
     for (int which = 0; which < (k2 ? 2 : 1); ++which) {
         const float *kh = which == 0 ? k1 : k2;
@@ -382,6 +394,7 @@ BlockMap Engine<T>::block_map(const Plan<T> &pl, const BlockPlace &bp) const
         bm.ooff[d] = bp.ooff[d];
         bm.OD[d] = bp.OD[d];
     }
+    bm.fast_x = block_fast_x(bm);
     return bm;
 }
 
@@ -519,6 +532,7 @@ int Engine<T>::convolve(const Plan<T> &pl, const T *blk, int src_kind, float *ou
         bm.OD[d] = pl.b[d];
         bm.whi[d] = pl.b[d];
     }
+    bm.fast_x = block_fast_x(bm);
     const long long nrows = (long long)pl.P[1] * pl.P[2];
     const unsigned grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
     if (src_kind == SRC_ZERO)

@@ -18,11 +18,18 @@ namespace mvr {
 
 constexpr int kMaxStages = 24;
 
-// Stage list of one transform length, passed by value in kernel parameters.
+// Stage list of one transform length, passed by value in kernel parameters.  For
+// stage s: radix[s], Ns[s] = product of the previous radices, twstep[s] = n / (Ns R),
+// and exact reciprocals for division by Ns[s] and by n / radix[s] of any index below
+// 2^16 (q = umulhi(j, magic) with magic = ceil(2^32 / divisor)).
 struct FftDesc {
     int n;
     int ns;
     int radix[kMaxStages];
+    int Ns[kMaxStages];
+    int twstep[kMaxStages];
+    unsigned ns_magic[kMaxStages];
+    unsigned nb_magic[kMaxStages];
 };
 
 template <typename T> struct Cx;
@@ -147,19 +154,19 @@ __device__ __forceinline__ void dft(V *v, const V *tw, int n, int twmul)
     else dftg<R, INV>(v, tw, n, twmul);
 }
 
-// One butterfly of one stage.
+// One butterfly of one stage: group q = j / Ns, position k = j mod Ns.
 template <int R, bool INV, typename V>
-__device__ __forceinline__ void stage_bfly(const V *__restrict__ src, V *__restrict__ dst, int p, int j,
-                                           int Ns, int n, int ps, int es, const V *__restrict__ tw, int twmul)
+__device__ __forceinline__ void stage_bfly(const V *__restrict__ src, V *__restrict__ dst, int p, int j, int q, int k,
+                                           int Ns, int n, int twstep, int ps, int es, const V *__restrict__ tw,
+                                           int twmul)
 {
     const int nR = n / R;
     V v[R];
     const V *s = src + p * ps;
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = s[(j + r * nR) * es];
-    const int k = j % Ns;
     if (Ns > 1) {
-        const int step = k * (n / (Ns * R)) * twmul;
+        const int step = k * twstep * twmul;
 #pragma unroll
         for (int r = 1; r < R; ++r) {
             V w = tw[r * step];
@@ -168,44 +175,63 @@ __device__ __forceinline__ void stage_bfly(const V *__restrict__ src, V *__restr
         }
     }
     dft<R, INV>(v, tw, n, twmul);
-    const int idxD = (j / Ns) * Ns * R + k;
+    const int idxD = q * Ns * R + k;
     V *d = dst + p * ps;
 #pragma unroll
     for (int r = 0; r < R; ++r) d[(idxD + r * Ns) * es] = v[r];
 }
 
+// All butterflies of stage s on npen pencils, without integer division.
+template <int R, bool INV, bool PFAST, typename V>
+__device__ __forceinline__ void stage_loop(const V *__restrict__ a, V *__restrict__ b, int npen, int ps, int es,
+                                           const FftDesc &d, int s, const V *__restrict__ tw, int twmul)
+{
+    const int nb = d.n / R;
+    const int total = nb * npen;
+    const int Ns = d.Ns[s];
+    const int twstep = d.twstep[s];
+    const unsigned nsm = d.ns_magic[s];
+    if (PFAST) {  // npen is a power of two
+        const int lg = __ffs(npen) - 1;
+        for (int t = threadIdx.x; t < total; t += blockDim.x) {
+            const int p = t & (npen - 1);
+            const int j = t >> lg;
+            const int q = Ns == 1 ? j : (int)__umulhi((unsigned)j, nsm);
+            stage_bfly<R, INV>(a, b, p, j, q, j - q * Ns, Ns, d.n, twstep, ps, es, tw, twmul);
+        }
+    } else {
+        const unsigned nbm = d.nb_magic[s];
+        for (int t = threadIdx.x; t < total; t += blockDim.x) {
+            const int p = nb == 1 ? t : (int)__umulhi((unsigned)t, nbm);
+            const int j = t - p * nb;
+            const int q = Ns == 1 ? j : (int)__umulhi((unsigned)j, nsm);
+            stage_bfly<R, INV>(a, b, p, j, q, j - q * Ns, Ns, d.n, twstep, ps, es, tw, twmul);
+        }
+    }
+}
+
 // Run all stages on npen pencils.  Input in a (synchronised by the caller); returns
 // the buffer that holds the result (a or b).  PFAST: thread index runs over pencils
-// first (column tiles), else over butterflies first (rows).
+// first (column tiles, npen a power of two), else over butterflies first (rows).
 template <bool INV, bool PFAST, typename V>
 __device__ V *fft_run(V *a, V *b, int npen, int ps, int es, const FftDesc &d, const V *__restrict__ tw,
                       int twmul)
 {
-    int Ns = 1;
     for (int s = 0; s < d.ns; ++s) {
-        const int R = d.radix[s];
-        const int nb = d.n / R;
-        const int total = nb * npen;
-        for (int t = threadIdx.x; t < total; t += blockDim.x) {
-            int p, j;
-            if (PFAST) { p = t % npen; j = t / npen; }
-            else { j = t % nb; p = t / nb; }
-            switch (R) {
-            case 2: stage_bfly<2, INV>(a, b, p, j, Ns, d.n, ps, es, tw, twmul); break;
-            case 3: stage_bfly<3, INV>(a, b, p, j, Ns, d.n, ps, es, tw, twmul); break;
-            case 4: stage_bfly<4, INV>(a, b, p, j, Ns, d.n, ps, es, tw, twmul); break;
-            case 5: stage_bfly<5, INV>(a, b, p, j, Ns, d.n, ps, es, tw, twmul); break;
-            case 7: stage_bfly<7, INV>(a, b, p, j, Ns, d.n, ps, es, tw, twmul); break;
-            case 8: stage_bfly<8, INV>(a, b, p, j, Ns, d.n, ps, es, tw, twmul); break;
-            case 11: stage_bfly<11, INV>(a, b, p, j, Ns, d.n, ps, es, tw, twmul); break;
-            default: stage_bfly<13, INV>(a, b, p, j, Ns, d.n, ps, es, tw, twmul); break;
-            }
+        switch (d.radix[s]) {
+        case 2: stage_loop<2, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
+        case 3: stage_loop<3, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
+        case 4: stage_loop<4, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
+        case 5: stage_loop<5, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
+        case 7: stage_loop<7, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
+        case 8: stage_loop<8, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
+        case 11: stage_loop<11, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
+        default: stage_loop<13, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
         }
         __syncthreads();
         V *t = a;
         a = b;
         b = t;
-        Ns *= R;
     }
     return a;
 }

@@ -36,17 +36,25 @@ struct BlockMap {
     int wlo[3], whi[3];  // block-local region written to the output volume [lo, hi)
     long long ooff[3];   // volume coordinate of block-local (0,0,0) in the output volume
     long long OD[3];     // output volume dims
+    int fast_x;          // 1: domain x == block x and the block row lies inside the volume
 };
+
+// 1 when every domain x maps to volume x = off + x without extension or mirroring.
+inline int block_fast_x(const BlockMap &m)
+{
+    return (m.L[0] == 0 && m.P[0] == m.b[0] && m.off[0] >= 0 && m.off[0] + m.b[0] <= m.D[0]) ? 1 : 0;
+}
 
 __device__ __forceinline__ int ext_e(int j, int P, int L) { return j >= P - L ? j - P : j; }
 
 __device__ __forceinline__ long long mirror1(long long i, long long n)
 {
+    if (i >= 0 && i < n) return i;  // inside: no reflection
     if (n <= 1) return 0;
-    const long long p = 2 * n - 2;
-    i %= p;
-    if (i < 0) i += p;
-    return i >= n ? p - i : i;
+    const int p = (int)(2 * n - 2);
+    int j = (int)(i % p);
+    if (j < 0) j += p;
+    return j >= n ? p - j : j;
 }
 
 // Volume index of block coordinate (bx, by, bz) under mirror-single on the volume.
@@ -64,6 +72,7 @@ __device__ __forceinline__ MirrorRow mirror_row(const BlockMap &m, int y, int z)
 }
 __device__ __forceinline__ long long mirror_x(const BlockMap &m, int x)
 {
+    if (m.fast_x) return m.off[0] + x;
     const int ex = ext_e(x, m.P[0], m.L[0]);
     return mirror1(m.off[0] + mirror1(ex, m.b[0]), m.D[0]);
 }
@@ -82,7 +91,7 @@ __device__ __forceinline__ ZeroRow zero_row(const BlockMap &m, int by, int bz)
 __device__ __forceinline__ float zero_at(const float *__restrict__ v, const BlockMap &m, ZeroRow r, int bx)
 {
     const long long gx = m.off[0] + bx;
-    if (r.base < 0 || gx < 0 || gx >= m.D[0]) return 0.0f;
+    if (r.base < 0 || (!m.fast_x && (gx < 0 || gx >= m.D[0]))) return 0.0f;
     return __ldg(v + r.base + gx);
 }
 
@@ -165,7 +174,10 @@ __device__ __forceinline__ void r2c_post_store(const V *Z, int ps, V *__restrict
     }
 }
 
-// S rows -> packed Z' for the inverse m-point FFT (yields Px * x after it).
+// S rows -> packed Z' for the inverse m-point FFT (yields Px * x after it).  A warp
+// takes a row; each lane keeps its loads of one 256-wide chunk in registers.
+constexpr int kRowBatch = 8;  // 8 x 32 lanes = 256 values per chunk
+
 template <typename V>
 __device__ __forceinline__ void c2r_pre_load(const V *__restrict__ S, V *A, int ps, long long row0, int nr, int m,
                                              const V *tw)
@@ -174,12 +186,25 @@ __device__ __forceinline__ void c2r_pre_load(const V *__restrict__ S, V *A, int 
     for (int r = warp; r < nr; r += nw) {
         const V *in = S + (row0 + r) * (long long)(m + 1);
         V *a = A + r * ps;
-        for (int k = lane; k < m; k += 32) {
-            const V xk = in[k];
-            const V xc = cconj(in[m - k]);
-            const V e = cadd(xk, xc);
-            const V o = cmul(csub(xk, xc), cconj(tw[k]));
-            a[k] = cx<V>(e.x - o.y, e.y + o.x);  // e + i*o
+        for (int c0 = 0; c0 < m; c0 += 32 * kRowBatch) {
+            V xk[kRowBatch], xc[kRowBatch];
+#pragma unroll
+            for (int u = 0; u < kRowBatch; ++u) {
+                const int k = c0 + lane + 32 * u;
+                if (k < m) {
+                    xk[u] = in[k];
+                    xc[u] = in[m - k];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kRowBatch; ++u) {
+                const int k = c0 + lane + 32 * u;
+                if (k < m) {
+                    const V e = cadd(xk[u], cconj(xc[u]));
+                    const V o = cmul(csub(xk[u], cconj(xc[u])), cconj(tw[k]));
+                    a[k] = cx<V>(e.x - o.y, e.y + o.x);  // e + i*o
+                }
+            }
         }
     }
 }
@@ -204,8 +229,22 @@ __global__ void __launch_bounds__(256) k_rows_fwd(Src src, typename Cx<T>::t *__
         const long long row = row0 + r;
         const int y = (int)(row % bm.P[1]), z = (int)(row / bm.P[1]);
         const typename Src::Row R = src.row(bm, y, z);
-        for (int q = lane; q < m; q += 32)
-            A[r * ps + q] = cx<V>(src.template at<T>(R, bm, 2 * q), src.template at<T>(R, bm, 2 * q + 1));
+        for (int c0 = 0; c0 < m; c0 += 32 * kRowBatch) {
+            T v0[kRowBatch], v1[kRowBatch];
+#pragma unroll
+            for (int u = 0; u < kRowBatch; ++u) {
+                const int q = c0 + lane + 32 * u;
+                if (q < m) {
+                    v0[u] = src.template at<T>(R, bm, 2 * q);
+                    v1[u] = src.template at<T>(R, bm, 2 * q + 1);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kRowBatch; ++u) {
+                const int q = c0 + lane + 32 * u;
+                if (q < m) A[r * ps + q] = cx<V>(v0[u], v1[u]);
+            }
+        }
     }
     __syncthreads();
     V *Z = fft_run<false, false>(A, B, nr, ps, 1, d, tw, 2);
@@ -213,7 +252,11 @@ __global__ void __launch_bounds__(256) k_rows_fwd(Src src, typename Cx<T>::t *__
 }
 
 // ---- column passes (y or z axis) ----------------------------------------------------
-// MODE 0: forward, 1: inverse, 2: forward, multiply by Kh, inverse.
+// MODE 0: forward, 1: inverse, 2: forward, multiply by Kh, inverse.  NP (a power of
+// two) consecutive x' columns at one other-axis index form the tile; every thread
+// keeps kLoadBatch independent global accesses in flight.
+constexpr int kLoadBatch = 8;
+
 template <typename T, int MODE>
 __global__ void __launch_bounds__(256) k_cols(const typename Cx<T>::t *src, typename Cx<T>::t *dst,
                                               const typename Cx<T>::t *__restrict__ Kh, int Hx, long long estride,
@@ -231,22 +274,44 @@ __global__ void __launch_bounds__(256) k_cols(const typename Cx<T>::t *src, type
     const long long base = (long long)blockIdx.y * ostride + x0;
     const int np = min(NP, Hx - x0);
     const int tot = n * NP;
-    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-        const int p = t % NP, i = t / NP;
-        A[t] = p < np ? src[base + i * estride + p] : cx<V>((T)0, (T)0);
+    const int lg = __ffs(NP) - 1;
+    const int step = blockDim.x * kLoadBatch;
+    for (int t0 = threadIdx.x; t0 < tot; t0 += step) {
+        V r[kLoadBatch];
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            const int t = t0 + u * blockDim.x;
+            const int p = t & (NP - 1), i = t >> lg;
+            r[u] = (t < tot && p < np) ? src[base + i * estride + p] : cx<V>((T)0, (T)0);
+        }
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            const int t = t0 + u * blockDim.x;
+            if (t < tot) A[t] = r[u];
+        }
     }
     __syncthreads();
     V *R = fft_run<MODE == 1, true>(A, B, NP, 1, NP, d, tw, 1);
     if (MODE == 2) {
-        for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-            const int p = t % NP, i = t / NP;
-            if (p < np) R[t] = cmul(R[t], __ldg(&Kh[base + i * estride + p]));
+        for (int t0 = threadIdx.x; t0 < tot; t0 += step) {
+            V k[kLoadBatch];
+#pragma unroll
+            for (int u = 0; u < kLoadBatch; ++u) {
+                const int t = t0 + u * blockDim.x;
+                const int p = t & (NP - 1), i = t >> lg;
+                k[u] = (t < tot && p < np) ? __ldg(&Kh[base + i * estride + p]) : cx<V>((T)0, (T)0);
+            }
+#pragma unroll
+            for (int u = 0; u < kLoadBatch; ++u) {
+                const int t = t0 + u * blockDim.x;
+                if (t < tot) R[t] = cmul(R[t], k[u]);
+            }
         }
         __syncthreads();
         R = fft_run<true, true>(R, R == A ? B : A, NP, 1, NP, d, tw, 1);
     }
     for (int t = threadIdx.x; t < tot; t += blockDim.x) {
-        const int p = t % NP, i = t / NP;
+        const int p = t & (NP - 1), i = t >> lg;
         if (p < np) dst[base + i * estride + p] = R[t];
     }
 }
@@ -262,13 +327,26 @@ __device__ __forceinline__ double tikhonov(double v, double lambda)
     return __ddiv_rn(__dsub_rn(__dsqrt_rn(__dadd_rn(1.0, __dmul_rn(__dmul_rn(2.0, lambda), v))), 1.0), lambda);
 }
 
-// computeNextValue (DeconvolutionMethods.java:320-358) in float, as Java evaluates it.
+// The Tikhonov factor in float, from the algebraically equal form without the
+// cancellation of sqrt(1+x)-1: (sqrt(1 + 2 l v) - 1) / l == 2 v / (sqrt(1 + 2 l v) + 1).
+// Within a few float ulp of the reference's double evaluation rounded to float (the
+// reference rounds it to float too); the GPU's double rate is a small fraction of its
+// float rate, so the double form would dominate the whole iteration.
+__device__ __forceinline__ float tikhonov_f(float v, float two_lambda)
+{
+    const float r = __fsqrt_rn(__fadd_rn(1.0f, __fmul_rn(two_lambda, v)));
+    return __fdiv_rn(__fmul_rn(2.0f, v), __fadd_rn(r, 1.0f));
+}
+
+// computeNextValue (DeconvolutionMethods.java:320-358) in float: every operation the
+// reference does in float is done in float here with IEEE rounding and no contraction.
 __device__ __forceinline__ float next_value(float last, float integral, float weight, double lambda, float minI,
                                             float maxI)
 {
     const float value = __fmul_rn(last, integral);
     float adjusted;
-    if (value > 0.0f) adjusted = lambda > 0 ? __fmul_rn((float)tikhonov((double)__fdiv_rn(value, maxI), lambda), maxI) : value;
+    if (value > 0.0f)
+        adjusted = lambda > 0 ? __fmul_rn(tikhonov_f(__fdiv_rn(value, maxI), (float)(2.0 * lambda)), maxI) : value;
     else adjusted = minI;
     const float next = isnan(adjusted) ? minI : (minI >= adjusted ? minI : adjusted);
     return __fadd_rn(last, __fmul_rn(__fsub_rn(next, last), weight));
@@ -313,17 +391,28 @@ __global__ void __launch_bounds__(256) k_rows_ratio(typename Cx<T>::t *__restric
         const bool rin = ey >= 0 && ey < bm.b[1] && ez >= 0 && ez < bm.b[2];
         const ZeroRow zr = rin ? zero_row(bm, ey, ez) : ZeroRow{-1};
         V *zz = Z + r * ps;
-        for (int q = lane; q < m; q += 32) {
-            V c = zz[q];  // conv1 at x = 2q, 2q+1 (kernel spectrum carries 1/(Px Py Pz))
-            T out[2] = {c.x, c.y};
+        for (int c0 = 0; c0 < m; c0 += 32 * kRowBatch) {
+            float im[kRowBatch][2];
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int ex = ext_e(2 * q + h, Px, bm.L[0]);
-                T ratio = (T)1;  // value-1 extension of the quotient outside the block
-                if (rin && ex >= 0 && ex < bm.b[0]) ratio = (T)quotient(zero_at(img, bm, zr, ex), out[h]);
-                out[h] = ratio;
+            for (int u = 0; u < kRowBatch; ++u) {
+                const int q = c0 + lane + 32 * u;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int ex = ext_e(2 * q + h, Px, bm.L[0]);
+                    im[u][h] = (q < m && rin && ex >= 0 && ex < bm.b[0]) ? zero_at(img, bm, zr, ex) : -1.0f;
+                }
             }
-            zz[q] = cx<V>(out[0], out[1]);
+#pragma unroll
+            for (int u = 0; u < kRowBatch; ++u) {
+                const int q = c0 + lane + 32 * u;
+                if (q >= m) continue;
+                const V c = zz[q];  // conv1 at x = 2q, 2q+1 (kernel spectrum carries 1/(Px Py Pz))
+                T out[2] = {c.x, c.y};
+#pragma unroll
+                for (int h = 0; h < 2; ++h)  // -1 marks the value-1 extension outside the block
+                    out[h] = im[u][h] < 0.0f ? (T)1 : (T)quotient(im[u][h], out[h]);
+                zz[q] = cx<V>(out[0], out[1]);
+            }
         }
     }
     __syncthreads();
@@ -380,37 +469,60 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
         const long long orow = ((bm.ooff[2] + z) * bm.OD[1] + (bm.ooff[1] + y)) * bm.OD[0] + bm.ooff[0];
         const long long brow = ((long long)z * bm.b[1] + y) * bm.b[0];
         const V *zz = Z + r * ps;
-        for (int q = lane; q < m; q += 32) {
-            const V c = zz[q];
-            const T cv[2] = {c.x, c.y};
+        for (int c0 = 0; c0 < m; c0 += 32 * kRowBatch) {
+            T lastv[kRowBatch][2];
+            float wv[kRowBatch][2];
+            if (EPI == EPI_SEQ || EPI == EPI_MUL_FINAL) {  // psi and the first weight, batched
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int x = 2 * q + h;
-                if (x >= bm.b[0]) continue;
-                const T integral = cv[h];
-                if (EPI == EPI_STORE) {
-                    ua.store[brow + x] = (float)integral;
-                    continue;
+                for (int u = 0; u < kRowBatch; ++u) {
+                    const int q = c0 + lane + 32 * u;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int x = 2 * q + h;
+                        const bool ok = q < m && x < bm.b[0];
+                        lastv[u][h] = ok ? psrc[mr.base + mirror_x(bm, x)] : (T)0;
+                        wv[u][h] = (ok && EPI == EPI_SEQ) ? zero_at(ua.weight[0], bm, zr, x) : 0.0f;
+                    }
                 }
-                if (EPI == EPI_MUL_FIRST) { ua.prod[brow + x] = (double)integral; continue; }
-                if (EPI == EPI_MUL_ACC) { ua.prod[brow + x] *= (double)integral; continue; }
-                const T last = psrc[mr.base + mirror_x(bm, x)];
-                T next;
-                if (EPI == EPI_SEQ) {
-                    const float w = zero_at(ua.weight[0], bm, zr, x);
-                    next = next_value(last, integral, (T)w, ua.lambda, (T)ua.minI, (T)ua.maxI);
-                } else {  // EPI_MUL_FINAL: DeconvolutionMethods.computeNextValueMul 370-419
-                    double prod = (ua.nviews == 1 ? 1.0 : ua.prod[brow + x]) * (double)integral;
-                    double sumW = 0.0;
-                    for (int v = 0; v < ua.nviews; ++v) sumW += (double)zero_at(ua.weight[v], bm, zr, x);
-                    prod = pow(prod, 1.0 / ua.nviews);
-                    sumW = sumW < 1.0 ? sumW : 1.0;
-                    next = next_value(last, (T)prod, (T)sumW, ua.lambda, (T)ua.minI, (T)ua.maxI);
+            }
+#pragma unroll
+            for (int u = 0; u < kRowBatch; ++u) {
+                const int q = c0 + lane + 32 * u;
+                if (q >= m) continue;
+                const V c = zz[q];
+                const T cv[2] = {c.x, c.y};
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int x = 2 * q + h;
+                    if (x >= bm.b[0]) continue;
+                    const T integral = cv[h];
+                    if (EPI == EPI_STORE) {
+                        ua.store[brow + x] = (float)integral;
+                        continue;
+                    }
+                    if (EPI == EPI_MUL_FIRST) { ua.prod[brow + x] = (double)integral; continue; }
+                    if (EPI == EPI_MUL_ACC) { ua.prod[brow + x] *= (double)integral; continue; }
+                    const T last = lastv[u][h];
+                    T next;
+                    if (EPI == EPI_SEQ) {
+                        next = next_value(last, integral, (T)wv[u][h], ua.lambda, (T)ua.minI, (T)ua.maxI);
+                    } else {  // EPI_MUL_FINAL: DeconvolutionMethods.computeNextValueMul 370-419
+                        double prod = (ua.nviews == 1 ? 1.0 : ua.prod[brow + x]) * (double)integral;
+                        double sumW = 0.0;
+                        for (int v = 0; v < ua.nviews; ++v) sumW += (double)zero_at(ua.weight[v], bm, zr, x);
+                        T root;
+                        if (sizeof(T) == sizeof(double)) root = (T)pow(prod, 1.0 / ua.nviews);
+                        else if (ua.nviews == 1) root = (T)prod;
+                        else if (ua.nviews == 2) root = (T)__fsqrt_rn((float)prod);
+                        else root = (T)powf((float)prod, 1.0f / (float)ua.nviews);  // float rate, see tikhonov_f
+                        sumW = sumW < 1.0 ? sumW : 1.0;
+                        next = next_value(last, root, (T)sumW, ua.lambda, (T)ua.minI, (T)ua.maxI);
+                    }
+                    const T ch = next - last;  // signed change (DeconvolutionMethods.java:308)
+                    lsum += (double)ch;
+                    lmax = fmax(lmax, (double)ch);
+                    if (wrow && x >= bm.wlo[0] && x < bm.whi[0]) pdst[orow + x] = next;
                 }
-                const T ch = next - last;  // signed change (DeconvolutionMethods.java:308)
-                lsum += (double)ch;
-                lmax = fmax(lmax, (double)ch);
-                if (wrow && x >= bm.wlo[0] && x < bm.whi[0]) pdst[orow + x] = next;
             }
         }
     }
