@@ -87,6 +87,17 @@ int Engine<T>::cuda_check(cudaError_t e, const char *what)
     } while (0)
 #define MVR_CUDA(expr) MVR_TRY(cuda_check((expr), #expr))
 #define MVR_LAUNCHED(name) MVR_TRY(cuda_check(cudaGetLastError(), name))
+// Launches the kernel expression with B = the plan's radix set (see fft_run).
+#define MVR_WITH_BIG(big, ...)            \
+    do {                                  \
+        if (big) {                        \
+            constexpr bool B = true;      \
+            __VA_ARGS__;                  \
+        } else {                          \
+            constexpr bool B = false;     \
+            __VA_ARGS__;                  \
+        }                                 \
+    } while (0)
 
 namespace {
 template <typename V>
@@ -109,6 +120,23 @@ V *dev_twiddles_impl(int n, cudaStream_t s, std::string &err)
     return d;
 }
 
+template <typename T, bool B>
+void set_smem_limits_big(int m)
+{
+    cudaFuncSetAttribute(k_rows_fwd<T, SrcMirror<T>, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_rows_fwd<T, SrcZero<T>, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_rows_fwd<T, SrcKernel, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_cols<T, 0, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_cols<T, 1, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_cols<T, 2, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_rows_ratio<T, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_rows_update<T, EPI_SEQ, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_rows_update<T, EPI_MUL_FIRST, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_rows_update<T, EPI_MUL_ACC, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_rows_update<T, EPI_MUL_FINAL, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_rows_update<T, EPI_STORE, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+}
+
 template <typename T>
 void set_smem_limits()
 {
@@ -116,19 +144,8 @@ void set_smem_limits()
     static std::once_flag once;
     std::call_once(once, [] {
         const int m = (int)kSmemMax;
-        cudaFuncSetAttribute(k_rows_fwd<T, SrcMirror<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_rows_fwd<T, SrcMirror<float>>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_rows_fwd<T, SrcZero<T>>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_rows_fwd<T, SrcKernel>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_cols<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_cols<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_cols<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_rows_ratio<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_rows_update<T, EPI_SEQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_rows_update<T, EPI_MUL_FIRST>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_rows_update<T, EPI_MUL_ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_rows_update<T, EPI_MUL_FINAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-        cudaFuncSetAttribute(k_rows_update<T, EPI_STORE>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+        set_smem_limits_big<T, false>(m);
+        set_smem_limits_big<T, true>(m);
     });
 }
 }  // namespace
@@ -283,6 +300,10 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
     pl.dx = make_desc(pl.P[0] / 2);
     pl.dy = make_desc(pl.P[1]);
     pl.dz = make_desc(pl.P[2]);
+    pl.big = false;
+    for (const FftDesc *dd : {&pl.dx, &pl.dy, &pl.dz})
+        for (int st = 0; st < dd->ns; ++st)
+            if (dd->radix[st] == 7 || dd->radix[st] == 11 || dd->radix[st] == 13) pl.big = true;
     std::string e;
     pl.twx = dev_twiddles_impl<V>(pl.P[0], stream_, e);
     pl.twy = dev_twiddles_impl<V>(pl.P[1], stream_, e);
@@ -335,7 +356,8 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
         }
         SrcKernel src{kdev, {kd1[0], kd1[1], kd1[2]}, scale};
         const unsigned grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
-        k_rows_fwd<T, SrcKernel><<<grid, kThreads, pl.smem_row, stream_>>>(src, S0_, bm, pl.dx, pl.twx, pl.RP);
+        MVR_WITH_BIG(pl.big, (k_rows_fwd<T, SrcKernel, B><<<grid, kThreads, pl.smem_row, stream_>>>(src, S0_, bm, pl.dx,
+                                                                                                   pl.twx, pl.RP)));
         MVR_LAUNCHED("k_rows_fwd(kernel)");
         MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
         MVR_TRY(launch_cols(pl, 2, 0, S0_, which == 0 ? pl.k1h : pl.k2h, nullptr));
@@ -372,9 +394,11 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
     const double cb = (double)sizeof(V) * (double)pl.Pc;
     const int kind = mode == 2 ? KK_COLS_ZMUL : (mode == 1 ? KK_COLS_INV : KK_COLS_FWD);
     MVR_TRY(prof_begin(kind, mode == 2 ? 3.0 * cb : 2.0 * cb));
-    if (mode == 0) k_cols<T, 0><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
-    else if (mode == 1) k_cols<T, 1><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
-    else k_cols<T, 2><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
+    MVR_WITH_BIG(pl.big, {
+        if (mode == 0) k_cols<T, 0, B><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
+        else if (mode == 1) k_cols<T, 1, B><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
+        else k_cols<T, 2, B><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
+    });
     MVR_LAUNCHED("k_cols");
     return prof_end();
 }
@@ -405,8 +429,8 @@ int Engine<T>::launch_fwd_mirror(const Plan<T> &pl, const BlockMap &bm, const T 
     const unsigned grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
     const double nb = (double)pl.b[0] * pl.b[1] * pl.b[2];
     MVR_TRY(prof_begin(KK_ROWS_FWD, sizeof(T) * nb + sizeof(V) * (double)pl.Pc));
-    k_rows_fwd<T, SrcMirror<T>><<<grid, kThreads, pl.smem_row, stream_>>>(SrcMirror<T>{src}, S, bm, pl.dx, pl.twx,
-                                                                           pl.RP);
+    MVR_WITH_BIG(pl.big, (k_rows_fwd<T, SrcMirror<T>, B><<<grid, kThreads, pl.smem_row, stream_>>>(
+                             SrcMirror<T>{src}, S, bm, pl.dx, pl.twx, pl.RP)));
     MVR_LAUNCHED("k_rows_fwd");
     return prof_end();
 }
@@ -426,7 +450,8 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace &bp, const float *img
     const double nb = (double)pl.b[0] * pl.b[1] * pl.b[2];
     const double sb = (double)sizeof(V) * (double)pl.Pc;
     MVR_TRY(prof_begin(KK_ROWS_RATIO, 2.0 * sb + 4.0 * nb));
-    k_rows_ratio<T><<<grid, kThreads, pl.smem_row, stream_>>>(S0_, img, bm, pl.dx, pl.twx, pl.RP);
+    MVR_WITH_BIG(pl.big, (k_rows_ratio<T, B><<<grid, kThreads, pl.smem_row, stream_>>>(S0_, img, bm, pl.dx, pl.twx,
+                                                                                     pl.RP)));
     MVR_LAUNCHED("k_rows_ratio");
     MVR_TRY(prof_end());
     MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
@@ -443,7 +468,8 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace &bp, const float *img
     ua.partials = partials_;
     const double neff = (double)(bp.whi[0] - bp.wlo[0]) * (bp.whi[1] - bp.wlo[1]) * (bp.whi[2] - bp.wlo[2]);
     MVR_TRY(prof_begin(KK_ROWS_UPDATE, sb + (sizeof(T) + 4.0) * nb + sizeof(T) * neff));
-    k_rows_update<T, EPI_SEQ><<<grid, kThreads, pl.smem_row, stream_>>>(S0_, ua, bm, pl.dx, pl.twx, pl.RP);
+    MVR_WITH_BIG(pl.big, (k_rows_update<T, EPI_SEQ, B><<<grid, kThreads, pl.smem_row, stream_>>>(S0_, ua, bm, pl.dx,
+                                                                                               pl.twx, pl.RP)));
     MVR_LAUNCHED("k_rows_update");
     MVR_TRY(prof_end());
     if (stats_dev) {
@@ -490,7 +516,8 @@ int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace
         const double nb = (double)pl.b[0] * pl.b[1] * pl.b[2];
         const double sb = (double)sizeof(V) * (double)pl.Pc;
         MVR_TRY(prof_begin(KK_ROWS_RATIO, 2.0 * sb + 4.0 * nb));
-        k_rows_ratio<T><<<grid, kThreads, pl.smem_row, stream_>>>(S1_, imgs[v], bm, pl.dx, pl.twx, pl.RP);
+        MVR_WITH_BIG(pl.big, (k_rows_ratio<T, B><<<grid, kThreads, pl.smem_row, stream_>>>(S1_, imgs[v], bm, pl.dx,
+                                                                                         pl.twx, pl.RP)));
         MVR_LAUNCHED("k_rows_ratio");
         MVR_TRY(prof_end());
         MVR_TRY(launch_cols(pl, 1, 0, S1_, S1_, nullptr));
@@ -501,12 +528,14 @@ int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace
                                                         : sb + (v == 0 ? 8.0 : 16.0) * nb));
         if (v == nv - 1) {
             ua.nviews = nv;
-            k_rows_update<T, EPI_MUL_FINAL><<<grid, kThreads, pl.smem_row, stream_>>>(S1_, ua, bm, pl.dx, pl.twx,
-                                                                                      pl.RP);
+            MVR_WITH_BIG(pl.big, (k_rows_update<T, EPI_MUL_FINAL, B><<<grid, kThreads, pl.smem_row, stream_>>>(
+                                     S1_, ua, bm, pl.dx, pl.twx, pl.RP)));
         } else if (v == 0) {
-            k_rows_update<T, EPI_MUL_FIRST><<<grid, kThreads, pl.smem_row, stream_>>>(S1_, ua, bm, pl.dx, pl.twx, pl.RP);
+            MVR_WITH_BIG(pl.big, (k_rows_update<T, EPI_MUL_FIRST, B><<<grid, kThreads, pl.smem_row, stream_>>>(
+                                     S1_, ua, bm, pl.dx, pl.twx, pl.RP)));
         } else {
-            k_rows_update<T, EPI_MUL_ACC><<<grid, kThreads, pl.smem_row, stream_>>>(S1_, ua, bm, pl.dx, pl.twx, pl.RP);
+            MVR_WITH_BIG(pl.big, (k_rows_update<T, EPI_MUL_ACC, B><<<grid, kThreads, pl.smem_row, stream_>>>(
+                                     S1_, ua, bm, pl.dx, pl.twx, pl.RP)));
         }
         MVR_LAUNCHED("k_rows_update(mul)");
         MVR_TRY(prof_end());
@@ -536,10 +565,11 @@ int Engine<T>::convolve(const Plan<T> &pl, const T *blk, int src_kind, float *ou
     const long long nrows = (long long)pl.P[1] * pl.P[2];
     const unsigned grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
     if (src_kind == SRC_ZERO)
-        k_rows_fwd<T, SrcZero<T>><<<grid, kThreads, pl.smem_row, stream_>>>(SrcZero<T>{blk}, S0_, bm, pl.dx, pl.twx, pl.RP);
+        MVR_WITH_BIG(pl.big, (k_rows_fwd<T, SrcZero<T>, B><<<grid, kThreads, pl.smem_row, stream_>>>(
+                                 SrcZero<T>{blk}, S0_, bm, pl.dx, pl.twx, pl.RP)));
     else
-        k_rows_fwd<T, SrcMirror<T>><<<grid, kThreads, pl.smem_row, stream_>>>(SrcMirror<T>{blk}, S0_, bm, pl.dx, pl.twx,
-                                                                               pl.RP);
+        MVR_WITH_BIG(pl.big, (k_rows_fwd<T, SrcMirror<T>, B><<<grid, kThreads, pl.smem_row, stream_>>>(
+                                 SrcMirror<T>{blk}, S0_, bm, pl.dx, pl.twx, pl.RP)));
     MVR_LAUNCHED("k_rows_fwd(conv)");
     MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
     MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h));
@@ -547,7 +577,8 @@ int Engine<T>::convolve(const Plan<T> &pl, const T *blk, int src_kind, float *ou
     UpdateArgs ua{};
     ua.store = out;
     ua.partials = partials_;
-    k_rows_update<T, EPI_STORE><<<grid, kThreads, pl.smem_row, stream_>>>(S0_, ua, bm, pl.dx, pl.twx, pl.RP);
+    MVR_WITH_BIG(pl.big, (k_rows_update<T, EPI_STORE, B><<<grid, kThreads, pl.smem_row, stream_>>>(S0_, ua, bm, pl.dx,
+                                                                                                 pl.twx, pl.RP)));
     MVR_LAUNCHED("k_rows_update(store)");
     return OK;
 }

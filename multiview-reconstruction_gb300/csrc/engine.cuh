@@ -52,6 +52,7 @@ struct Plan {
     V *twx = nullptr, *twy = nullptr, *twz = nullptr;
     V *k1h = nullptr, *k2h = nullptr;
     int RP = 1, NPy = 1, NPz = 1;
+    bool big = false;  // some axis needs radix 7, 11 or 13
     size_t smem_row = 0, smem_coly = 0, smem_colz = 0;
 };
 

@@ -213,7 +213,9 @@ __device__ __forceinline__ void stage_loop(const V *__restrict__ a, V *__restric
 // Run all stages on npen pencils.  Input in a (synchronised by the caller); returns
 // the buffer that holds the result (a or b).  PFAST: thread index runs over pencils
 // first (column tiles, npen a power of two), else over butterflies first (rows).
-template <bool INV, bool PFAST, typename V>
+// BIG: the stage list may contain radix 7, 11 or 13 (generic DFT, many registers);
+// otherwise only 2, 3, 4, 5, 8 occur and the kernel stays lean.
+template <bool INV, bool PFAST, bool BIG, typename V>
 __device__ V *fft_run(V *a, V *b, int npen, int ps, int es, const FftDesc &d, const V *__restrict__ tw,
                       int twmul)
 {
@@ -223,10 +225,14 @@ __device__ V *fft_run(V *a, V *b, int npen, int ps, int es, const FftDesc &d, co
         case 3: stage_loop<3, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
         case 4: stage_loop<4, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
         case 5: stage_loop<5, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
-        case 7: stage_loop<7, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
         case 8: stage_loop<8, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
-        case 11: stage_loop<11, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
-        default: stage_loop<13, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul); break;
+        default:
+            if (BIG) {
+                if (d.radix[s] == 7) stage_loop<7, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul);
+                else if (d.radix[s] == 11) stage_loop<11, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul);
+                else stage_loop<13, INV, PFAST>(a, b, npen, ps, es, d, s, tw, twmul);
+            }
+            break;
         }
         __syncthreads();
         V *t = a;

@@ -210,7 +210,7 @@ __device__ __forceinline__ void c2r_pre_load(const V *__restrict__ S, V *A, int 
 }
 
 // ---- forward row pass with a fused source -------------------------------------------
-template <typename T, class Src>
+template <typename T, class Src, bool BIG>
 __global__ void __launch_bounds__(256) k_rows_fwd(Src src, typename Cx<T>::t *__restrict__ S, BlockMap bm, FftDesc d,
                                                   const typename Cx<T>::t *__restrict__ twg, int RP)
 {
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(256) k_rows_fwd(Src src, typename Cx<T>::t *__
         }
     }
     __syncthreads();
-    V *Z = fft_run<false, false>(A, B, nr, ps, 1, d, tw, 2);
+    V *Z = fft_run<false, false, BIG>(A, B, nr, ps, 1, d, tw, 2);
     r2c_post_store(Z, ps, S, row0, nr, m, tw);
 }
 
@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(256) k_rows_fwd(Src src, typename Cx<T>::t *__
 // keeps kLoadBatch independent global accesses in flight.
 constexpr int kLoadBatch = 8;
 
-template <typename T, int MODE>
+template <typename T, int MODE, bool BIG>
 __global__ void __launch_bounds__(256) k_cols(const typename Cx<T>::t *src, typename Cx<T>::t *dst,
                                               const typename Cx<T>::t *__restrict__ Kh, int Hx, long long estride,
                                               long long ostride, int NP, FftDesc d,
@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(256) k_cols(const typename Cx<T>::t *src, type
         }
     }
     __syncthreads();
-    V *R = fft_run<MODE == 1, true>(A, B, NP, 1, NP, d, tw, 1);
+    V *R = fft_run<MODE == 1, true, BIG>(A, B, NP, 1, NP, d, tw, 1);
     if (MODE == 2) {
         for (int t0 = threadIdx.x; t0 < tot; t0 += step) {
             V k[kLoadBatch];
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(256) k_cols(const typename Cx<T>::t *src, type
             }
         }
         __syncthreads();
-        R = fft_run<true, true>(R, R == A ? B : A, NP, 1, NP, d, tw, 1);
+        R = fft_run<true, true, BIG>(R, R == A ? B : A, NP, 1, NP, d, tw, 1);
     }
     for (int t = threadIdx.x; t < tot; t += blockDim.x) {
         const int p = t & (NP - 1), i = t >> lg;
@@ -364,7 +364,7 @@ __device__ __forceinline__ double next_value(double last, double integral, doubl
 }
 
 // ---- C2R -> quotient -> R2C (conv1 of one view, then the input of conv2) -------------
-template <typename T>
+template <typename T, bool BIG>
 __global__ void __launch_bounds__(256) k_rows_ratio(typename Cx<T>::t *__restrict__ S, const float *__restrict__ img,
                                                     BlockMap bm, FftDesc d, const typename Cx<T>::t *__restrict__ twg,
                                                     int RP)
@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(256) k_rows_ratio(typename Cx<T>::t *__restric
     __syncthreads();
     c2r_pre_load(S, A, ps, row0, nr, m, tw);
     __syncthreads();
-    V *Z = fft_run<true, false>(A, B, nr, ps, 1, d, tw, 2);
+    V *Z = fft_run<true, false, BIG>(A, B, nr, ps, 1, d, tw, 2);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int r = warp; r < nr; r += nw) {
         const long long row = row0 + r;
@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(256) k_rows_ratio(typename Cx<T>::t *__restric
         }
     }
     __syncthreads();
-    V *Z2 = fft_run<false, false>(Z, Z == A ? B : A, nr, ps, 1, d, tw, 2);
+    V *Z2 = fft_run<false, false, BIG>(Z, Z == A ? B : A, nr, ps, 1, d, tw, 2);
     r2c_post_store(Z2, ps, S, row0, nr, m, tw);
 }
 
@@ -436,7 +436,7 @@ struct UpdateArgs {
     double *partials;     // per CTA {sum, max}
 };
 
-template <typename T, int EPI>
+template <typename T, int EPI, bool BIG>
 __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restrict__ S, UpdateArgs ua, BlockMap bm,
                                                      FftDesc d, const typename Cx<T>::t *__restrict__ twg, int RP)
 {
@@ -454,10 +454,12 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
     __syncthreads();
     c2r_pre_load(S, A, ps, row0, nr, m, tw);
     __syncthreads();
-    V *Z = fft_run<true, false>(A, B, nr, ps, 1, d, tw, 2);
+    V *Z = fft_run<true, false, BIG>(A, B, nr, ps, 1, d, tw, 2);
     const T *psrc = reinterpret_cast<const T *>(ua.psi_src);
     T *pdst = reinterpret_cast<T *>(ua.psi_dst);
-    double lsum = 0.0, lmax = -1.0;
+    // signed-change statistics: per thread in T with Kahan compensation (T = float:
+    // the double rate is a small fraction of the float rate), per block in double
+    T ksum = 0, kcomp = 0, kmax = (T)-1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int r = warp; r < nr; r += nw) {
         const long long row = row0 + r;
@@ -469,12 +471,13 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
         const long long orow = ((bm.ooff[2] + z) * bm.OD[1] + (bm.ooff[1] + y)) * bm.OD[0] + bm.ooff[0];
         const long long brow = ((long long)z * bm.b[1] + y) * bm.b[0];
         const V *zz = Z + r * ps;
-        for (int c0 = 0; c0 < m; c0 += 32 * kRowBatch) {
-            T lastv[kRowBatch][2];
-            float wv[kRowBatch][2];
+        constexpr int UB = kRowBatch / 2;
+        for (int c0 = 0; c0 < m; c0 += 32 * UB) {
+            T lastv[UB][2];
+            float wv[UB][2];
             if (EPI == EPI_SEQ || EPI == EPI_MUL_FINAL) {  // psi and the first weight, batched
 #pragma unroll
-                for (int u = 0; u < kRowBatch; ++u) {
+                for (int u = 0; u < UB; ++u) {
                     const int q = c0 + lane + 32 * u;
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
@@ -486,7 +489,7 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
                 }
             }
 #pragma unroll
-            for (int u = 0; u < kRowBatch; ++u) {
+            for (int u = 0; u < UB; ++u) {
                 const int q = c0 + lane + 32 * u;
                 if (q >= m) continue;
                 const V c = zz[q];
@@ -519,8 +522,11 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
                         next = next_value(last, root, (T)sumW, ua.lambda, (T)ua.minI, (T)ua.maxI);
                     }
                     const T ch = next - last;  // signed change (DeconvolutionMethods.java:308)
-                    lsum += (double)ch;
-                    lmax = fmax(lmax, (double)ch);
+                    const T ky = ch - kcomp;
+                    const T kt = ksum + ky;
+                    kcomp = (kt - ksum) - ky;
+                    ksum = kt;
+                    kmax = kmax > ch ? kmax : ch;
                     if (wrow && x >= bm.wlo[0] && x < bm.whi[0]) pdst[orow + x] = next;
                 }
             }
@@ -528,6 +534,7 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
     }
     if (EPI == EPI_SEQ || EPI == EPI_MUL_FINAL) {
         // deterministic block reduction -> partials[blockIdx.x]
+        double lsum = (double)ksum - (double)kcomp, lmax = (double)kmax;
         for (int o = 16; o > 0; o >>= 1) {
             lsum += __shfl_down_sync(0xffffffffu, lsum, o);
             lmax = fmax(lmax, __shfl_down_sync(0xffffffffu, lmax, o));

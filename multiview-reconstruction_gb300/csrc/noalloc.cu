@@ -48,12 +48,12 @@ int setup_device(int dev, char *err, int err_len)
         return MVR_ERR_CUDA;
     }
     const int m = 227 * 1024;
-    cudaFuncSetAttribute(k_rows_fwd<float, SrcKernel>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    cudaFuncSetAttribute(k_rows_fwd<float, SrcZero<float>>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    cudaFuncSetAttribute(k_cols<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    cudaFuncSetAttribute(k_cols<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    cudaFuncSetAttribute(k_cols<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    cudaFuncSetAttribute(k_rows_update<float, EPI_STORE>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_rows_fwd<float, SrcKernel, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_rows_fwd<float, SrcZero<float>, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_cols<float, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_cols<float, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_cols<float, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_rows_update<float, EPI_STORE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     s.scratch = static_cast<float2 *>(p);
     s.ready = true;
     return MVR_OK;
@@ -150,17 +150,17 @@ extern "C" int mvr_convolve_static(const float *img, const int img_size[3], cons
         bm.whi[d] = b[d];
     }
     const double scale = 1.0 / ((double)P[0] * P[1] * P[2]);
-    k_rows_fwd<float, SrcKernel><<<grid_rows, 256, smem_row, s>>>(SrcKernel{kernel, {kd[0], kd[1], kd[2]}, scale}, Sk,
+    k_rows_fwd<float, SrcKernel, true><<<grid_rows, 256, smem_row, s>>>(SrcKernel{kernel, {kd[0], kd[1], kd[2]}, scale}, Sk,
                                                                  km, dx, tw[0], RP);
-    k_cols<float, 0><<<gy, 256, smem_y, s>>>(Sk, Sk, nullptr, (int)Hx, ey, oy, NPy, dy, tw[1]);
-    k_cols<float, 0><<<gz, 256, smem_z, s>>>(Sk, Sk, nullptr, (int)Hx, ez, oz, NPz, dz, tw[2]);
-    k_rows_fwd<float, SrcZero<float>><<<grid_rows, 256, smem_row, s>>>(SrcZero<float>{img}, S, bm, dx, tw[0], RP);
-    k_cols<float, 0><<<gy, 256, smem_y, s>>>(S, S, nullptr, (int)Hx, ey, oy, NPy, dy, tw[1]);
-    k_cols<float, 2><<<gz, 256, smem_z, s>>>(S, S, Sk, (int)Hx, ez, oz, NPz, dz, tw[2]);
-    k_cols<float, 1><<<gy, 256, smem_y, s>>>(S, S, nullptr, (int)Hx, ey, oy, NPy, dy, tw[1]);
+    k_cols<float, 0, true><<<gy, 256, smem_y, s>>>(Sk, Sk, nullptr, (int)Hx, ey, oy, NPy, dy, tw[1]);
+    k_cols<float, 0, true><<<gz, 256, smem_z, s>>>(Sk, Sk, nullptr, (int)Hx, ez, oz, NPz, dz, tw[2]);
+    k_rows_fwd<float, SrcZero<float>, true><<<grid_rows, 256, smem_row, s>>>(SrcZero<float>{img}, S, bm, dx, tw[0], RP);
+    k_cols<float, 0, true><<<gy, 256, smem_y, s>>>(S, S, nullptr, (int)Hx, ey, oy, NPy, dy, tw[1]);
+    k_cols<float, 2, true><<<gz, 256, smem_z, s>>>(S, S, Sk, (int)Hx, ez, oz, NPz, dz, tw[2]);
+    k_cols<float, 1, true><<<gy, 256, smem_y, s>>>(S, S, nullptr, (int)Hx, ey, oy, NPy, dy, tw[1]);
     UpdateArgs ua{};
     ua.store = out;
-    k_rows_update<float, EPI_STORE><<<grid_rows, 256, smem_row, s>>>(S, ua, bm, dx, tw[0], RP);
+    k_rows_update<float, EPI_STORE, true><<<grid_rows, 256, smem_row, s>>>(S, ua, bm, dx, tw[0], RP);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         put_error(err, err_len, cudaGetErrorString(e));
