@@ -246,6 +246,7 @@ def run_gb300(args, ws, rank, local):
         dec.set_view_device(v, d_img[v].data_ptr(), d_w[v].data_ptr(), ds.psfs[v])
     dec.prepare()
     stream = torch.cuda.ExternalStream(dec.stream_ptr(), device=f"cuda:{dev}")
+    batch = dec.batch()
     for _ in range(args.warmup):
         dec.run_iterations(1)
     dec.synchronize()
@@ -296,6 +297,37 @@ def run_gb300(args, ws, rank, local):
                 "path_achieved": path_bytes / (total_ms / 1e3) / 1e9, "kernels": kernels}
 
     # ---- e2e: public C ABI with pinned host buffers, copies inside the timed region ----
+    if args.no_e2e:
+        e2e = None
+    else:
+        e2e = run_e2e(args, ws, dev, ds, dec, shape, boundary)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        import oracle
+
+        oracle.build()
+        k1s, k2s, mx = prepare_reference_inputs(ds)
+        t_vb, threads = cpu_block_sample(ds, k1s, k2s, mx, args.cpu_blocks)
+        cpu = {"value": NVOX / (t_vb * VIEW_BLOCKS_PER_ITER), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_blocks} view-block(s) of 192^3 (reference boundary, FFT domain "
+                         f"222x222x252), extrapolated to the {VIEW_BLOCKS_PER_ITER} view-blocks of one iteration"}
+    dec.close()
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": dict(workload_config(args.boundary), batch_blocks=batch), "clocks": clocks,
+                "gpu_launches": launches, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+
+
+def run_e2e(args, ws, dev, ds, dec, shape, boundary):
+    """The public C ABI with pinned host buffers: every step uploads the 4 images, the 4
+    raw weights and psi, runs one iteration and reads psi back."""
+    import torch
+
+    import mvrgb300 as M
+
     h_img = [torch.from_numpy(a).pin_memory() for a in ds.images]
     h_w = [torch.from_numpy(a).pin_memory() for a in ds.weights]
     h_psi = torch.empty(shape, dtype=torch.float32).pin_memory()
@@ -327,28 +359,8 @@ def run_gb300(args, ws, rank, local):
     h2d = VIEWS * 2 * NVOX * 4 + NVOX * 4
     d2h = NVOX * 4
     e2e_dec.close()
-
-    # ---- CPU baseline: the oracle on a bounded sample (rank 0, N = 1 only) ----
-    cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu:
-        import oracle
-
-        oracle.build()
-        k1s, k2s, mx = prepare_reference_inputs(ds)
-        t_vb, threads = cpu_block_sample(ds, k1s, k2s, mx, args.cpu_blocks)
-        cpu = {"value": NVOX / (t_vb * VIEW_BLOCKS_PER_ITER), "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_blocks} view-block(s) of 192^3 (reference boundary, FFT domain "
-                         f"222x222x252), extrapolated to the {VIEW_BLOCKS_PER_ITER} view-blocks of one iteration"}
-    dec.close()
-    if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": workload_config(args.boundary), "clocks": clocks, "gpu_launches": launches,
-                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                        "steps": e2e_steps},
-                "roofline": roofline, "cpu_baseline": cpu}
-        print(json.dumps(line), flush=True)
+    return {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "steps": e2e_steps}
 
 
 def main():
@@ -360,6 +372,7 @@ def main():
     ap.add_argument("--boundary", choices=["circular", "reference"], default="circular")
     ap.add_argument("--cpu-blocks", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     ws, rank, local = dist_setup(args)
     if args.impl == "reference":

@@ -143,6 +143,7 @@ typedef struct mvr_decon_params {
     float osem_speedup;   /* OSEM speed-up of the weight normalisation (1 = none) */
     float max_diff_range; /* smoothWeights parameters (reference 0.1, 0.05) */
     float scaling_range;
+    int batch_blocks;     /* blocks per batched launch, 1..16; 0 = autotuned in mvr_decon_prepare */
     int device;           /* CUDA device ordinal */
 } mvr_decon_params;
 
@@ -189,6 +190,8 @@ MVR_API int mvr_decon_set_profiling(mvr_decon *h, int on);
  * synchronises the stream. */
 MVR_API int mvr_decon_get_profile(mvr_decon *h, double *ms, long long *launches, double *bytes);
 MVR_API const char *mvr_kernel_name(int kind);
+/* Blocks per batched launch in use (chosen by the autotuner unless fixed). */
+MVR_API int mvr_decon_batch(const mvr_decon *h);
 
 /* ---- convolution without device allocation ------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot call

@@ -139,7 +139,7 @@ static int run_seq_impl(mvr_block *h, int view, const float *psi_src, float *psi
         bp.OD[d] = h->b[d];
         bp.whi[d] = h->b[d];
     }
-    return h->from_engine(h->eng.run_seq(h->plans[view], bp, img, w, maxI, stats_dev));
+    return h->from_engine(h->eng.run_seq(h->plans[view], &bp, 1, img, w, maxI, stats_dev));
 }
 
 extern "C" int mvr_block_run_seq(mvr_block *h, int view, float *psi, const float *img, const float *w, float maxI,
@@ -219,7 +219,7 @@ extern "C" int mvr_block_run_mul(mvr_block *h, float *psi, const float *const *i
         bp.whi[d] = h->b[d];
     }
     std::vector<const float *> di(h->d_img.begin(), h->d_img.end()), dw(h->d_w.begin(), h->d_w.end());
-    int rc = h->from_engine(h->eng.run_mul(pls, bp, di.data(), dw.data(), (float)miv, h->d_stats));
+    int rc = h->from_engine(h->eng.run_mul(pls, &bp, 1, di.data(), dw.data(), (float)miv, h->d_stats));
     if (rc != MVR_OK) return rc;
     BLK_CUDA(h, cudaMemcpyAsync(psi, h->d_psi, bytes, cudaMemcpyDeviceToHost, s));
     double st[2] = {0.0, -1.0};

@@ -341,6 +341,7 @@ public:
     virtual long long launches() const = 0;
     virtual void set_profiling(bool on) = 0;
     virtual int profile(KernelProfile &out) = 0;
+    virtual int batch() const = 0;
 };
 
 template <typename T>
@@ -366,6 +367,7 @@ public:
     long long launches() const override { return engine_.launches(); }
     void set_profiling(bool on) override { engine_.set_profiling(on); }
     int profile(KernelProfile &out) override { return eng(engine_.profile_collect(out)); }
+    int batch() const override { return batch_; }
 
 private:
     struct View {
@@ -396,8 +398,11 @@ private:
     int invert(const float *in, float *out, const int kd[3]);
     int conv_zero(const float *in, const int id[3], const float *k, const int kd[3], float *out);
     int psf_init();
-    int run_step(int s, double *stats_slot);
+    int run_step(int s, double *stats_slot, bool trial, int batch);
+    int autotune();
     int normalize_weights();
+    int batch_ = 1;
+    std::vector<std::pair<int, float>> tune_;  // (blocks per launch, ms per view-step)
     bool weights_dirty_ = false;
 
     mvr_decon_params p_;
@@ -730,6 +735,7 @@ int Decon<T>::prepare()
         D_CUDA(cudaMemcpyAsync(max_.data(), mx, sizeof(float) * nv, cudaMemcpyDeviceToHost, s));
     }
     D_CUDA(cudaStreamSynchronize(s));
+    D_TRY(autotune());
     prepared_ = true;
     return MVR_OK;
 }
@@ -837,9 +843,11 @@ int Decon<T>::synchronize()
     return MVR_OK;
 }
 
-// One view-step (Seq) or one iteration (Mul): blocks in slab batches.
+// One view-step (Seq) or one iteration (Mul): blocks in slab batches, each slab in
+// launches of up to batch_ blocks.  trial: time-only run for the autotuner (psi is
+// read, the staging volume written, nothing pasted or swapped).
 template <typename T>
-int Decon<T>::run_step(int st, double *stats_slot)
+int Decon<T>::run_step(int st, double *stats_slot, bool trial, int batch)
 {
     cudaStream_t s = engine_.stream();
     const std::vector<BlockDesc> &bl = blocks_[st];
@@ -869,40 +877,86 @@ int Decon<T>::run_step(int st, double *stats_slot)
         D_TRY(cuda(cudaGetLastError(), "k_paste"));
         return eng(engine_.prof_end());
     };
+    auto run_blocks = [&](const std::vector<const BlockDesc *> &grp, double *sd) -> int {
+        std::vector<BlockPlace> bps;
+        for (const BlockDesc *b : grp) bps.push_back(place(*b));
+        if (!p_.mul) {
+            const View &vw = views_[st];
+            return eng(engine_.run_seq(vw.plan, bps.data(), (int)bps.size(), vw.img, vw.w, max_[st], sd));
+        }
+        std::vector<const Plan<T> *> pls;
+        std::vector<const float *> imgs, ws;
+        double miv = 0.0;
+        for (auto &vw : views_) {
+            pls.push_back(&vw.plan);
+            imgs.push_back(vw.img);
+            ws.push_back(vw.w);
+        }
+        for (float m : max_) miv += m;
+        miv /= (double)max_.size();
+        return eng(engine_.run_mul(pls, bps.data(), (int)bps.size(), imgs.data(), ws.data(), (float)miv, sd));
+    };
     int slot = 0;
     std::vector<const BlockDesc *> prev;
-    for (int j = 0; j < nb; ++j) {
+    // Jacobi: every block reads psi before the step, so all slabs go out together
+    const int nslabs = jac ? 1 : nb;
+    for (int j = 0; j < nslabs; ++j) {
         std::vector<const BlockDesc *> cur;
         for (const auto &b : bl)
-            if (b.batch == j) cur.push_back(&b);
-        for (const BlockDesc *b : cur) {
-            const BlockPlace bp = place(*b);
-            double *sd = stats_slot ? stats_slot + 2 * (slot++) : nullptr;
-            if (!p_.mul) {
-                const View &vw = views_[st];
-                D_TRY(eng(engine_.run_seq(vw.plan, bp, vw.img, vw.w, max_[st], sd)));
-            } else {
-                std::vector<const Plan<T> *> pls;
-                std::vector<const float *> imgs, ws;
-                double miv = 0.0;
-                for (auto &vw : views_) {
-                    pls.push_back(&vw.plan);
-                    imgs.push_back(vw.img);
-                    ws.push_back(vw.w);
-                }
-                for (float m : max_) miv += m;
-                miv /= (double)max_.size();
-                D_TRY(eng(engine_.run_mul(pls, bp, imgs.data(), ws.data(), (float)miv, sd)));
-            }
+            if (jac || b.batch == j) cur.push_back(&b);
+        for (size_t i0 = 0; i0 < cur.size(); i0 += (size_t)batch) {
+            std::vector<const BlockDesc *> grp(cur.begin() + i0, cur.begin() + std::min(cur.size(), i0 + batch));
+            D_TRY(run_blocks(grp, stats_slot ? stats_slot + 2 * slot : nullptr));
+            slot += (int)grp.size();
         }
-        if (!jac) {
+        if (!jac && !trial) {
             for (const BlockDesc *b : prev) D_TRY(paste(*b));
             prev = cur;
         }
     }
+    if (trial) return MVR_OK;
     if (jac) std::swap(psi_, stage_);
     else
         for (const BlockDesc *b : prev) D_TRY(paste(*b));
+    return MVR_OK;
+}
+
+// Batch size per launch: the fastest of 1, 2, 4, 8, 16 blocks on one view-step
+// (CUDA events on the engine stream), unless fixed by the parameters.
+template <typename T>
+int Decon<T>::autotune()
+{
+    size_t maxb = 1;
+    for (auto &b : blocks_) maxb = std::max(maxb, b.size());
+    const int cap = (int)std::min<size_t>(maxb, kMaxBatch);
+    if (p_.batch_blocks > 0) {
+        batch_ = std::min(p_.batch_blocks, kMaxBatch);
+        return MVR_OK;
+    }
+    batch_ = 1;
+    if (cap <= 1 || !jacobi_[0]) return MVR_OK;
+    cudaStream_t s = engine_.stream();
+    cudaEvent_t a, b;
+    D_CUDA(cudaEventCreate(&a));
+    D_CUDA(cudaEventCreate(&b));
+    float best = 1e30f;
+    tune_.clear();
+    for (int cand = 1; cand <= cap; cand *= 2) {
+        D_TRY(run_step(0, nullptr, true, cand));  // warm (allocates the batch's scratch)
+        D_CUDA(cudaEventRecord(a, s));
+        D_TRY(run_step(0, nullptr, true, cand));
+        D_CUDA(cudaEventRecord(b, s));
+        D_CUDA(cudaEventSynchronize(b));
+        float ms = 0.0f;
+        D_CUDA(cudaEventElapsedTime(&ms, a, b));
+        tune_.push_back({cand, ms});
+        if (ms < best) {
+            best = ms;
+            batch_ = cand;
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
     return MVR_OK;
 }
 
@@ -926,7 +980,8 @@ int Decon<T>::run(int iterations, double *stats)
     }
     std::vector<double> hs;
     for (int it = 0; it < iterations; ++it) {
-        for (int st = 0; st < steps; ++st) D_TRY(run_step(st, stats ? d_stats_ + (size_t)st * maxb * 2 : nullptr));
+        for (int st = 0; st < steps; ++st)
+            D_TRY(run_step(st, stats ? d_stats_ + (size_t)st * maxb * 2 : nullptr, false, batch_));
         if (stats) {
             hs.resize((size_t)need);
             D_CUDA(cudaMemcpyAsync(hs.data(), d_stats_, sizeof(double) * (size_t)need, cudaMemcpyDeviceToHost,
@@ -1063,3 +1118,4 @@ extern "C" int mvr_decon_get_profile(mvr_decon *h, double *ms, long long *launch
     return MVR_OK;
 }
 extern "C" const char *mvr_kernel_name(int kind) { return mvr::kernel_kind_name(kind); }
+extern "C" int mvr_decon_batch(const mvr_decon *h) { return h ? h->impl->batch() : -1; }

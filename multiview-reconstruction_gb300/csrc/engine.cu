@@ -229,30 +229,38 @@ int Engine<T>::init(int device, int boundary, double lambda, float min_value)
 }
 
 template <typename T>
-int Engine<T>::reserve(long long Pc, long long nvox_block, long long rows)
+int Engine<T>::reserve(long long Pc, long long nvox_block, long long rows, int nb)
 {
-    if (Pc > Scap_) {
+    if (nb < 1) nb = 1;
+    if (Pc * nb > Scap_) {
         cudaFree(S0_);
         cudaFree(S1_);
         S0_ = S1_ = nullptr;
         Scap_ = 0;
-        MVR_CUDA(cudaMalloc(&S0_, sizeof(V) * (size_t)Pc));
-        MVR_CUDA(cudaMalloc(&S1_, sizeof(V) * (size_t)Pc));
-        Scap_ = Pc;
+        MVR_CUDA(cudaMalloc(&S0_, sizeof(V) * (size_t)(Pc * nb)));
+        MVR_CUDA(cudaMalloc(&S1_, sizeof(V) * (size_t)(Pc * nb)));
+        Scap_ = Pc * nb;
     }
-    if (nvox_block > prodcap_) {
-        cudaFree(prod_);
-        prod_ = nullptr;
-        prodcap_ = 0;
-        MVR_CUDA(cudaMalloc(&prod_, sizeof(double) * (size_t)nvox_block));
-        prodcap_ = nvox_block;
-    }
-    if (rows > partcap_) {
+    if (rows * nb > partcap_) {
         cudaFree(partials_);
         partials_ = nullptr;
         partcap_ = 0;
-        MVR_CUDA(cudaMalloc(&partials_, sizeof(double) * 2 * (size_t)rows));
-        partcap_ = rows;
+        MVR_CUDA(cudaMalloc(&partials_, sizeof(double) * 2 * (size_t)(rows * nb)));
+        partcap_ = rows * nb;
+    }
+    (void)nvox_block;
+    return OK;
+}
+
+template <typename T>
+int Engine<T>::reserve_prod(long long n)
+{
+    if (n > prodcap_) {
+        cudaFree(prod_);
+        prod_ = nullptr;
+        prodcap_ = 0;
+        MVR_CUDA(cudaMalloc(&prod_, sizeof(double) * (size_t)n));
+        prodcap_ = n;
     }
     return OK;
 }
@@ -327,7 +335,7 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
     if (!col_np(pl.P[1], pl.NPy, pl.smem_coly) || !col_np(pl.P[2], pl.NPz, pl.smem_colz))
         return fail(ERR_UNSUPPORTED, "column too long for shared memory");
     const long long nrows = (long long)pl.P[1] * pl.P[2];
-    MVR_TRY(reserve(pl.Pc, (long long)b[0] * b[1] * b[2], (nrows + pl.RP - 1) / pl.RP));
+    MVR_TRY(reserve(pl.Pc, (long long)b[0] * b[1] * b[2], (nrows + pl.RP - 1) / pl.RP, 1));
     // kernel spectra, scaled by 1 / (Px Py Pz) so that the inverse needs no scaling
     MVR_CUDA(cudaMalloc(&pl.k1h, sizeof(V) * (size_t)pl.Pc));
     if (k2) MVR_CUDA(cudaMalloc(&pl.k2h, sizeof(V) * (size_t)pl.Pc));
@@ -339,7 +347,8 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
         MVR_CUDA(cudaMalloc(&kbuf_, sizeof(float) * (size_t)kn));
         kcap_ = kn;
     }
-    BlockMap bm{};
+    BlockMaps bms{};
+    BlockMap &bm = bms.m[0];
     for (int d = 0; d < 3; ++d) {
         bm.P[d] = pl.P[d];
         bm.b[d] = pl.P[d];
@@ -355,19 +364,19 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
             kdev = kbuf_;
         }
         SrcKernel src{kdev, {kd1[0], kd1[1], kd1[2]}, scale};
-        const unsigned grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
-        MVR_WITH_BIG(pl.big, (k_rows_fwd<T, SrcKernel, B><<<grid, kThreads, pl.smem_row, stream_>>>(src, S0_, bm, pl.dx,
-                                                                                                   pl.twx, pl.RP)));
+        const dim3 grid((unsigned)((nrows + pl.RP - 1) / pl.RP), 1);
+        MVR_WITH_BIG(pl.big, (k_rows_fwd<T, SrcKernel, B><<<grid, kThreads, pl.smem_row, stream_>>>(
+                                 src, S0_, bms, pl.Pc, pl.dx, pl.twx, pl.RP)));
         MVR_LAUNCHED("k_rows_fwd(kernel)");
-        MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
-        MVR_TRY(launch_cols(pl, 2, 0, S0_, which == 0 ? pl.k1h : pl.k2h, nullptr));
+        MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, 1));
+        MVR_TRY(launch_cols(pl, 2, 0, S0_, which == 0 ? pl.k1h : pl.k2h, nullptr, 1));
     }
     MVR_CUDA(cudaStreamSynchronize(stream_));
     return OK;
 }
 
 template <typename T>
-int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh)
+int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh, int nb)
 {
     const int Hx = pl.Hx;
     long long estride, ostride;
@@ -390,91 +399,108 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
         d = &pl.dz;
     }
     const V *tw = axis == 1 ? pl.twy : pl.twz;
-    dim3 grid((unsigned)((Hx + NP - 1) / NP), (unsigned)nother);
-    const double cb = (double)sizeof(V) * (double)pl.Pc;
+    const dim3 grid((unsigned)((Hx + NP - 1) / NP), (unsigned)nother, (unsigned)nb);
+    const double cb = (double)sizeof(V) * (double)pl.Pc * nb;
     const int kind = mode == 2 ? KK_COLS_ZMUL : (mode == 1 ? KK_COLS_INV : KK_COLS_FWD);
     MVR_TRY(prof_begin(kind, mode == 2 ? 3.0 * cb : 2.0 * cb));
+    const long long Pc = pl.Pc;
     MVR_WITH_BIG(pl.big, {
-        if (mode == 0) k_cols<T, 0, B><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
-        else if (mode == 1) k_cols<T, 1, B><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
-        else k_cols<T, 2, B><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, *d, tw);
+        if (mode == 0)
+            k_cols<T, 0, B><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, Pc, *d, tw);
+        else if (mode == 1)
+            k_cols<T, 1, B><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, Pc, *d, tw);
+        else
+            k_cols<T, 2, B><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, Pc, *d, tw);
     });
     MVR_LAUNCHED("k_cols");
     return prof_end();
 }
 
 template <typename T>
-BlockMap Engine<T>::block_map(const Plan<T> &pl, const BlockPlace &bp) const
+BlockMaps Engine<T>::block_maps(const Plan<T> &pl, const BlockPlace *bps, int nb) const
 {
-    BlockMap bm{};
-    for (int d = 0; d < 3; ++d) {
-        bm.P[d] = pl.P[d];
-        bm.b[d] = pl.b[d];
-        bm.L[d] = pl.L[d];
-        bm.off[d] = bp.off[d];
-        bm.D[d] = bp.D[d];
-        bm.wlo[d] = bp.wlo[d];
-        bm.whi[d] = bp.whi[d];
-        bm.ooff[d] = bp.ooff[d];
-        bm.OD[d] = bp.OD[d];
+    BlockMaps bms{};
+    for (int i = 0; i < nb; ++i) {
+        BlockMap &bm = bms.m[i];
+        const BlockPlace &bp = bps[i];
+        for (int d = 0; d < 3; ++d) {
+            bm.P[d] = pl.P[d];
+            bm.b[d] = pl.b[d];
+            bm.L[d] = pl.L[d];
+            bm.off[d] = bp.off[d];
+            bm.D[d] = bp.D[d];
+            bm.wlo[d] = bp.wlo[d];
+            bm.whi[d] = bp.whi[d];
+            bm.ooff[d] = bp.ooff[d];
+            bm.OD[d] = bp.OD[d];
+        }
+        bm.fast_x = block_fast_x(bm);
     }
-    bm.fast_x = block_fast_x(bm);
-    return bm;
+    return bms;
 }
 
 template <typename T>
-int Engine<T>::launch_fwd_mirror(const Plan<T> &pl, const BlockMap &bm, const T *src, V *S)
+int Engine<T>::launch_fwd_mirror(const Plan<T> &pl, const BlockMaps &bms, int nb, const T *src, V *S)
 {
     const long long nrows = (long long)pl.P[1] * pl.P[2];
-    const unsigned grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
-    const double nb = (double)pl.b[0] * pl.b[1] * pl.b[2];
-    MVR_TRY(prof_begin(KK_ROWS_FWD, sizeof(T) * nb + sizeof(V) * (double)pl.Pc));
+    const dim3 grid((unsigned)((nrows + pl.RP - 1) / pl.RP), (unsigned)nb);
+    const double nv = (double)pl.b[0] * pl.b[1] * pl.b[2];
+    MVR_TRY(prof_begin(KK_ROWS_FWD, nb * (sizeof(T) * nv + sizeof(V) * (double)pl.Pc)));
     MVR_WITH_BIG(pl.big, (k_rows_fwd<T, SrcMirror<T>, B><<<grid, kThreads, pl.smem_row, stream_>>>(
-                             SrcMirror<T>{src}, S, bm, pl.dx, pl.twx, pl.RP)));
+                             SrcMirror<T>{src}, S, bms, pl.Pc, pl.dx, pl.twx, pl.RP)));
     MVR_LAUNCHED("k_rows_fwd");
     return prof_end();
 }
 
 template <typename T>
-int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace &bp, const float *img, const float *w, float maxI,
-                       double *stats_dev)
+int Engine<T>::launch_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img)
 {
-    if (!pl.k1h || !pl.k2h) return fail(ERR_STATE, "kernels not set for this view");
-    const BlockMap bm = block_map(pl, bp);
     const long long nrows = (long long)pl.P[1] * pl.P[2];
-    const unsigned grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
-    MVR_TRY(launch_fwd_mirror(pl, bm, reinterpret_cast<const T *>(bp.psi_src), S0_));
-    MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
-    MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h));
-    MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr));
-    const double nb = (double)pl.b[0] * pl.b[1] * pl.b[2];
-    const double sb = (double)sizeof(V) * (double)pl.Pc;
-    MVR_TRY(prof_begin(KK_ROWS_RATIO, 2.0 * sb + 4.0 * nb));
-    MVR_WITH_BIG(pl.big, (k_rows_ratio<T, B><<<grid, kThreads, pl.smem_row, stream_>>>(S0_, img, bm, pl.dx, pl.twx,
-                                                                                     pl.RP)));
+    const dim3 grid((unsigned)((nrows + pl.RP - 1) / pl.RP), (unsigned)nb);
+    const double nv = (double)pl.b[0] * pl.b[1] * pl.b[2];
+    MVR_TRY(prof_begin(KK_ROWS_RATIO, nb * (2.0 * sizeof(V) * (double)pl.Pc + 4.0 * nv)));
+    MVR_WITH_BIG(pl.big, (k_rows_ratio<T, B><<<grid, kThreads, pl.smem_row, stream_>>>(S, img, bms, pl.Pc, pl.dx,
+                                                                                          pl.twx, pl.RP)));
     MVR_LAUNCHED("k_rows_ratio");
-    MVR_TRY(prof_end());
-    MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
-    MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k2h));
-    MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr));
-    UpdateArgs ua{};
-    ua.psi_src = bp.psi_src;
-    ua.psi_dst = bp.psi_dst;
-    ua.weight[0] = w;
-    ua.nviews = 1;
-    ua.lambda = lambda_;
-    ua.minI = min_value_;
-    ua.maxI = maxI;
-    ua.partials = partials_;
-    const double neff = (double)(bp.whi[0] - bp.wlo[0]) * (bp.whi[1] - bp.wlo[1]) * (bp.whi[2] - bp.wlo[2]);
-    MVR_TRY(prof_begin(KK_ROWS_UPDATE, sb + (sizeof(T) + 4.0) * nb + sizeof(T) * neff));
-    MVR_WITH_BIG(pl.big, (k_rows_update<T, EPI_SEQ, B><<<grid, kThreads, pl.smem_row, stream_>>>(S0_, ua, bm, pl.dx,
-                                                                                               pl.twx, pl.RP)));
+    return prof_end();
+}
+
+template <typename T>
+int Engine<T>::launch_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const UpdateArgs &ua, int epi,
+                             double bytes, double *stats_dev)
+{
+    const long long nrows = (long long)pl.P[1] * pl.P[2];
+    const unsigned gx = (unsigned)((nrows + pl.RP - 1) / pl.RP);
+    const dim3 grid(gx, (unsigned)nb);
+    MVR_TRY(prof_begin(KK_ROWS_UPDATE, bytes));
+    MVR_WITH_BIG(pl.big, {
+        switch (epi) {
+        case EPI_SEQ:
+            k_rows_update<T, EPI_SEQ, B><<<grid, kThreads, pl.smem_row, stream_>>>(S, ua, bms, pl.Pc, pl.dx, pl.twx, pl.RP);
+            break;
+        case EPI_MUL_FIRST:
+            k_rows_update<T, EPI_MUL_FIRST, B><<<grid, kThreads, pl.smem_row, stream_>>>(S, ua, bms, pl.Pc, pl.dx,
+                                                                                         pl.twx, pl.RP);
+            break;
+        case EPI_MUL_ACC:
+            k_rows_update<T, EPI_MUL_ACC, B><<<grid, kThreads, pl.smem_row, stream_>>>(S, ua, bms, pl.Pc, pl.dx, pl.twx,
+                                                                                       pl.RP);
+            break;
+        case EPI_MUL_FINAL:
+            k_rows_update<T, EPI_MUL_FINAL, B><<<grid, kThreads, pl.smem_row, stream_>>>(S, ua, bms, pl.Pc, pl.dx,
+                                                                                         pl.twx, pl.RP);
+            break;
+        default:
+            k_rows_update<T, EPI_STORE, B><<<grid, kThreads, pl.smem_row, stream_>>>(S, ua, bms, pl.Pc, pl.dx, pl.twx,
+                                                                                     pl.RP);
+            break;
+        }
+    });
     MVR_LAUNCHED("k_rows_update");
     MVR_TRY(prof_end());
-    if (stats_dev) {
-        MVR_TRY(prof_begin(KK_REDUCE, 16.0 * grid));
-        k_reduce_stats<double><<<1, 1024, 0, stream_>>>(partials_, (int)grid, stats_dev);
+    if (stats_dev && (epi == EPI_SEQ || epi == EPI_MUL_FINAL)) {
+        MVR_TRY(prof_begin(KK_REDUCE, 16.0 * gx * nb));
+        k_reduce_stats<double><<<nb, 1024, 0, stream_>>>(partials_, (int)gx, stats_dev);
         MVR_LAUNCHED("k_reduce_stats");
         MVR_TRY(prof_end());
     }
@@ -482,69 +508,84 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace &bp, const float *img
 }
 
 template <typename T>
-int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace &bp, const float *const *imgs,
-                       const float *const *ws, float maxI, double *stats_dev)
+int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const float *img, const float *w, float maxI,
+                       double *stats_dev)
 {
-    const int nv = (int)pls.size();
-    if (nv < 1 || nv > kMaxViews) return fail(ERR_ARG, "number of views must be 1..16");
+    if (!pl.k1h || !pl.k2h) return fail(ERR_STATE, "kernels not set for this view");
+    if (nb < 1 || nb > kMaxBatch) return fail(ERR_ARG, "batch of 1..16 blocks");
+    const long long nrows = (long long)pl.P[1] * pl.P[2];
+    MVR_TRY(reserve(pl.Pc, (long long)pl.b[0] * pl.b[1] * pl.b[2], (nrows + pl.RP - 1) / pl.RP, nb));
+    const BlockMaps bms = block_maps(pl, bps, nb);
+    MVR_TRY(launch_fwd_mirror(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
+    MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
+    MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb));
+    MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr, nb));
+    MVR_TRY(launch_ratio(pl, bms, nb, S0_, img));
+    MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
+    MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k2h, nb));
+    MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr, nb));
     UpdateArgs ua{};
-    ua.psi_src = bp.psi_src;
-    ua.psi_dst = bp.psi_dst;
-    for (int v = 0; v < nv; ++v) ua.weight[v] = ws[v];
-    ua.nviews = nv;
-    ua.prod = prod_;
+    ua.psi_src = bps[0].psi_src;
+    ua.psi_dst = bps[0].psi_dst;
+    ua.weight[0] = w;
+    ua.nviews = 1;
     ua.lambda = lambda_;
     ua.minI = min_value_;
     ua.maxI = maxI;
     ua.partials = partials_;
+    const double nv = (double)pl.b[0] * pl.b[1] * pl.b[2];
+    double bytes = 0.0;
+    for (int i = 0; i < nb; ++i) {
+        const BlockPlace &bp = bps[i];
+        const double neff = (double)(bp.whi[0] - bp.wlo[0]) * (bp.whi[1] - bp.wlo[1]) * (bp.whi[2] - bp.wlo[2]);
+        bytes += sizeof(V) * (double)pl.Pc + (sizeof(T) + 4.0) * nv + sizeof(T) * neff;
+    }
+    return launch_update(pl, bms, nb, S0_, ua, EPI_SEQ, bytes, stats_dev);
+}
+
+template <typename T>
+int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace *bps, int nb,
+                       const float *const *imgs, const float *const *ws, float maxI, double *stats_dev)
+{
+    const int nv = (int)pls.size();
+    if (nv < 1 || nv > kMaxViews) return fail(ERR_ARG, "number of views must be 1..16");
+    if (nb < 1 || nb > kMaxBatch) return fail(ERR_ARG, "batch of 1..16 blocks");
+    UpdateArgs ua{};
+    ua.psi_src = bps[0].psi_src;
+    ua.psi_dst = bps[0].psi_dst;
+    for (int v = 0; v < nv; ++v) ua.weight[v] = ws[v];
+    ua.nviews = nv;
+    ua.lambda = lambda_;
+    ua.minI = min_value_;
+    ua.maxI = maxI;
     const Plan<T> *prev = nullptr;
-    unsigned grid = 0;
     for (int v = 0; v < nv; ++v) {
         const Plan<T> &pl = *pls[v];
         if (!pl.k1h || !pl.k2h) return fail(ERR_STATE, "kernels not set for a view");
-        const BlockMap bm = block_map(pl, bp);
         const long long nrows = (long long)pl.P[1] * pl.P[2];
-        grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
+        const long long bvox = (long long)pl.b[0] * pl.b[1] * pl.b[2];
+        MVR_TRY(reserve(pl.Pc, bvox, (nrows + pl.RP - 1) / pl.RP, nb));
+        if (nv > 1) MVR_TRY(reserve_prod(bvox * nb));
+        ua.prod = prod_;
+        ua.partials = partials_;
+        const BlockMaps bms = block_maps(pl, bps, nb);
         if (!prev || std::memcmp(prev->P, pl.P, sizeof(pl.P)) != 0 || std::memcmp(prev->L, pl.L, sizeof(pl.L)) != 0) {
             // FFT of psi along x and y, shared by every view with this domain
-            MVR_TRY(launch_fwd_mirror(pl, bm, reinterpret_cast<const T *>(bp.psi_src), S0_));
-            MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
+            MVR_TRY(launch_fwd_mirror(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
+            MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
         }
         prev = &pl;
-        MVR_TRY(launch_cols(pl, 2, 2, S0_, S1_, pl.k1h));
-        MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr));
-        const double nb = (double)pl.b[0] * pl.b[1] * pl.b[2];
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S1_, pl.k1h, nb));
+        MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr, nb));
+        MVR_TRY(launch_ratio(pl, bms, nb, S1_, imgs[v]));
+        MVR_TRY(launch_cols(pl, 1, 0, S1_, S1_, nullptr, nb));
+        MVR_TRY(launch_cols(pl, 2, 2, S1_, S1_, pl.k2h, nb));
+        MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr, nb));
         const double sb = (double)sizeof(V) * (double)pl.Pc;
-        MVR_TRY(prof_begin(KK_ROWS_RATIO, 2.0 * sb + 4.0 * nb));
-        MVR_WITH_BIG(pl.big, (k_rows_ratio<T, B><<<grid, kThreads, pl.smem_row, stream_>>>(S1_, imgs[v], bm, pl.dx,
-                                                                                         pl.twx, pl.RP)));
-        MVR_LAUNCHED("k_rows_ratio");
-        MVR_TRY(prof_end());
-        MVR_TRY(launch_cols(pl, 1, 0, S1_, S1_, nullptr));
-        MVR_TRY(launch_cols(pl, 2, 2, S1_, S1_, pl.k2h));
-        MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr));
-        const double neff = (double)(bp.whi[0] - bp.wlo[0]) * (bp.whi[1] - bp.wlo[1]) * (bp.whi[2] - bp.wlo[2]);
-        MVR_TRY(prof_begin(KK_ROWS_UPDATE, v == nv - 1 ? sb + (sizeof(T) + 12.0 + 4.0 * nv) * nb + sizeof(T) * neff
-                                                        : sb + (v == 0 ? 8.0 : 16.0) * nb));
-        if (v == nv - 1) {
-            ua.nviews = nv;
-            MVR_WITH_BIG(pl.big, (k_rows_update<T, EPI_MUL_FINAL, B><<<grid, kThreads, pl.smem_row, stream_>>>(
-                                     S1_, ua, bm, pl.dx, pl.twx, pl.RP)));
-        } else if (v == 0) {
-            MVR_WITH_BIG(pl.big, (k_rows_update<T, EPI_MUL_FIRST, B><<<grid, kThreads, pl.smem_row, stream_>>>(
-                                     S1_, ua, bm, pl.dx, pl.twx, pl.RP)));
-        } else {
-            MVR_WITH_BIG(pl.big, (k_rows_update<T, EPI_MUL_ACC, B><<<grid, kThreads, pl.smem_row, stream_>>>(
-                                     S1_, ua, bm, pl.dx, pl.twx, pl.RP)));
-        }
-        MVR_LAUNCHED("k_rows_update(mul)");
-        MVR_TRY(prof_end());
-    }
-    if (stats_dev) {
-        MVR_TRY(prof_begin(KK_REDUCE, 16.0 * grid));
-        k_reduce_stats<double><<<1, 1024, 0, stream_>>>(partials_, (int)grid, stats_dev);
-        MVR_LAUNCHED("k_reduce_stats");
-        MVR_TRY(prof_end());
+        const double bytes = nb * (v == nv - 1 ? sb + (sizeof(T) + 12.0 + 4.0 * nv) * bvox + sizeof(T) * bvox
+                                               : sb + (v == 0 ? 8.0 : 16.0) * bvox);
+        const int epi = v == nv - 1 ? EPI_MUL_FINAL : (v == 0 ? EPI_MUL_FIRST : EPI_MUL_ACC);
+        MVR_TRY(launch_update(pl, bms, nb, S1_, ua, epi, bytes, stats_dev));
     }
     return OK;
 }
@@ -552,7 +593,8 @@ int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace
 template <typename T>
 int Engine<T>::convolve(const Plan<T> &pl, const T *blk, int src_kind, float *out)
 {
-    BlockMap bm{};
+    BlockMaps bms{};
+    BlockMap &bm = bms.m[0];
     for (int d = 0; d < 3; ++d) {
         bm.P[d] = pl.P[d];
         bm.b[d] = pl.b[d];
@@ -563,24 +605,21 @@ int Engine<T>::convolve(const Plan<T> &pl, const T *blk, int src_kind, float *ou
     }
     bm.fast_x = block_fast_x(bm);
     const long long nrows = (long long)pl.P[1] * pl.P[2];
-    const unsigned grid = (unsigned)((nrows + pl.RP - 1) / pl.RP);
+    const dim3 grid((unsigned)((nrows + pl.RP - 1) / pl.RP), 1);
     if (src_kind == SRC_ZERO)
         MVR_WITH_BIG(pl.big, (k_rows_fwd<T, SrcZero<T>, B><<<grid, kThreads, pl.smem_row, stream_>>>(
-                                 SrcZero<T>{blk}, S0_, bm, pl.dx, pl.twx, pl.RP)));
+                                 SrcZero<T>{blk}, S0_, bms, pl.Pc, pl.dx, pl.twx, pl.RP)));
     else
         MVR_WITH_BIG(pl.big, (k_rows_fwd<T, SrcMirror<T>, B><<<grid, kThreads, pl.smem_row, stream_>>>(
-                                 SrcMirror<T>{blk}, S0_, bm, pl.dx, pl.twx, pl.RP)));
+                                 SrcMirror<T>{blk}, S0_, bms, pl.Pc, pl.dx, pl.twx, pl.RP)));
     MVR_LAUNCHED("k_rows_fwd(conv)");
-    MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr));
-    MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h));
-    MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr));
+    MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, 1));
+    MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, 1));
+    MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr, 1));
     UpdateArgs ua{};
     ua.store = out;
     ua.partials = partials_;
-    MVR_WITH_BIG(pl.big, (k_rows_update<T, EPI_STORE, B><<<grid, kThreads, pl.smem_row, stream_>>>(S0_, ua, bm, pl.dx,
-                                                                                                 pl.twx, pl.RP)));
-    MVR_LAUNCHED("k_rows_update(store)");
-    return OK;
+    return launch_update(pl, bms, 1, S0_, ua, EPI_STORE, 0.0, nullptr);
 }
 
 template class Engine<float>;

@@ -84,11 +84,13 @@ public:
                   const int kd2[3], bool k_on_device = false);
     void free_plan(Plan<T> &pl);
 
-    // One sequential iteration (ComputeBlockSeqThread.runIteration) of view plan pl.
-    int run_seq(const Plan<T> &pl, const BlockPlace &bp, const float *img, const float *w, float maxI,
+    // One sequential iteration (ComputeBlockSeqThread.runIteration) of view plan pl on
+    // nb (1..16) blocks in one batched launch per pass; all blocks read the same psi
+    // source and write the same output volume.  stats_dev: 2 doubles per block.
+    int run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const float *img, const float *w, float maxI,
                 double *stats_dev);
     // One multiplicative iteration over views (ComputeBlockMulThread.runIteration).
-    int run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace &bp, const float *const *imgs,
+    int run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace *bps, int nb, const float *const *imgs,
                 const float *const *ws, float maxI, double *stats_dev);
     // Linear convolution of a T block (mirror or zero extension) with pl's k1, result
     // to a float block of the same size.
@@ -106,12 +108,16 @@ public:
     const std::string &error() const { return err_; }
     int fail(int code, const std::string &msg);
     int cuda_check(cudaError_t e, const char *what);
-    int reserve(long long Pc, long long nvox_block, long long rows);
+    int reserve(long long Pc, long long nvox_block, long long rows, int nb);
+    int reserve_prod(long long n);
 
 private:
-    int launch_fwd_mirror(const Plan<T> &pl, const BlockMap &bm, const T *src, V *S);
-    int launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh);
-    BlockMap block_map(const Plan<T> &pl, const BlockPlace &bp) const;
+    int launch_fwd_mirror(const Plan<T> &pl, const BlockMaps &bms, int nb, const T *src, V *S);
+    int launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh, int nb);
+    int launch_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img);
+    int launch_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const UpdateArgs &ua, int epi,
+                      double bytes, double *stats_dev);
+    BlockMaps block_maps(const Plan<T> &pl, const BlockPlace *bps, int nb) const;
 
     int device_ = -1;
     int boundary_ = BOUNDARY_REFERENCE;

@@ -39,6 +39,13 @@ struct BlockMap {
     int fast_x;          // 1: domain x == block x and the block row lies inside the volume
 };
 
+// The blocks of one batched launch: blockIdx.y (rows) / blockIdx.z (columns) picks
+// the block; block i's spectrum starts at i * Pc.
+constexpr int kMaxBatch = 16;
+struct BlockMaps {
+    BlockMap m[kMaxBatch];
+};
+
 // 1 when every domain x maps to volume x = off + x without extension or mirroring.
 inline int block_fast_x(const BlockMap &m)
 {
@@ -211,10 +218,13 @@ __device__ __forceinline__ void c2r_pre_load(const V *__restrict__ S, V *A, int 
 
 // ---- forward row pass with a fused source -------------------------------------------
 template <typename T, class Src, bool BIG>
-__global__ void __launch_bounds__(256) k_rows_fwd(Src src, typename Cx<T>::t *__restrict__ S, BlockMap bm, FftDesc d,
-                                                  const typename Cx<T>::t *__restrict__ twg, int RP)
+__global__ void __launch_bounds__(256) k_rows_fwd(Src src, typename Cx<T>::t *__restrict__ S, const BlockMaps bms,
+                                                  long long Pc, FftDesc d, const typename Cx<T>::t *__restrict__ twg,
+                                                  int RP)
 {
     typedef typename Cx<T>::t V;
+    const BlockMap &bm = bms.m[blockIdx.y];
+    S += (long long)blockIdx.y * Pc;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int Px = bm.P[0], m = Px >> 1, ps = m + 1;
     V *tw = reinterpret_cast<V *>(smem_raw);
@@ -260,7 +270,7 @@ constexpr int kLoadBatch = 8;
 template <typename T, int MODE, bool BIG>
 __global__ void __launch_bounds__(256) k_cols(const typename Cx<T>::t *src, typename Cx<T>::t *dst,
                                               const typename Cx<T>::t *__restrict__ Kh, int Hx, long long estride,
-                                              long long ostride, int NP, FftDesc d,
+                                              long long ostride, int NP, long long Pc, FftDesc d,
                                               const typename Cx<T>::t *__restrict__ twg)
 {
     typedef typename Cx<T>::t V;
@@ -272,6 +282,8 @@ __global__ void __launch_bounds__(256) k_cols(const typename Cx<T>::t *src, type
     load_twiddles(tw, twg, n);
     const int x0 = blockIdx.x * NP;
     const long long base = (long long)blockIdx.y * ostride + x0;
+    src += (long long)blockIdx.z * Pc;
+    dst += (long long)blockIdx.z * Pc;
     const int np = min(NP, Hx - x0);
     const int tot = n * NP;
     const int lg = __ffs(NP) - 1;
@@ -366,10 +378,12 @@ __device__ __forceinline__ double next_value(double last, double integral, doubl
 // ---- C2R -> quotient -> R2C (conv1 of one view, then the input of conv2) -------------
 template <typename T, bool BIG>
 __global__ void __launch_bounds__(256) k_rows_ratio(typename Cx<T>::t *__restrict__ S, const float *__restrict__ img,
-                                                    BlockMap bm, FftDesc d, const typename Cx<T>::t *__restrict__ twg,
-                                                    int RP)
+                                                    const BlockMaps bms, long long Pc, FftDesc d,
+                                                    const typename Cx<T>::t *__restrict__ twg, int RP)
 {
     typedef typename Cx<T>::t V;
+    const BlockMap &bm = bms.m[blockIdx.y];
+    S += (long long)blockIdx.y * Pc;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int Px = bm.P[0], m = Px >> 1, ps = m + 1;
     V *tw = reinterpret_cast<V *>(smem_raw);
@@ -437,10 +451,16 @@ struct UpdateArgs {
 };
 
 template <typename T, int EPI, bool BIG>
-__global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restrict__ S, UpdateArgs ua, BlockMap bm,
-                                                     FftDesc d, const typename Cx<T>::t *__restrict__ twg, int RP)
+__global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restrict__ S, UpdateArgs ua,
+                                                     const BlockMaps bms, long long Pc, FftDesc d,
+                                                     const typename Cx<T>::t *__restrict__ twg, int RP)
 {
     typedef typename Cx<T>::t V;
+    const BlockMap &bm = bms.m[blockIdx.y];
+    S += (long long)blockIdx.y * Pc;
+    const long long bvox = (long long)bm.b[0] * bm.b[1] * bm.b[2];
+    if (ua.prod) ua.prod += (long long)blockIdx.y * bvox;
+    if (ua.store) ua.store += (long long)blockIdx.y * bvox;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double red_s[32], red_m[32];
     const int Px = bm.P[0], m = Px >> 1, ps = m + 1;
@@ -544,8 +564,9 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
         if (threadIdx.x == 0) {
             double s = 0.0, mx = -1.0;
             for (int w = 0; w < nw; ++w) { s += red_s[w]; mx = fmax(mx, red_m[w]); }
-            ua.partials[2 * blockIdx.x] = s;
-            ua.partials[2 * blockIdx.x + 1] = mx;
+            const long long slot = (long long)blockIdx.y * gridDim.x + blockIdx.x;
+            ua.partials[2 * slot] = s;
+            ua.partials[2 * slot + 1] = mx;
         }
     }
 }
@@ -554,6 +575,8 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
 template <typename D>
 __global__ void k_reduce_stats(const D *__restrict__ partials, int n, D *out)
 {
+    partials += 2LL * n * blockIdx.x;  // block of the batch
+    out += 2 * blockIdx.x;
     __shared__ double s_s[1024], s_m[1024];
     double s = 0.0, mx = -1.0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) { s += partials[2 * i]; mx = fmax(mx, partials[2 * i + 1]); }

@@ -137,8 +137,10 @@ extern "C" int mvr_convolve_static(const float *img, const int img_size[3], cons
     const dim3 gz((unsigned)((Hx + NPz - 1) / NPz), (unsigned)P[1]);
     const long long ey = Hx, oy = (long long)P[1] * Hx, ez = (long long)P[1] * Hx, oz = Hx;
 
-    BlockMap km{};  // the kernel's spectrum: whole domain
-    BlockMap bm{};  // the image: block at the origin, k-1-k/2 wrapped before it
+    BlockMaps kms{};  // the kernel's spectrum: whole domain
+    BlockMaps bms{};  // the image: block at the origin, k-1-k/2 wrapped before it
+    BlockMap &km = kms.m[0];
+    BlockMap &bm = bms.m[0];
     for (int d = 0; d < 3; ++d) {
         km.P[d] = km.b[d] = P[d];
         km.D[d] = P[d];
@@ -151,16 +153,16 @@ extern "C" int mvr_convolve_static(const float *img, const int img_size[3], cons
     }
     const double scale = 1.0 / ((double)P[0] * P[1] * P[2]);
     k_rows_fwd<float, SrcKernel, true><<<grid_rows, 256, smem_row, s>>>(SrcKernel{kernel, {kd[0], kd[1], kd[2]}, scale}, Sk,
-                                                                 km, dx, tw[0], RP);
-    k_cols<float, 0, true><<<gy, 256, smem_y, s>>>(Sk, Sk, nullptr, (int)Hx, ey, oy, NPy, dy, tw[1]);
-    k_cols<float, 0, true><<<gz, 256, smem_z, s>>>(Sk, Sk, nullptr, (int)Hx, ez, oz, NPz, dz, tw[2]);
-    k_rows_fwd<float, SrcZero<float>, true><<<grid_rows, 256, smem_row, s>>>(SrcZero<float>{img}, S, bm, dx, tw[0], RP);
-    k_cols<float, 0, true><<<gy, 256, smem_y, s>>>(S, S, nullptr, (int)Hx, ey, oy, NPy, dy, tw[1]);
-    k_cols<float, 2, true><<<gz, 256, smem_z, s>>>(S, S, Sk, (int)Hx, ez, oz, NPz, dz, tw[2]);
-    k_cols<float, 1, true><<<gy, 256, smem_y, s>>>(S, S, nullptr, (int)Hx, ey, oy, NPy, dy, tw[1]);
+                                                                 kms, Pc, dx, tw[0], RP);
+    k_cols<float, 0, true><<<gy, 256, smem_y, s>>>(Sk, Sk, nullptr, (int)Hx, ey, oy, NPy, Pc, dy, tw[1]);
+    k_cols<float, 0, true><<<gz, 256, smem_z, s>>>(Sk, Sk, nullptr, (int)Hx, ez, oz, NPz, Pc, dz, tw[2]);
+    k_rows_fwd<float, SrcZero<float>, true><<<grid_rows, 256, smem_row, s>>>(SrcZero<float>{img}, S, bms, Pc, dx, tw[0], RP);
+    k_cols<float, 0, true><<<gy, 256, smem_y, s>>>(S, S, nullptr, (int)Hx, ey, oy, NPy, Pc, dy, tw[1]);
+    k_cols<float, 2, true><<<gz, 256, smem_z, s>>>(S, S, Sk, (int)Hx, ez, oz, NPz, Pc, dz, tw[2]);
+    k_cols<float, 1, true><<<gy, 256, smem_y, s>>>(S, S, nullptr, (int)Hx, ey, oy, NPy, Pc, dy, tw[1]);
     UpdateArgs ua{};
     ua.store = out;
-    k_rows_update<float, EPI_STORE, true><<<grid_rows, 256, smem_row, s>>>(S, ua, bm, dx, tw[0], RP);
+    k_rows_update<float, EPI_STORE, true><<<grid_rows, 256, smem_row, s>>>(S, ua, bms, Pc, dx, tw[0], RP);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         put_error(err, err_len, cudaGetErrorString(e));

@@ -43,7 +43,7 @@ EXPORTS = [
     "mvr_decon_set_psi_device", "mvr_decon_get_psi", "mvr_decon_run", "mvr_decon_get_kernels",
     "mvr_decon_get_max", "mvr_decon_get_weights", "mvr_decon_psi_device", "mvr_decon_synchronize",
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
-    "mvr_kernel_name", "mvr_convolve_static",
+    "mvr_kernel_name", "mvr_convolve_static", "mvr_decon_batch",
     "convolution3DfftCUDA", "convolution3DfftCUDAInPlace", "getNumDevicesCUDA", "getNameDeviceCUDA",
     "getMemDeviceCUDA", "getFreeMemDeviceCUDA", "getCUDAcomputeCapabilityMajorVersion",
     "getCUDAcomputeCapabilityMinorVersion", "mvr_free",
@@ -66,7 +66,8 @@ class _DeconParams(C.Structure):
                 ("psf_type", C.c_int), ("psf_norm_threads", C.c_int), ("lambda_", C.c_float),
                 ("min_value", C.c_float), ("boundary", C.c_int), ("precision", C.c_int),
                 ("filter_blocks", C.c_int), ("weight_norm", C.c_int), ("osem_speedup", C.c_float),
-                ("max_diff_range", C.c_float), ("scaling_range", C.c_float), ("device", C.c_int)]
+                ("max_diff_range", C.c_float), ("scaling_range", C.c_float), ("batch_blocks", C.c_int),
+                ("device", C.c_int)]
 
 
 _lib = None
@@ -134,6 +135,7 @@ def load() -> C.CDLL:
     L.mvr_kernel_name.argtypes = [C.c_int]
     L.mvr_kernel_name.restype = C.c_char_p
     L.mvr_convolve_static.argtypes = [P, P, P, P, P, P, C.c_char_p, C.c_int]
+    L.mvr_decon_batch.argtypes = [P]
     _lib = L
     return L
 
@@ -249,11 +251,11 @@ class Deconvolution:
     def __init__(self, dims, num_views, block_size, mul=False, psf_type=PSF_OPTIMIZATION_I,
                  psf_norm_threads=0, lam=0.006, min_value=1e-4, boundary=BOUNDARY_REFERENCE,
                  precision=PRECISION_FP32, filter_blocks=True, weight_norm=WEIGHTS_AS_GIVEN, osem_speedup=1.0,
-                 max_diff_range=0.1, scaling_range=0.05, device=0):
+                 max_diff_range=0.1, scaling_range=0.05, batch_blocks=0, device=0):
         self._lib = load()
         prm = _DeconParams((C.c_int * 3)(*dims), num_views, (C.c_int * 3)(*block_size), int(mul), psf_type,
                            psf_norm_threads, lam, min_value, boundary, precision, int(filter_blocks), weight_norm,
-                           osem_speedup, max_diff_range, scaling_range, device)
+                           osem_speedup, max_diff_range, scaling_range, batch_blocks, device)
         h = C.c_void_p()
         rc = self._lib.mvr_decon_create(C.byref(prm), C.byref(h))
         if rc != OK:
@@ -349,6 +351,10 @@ class Deconvolution:
     def stream_ptr(self) -> int:
         """cudaStream_t of the handle (for torch.cuda.ExternalStream / events)."""
         return int(self._lib.mvr_decon_stream(self._h) or 0)
+
+    def batch(self) -> int:
+        """Blocks per batched launch in use."""
+        return int(self._lib.mvr_decon_batch(self._h))
 
     def launch_count(self) -> int:
         return int(self._lib.mvr_decon_launch_count(self._h))
