@@ -192,6 +192,11 @@ MVR_API int mvr_decon_get_profile(mvr_decon *h, double *ms, long long *launches,
 MVR_API const char *mvr_kernel_name(int kind);
 /* Blocks per batched launch in use (chosen by the autotuner unless fixed). */
 MVR_API int mvr_decon_batch(const mvr_decon *h);
+/* Data-likelihood residual of the current psi (no reference counterpart; the reference
+ * logs only the change statistics): the Poisson negative log-likelihood
+ * sum_v sum_x w_v (conv1_v - img_v ln conv1_v) over img_v > 0, each voxel once, reduced
+ * in FP64.  per_view (or NULL) receives num_views partial sums. */
+MVR_API int mvr_decon_likelihood(mvr_decon *h, double *total, double *per_view);
 
 /* ---- convolution without device allocation ------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot call

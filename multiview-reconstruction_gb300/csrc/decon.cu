@@ -342,6 +342,7 @@ public:
     virtual void set_profiling(bool on) = 0;
     virtual int profile(KernelProfile &out) = 0;
     virtual int batch() const = 0;
+    virtual int likelihood(double *total, double *per_view) = 0;
 };
 
 template <typename T>
@@ -368,6 +369,7 @@ public:
     void set_profiling(bool on) override { engine_.set_profiling(on); }
     int profile(KernelProfile &out) override { return eng(engine_.profile_collect(out)); }
     int batch() const override { return batch_; }
+    int likelihood(double *total, double *per_view) override;
 
 private:
     struct View {
@@ -1001,6 +1003,63 @@ int Decon<T>::run(int iterations, double *stats)
     return MVR_OK;
 }
 
+// Poisson negative log-likelihood of the current psi, summed over views in FP64:
+// sum_v sum_x w_v (conv1_v - img_v ln conv1_v) over img_v > 0 (each voxel once).
+template <typename T>
+int Decon<T>::likelihood(double *total, double *per_view)
+{
+    if (!prepared_) return fail(MVR_ERR_STATE, "mvr_decon_prepare was not called");
+    D_CUDA(cudaSetDevice(p_.device));
+    if (weights_dirty_) D_TRY(normalize_weights());
+    cudaStream_t s = engine_.stream();
+    const long long D[3] = {p_.dims[0], p_.dims[1], p_.dims[2]};
+    size_t maxb = 1;
+    for (auto &b : blocks_) maxb = std::max(maxb, b.size());
+    const long long need = (long long)p_.num_views * (long long)maxb * 2;
+    if (need > stats_cap_) {
+        cudaFree(d_stats_);
+        d_stats_ = nullptr;
+        stats_cap_ = 0;
+        D_CUDA(cudaMalloc(&d_stats_, sizeof(double) * (size_t)need));
+        stats_cap_ = need;
+    }
+    for (int v = 0; v < p_.num_views; ++v) {
+        const std::vector<BlockDesc> &bl = blocks_[p_.mul ? 0 : v];
+        const View &vw = views_[v];
+        for (size_t i0 = 0; i0 < bl.size(); i0 += (size_t)batch_) {
+            std::vector<BlockPlace> bps;
+            for (size_t i = i0; i < std::min(bl.size(), i0 + (size_t)batch_); ++i) {
+                const BlockDesc &b = bl[i];
+                BlockPlace bp;
+                bp.psi_src = psi_;
+                for (int d = 0; d < 3; ++d) {
+                    bp.D[d] = D[d];
+                    bp.off[d] = b.off[d];
+                    bp.OD[d] = D[d];
+                    bp.ooff[d] = b.off[d];
+                    bp.wlo[d] = b.eloc[d];
+                    bp.whi[d] = b.eloc[d] + b.esize[d];
+                }
+                bps.push_back(bp);
+            }
+            D_TRY(eng(engine_.likelihood(vw.plan, bps.data(), (int)bps.size(), vw.img, vw.w,
+                                         d_stats_ + ((size_t)v * maxb + i0) * 2)));
+        }
+    }
+    std::vector<double> hs((size_t)need);
+    D_CUDA(cudaMemcpyAsync(hs.data(), d_stats_, sizeof(double) * (size_t)need, cudaMemcpyDeviceToHost, s));
+    D_CUDA(cudaStreamSynchronize(s));
+    double tot = 0.0;
+    for (int v = 0; v < p_.num_views; ++v) {
+        double sv = 0.0;
+        for (size_t b = 0; b < blocks_[p_.mul ? 0 : v].size(); ++b) sv += hs[((size_t)v * maxb + b) * 2];
+        if (per_view) per_view[v] = sv;
+        tot += sv;
+    }
+    if (total) *total = tot;
+    return MVR_OK;
+}
+
 template class Decon<float>;
 template class Decon<double>;
 
@@ -1119,3 +1178,7 @@ extern "C" int mvr_decon_get_profile(mvr_decon *h, double *ms, long long *launch
 }
 extern "C" const char *mvr_kernel_name(int kind) { return mvr::kernel_kind_name(kind); }
 extern "C" int mvr_decon_batch(const mvr_decon *h) { return h ? h->impl->batch() : -1; }
+extern "C" int mvr_decon_likelihood(mvr_decon *h, double *total, double *per_view)
+{
+    return h ? h->impl->likelihood(total, per_view) : MVR_ERR_ARG;
+}

@@ -490,6 +490,10 @@ int Engine<T>::launch_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V 
             k_rows_update<T, EPI_MUL_FINAL, B><<<grid, kThreads, pl.smem_row, stream_>>>(S, ua, bms, pl.Pc, pl.dx,
                                                                                          pl.twx, pl.RP);
             break;
+        case EPI_NLL:
+            k_rows_update<T, EPI_NLL, B><<<grid, kThreads, pl.smem_row, stream_>>>(S, ua, bms, pl.Pc, pl.dx, pl.twx,
+                                                                                   pl.RP);
+            break;
         default:
             k_rows_update<T, EPI_STORE, B><<<grid, kThreads, pl.smem_row, stream_>>>(S, ua, bms, pl.Pc, pl.dx, pl.twx,
                                                                                      pl.RP);
@@ -498,7 +502,7 @@ int Engine<T>::launch_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V 
     });
     MVR_LAUNCHED("k_rows_update");
     MVR_TRY(prof_end());
-    if (stats_dev && (epi == EPI_SEQ || epi == EPI_MUL_FINAL)) {
+    if (stats_dev && (epi == EPI_SEQ || epi == EPI_MUL_FINAL || epi == EPI_NLL)) {
         MVR_TRY(prof_begin(KK_REDUCE, 16.0 * gx * nb));
         k_reduce_stats<double><<<nb, 1024, 0, stream_>>>(partials_, (int)gx, stats_dev);
         MVR_LAUNCHED("k_reduce_stats");
@@ -588,6 +592,29 @@ int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace
         MVR_TRY(launch_update(pl, bms, nb, S1_, ua, epi, bytes, stats_dev));
     }
     return OK;
+}
+
+template <typename T>
+int Engine<T>::likelihood(const Plan<T> &pl, const BlockPlace *bps, int nb, const float *img, const float *w,
+                          double *stats_dev)
+{
+    if (!pl.k1h) return fail(ERR_STATE, "kernels not set for this view");
+    if (nb < 1 || nb > kMaxBatch) return fail(ERR_ARG, "batch of 1..16 blocks");
+    const long long nrows = (long long)pl.P[1] * pl.P[2];
+    MVR_TRY(reserve(pl.Pc, (long long)pl.b[0] * pl.b[1] * pl.b[2], (nrows + pl.RP - 1) / pl.RP, nb));
+    const BlockMaps bms = block_maps(pl, bps, nb);
+    MVR_TRY(launch_fwd_mirror(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
+    MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
+    MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb));
+    MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr, nb));
+    UpdateArgs ua{};
+    ua.psi_src = bps[0].psi_src;
+    ua.img = img;
+    ua.weight[0] = w;
+    ua.nviews = 1;
+    ua.partials = partials_;
+    const double nv = (double)pl.b[0] * pl.b[1] * pl.b[2];
+    return launch_update(pl, bms, nb, S0_, ua, EPI_NLL, nb * (sizeof(V) * (double)pl.Pc + 8.0 * nv), stats_dev);
 }
 
 template <typename T>

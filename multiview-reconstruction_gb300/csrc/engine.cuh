@@ -92,6 +92,11 @@ public:
     // One multiplicative iteration over views (ComputeBlockMulThread.runIteration).
     int run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace *bps, int nb, const float *const *imgs,
                 const float *const *ws, float maxI, double *stats_dev);
+    // Poisson negative log-likelihood of psi under view pl: per block (stats_dev, 2
+    // doubles each, [0] = sum) the FP64 sum over the block's write region of
+    // w * (conv1 - img ln conv1) where img > 0.
+    int likelihood(const Plan<T> &pl, const BlockPlace *bps, int nb, const float *img, const float *w,
+                   double *stats_dev);
     // Linear convolution of a T block (mirror or zero extension) with pl's k1, result
     // to a float block of the same size.
     int convolve(const Plan<T> &pl, const T *blk, int src_kind, float *out);

@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(256) k_rows_ratio(typename Cx<T>::t *__restric
 }
 
 // ---- C2R -> update -------------------------------------------------------------------
-enum { EPI_SEQ = 0, EPI_MUL_FIRST = 1, EPI_MUL_ACC = 2, EPI_MUL_FINAL = 3, EPI_STORE = 4 };
+enum { EPI_SEQ = 0, EPI_MUL_FIRST = 1, EPI_MUL_ACC = 2, EPI_MUL_FINAL = 3, EPI_STORE = 4, EPI_NLL = 5 };
 
 struct UpdateArgs {
     const void *psi_src;  // T volume, read under the mirror mapping
@@ -444,6 +444,7 @@ struct UpdateArgs {
     int nviews;
     double *prod;         // Mul: running product over views, block layout [bz][by][bx]
     float *store;         // EPI_STORE: conv result, block layout
+    const float *img;     // EPI_NLL: the view's image (zero outside the volume)
     double lambda;
     float minI;
     float maxI;
@@ -524,6 +525,21 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
                         continue;
                     }
                     if (EPI == EPI_MUL_FIRST) { ua.prod[brow + x] = (double)integral; continue; }
+                    if (EPI == EPI_NLL) {
+                        // Poisson negative log-likelihood w * (conv1 - img ln conv1) over img > 0,
+                        // each volume voxel once (write region of its block)
+                        if (!(wrow && x >= bm.wlo[0] && x < bm.whi[0])) continue;
+                        const float im = zero_at(ua.img, bm, zr, x);
+                        const float wt = zero_at(ua.weight[0], bm, zr, x);
+                        if (!(im > 0.0f) || !(integral > (T)0)) continue;
+                        const T lg = sizeof(T) == sizeof(float) ? (T)logf((float)integral) : (T)log((double)integral);
+                        const T term = (T)wt * (integral - (T)im * lg);
+                        const T ky = term - kcomp;
+                        const T kt = ksum + ky;
+                        kcomp = (kt - ksum) - ky;
+                        ksum = kt;
+                        continue;
+                    }
                     if (EPI == EPI_MUL_ACC) { ua.prod[brow + x] *= (double)integral; continue; }
                     const T last = lastv[u][h];
                     T next;
@@ -552,7 +568,7 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
             }
         }
     }
-    if (EPI == EPI_SEQ || EPI == EPI_MUL_FINAL) {
+    if (EPI == EPI_SEQ || EPI == EPI_MUL_FINAL || EPI == EPI_NLL) {
         // deterministic block reduction -> partials[blockIdx.x]
         double lsum = (double)ksum - (double)kcomp, lmax = (double)kmax;
         for (int o = 16; o > 0; o >>= 1) {

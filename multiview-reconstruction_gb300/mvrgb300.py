@@ -43,7 +43,7 @@ EXPORTS = [
     "mvr_decon_set_psi_device", "mvr_decon_get_psi", "mvr_decon_run", "mvr_decon_get_kernels",
     "mvr_decon_get_max", "mvr_decon_get_weights", "mvr_decon_psi_device", "mvr_decon_synchronize",
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
-    "mvr_kernel_name", "mvr_convolve_static", "mvr_decon_batch",
+    "mvr_kernel_name", "mvr_convolve_static", "mvr_decon_batch", "mvr_decon_likelihood",
     "convolution3DfftCUDA", "convolution3DfftCUDAInPlace", "getNumDevicesCUDA", "getNameDeviceCUDA",
     "getMemDeviceCUDA", "getFreeMemDeviceCUDA", "getCUDAcomputeCapabilityMajorVersion",
     "getCUDAcomputeCapabilityMinorVersion", "mvr_free",
@@ -136,6 +136,7 @@ def load() -> C.CDLL:
     L.mvr_kernel_name.restype = C.c_char_p
     L.mvr_convolve_static.argtypes = [P, P, P, P, P, P, C.c_char_p, C.c_int]
     L.mvr_decon_batch.argtypes = [P]
+    L.mvr_decon_likelihood.argtypes = [P, P, P]
     _lib = L
     return L
 
@@ -351,6 +352,13 @@ class Deconvolution:
     def stream_ptr(self) -> int:
         """cudaStream_t of the handle (for torch.cuda.ExternalStream / events)."""
         return int(self._lib.mvr_decon_stream(self._h) or 0)
+
+    def likelihood(self):
+        """Poisson NLL of the current psi: (total, per-view array), FP64 sums."""
+        tot = np.zeros(1, np.float64)
+        pv = np.zeros(self.num_views, np.float64)
+        self._check(self._lib.mvr_decon_likelihood(self._h, _p(tot), _p(pv)))
+        return float(tot[0]), pv
 
     def batch(self) -> int:
         """Blocks per batched launch in use."""

@@ -147,3 +147,22 @@ def test_errors(vol):
         with pytest.raises(M.MvrError) as e:
             d.prepare()
         assert e.value.code == M.ERR_ARG
+
+
+def test_likelihood_residual(vol):
+    """FP64 Poisson NLL sum_v sum_x w_v (conv1_v - img_v ln conv1_v), img_v > 0, against
+    the oracle's whole-volume convolution with mirror-single extension."""
+    with make(vol, (28, 28, 28)) as d:
+        d.run_iterations(1)
+        psi = d.get_psi()
+        tot, pv = d.likelihood()
+    ref_tot = 0.0
+    for v in range(2):
+        c1 = O.convolve(psi, vol[f"k1_{v}"], O.EXT_MIRROR_SINGLE)
+        img = vol[f"img{v}"].astype(np.float64)
+        w = vol[f"w{v}"].astype(np.float64)
+        m = (img > 0) & (c1 > 0)
+        ref = float((w[m] * (c1[m] - img[m] * np.log(c1[m]))).sum())
+        assert abs(pv[v] - ref) <= 1e-5 * abs(ref)
+        ref_tot += ref
+    assert abs(tot - ref_tot) <= 1e-5 * abs(ref_tot)
