@@ -198,6 +198,43 @@ MVR_API int mvr_decon_batch(const mvr_decon *h);
  * in FP64.  per_view (or NULL) receives num_views partial sums. */
 MVR_API int mvr_decon_likelihood(mvr_decon *h, double *total, double *per_view);
 
+/* ---- learned multi-iteration proposal (no counterpart in the reference) ---------------
+ * A 3-level 3D U-Net (16/32/64 channels, 3x3x3 convolutions, BF16 weights and
+ * activations, FP32 accumulation on the tcgen05 tensor cores) with its own forward and
+ * backward kernels and Adam, for patches [batch][z][y][x] of sizes {x, y, z} (multiples
+ * of 4).  Inputs are device float volumes: psi_k and the plain method's one-iteration
+ * ratio psi_{k+1} / psi_k; the network predicts log(psi_{k+m} / psi_k).  Callers gate
+ * its proposals with mvr_decon_likelihood. */
+typedef struct mvr_unet mvr_unet;
+MVR_API int mvr_unet_create(int batch, const int dims[3], unsigned seed, int device, mvr_unet **out);
+MVR_API void mvr_unet_destroy(mvr_unet *h);
+MVR_API const char *mvr_unet_last_error(const mvr_unet *h);
+MVR_API long long mvr_unet_num_params(const mvr_unet *h);
+/* FP32 master parameters (host copies): per layer W[co][27][ci] then b[co], head w[16], b. */
+MVR_API int mvr_unet_get_params(mvr_unet *h, float *params);
+MVR_API int mvr_unet_set_params(mvr_unet *h, const float *params);
+/* Gradients of the last training step (same layout as the parameters). */
+MVR_API int mvr_unet_get_grads(mvr_unet *h, float *grads);
+/* Features from psi_k and ratio_k (device, may be NULL) and the target
+ * log(psi_target / psi_k) (psi_target may be NULL for inference). */
+MVR_API int mvr_unet_set_input(mvr_unet *h, const float *psi, const float *ratio, const float *psi_target);
+/* Forward pass; pred (device, or NULL) receives the predicted log-ratio. */
+MVR_API int mvr_unet_forward(mvr_unet *h, float *pred);
+/* Forward, mean-squared-error loss against the target, backward, one Adam step. */
+MVR_API int mvr_unet_train_step(mvr_unet *h, float lr, double *loss);
+/* Forward and psi_out = psi * exp(clamp(pred, -cap, cap)) (device volumes). */
+MVR_API int mvr_unet_propose(mvr_unet *h, const float *psi, float *psi_out, float cap);
+/* One 3x3x3 convolution layer on the tensor cores (device BF16 [B][z][y][x][C] volumes,
+ * dims {x, y, z, B}): transposed == 0 is the forward pass (weights [n_out][27][c_act],
+ * bias, ReLU, BF16 output), transposed == 1 the data gradient (weights transposed
+ * [n_out][27][c_act], FP32 output).  err_dev: device int, set on a tensor-core timeout. */
+MVR_API int mvr_conv3d_tc(const void *act, int c_act, const void *weights, int n_out, const float *bias, int relu,
+                          int transposed, void *out, const int dims[4], int *err_dev, void *stream);
+/* Weight gradient dw[c_out][27][c_in] += sum_n g[n][c_out] x[n + off][c_in] (FP32). */
+MVR_API int mvr_conv3d_tc_wgrad(const void *x, int c_in, const void *g, int c_out, float *dw, const int dims[4],
+                                int *err_dev, void *stream);
+MVR_API const char *mvr_conv3d_tc_last_error(void);
+
 /* ---- convolution without device allocation ------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot call
  * cudaMalloc -- code running inside another framework's CUDA context whose caching

@@ -1,0 +1,258 @@
+// 3x3x3 convolution (stride 1, zero padding 1) on channels-last BF16 volumes as
+// implicit GEMMs on the tcgen05 tensor cores, FP32 accumulation in tensor memory.
+//
+//   forward  Y[n][co] = act( sum_{t,ci} X[n + off(t)][ci] W[co][t][ci] + b[co] )
+//            M = 128 voxels per CTA, N = C_out, K = 27 C_in, one tap per stage
+//   dgrad    dX[n][ci] = sum_{t,co} G[n - off(t)][co] W[co][t][ci]
+//            the same kernel with the offsets negated and WT[ci][t][co] as B
+//   wgrad    dW[co][t][ci] += sum_n G[n][co] X[n + off(t)][ci]
+//            M = 128 (t, ci) rows per CTA, N = C_out, K = voxels (split over CTAs,
+//            FP32 atomics into dW)
+//
+// Volumes are [B][D][H][W][C] (x fastest, then y, z, batch), C a multiple of 16.
+// Stages are double buffered: the gather of tap t+1 overlaps the MMAs of tap t; a
+// buffer is refilled only after the mbarrier of its previous MMAs completed.  Every
+// wait is bounded and reports a timeout through err instead of hanging.
+#pragma once
+#include "tcgen05.cuh"
+
+namespace mvr {
+
+struct ConvGeom {
+    int B, D, H, W;
+    long long nvox;  // B * D * H * W
+};
+
+constexpr long long kTcWaitIter = 1LL << 24;
+
+__device__ __forceinline__ void vox_coords(const ConvGeom &g, long long n, int &x, int &y, int &z, int &b)
+{
+    x = (int)(n % g.W);
+    long long t = n / g.W;
+    y = (int)(t % g.H);
+    t /= g.H;
+    z = (int)(t % g.D);
+    b = (int)(t / g.D);
+}
+
+// Index of the neighbour of (x,y,z,b) at tap t (offsets in {-1,0,1}, times sign), or
+// -1 outside the volume.
+__device__ __forceinline__ long long neighbour(const ConvGeom &g, int x, int y, int z, int b, int t, int sign)
+{
+    const int dz = (t / 9 - 1) * sign, dy = ((t / 3) % 3 - 1) * sign, dx = (t % 3 - 1) * sign;
+    const int xx = x + dx, yy = y + dy, zz = z + dz;
+    if (xx < 0 || yy < 0 || zz < 0 || xx >= g.W || yy >= g.H || zz >= g.D) return -1;
+    return (((long long)b * g.D + zz) * g.H + yy) * g.W + xx;
+}
+
+template <int N>
+struct TmemCols {
+    static constexpr uint32_t value = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+};
+
+// OUT_MODE 0: BF16 output with bias (+ReLU when relu != 0); 1: FP32 output, no bias.
+template <int N, int C, int OUT_MODE>
+__global__ void __launch_bounds__(128) k_conv3d_tc(const __nv_bfloat16 *__restrict__ act,
+                                                   const __nv_bfloat16 *__restrict__ wk, const float *__restrict__ bias,
+                                                   void *out, ConvGeom g, int sign, int relu, int *err)
+{
+    static_assert(N % 16 == 0 && N <= 256 && C % 16 == 0 && C <= 128, "tile shape");
+    constexpr int A_BYTES = 128 * C * 2, B_BYTES = N * C * 2;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *sA[2] = {smem, smem + A_BYTES};
+    uint8_t *sB[2] = {smem + 2 * A_BYTES, smem + 2 * A_BYTES + B_BYTES};
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    constexpr uint32_t ncols = TmemCols<N>::value;
+    if (warp == 0) tc::tmem_alloc(&tbase, ncols);
+    if (tid == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tbase;
+    const long long n = (long long)blockIdx.x * 128 + tid;  // this thread's row (voxel)
+    int x = 0, y = 0, z = 0, b = 0;
+    const bool rv = n < g.nvox;
+    if (rv) vox_coords(g, n, x, y, z, b);
+    const uint32_t idesc = tc::idesc_bf16(128, N);
+    bool ok = true;
+    uint32_t uses[2] = {0, 0};
+    for (int t = 0; t < 27; ++t) {
+        const int buf = t & 1;
+        if (t >= 2) {  // the MMAs that last read this buffer must be done
+            ok = ok && tc::mbar_wait(&mbar[buf], (uses[buf] - 1) & 1, kTcWaitIter);
+        }
+        // A: this thread's row, C channels of the neighbour at tap t
+        const long long src = rv ? neighbour(g, x, y, z, b, t, sign) : -1;
+        const uint4 *ap = reinterpret_cast<const uint4 *>(act + (src < 0 ? 0 : src * C));
+#pragma unroll
+        for (int j = 0; j < C / 8; ++j) {
+            const uint4 v = src < 0 ? make_uint4(0, 0, 0, 0) : __ldg(ap + j);
+            *reinterpret_cast<uint4 *>(sA[buf] + tc::core_offset(tid, 8 * j, C)) = v;
+        }
+        // B: N rows of K = (t, 0..C-1)
+        for (int s = tid; s < N * (C / 8); s += 128) {
+            const int r = s / (C / 8), j = s % (C / 8);
+            const uint4 v = __ldg(reinterpret_cast<const uint4 *>(wk + ((long long)r * 27 + t) * C) + j);
+            *reinterpret_cast<uint4 *>(sB[buf] + tc::core_offset(r, 8 * j, C)) = v;
+        }
+        tc::fence_proxy_async();
+        __syncthreads();
+        if (tid == 0 && ok) {
+            tc::fence_after_sync();
+#pragma unroll
+            for (int c = 0; c < C / 16; ++c) {
+                const uint64_t ad = tc::smem_desc(tc::smem_u32(sA[buf]) + c * 256, 128, C * 16);
+                const uint64_t bd = tc::smem_desc(tc::smem_u32(sB[buf]) + c * 256, 128, C * 16);
+                tc::mma_bf16(tmem, ad, bd, idesc, (t > 0 || c > 0) ? 1 : 0);
+            }
+            tc::mma_commit(&mbar[buf]);
+        }
+        ++uses[buf];
+    }
+    // drain: both buffers' last commits
+    for (int bb = 0; bb < 2; ++bb)
+        if (uses[bb]) ok = tc::mbar_wait(&mbar[bb], (uses[bb] - 1) & 1, kTcWaitIter) && ok;
+    tc::fence_after_sync();
+    __syncthreads();
+    if (!ok) {
+        if (tid == 0) atomicExch(err, 1);
+    } else {
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            float v[16];
+            tc::tmem_ld16(trow + c0, v);
+            if (!rv) continue;
+            if (OUT_MODE == 0) {
+                __align__(16) __nv_bfloat16 o[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    float a = v[j] + (bias ? bias[c0 + j] : 0.0f);
+                    if (relu) a = fmaxf(a, 0.0f);
+                    o[j] = __float2bfloat16(a);
+                }
+                uint4 *op = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(out) + n * N + c0);
+                op[0] = reinterpret_cast<const uint4 *>(o)[0];
+                op[1] = reinterpret_cast<const uint4 *>(o)[1];
+            } else {
+                float4 *op = reinterpret_cast<float4 *>(reinterpret_cast<float *>(out) + n * N + c0);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) op[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
+// wgrad: D[(t,ci) rows][co] over the voxels [blockIdx.y * vpc, +vpc), atomically added
+// to dW[co][t][ci] (FP32).
+template <int N, int C>
+__global__ void __launch_bounds__(128) k_wgrad_tc(const __nv_bfloat16 *__restrict__ X,
+                                                  const __nv_bfloat16 *__restrict__ G, float *dW, ConvGeom g,
+                                                  long long vpc, int *err)
+{
+    constexpr int KT = 64;  // voxels per stage
+    constexpr int A_BYTES = 128 * KT * 2, B_BYTES = N * KT * 2;
+    constexpr int ROWS = 27 * C;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *sA[2] = {smem, smem + A_BYTES};
+    uint8_t *sB[2] = {smem + 2 * A_BYTES, smem + 2 * A_BYTES + B_BYTES};
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    constexpr uint32_t ncols = TmemCols<N>::value;
+    if (warp == 0) tc::tmem_alloc(&tbase, ncols);
+    if (tid == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tbase;
+    const int row0 = blockIdx.x * 128;
+    const long long n0 = (long long)blockIdx.y * vpc;
+    const long long n1 = n0 + vpc < g.nvox ? n0 + vpc : g.nvox;
+    const uint32_t idesc = tc::idesc_bf16(128, N);
+    bool ok = true;
+    uint32_t uses[2] = {0, 0};
+    int stage = 0;
+    for (long long k0 = n0; k0 < n1; k0 += KT, ++stage) {
+        const int buf = stage & 1;
+        if (stage >= 2) ok = ok && tc::mbar_wait(&mbar[buf], (uses[buf] - 1) & 1, kTcWaitIter);
+        // A: 16 row groups x KT voxels; a row group is 8 channels of one tap
+        for (int s = tid; s < 16 * KT; s += 128) {
+            const int rg = s / KT, k = s % KT;
+            const int r = row0 + 8 * rg;
+            const long long nn = k0 + k;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (r < ROWS && nn < n1) {
+                const int t = r / C, ci = r % C;
+                int x, y, z, b;
+                vox_coords(g, nn, x, y, z, b);
+                const long long src = neighbour(g, x, y, z, b, t, 1);
+                if (src >= 0) v = __ldg(reinterpret_cast<const uint4 *>(X + src * C + ci));
+            }
+            const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&v);
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                *reinterpret_cast<__nv_bfloat16 *>(sA[buf] + tc::core_offset(8 * rg + q, k, KT)) = e[q];
+        }
+        // B: N channels of G at KT voxels
+        for (int s = tid; s < (N / 8) * KT; s += 128) {
+            const int cg = s / KT, k = s % KT;
+            const long long nn = k0 + k;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (nn < n1) v = __ldg(reinterpret_cast<const uint4 *>(G + nn * N + 8 * cg));
+            const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(&v);
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                *reinterpret_cast<__nv_bfloat16 *>(sB[buf] + tc::core_offset(8 * cg + q, k, KT)) = e[q];
+        }
+        tc::fence_proxy_async();
+        __syncthreads();
+        if (tid == 0 && ok) {
+            tc::fence_after_sync();
+#pragma unroll
+            for (int c = 0; c < KT / 16; ++c) {
+                const uint64_t ad = tc::smem_desc(tc::smem_u32(sA[buf]) + c * 256, 128, KT * 16);
+                const uint64_t bd = tc::smem_desc(tc::smem_u32(sB[buf]) + c * 256, 128, KT * 16);
+                tc::mma_bf16(tmem, ad, bd, idesc, (stage > 0 || c > 0) ? 1 : 0);
+            }
+            tc::mma_commit(&mbar[buf]);
+        }
+        ++uses[buf];
+    }
+    for (int bb = 0; bb < 2; ++bb)
+        if (uses[bb]) ok = tc::mbar_wait(&mbar[bb], (uses[bb] - 1) & 1, kTcWaitIter) && ok;
+    tc::fence_after_sync();
+    __syncthreads();
+    if (!ok) {
+        if (tid == 0) atomicExch(err, 1);
+    } else if (stage > 0) {
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+        const int r = row0 + tid;  // (t, ci)
+#pragma unroll
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            float v[16];
+            tc::tmem_ld16(trow + c0, v);
+            if (r < ROWS)
+#pragma unroll
+                for (int j = 0; j < 16; ++j) atomicAdd(&dW[(long long)(c0 + j) * ROWS + r], v[j]);
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
+}  // namespace mvr

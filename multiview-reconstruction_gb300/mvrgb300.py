@@ -44,6 +44,9 @@ EXPORTS = [
     "mvr_decon_get_max", "mvr_decon_get_weights", "mvr_decon_psi_device", "mvr_decon_synchronize",
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
     "mvr_kernel_name", "mvr_convolve_static", "mvr_decon_batch", "mvr_decon_likelihood",
+    "mvr_unet_create", "mvr_unet_destroy", "mvr_unet_last_error", "mvr_unet_num_params", "mvr_unet_get_params",
+    "mvr_unet_set_params", "mvr_unet_get_grads", "mvr_unet_set_input", "mvr_unet_forward", "mvr_unet_train_step",
+    "mvr_unet_propose", "mvr_conv3d_tc", "mvr_conv3d_tc_wgrad", "mvr_conv3d_tc_last_error",
     "convolution3DfftCUDA", "convolution3DfftCUDAInPlace", "getNumDevicesCUDA", "getNameDeviceCUDA",
     "getMemDeviceCUDA", "getFreeMemDeviceCUDA", "getCUDAcomputeCapabilityMajorVersion",
     "getCUDAcomputeCapabilityMinorVersion", "mvr_free",
@@ -137,6 +140,22 @@ def load() -> C.CDLL:
     L.mvr_convolve_static.argtypes = [P, P, P, P, P, P, C.c_char_p, C.c_int]
     L.mvr_decon_batch.argtypes = [P]
     L.mvr_decon_likelihood.argtypes = [P, P, P]
+    L.mvr_unet_create.argtypes = [C.c_int, P, C.c_uint, C.c_int, C.POINTER(P)]
+    L.mvr_unet_destroy.argtypes = [P]
+    L.mvr_unet_destroy.restype = None
+    L.mvr_unet_last_error.argtypes = [P]
+    L.mvr_unet_last_error.restype = C.c_char_p
+    L.mvr_unet_num_params.argtypes = [P]
+    L.mvr_unet_num_params.restype = C.c_longlong
+    for f in ("mvr_unet_get_params", "mvr_unet_set_params", "mvr_unet_get_grads"):
+        getattr(L, f).argtypes = [P, P]
+    L.mvr_unet_set_input.argtypes = [P, P, P, P]
+    L.mvr_unet_forward.argtypes = [P, P]
+    L.mvr_unet_train_step.argtypes = [P, C.c_float, P]
+    L.mvr_unet_propose.argtypes = [P, P, P, C.c_float]
+    L.mvr_conv3d_tc.argtypes = [P, C.c_int, P, C.c_int, P, C.c_int, C.c_int, P, P, P, P]
+    L.mvr_conv3d_tc_wgrad.argtypes = [P, C.c_int, P, C.c_int, P, P, P, P]
+    L.mvr_conv3d_tc_last_error.restype = C.c_char_p
     _lib = L
     return L
 
@@ -378,6 +397,90 @@ class Deconvolution:
         by = np.zeros(n, np.float64)
         self._check(self._lib.mvr_decon_get_profile(self._h, _p(ms), _p(la), _p(by)))
         return {self._lib.mvr_kernel_name(k).decode(): (float(ms[k]), int(la[k]), float(by[k])) for k in range(n)}
+
+
+class UNet:
+    """The learned-proposal network (3-level 3D U-Net, tcgen05 BF16 kernels) on device
+    volumes given as raw addresses of float32 [batch][z][y][x] tensors."""
+
+    def __init__(self, batch, dims, seed=0, device=0):
+        self._lib = load()
+        h = C.c_void_p()
+        rc = self._lib.mvr_unet_create(batch, (C.c_int * 3)(*dims), seed, device, C.byref(h))
+        if rc != OK:
+            raise MvrError(rc, self._lib.mvr_unet_last_error(None).decode())
+        self._h = h
+        self.batch = batch
+        self.dims = tuple(dims)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.mvr_unet_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != OK:
+            raise MvrError(rc, self._lib.mvr_unet_last_error(self._h).decode())
+
+    @property
+    def num_params(self) -> int:
+        return int(self._lib.mvr_unet_num_params(self._h))
+
+    def params(self):
+        p = np.empty(self.num_params, np.float32)
+        self._check(self._lib.mvr_unet_get_params(self._h, _p(p)))
+        return p
+
+    def set_params(self, p):
+        p = _f32(p)
+        self._check(self._lib.mvr_unet_set_params(self._h, _p(p)))
+
+    def grads(self):
+        g = np.empty(self.num_params, np.float32)
+        self._check(self._lib.mvr_unet_get_grads(self._h, _p(g)))
+        return g
+
+    def set_input(self, psi_ptr: int, ratio_ptr: int = 0, target_ptr: int = 0):
+        self._check(self._lib.mvr_unet_set_input(self._h, C.c_void_p(psi_ptr), C.c_void_p(ratio_ptr) if ratio_ptr else None,
+                                                 C.c_void_p(target_ptr) if target_ptr else None))
+
+    def forward(self, pred_ptr: int = 0):
+        self._check(self._lib.mvr_unet_forward(self._h, C.c_void_p(pred_ptr) if pred_ptr else None))
+
+    def train_step(self, lr: float) -> float:
+        loss = np.zeros(1, np.float64)
+        self._check(self._lib.mvr_unet_train_step(self._h, lr, _p(loss)))
+        return float(loss[0])
+
+    def propose(self, psi_ptr: int, out_ptr: int, cap: float = 1.0):
+        self._check(self._lib.mvr_unet_propose(self._h, C.c_void_p(psi_ptr), C.c_void_p(out_ptr), cap))
+
+
+def conv3d_tc(act_ptr, c_act, w_ptr, n_out, bias_ptr, relu, transposed, out_ptr, dims_xyzb, err_ptr, stream=0):
+    """One tensor-core 3x3x3 convolution layer (forward or data gradient) on device buffers."""
+    L = load()
+    rc = L.mvr_conv3d_tc(C.c_void_p(act_ptr), c_act, C.c_void_p(w_ptr), n_out,
+                         C.c_void_p(bias_ptr) if bias_ptr else None, int(relu), int(transposed), C.c_void_p(out_ptr),
+                         (C.c_int * 4)(*dims_xyzb), C.c_void_p(err_ptr), C.c_void_p(stream) if stream else None)
+    if rc != OK:
+        raise MvrError(rc, L.mvr_conv3d_tc_last_error().decode())
+
+
+def conv3d_tc_wgrad(x_ptr, c_in, g_ptr, c_out, dw_ptr, dims_xyzb, err_ptr, stream=0):
+    L = load()
+    rc = L.mvr_conv3d_tc_wgrad(C.c_void_p(x_ptr), c_in, C.c_void_p(g_ptr), c_out, C.c_void_p(dw_ptr),
+                               (C.c_int * 4)(*dims_xyzb), C.c_void_p(err_ptr), C.c_void_p(stream) if stream else None)
+    if rc != OK:
+        raise MvrError(rc, L.mvr_conv3d_tc_last_error().decode())
 
 
 def convolution3d_fft_cuda_in_place(im, kernel, device: int = 0) -> np.ndarray:
