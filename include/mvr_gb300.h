@@ -167,6 +167,9 @@ MVR_API int mvr_decon_prepare(mvr_decon *h);
 MVR_API int mvr_decon_set_psi(mvr_decon *h, const float *psi);
 MVR_API int mvr_decon_set_psi_device(mvr_decon *h, const float *psi);
 MVR_API int mvr_decon_get_psi(mvr_decon *h, float *psi);
+/* Copy of psi as float into a device buffer of the volume's size (queued on the handle's
+ * stream, then synchronised). */
+MVR_API int mvr_decon_get_psi_device(mvr_decon *h, float *psi_device);
 /* runIterations: `iterations` more iterations.  stats (or NULL) receives per iteration
  * and view-step {sumChange, maxChange} (Seq: num_views steps, Mul: 1 step). */
 MVR_API int mvr_decon_run(mvr_decon *h, int iterations, double *stats);
@@ -202,9 +205,9 @@ MVR_API int mvr_decon_likelihood(mvr_decon *h, double *total, double *per_view);
  * A 3-level 3D U-Net (16/32/64 channels, 3x3x3 convolutions, BF16 weights and
  * activations, FP32 accumulation on the tcgen05 tensor cores) with its own forward and
  * backward kernels and Adam, for patches [batch][z][y][x] of sizes {x, y, z} (multiples
- * of 4).  Inputs are device float volumes: psi_k and the plain method's one-iteration
- * ratio psi_{k+1} / psi_k; the network predicts log(psi_{k+m} / psi_k).  Callers gate
- * its proposals with mvr_decon_likelihood. */
+ * of 4).  Inputs are device float volumes: psi_k and the plain method's next iterate
+ * psi_{k+1} (the network sees the ratio psi_{k+1} / psi_k); it predicts
+ * log(psi_{k+m} / psi_k).  Callers gate its proposals with mvr_decon_likelihood. */
 typedef struct mvr_unet mvr_unet;
 MVR_API int mvr_unet_create(int batch, const int dims[3], unsigned seed, int device, mvr_unet **out);
 MVR_API void mvr_unet_destroy(mvr_unet *h);
@@ -215,9 +218,9 @@ MVR_API int mvr_unet_get_params(mvr_unet *h, float *params);
 MVR_API int mvr_unet_set_params(mvr_unet *h, const float *params);
 /* Gradients of the last training step (same layout as the parameters). */
 MVR_API int mvr_unet_get_grads(mvr_unet *h, float *grads);
-/* Features from psi_k and ratio_k (device, may be NULL) and the target
+/* Features from psi_k and psi_{k+1} (device, may be NULL) and the target
  * log(psi_target / psi_k) (psi_target may be NULL for inference). */
-MVR_API int mvr_unet_set_input(mvr_unet *h, const float *psi, const float *ratio, const float *psi_target);
+MVR_API int mvr_unet_set_input(mvr_unet *h, const float *psi, const float *psi_next, const float *psi_target);
 /* Forward pass; pred (device, or NULL) receives the predicted log-ratio. */
 MVR_API int mvr_unet_forward(mvr_unet *h, float *pred);
 /* Forward, mean-squared-error loss against the target, backward, one Adam step. */

@@ -329,6 +329,7 @@ public:
     virtual int prepare() = 0;
     virtual int set_psi(const float *psi, bool on_device) = 0;
     virtual int get_psi(float *psi) = 0;
+    virtual int get_psi_device(float *psi) = 0;
     virtual int run(int iterations, double *stats) = 0;
     virtual int get_kernels(int v, float *k1, float *k2) = 0;
     virtual int get_max(float *mx) = 0;
@@ -356,6 +357,7 @@ public:
     int prepare() override;
     int set_psi(const float *psi, bool on_device) override;
     int get_psi(float *psi) override;
+    int get_psi_device(float *psi) override;
     int run(int iterations, double *stats) override;
     int get_kernels(int v, float *k1, float *k2) override;
     int get_max(float *mx) override;
@@ -806,6 +808,22 @@ int Decon<T>::get_psi(float *psi)
 }
 
 template <typename T>
+int Decon<T>::get_psi_device(float *psi)
+{
+    if (!psi) return fail(MVR_ERR_ARG, "psi must not be NULL");
+    D_CUDA(cudaSetDevice(p_.device));
+    cudaStream_t s = engine_.stream();
+    if (sizeof(T) == sizeof(float)) {
+        D_CUDA(cudaMemcpyAsync(psi, psi_, sizeof(float) * (size_t)n_, cudaMemcpyDeviceToDevice, s));
+    } else {
+        k_convert<T, float><<<grid_for(n_), 256, 0, s>>>(psi_, psi, n_);
+        D_CUDA(cudaGetLastError());
+    }
+    D_CUDA(cudaStreamSynchronize(s));
+    return MVR_OK;
+}
+
+template <typename T>
 int Decon<T>::get_kernels(int v, float *k1, float *k2)
 {
     if (v < 0 || v >= p_.num_views || !prepared_) return fail(MVR_ERR_STATE, "not prepared or view out of range");
@@ -1139,6 +1157,10 @@ extern "C" int mvr_decon_set_psi_device(mvr_decon *h, const float *psi)
     return h ? h->impl->set_psi(psi, true) : MVR_ERR_ARG;
 }
 extern "C" int mvr_decon_get_psi(mvr_decon *h, float *psi) { return h ? h->impl->get_psi(psi) : MVR_ERR_ARG; }
+extern "C" int mvr_decon_get_psi_device(mvr_decon *h, float *psi)
+{
+    return h ? h->impl->get_psi_device(psi) : MVR_ERR_ARG;
+}
 extern "C" int mvr_decon_run(mvr_decon *h, int iterations, double *stats)
 {
     return h ? h->impl->run(iterations, stats) : MVR_ERR_ARG;

@@ -12,7 +12,8 @@
 //   d2 = relu(conv([up(b3), e2], 96 -> 32))      level 2
 //   d1 = relu(conv([up(d2), e1], 48 -> 16))      level 1
 //   out = head(d1) (1x1x1, 16 -> 1)
-// Input features: channel 0 = log(psi_k / mean psi_k), channel 1 = log(ratio_k), the
+// Input features: channel 0 = log(psi_k / mean psi_k), channel 1 = log(ratio_k) with
+// ratio_k = psi_{k+1} / psi_k the plain method's one-iteration update, the
 // other 14 input channels are zero (the tensor-core K step is 16 channels).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -117,8 +118,8 @@ __global__ void k_patch_mean(const float *psi, long long per, double *mean)
     if (threadIdx.x == 0) mean[blockIdx.x] = sm[0] / (double)per;
 }
 
-// features: [log(psi / mean), log(ratio), 0 x 14] as BF16; target log(psi_m / psi)
-__global__ void k_features(const float *psi, const float *ratio, const float *psi_m, long long n, long long per,
+// features: [log(psi / mean), log(psi_next / psi), 0 x 14] as BF16; target log(psi_m / psi)
+__global__ void k_features(const float *psi, const float *psi_next, const float *psi_m, long long n, long long per,
                            const double *mean, bf16 *in16, float *target)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -126,7 +127,7 @@ __global__ void k_features(const float *psi, const float *ratio, const float *ps
         const float m = (float)mean[i / per];
         __align__(16) bf16 f[16];
         f[0] = __float2bfloat16(logf(p / fmaxf(m, 1e-12f)));
-        f[1] = __float2bfloat16(ratio ? logf(fmaxf(ratio[i], 1e-12f)) : 0.0f);
+        f[1] = __float2bfloat16(psi_next ? logf(fmaxf(psi_next[i], 1e-12f) / p) : 0.0f);
 #pragma unroll
         for (int c = 2; c < 16; ++c) f[c] = __float2bfloat16(0.0f);
         uint4 *o = reinterpret_cast<uint4 *>(in16 + i * 16);
@@ -328,7 +329,7 @@ public:
     }
     ~UNet();
     int init();
-    int set_input(const float *psi, const float *ratio, const float *psi_target);
+    int set_input(const float *psi, const float *psi_next, const float *psi_target);
     int forward(float *pred);
     int train_step(float lr, double *loss);
     int propose(const float *psi, float *out, float cap);
@@ -470,13 +471,13 @@ int UNet::refresh_weights()
     return cuda(cudaGetLastError(), "k_weights_bf16");
 }
 
-int UNet::set_input(const float *psi, const float *ratio, const float *psi_target)
+int UNet::set_input(const float *psi, const float *psi_next, const float *psi_target)
 {
     if (!psi) return fail(MVR_ERR_ARG, "psi must not be NULL");
     cudaSetDevice(dev_);
     const long long per = g1_.nvox / B_;
     k_patch_mean<<<B_, 256, 0, s_>>>(psi, per, mean_);
-    k_features<<<gsize(g1_.nvox), 256, 0, s_>>>(psi, ratio, psi_target, g1_.nvox, per, mean_, in16_,
+    k_features<<<gsize(g1_.nvox), 256, 0, s_>>>(psi, psi_next, psi_target, g1_.nvox, per, mean_, in16_,
                                                 psi_target ? target_ : nullptr);
     return cuda(cudaGetLastError(), "k_features");
 }
@@ -654,9 +655,9 @@ extern "C" long long mvr_unet_num_params(const mvr_unet *h) { return h ? h->net-
 extern "C" int mvr_unet_get_params(mvr_unet *h, float *p) { return h && p ? h->net->get_params(p) : MVR_ERR_ARG; }
 extern "C" int mvr_unet_set_params(mvr_unet *h, const float *p) { return h && p ? h->net->set_params(p) : MVR_ERR_ARG; }
 extern "C" int mvr_unet_get_grads(mvr_unet *h, float *g) { return h && g ? h->net->get_grads(g) : MVR_ERR_ARG; }
-extern "C" int mvr_unet_set_input(mvr_unet *h, const float *psi, const float *ratio, const float *psi_target)
+extern "C" int mvr_unet_set_input(mvr_unet *h, const float *psi, const float *psi_next, const float *psi_target)
 {
-    return h ? h->net->set_input(psi, ratio, psi_target) : MVR_ERR_ARG;
+    return h ? h->net->set_input(psi, psi_next, psi_target) : MVR_ERR_ARG;
 }
 extern "C" int mvr_unet_forward(mvr_unet *h, float *pred) { return h ? h->net->forward(pred) : MVR_ERR_ARG; }
 extern "C" int mvr_unet_train_step(mvr_unet *h, float lr, double *loss)

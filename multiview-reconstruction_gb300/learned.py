@@ -1,0 +1,184 @@
+"""Learned multi-iteration proposals for the multiview RL iteration (no counterpart in
+the reference).
+
+* generate_pairs: the plain GPU method itself, run on seeded synthetic objects, yields
+  (psi_k, psi_{k+1}, psi_{k+m}) crops.
+* train: the tcgen05 U-Net (mvr_unet_*) learns log(psi_{k+m} / psi_k) from
+  [log psi_k, log(psi_{k+1} / psi_k)].
+* run: each step runs one plain iteration, proposes psi_k * exp(f(...)) from it, and
+  keeps the proposal only when the FP64 data-likelihood residual of the proposal is
+  below that of the plain update (mvr_decon_likelihood); otherwise the plain update
+  stands.
+
+Device buffers are torch tensors (plumbing only); every computation runs in the
+library's kernels.
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+
+import mvrgb300 as M
+import synthetic
+
+ANGLES = (0.0, 45.0, 90.0, 135.0)
+
+
+def _friendly(n: int, even: bool = False) -> int:
+    m = n + (1 if even and n % 2 else 0)
+    while True:
+        k = m
+        for r in (2, 3, 5, 7):
+            while k % r == 0:
+                k //= r
+        if k == 1 and (not even or m % 2 == 0):
+            return m
+        m += 2 if even else 1
+
+
+def one_block(dims, psf_xyz):
+    """FFT-friendly compute block holding the whole volume (effective size >= dims)."""
+    return tuple(_friendly(dims[d] + 2 * (psf_xyz[d] - 1), even=(d == 0)) for d in range(3))
+
+
+def make_decon(ds, dims, block, device=0, lam=0.006, boundary=M.BOUNDARY_CIRCULAR, precision=M.PRECISION_FP32):
+    import torch
+
+    d = M.Deconvolution(dims, len(ds.images), block, psf_type=M.PSF_OPTIMIZATION_I, lam=lam, boundary=boundary,
+                        precision=precision, weight_norm=M.WEIGHTS_HARD, device=device)
+    keep = []
+    for v in range(len(ds.images)):
+        im = torch.from_numpy(ds.images[v]).to(f"cuda:{device}")
+        w = torch.from_numpy(ds.weights[v]).to(f"cuda:{device}")
+        keep += [im, w]
+        d.set_view_device(v, im.data_ptr(), w.data_ptr(), ds.psfs[v])
+    d.prepare()
+    d._keep = keep  # the device images must outlive the handle's use
+    return d
+
+
+def dataset(dims, seed, psf=(31, 31, 61), n_beads=None, side_lobes=True):
+    nb = n_beads if n_beads is not None else max(8, int(200 * np.prod(dims) / 256 ** 3 * 8))
+    return synthetic.make_dataset(dims, ANGLES, psf, n_beads=nb, seed=seed, side_lobes=side_lobes,
+                                  weights="cosine")
+
+
+def generate_pairs(n_objects=50, dims=(128, 128, 128), crop=(64, 64, 64), iters=45, m=5, pairs_per_object=40,
+                   seed0=2000, psf=(31, 31, 61), device=0):
+    """(psi_k, psi_{k+1}, psi_{k+m}) crops from the plain method on seeded objects.
+    Returns three device tensors [P][cz][cy][cx]."""
+    import torch
+
+    rng = np.random.default_rng(seed0)
+    shape = (dims[2], dims[1], dims[0])
+    block = one_block(dims, psf)
+    out = [[], [], []]
+    for o in range(n_objects):
+        ds = dataset(dims, seed0 + o, psf)
+        dec = make_decon(ds, dims, block, device)
+        hist = torch.empty((iters + 1,) + shape, dtype=torch.float32, device=f"cuda:{device}")
+        dec.get_psi_device(hist[0].data_ptr())
+        for k in range(iters):
+            dec.run_iterations(1)
+            dec.get_psi_device(hist[k + 1].data_ptr())
+        dec.close()
+        for _ in range(pairs_per_object):
+            k = int(rng.integers(0, iters - m))
+            z0, y0, x0 = (int(rng.integers(0, shape[i] - crop[2 - i] + 1)) for i in range(3))
+            sl = (slice(z0, z0 + crop[2]), slice(y0, y0 + crop[1]), slice(x0, x0 + crop[0]))
+            out[0].append(hist[k][sl].clone())
+            out[1].append(hist[k + 1][sl].clone())
+            out[2].append(hist[k + m][sl].clone())
+        del hist
+    return tuple(torch.stack(x) for x in out)
+
+
+def train(pairs, crop=(64, 64, 64), steps=1500, batch=4, lr=1e-3, seed=0, device=0):
+    """Trains the U-Net on the pairs; returns (parameters, per-step losses)."""
+    import torch
+
+    psi, nxt, tgt = pairs
+    rng = np.random.default_rng(seed)
+    net = M.UNet(batch, crop, seed=seed, device=device)
+    shape = (batch, crop[2], crop[1], crop[0])
+    bp = torch.empty(shape, dtype=torch.float32, device=f"cuda:{device}")
+    bn = torch.empty_like(bp)
+    bt = torch.empty_like(bp)
+    losses = []
+    for s in range(steps):
+        idx = torch.from_numpy(rng.integers(0, psi.shape[0], batch)).to(psi.device)
+        torch.index_select(psi, 0, idx, out=bp)
+        torch.index_select(nxt, 0, idx, out=bn)
+        torch.index_select(tgt, 0, idx, out=bt)
+        net.set_input(bp.data_ptr(), bn.data_ptr(), bt.data_ptr())
+        cur_lr = lr * 0.5 * (1 + math.cos(math.pi * s / steps))  # cosine schedule
+        losses.append(net.train_step(cur_lr))
+    params = net.params()
+    net.close()
+    return params, np.array(losses)
+
+
+class GatedProposer:
+    """Likelihood-gated learned proposals on a whole volume."""
+
+    def __init__(self, params, dims, cap=1.0, device=0):
+        import torch
+
+        self.net = M.UNet(1, dims, seed=0, device=device)
+        self.net.set_params(params)
+        shape = (1, dims[2], dims[1], dims[0])
+        self.psi = torch.empty(shape, dtype=torch.float32, device=f"cuda:{device}")
+        self.nxt = torch.empty_like(self.psi)
+        self.prop = torch.empty_like(self.psi)
+        self.cap = cap
+
+    def close(self):
+        self.net.close()
+
+    def step(self, dec):
+        """One gated step on dec; returns (accepted, nll_plain, nll_proposal)."""
+        dec.get_psi_device(self.psi.data_ptr())
+        dec.run_iterations(1)
+        dec.get_psi_device(self.nxt.data_ptr())
+        self.net.set_input(self.psi.data_ptr(), self.nxt.data_ptr())
+        self.net.propose(self.psi.data_ptr(), self.prop.data_ptr(), self.cap)
+        l_plain = dec.likelihood()[0]
+        dec.set_psi_device(self.prop.data_ptr())
+        l_prop = dec.likelihood()[0]
+        if l_prop < l_plain:
+            return True, l_plain, l_prop
+        dec.set_psi_device(self.nxt.data_ptr())
+        return False, l_plain, l_prop
+
+
+def convergence(dec, n_steps, ref=None, proposer=None):
+    """Runs n_steps plain iterations (or gated steps when proposer is given); returns per
+    step (seconds since start, relative L2 to ref or NaN, NLL, accepted)."""
+    import torch
+
+    hist = []
+    buf = None
+    if ref is not None:
+        buf = torch.empty_like(ref)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    elapsed = 0.0
+    for _ in range(n_steps):
+        ts = time.perf_counter()
+        if proposer is None:
+            dec.run_iterations(1)
+            dec.synchronize()
+            acc = False
+        else:
+            acc, _, _ = proposer.step(dec)
+        elapsed += time.perf_counter() - ts
+        nll = dec.likelihood()[0]  # bookkeeping outside the timed part
+        err = float("nan")
+        if ref is not None:
+            dec.get_psi_device(buf.data_ptr())
+            err = float(torch.linalg.vector_norm(buf.double() - ref.double()) / torch.linalg.vector_norm(ref.double()))
+        hist.append((elapsed, err, nll, acc))
+    _ = t0
+    return hist

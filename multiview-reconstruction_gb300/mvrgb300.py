@@ -40,7 +40,7 @@ EXPORTS = [
     "mvr_block_run_seq", "mvr_block_run_mul", "mvr_block_run_seq_device", "mvr_block_synchronize",
     "mvr_decon_create", "mvr_decon_destroy", "mvr_decon_last_error", "mvr_decon_set_view",
     "mvr_decon_set_view_device", "mvr_decon_update_images", "mvr_decon_prepare", "mvr_decon_set_psi",
-    "mvr_decon_set_psi_device", "mvr_decon_get_psi", "mvr_decon_run", "mvr_decon_get_kernels",
+    "mvr_decon_set_psi_device", "mvr_decon_get_psi", "mvr_decon_get_psi_device", "mvr_decon_run", "mvr_decon_get_kernels",
     "mvr_decon_get_max", "mvr_decon_get_weights", "mvr_decon_psi_device", "mvr_decon_synchronize",
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
     "mvr_kernel_name", "mvr_convolve_static", "mvr_decon_batch", "mvr_decon_likelihood",
@@ -122,6 +122,7 @@ def load() -> C.CDLL:
     L.mvr_decon_set_psi.argtypes = [P, P]
     L.mvr_decon_set_psi_device.argtypes = [P, P]
     L.mvr_decon_get_psi.argtypes = [P, P]
+    L.mvr_decon_get_psi_device.argtypes = [P, P]
     L.mvr_decon_run.argtypes = [P, C.c_int, P]
     L.mvr_decon_get_kernels.argtypes = [P, C.c_int, P, P]
     L.mvr_decon_get_max.argtypes = [P, P]
@@ -339,6 +340,10 @@ class Deconvolution:
         self._check(self._lib.mvr_decon_get_psi(self._h, _p(out)))
         return out
 
+    def get_psi_device(self, ptr: int):
+        """Copies psi (float) into the device buffer at ptr."""
+        self._check(self._lib.mvr_decon_get_psi_device(self._h, C.c_void_p(ptr)))
+
     def run_iterations(self, n: int, stats: bool = False):
         """runIterations; returns per (iteration, view-step) [sumChange, maxChange] if asked."""
         steps = 1 if self.mul else self.num_views
@@ -449,8 +454,9 @@ class UNet:
         self._check(self._lib.mvr_unet_get_grads(self._h, _p(g)))
         return g
 
-    def set_input(self, psi_ptr: int, ratio_ptr: int = 0, target_ptr: int = 0):
-        self._check(self._lib.mvr_unet_set_input(self._h, C.c_void_p(psi_ptr), C.c_void_p(ratio_ptr) if ratio_ptr else None,
+    def set_input(self, psi_ptr: int, next_ptr: int = 0, target_ptr: int = 0):
+        """psi_k, psi_{k+1} (network input) and psi_{k+m} (training target) device volumes."""
+        self._check(self._lib.mvr_unet_set_input(self._h, C.c_void_p(psi_ptr), C.c_void_p(next_ptr) if next_ptr else None,
                                                  C.c_void_p(target_ptr) if target_ptr else None))
 
     def forward(self, pred_ptr: int = 0):

@@ -102,13 +102,13 @@ def unpack(params):
     return out, wh, bh
 
 
-def features(psi, ratio):
-    """[log(psi / mean psi), log(ratio), 0 x 14] per patch (float32 psi [B][z][y][x])."""
+def features(psi, psi_next):
+    """[log(psi / mean psi), log(psi_next / psi), 0 x 14] per patch (float32 [B][z][y][x])."""
     psi = np.maximum(np.asarray(psi, np.float32), 1e-12)
     m = psi.reshape(psi.shape[0], -1).astype(np.float64).mean(axis=1).astype(np.float32)
     f = np.zeros(psi.shape + (16,), np.float32)
     f[..., 0] = np.log(psi / m[:, None, None, None])
-    f[..., 1] = np.log(np.maximum(np.asarray(ratio, np.float32), 1e-12))
+    f[..., 1] = np.log(np.maximum(np.asarray(psi_next, np.float32), 1e-12) / psi)
     return bf16(f)
 
 

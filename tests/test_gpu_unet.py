@@ -65,16 +65,16 @@ def test_unet_loss_and_gradients_match_numpy():
     rng = np.random.default_rng(11)
     shape = (1, 8, 8, 8)
     psi = rng.uniform(10, 100, shape).astype(np.float32)
-    ratio = rng.uniform(0.8, 1.25, shape).astype(np.float32)
+    psi_n = (psi * rng.uniform(0.8, 1.25, shape)).astype(np.float32)
     psi_t = (psi * rng.uniform(0.7, 1.4, shape)).astype(np.float32)
     with M.UNet(1, (8, 8, 8), seed=3) as net:
-        pd, rd, td = (torch.from_numpy(a).cuda() for a in (psi, ratio, psi_t))
+        pd, rd, td = (torch.from_numpy(a).cuda() for a in (psi, psi_n, psi_t))
         net.set_input(pd.data_ptr(), rd.data_ptr(), td.data_ptr())
         params = net.params()
         loss = net.train_step(0.0)  # learning rate 0: gradients only
         grads = net.grads()
         assert np.array_equal(net.params(), params)
-    x16 = U.features(psi, ratio)
+    x16 = U.features(psi, psi_n)
     target = np.log(psi_t / psi).astype(np.float64)
     loss_ref, g_ref, _ = U.forward_backward(params, x16, target)
     assert abs(loss - loss_ref) <= 1e-3 * loss_ref
@@ -95,9 +95,10 @@ def test_unet_training_lowers_the_loss():
     base = 50 + 40 * np.exp(-((x - 8) ** 2 + (y - 8) ** 2 + (z - 8) ** 2) / 20.0)
     psi = np.stack([base, base[::-1]]).astype(np.float32) * rng.uniform(0.9, 1.1, shape).astype(np.float32)
     ratio = (1.0 + 0.05 * np.sin(x / 3.0)).astype(np.float32)[None].repeat(2, 0)
+    psi_n = (psi * ratio).astype(np.float32)
     psi_t = (psi * ratio ** 4).astype(np.float32)  # a structured multi-iteration target
     with M.UNet(2, (16, 16, 16), seed=1) as net:
-        pd, rd, td = (torch.from_numpy(a).cuda() for a in (psi, ratio, psi_t))
+        pd, rd, td = (torch.from_numpy(a).cuda() for a in (psi, psi_n, psi_t))
         net.set_input(pd.data_ptr(), rd.data_ptr(), td.data_ptr())
         losses = [net.train_step(2e-3) for _ in range(60)]
     assert losses[-1] < 0.3 * losses[0], (losses[0], losses[-1])
