@@ -232,6 +232,13 @@ def run_gb300(args, ws, rank, local):
 
     import mvrgb300 as M
 
+    pre_datasets = None
+    if args.learned and rank == 0:
+        # CPU synthesis of the training objects before the first GPU call
+        import learned
+
+        pre_datasets = learned.synthesize((128, 128, 128), [2000 + o for o in range(args.learned_objects)],
+                                          (31, 31, 61))
     torch.cuda.set_device(local)
     dev = local
     ds = make_data()
@@ -312,12 +319,20 @@ def run_gb300(args, ws, rank, local):
                "sample": f"{args.cpu_blocks} view-block(s) of 192^3 (reference boundary, FFT domain "
                          f"222x222x252), extrapolated to the {VIEW_BLOCKS_PER_ITER} view-blocks of one iteration"}
     dec.close()
+    learned_res = None
+    if args.learned and rank == 0:
+        import learned
+
+        learned_res = learned.experiment(ds, DIMS, BLOCK, n_objects=args.learned_objects, device=dev,
+                                         datasets=pre_datasets)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": dict(workload_config(args.boundary), batch_blocks=batch), "clocks": clocks,
                 "gpu_launches": launches, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu}
+        if learned_res is not None:
+            line["learned"] = learned_res
         print(json.dumps(line), flush=True)
 
 
@@ -373,6 +388,9 @@ def main():
     ap.add_argument("--cpu-blocks", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--learned", action="store_true",
+                    help="also run the learned-proposal experiment (training + gated run vs plain)")
+    ap.add_argument("--learned-objects", type=int, default=50)
     args = ap.parse_args()
     ws, rank, local = dist_setup(args)
     if args.impl == "reference":

@@ -65,8 +65,27 @@ def dataset(dims, seed, psf=(31, 31, 61), n_beads=None, side_lobes=True):
                                   weights="cosine")
 
 
+def _dataset_job(args):
+    dims, seed, psf = args
+    return dataset(dims, seed, psf)
+
+
+def synthesize(dims, seeds, psf, workers=None):
+    """Seeded synthetic objects, generated in a process pool (spawn context, so it is
+    safe in a process that already uses the GPU)."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    import os
+
+    workers = workers or max(1, min(len(seeds), (os.cpu_count() or 2) // 2))
+    if workers == 1 or len(seeds) == 1:
+        return [dataset(dims, s, psf) for s in seeds]
+    with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        return list(ex.map(_dataset_job, [(dims, s, psf) for s in seeds]))
+
+
 def generate_pairs(n_objects=50, dims=(128, 128, 128), crop=(64, 64, 64), iters=45, m=5, pairs_per_object=40,
-                   seed0=2000, psf=(31, 31, 61), device=0):
+                   seed0=2000, psf=(31, 31, 61), device=0, datasets=None):
     """(psi_k, psi_{k+1}, psi_{k+m}) crops from the plain method on seeded objects.
     Returns three device tensors [P][cz][cy][cx]."""
     import torch
@@ -75,8 +94,10 @@ def generate_pairs(n_objects=50, dims=(128, 128, 128), crop=(64, 64, 64), iters=
     shape = (dims[2], dims[1], dims[0])
     block = one_block(dims, psf)
     out = [[], [], []]
+    if datasets is None:
+        datasets = synthesize(dims, [seed0 + o for o in range(n_objects)], psf)
     for o in range(n_objects):
-        ds = dataset(dims, seed0 + o, psf)
+        ds = datasets[o]
         dec = make_decon(ds, dims, block, device)
         hist = torch.empty((iters + 1,) + shape, dtype=torch.float32, device=f"cuda:{device}")
         dec.get_psi_device(hist[0].data_ptr())
@@ -182,3 +203,62 @@ def convergence(dec, n_steps, ref=None, proposer=None):
         hist.append((elapsed, err, nll, acc))
     _ = t0
     return hist
+
+
+def first_time(hist, pred):
+    for t, err, nll, _ in hist:
+        if pred(err, nll):
+            return t
+    return None
+
+
+def experiment(ds, dims, block, n_objects=50, train_dims=(128, 128, 128), crop=(64, 64, 64), iters=45, m=5,
+               pairs_per_object=40, train_steps=1500, batch=4, lr=1e-3, eval_iters=20, tol=1e-3, device=0,
+               datasets=None):
+    """Learned + gated vs plain GPU RL on ds: wall time to relative L2 <= tol against the
+    FP64 plain result after eval_iters iterations, and to that result's likelihood."""
+    import torch
+
+    t0 = time.perf_counter()
+    pairs = generate_pairs(n_objects, train_dims, crop, iters, m, pairs_per_object, psf=ds.psfs[0].shape[::-1],
+                           device=device, datasets=datasets)
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    params, losses = train(pairs, crop, train_steps, batch, lr, device=device)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    psi0, _, tgt0 = pairs
+    base = float(torch.mean(torch.log(tgt0 / psi0) ** 2))
+    del pairs, psi0, tgt0
+    shape = (dims[2], dims[1], dims[0])
+    # FP64 plain reference
+    d64 = make_decon(ds, dims, block, device, precision=M.PRECISION_FP64)
+    d64.run_iterations(eval_iters)
+    ref = torch.empty(shape, dtype=torch.float32, device=f"cuda:{device}")
+    d64.get_psi_device(ref.data_ptr())
+    nll_ref = d64.likelihood()[0]
+    d64.close()
+    plain = make_decon(ds, dims, block, device)
+    h_plain = convergence(plain, eval_iters, ref)
+    plain.close()
+    gated = make_decon(ds, dims, block, device)
+    prop = GatedProposer(params, dims, device=device)
+    h_gated = convergence(gated, eval_iters, ref, prop)
+    prop.close()
+    gated.close()
+
+    def summary(h):
+        return {"t_err": first_time(h, lambda e, n: e <= tol), "t_nll": first_time(h, lambda e, n: n <= nll_ref),
+                "final_err": h[-1][1], "final_nll": h[-1][2], "seconds": h[-1][0],
+                "accepted": int(sum(1 for x in h if x[3]))}
+
+    sp, sg = summary(h_plain), summary(h_gated)
+    speed = None
+    if sp["t_err"] and sg["t_err"]:
+        speed = sp["t_err"] / sg["t_err"]
+    return {"pairs": n_objects * pairs_per_object, "objects": n_objects, "m": m, "train_steps": train_steps,
+            "train_loss_first": float(np.mean(losses[:20])), "train_loss_last": float(np.mean(losses[-20:])),
+            "no_change_loss": base, "gen_s": gen_s, "train_s": train_s, "eval_iters": eval_iters, "tol": tol,
+            "nll_fp64_ref": nll_ref, "plain": sp, "learned": sg, "speedup_to_tol": speed,
+            "trace_plain": [(round(t, 5), e, n) for t, e, n, _ in h_plain],
+            "trace_learned": [(round(t, 5), e, n, a) for t, e, n, a in h_gated]}
