@@ -1,5 +1,7 @@
 // Host side of the block iteration (see engine.cuh).
 #include "engine.cuh"
+#include "rows_warp.cuh"
+#include "cols_warp.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -99,6 +101,52 @@ int Engine<T>::cuda_check(cudaError_t e, const char *what)
         }                                 \
     } while (0)
 
+// Launches the kernel expression with R_ = the warp-row radix (Px = 64 R_).
+#define WARP_ROWS(wr, ...)                                                   \
+    do {                                                                     \
+        if ((wr) == 2) {                                                     \
+            constexpr int R_ = 2;                                            \
+            __VA_ARGS__;                                                     \
+        } else if ((wr) == 3) {                                              \
+            constexpr int R_ = 3;                                            \
+            __VA_ARGS__;                                                     \
+        } else {                                                             \
+            constexpr int R_ = 4;                                            \
+            __VA_ARGS__;                                                     \
+        }                                                                    \
+    } while (0)
+
+// Launches the kernel expression with R_ = the warp-column radix (n = 32 R_).
+#define WARP_COLS(wc, ...)                    \
+    do {                                      \
+        switch (wc) {                         \
+        case 2: {                             \
+            constexpr int R_ = 2;             \
+            __VA_ARGS__;                      \
+        } break;                              \
+        case 3: {                             \
+            constexpr int R_ = 3;             \
+            __VA_ARGS__;                      \
+        } break;                              \
+        case 4: {                             \
+            constexpr int R_ = 4;             \
+            __VA_ARGS__;                      \
+        } break;                              \
+        case 5: {                             \
+            constexpr int R_ = 5;             \
+            __VA_ARGS__;                      \
+        } break;                              \
+        case 6: {                             \
+            constexpr int R_ = 6;             \
+            __VA_ARGS__;                      \
+        } break;                              \
+        default: {                            \
+            constexpr int R_ = 8;             \
+            __VA_ARGS__;                      \
+        } break;                              \
+        }                                     \
+    } while (0)
+
 namespace {
 template <typename V>
 V *dev_twiddles_impl(int n, cudaStream_t s, std::string &err)
@@ -137,6 +185,14 @@ void set_smem_limits_big(int m)
     cudaFuncSetAttribute(k_rows_update<T, EPI_STORE, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
 }
 
+template <int R>
+void set_smem_limits_wcols(int m)
+{
+    cudaFuncSetAttribute(k_wcols<R, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_wcols<R, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_wcols<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+}
+
 template <typename T>
 void set_smem_limits()
 {
@@ -146,7 +202,22 @@ void set_smem_limits()
         const int m = (int)kSmemMax;
         set_smem_limits_big<T, false>(m);
         set_smem_limits_big<T, true>(m);
+        set_smem_limits_wcols<2>(m);
+        set_smem_limits_wcols<3>(m);
+        set_smem_limits_wcols<4>(m);
+        set_smem_limits_wcols<5>(m);
+        set_smem_limits_wcols<6>(m);
+        set_smem_limits_wcols<8>(m);
     });
+}
+
+// Warp-shuffle column radix for an FP32 axis of length n (0: shared-memory kernels).
+template <typename T>
+int warp_col_radix(int n)
+{
+    if (sizeof(T) != sizeof(float) || n % 32) return 0;
+    const int r = n / 32;
+    return (r == 2 || r == 3 || r == 4 || r == 5 || r == 6 || r == 8) ? r : 0;
 }
 }  // namespace
 
@@ -326,6 +397,9 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
     if (tws + RP * per_row > kSmemMax) return fail(ERR_UNSUPPORTED, "row too long for shared memory");
     pl.RP = RP;
     pl.smem_row = tws + RP * per_row;
+    pl.wr = (sizeof(T) == sizeof(float) && (pl.P[0] == 128 || pl.P[0] == 192 || pl.P[0] == 256)) ? pl.P[0] / 64 : 0;
+    pl.wcy = warp_col_radix<T>(pl.P[1]);
+    pl.wcz = warp_col_radix<T>(pl.P[2]);
     auto col_np = [&](int n, int &NP, size_t &smem) -> bool {
         NP = 16;
         while (NP > 1 && sizeof(V) * (size_t)n * (1 + 2 * NP) > kColSmemTarget) NP >>= 1;
@@ -404,6 +478,23 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
     const int kind = mode == 2 ? KK_COLS_ZMUL : (mode == 1 ? KK_COLS_INV : KK_COLS_FWD);
     MVR_TRY(prof_begin(kind, mode == 2 ? 3.0 * cb : 2.0 * cb));
     const long long Pc = pl.Pc;
+    const int wc = axis == 1 ? pl.wcy : pl.wcz;
+    if constexpr (sizeof(T) == sizeof(float)) {
+        if (wc) {
+            const dim3 wgrid((unsigned)((Hx + kWColNP - 1) / kWColNP), (unsigned)nother, (unsigned)nb);
+            const size_t ws = wcols_smem(wc, mode);
+            WARP_COLS(wc, {
+                if (mode == 0)
+                    k_wcols<R_, 0><<<wgrid, kThreads, ws, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw);
+                else if (mode == 1)
+                    k_wcols<R_, 1><<<wgrid, kThreads, ws, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw);
+                else
+                    k_wcols<R_, 2><<<wgrid, kThreads, ws, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw);
+            });
+            MVR_LAUNCHED("k_wcols");
+            return prof_end();
+        }
+    }
     MVR_WITH_BIG(pl.big, {
         if (mode == 0)
             k_cols<T, 0, B><<<grid, kThreads, smem, stream_>>>(src, dst, Kh, Hx, estride, ostride, NP, Pc, *d, tw);
@@ -446,6 +537,14 @@ int Engine<T>::launch_fwd_mirror(const Plan<T> &pl, const BlockMaps &bms, int nb
     const dim3 grid((unsigned)((nrows + pl.RP - 1) / pl.RP), (unsigned)nb);
     const double nv = (double)pl.b[0] * pl.b[1] * pl.b[2];
     MVR_TRY(prof_begin(KK_ROWS_FWD, nb * (sizeof(T) * nv + sizeof(V) * (double)pl.Pc)));
+    if constexpr (sizeof(T) == sizeof(float)) {
+        if (pl.wr) {
+            WARP_ROWS(pl.wr, (k_wrows_fwd<R_, SrcMirror<T>><<<grid, kThreads, 0, stream_>>>(SrcMirror<T>{src}, S, bms,
+                                                                                            pl.Pc, pl.twx)));
+            MVR_LAUNCHED("k_wrows_fwd");
+            return prof_end();
+        }
+    }
     MVR_WITH_BIG(pl.big, (k_rows_fwd<T, SrcMirror<T>, B><<<grid, kThreads, pl.smem_row, stream_>>>(
                              SrcMirror<T>{src}, S, bms, pl.Pc, pl.dx, pl.twx, pl.RP)));
     MVR_LAUNCHED("k_rows_fwd");
@@ -459,6 +558,13 @@ int Engine<T>::launch_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *
     const dim3 grid((unsigned)((nrows + pl.RP - 1) / pl.RP), (unsigned)nb);
     const double nv = (double)pl.b[0] * pl.b[1] * pl.b[2];
     MVR_TRY(prof_begin(KK_ROWS_RATIO, nb * (2.0 * sizeof(V) * (double)pl.Pc + 4.0 * nv)));
+    if constexpr (sizeof(T) == sizeof(float)) {
+        if (pl.wr) {
+            WARP_ROWS(pl.wr, (k_wrows_ratio<R_><<<grid, kThreads, 0, stream_>>>(S, img, bms, pl.Pc, pl.twx)));
+            MVR_LAUNCHED("k_wrows_ratio");
+            return prof_end();
+        }
+    }
     MVR_WITH_BIG(pl.big, (k_rows_ratio<T, B><<<grid, kThreads, pl.smem_row, stream_>>>(S, img, bms, pl.Pc, pl.dx,
                                                                                           pl.twx, pl.RP)));
     MVR_LAUNCHED("k_rows_ratio");
@@ -473,7 +579,15 @@ int Engine<T>::launch_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V 
     const unsigned gx = (unsigned)((nrows + pl.RP - 1) / pl.RP);
     const dim3 grid(gx, (unsigned)nb);
     MVR_TRY(prof_begin(KK_ROWS_UPDATE, bytes));
-    MVR_WITH_BIG(pl.big, {
+    bool warp_done = false;
+    if constexpr (sizeof(T) == sizeof(float)) {
+        if (pl.wr && epi == EPI_SEQ) {
+            WARP_ROWS(pl.wr, (k_wrows_update<R_><<<grid, kThreads, 0, stream_>>>(S, ua, bms, pl.Pc, pl.twx)));
+            MVR_LAUNCHED("k_wrows_update");
+            warp_done = true;
+        }
+    }
+    if (!warp_done) MVR_WITH_BIG(pl.big, {
         switch (epi) {
         case EPI_SEQ:
             k_rows_update<T, EPI_SEQ, B><<<grid, kThreads, pl.smem_row, stream_>>>(S, ua, bms, pl.Pc, pl.dx, pl.twx, pl.RP);

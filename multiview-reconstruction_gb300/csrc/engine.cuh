@@ -53,6 +53,8 @@ struct Plan {
     V *k1h = nullptr, *k2h = nullptr;
     int RP = 1, NPy = 1, NPz = 1;
     bool big = false;  // some axis needs radix 7, 11 or 13
+    int wr = 0;        // FP32 rows of Px = 64 wr reals (wr = 2, 3, 4) take the warp-shuffle row kernels
+    int wcy = 0, wcz = 0;  // FP32 columns of 32 wc (wc = 2, 3, 4, 5, 6, 8) take the warp-shuffle column kernels
     size_t smem_row = 0, smem_coly = 0, smem_colz = 0;
 };
 
