@@ -1,0 +1,188 @@
+// Column passes (y or z axis) as a two-phase register FFT over a shared-memory tile, for
+// FP32 column lengths n = V * 16 (V = 4, 6, 8, 12, 16: n = 64 ... 256).
+//
+// With n = V * T (T = 16), column element i = t + T v (t < T, v < V):
+//   phase 1, item (column, t):  V-point DFT over v of x[t + T v], times W_n^(t k1),
+//                               written back in place to positions t + T k1;
+//   phase 2, item (column, k1): T-point DFT over t of positions t + T k1, written back in
+//                               place: position k2 + T k1 holds frequency k1 + V k2.
+// Every thread keeps its V or T values in registers; the exchange between the phases is
+// one pass through shared memory.  The spectrum stays in that order ("tile order"), and
+// every spectrum along the axis (data and kernel spectra K1^, K2^) is produced by the
+// same forward pass, so the spectral product is taken position by position.  The
+// inverse runs the exact inverse of each phase in reverse order and returns natural
+// order, unnormalised (n times the inverse DFT).
+//
+// A CTA of 256 threads takes 16 consecutive x' columns at one index of the other axis;
+// the tile moves between HBM and shared memory in coalesced 16-wide row segments.
+// MODE 2 reads K^ straight from HBM in phase 2, in the same 16-wide segments.
+#pragma once
+#include "cols_warp.cuh"
+
+namespace mvr {
+
+// 12 = 4 x 3 (Cooley-Tukey): inner 4-point DFTs over q = 3 q1 + q2, twiddle
+// W12^(q2 k1), outer 3-point DFTs; output k = k1 + 4 k2.
+template <bool INV>
+__device__ __forceinline__ void dft12(float2 *v)
+{
+    float2 u[3][4];
+#pragma unroll
+    for (int q2 = 0; q2 < 3; ++q2) {
+#pragma unroll
+        for (int q1 = 0; q1 < 4; ++q1) u[q2][q1] = v[3 * q1 + q2];
+        dft4<INV>(u[q2]);
+    }
+    const float h = 0.8660254037844386f;  // cos(pi/6) = sin(pi/3)
+    const float sg = INV ? 1.0f : -1.0f;
+    // W12^1 = (h, -1/2), W12^2 = (1/2, -h), W12^3 = -i, W12^4 = (-1/2, -h), W12^6 = -1
+    u[1][1] = cmul(u[1][1], make_float2(h, sg * 0.5f));
+    u[1][2] = cmul(u[1][2], make_float2(0.5f, sg * h));
+    u[1][3] = mul_j<INV>(u[1][3]);
+    u[2][1] = cmul(u[2][1], make_float2(0.5f, sg * h));
+    u[2][2] = cmul(u[2][2], make_float2(-0.5f, sg * h));
+    u[2][3] = make_float2(-u[2][3].x, -u[2][3].y);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+        float2 w[3] = {u[0][k1], u[1][k1], u[2][k1]};
+        dft3<INV>(w);
+#pragma unroll
+        for (int k2 = 0; k2 < 3; ++k2) v[k1 + 4 * k2] = w[k2];
+    }
+}
+
+// 16 = 4 x 4: inner 4-point DFTs over q = 4 q1 + q2, twiddle W16^(q2 k1), outer 4-point
+// DFTs; output k = k1 + 4 k2.
+template <bool INV>
+__device__ __forceinline__ void dft16(float2 *v)
+{
+    float2 u[4][4];
+#pragma unroll
+    for (int q2 = 0; q2 < 4; ++q2) {
+#pragma unroll
+        for (int q1 = 0; q1 < 4; ++q1) u[q2][q1] = v[4 * q1 + q2];
+        dft4<INV>(u[q2]);
+    }
+    const float c = 0.92387953251128674f, s = 0.38268343236508977f, r = 0.70710678118654752f;
+    const float sg = INV ? 1.0f : -1.0f;
+    // W16^j = (cos(2 pi j / 16), -+ sin(2 pi j / 16))
+    const float2 w1 = make_float2(c, sg * s), w2 = make_float2(r, sg * r), w3 = make_float2(s, sg * c);
+    const float2 w6 = make_float2(-r, sg * r), w9 = make_float2(-c, -sg * s);
+    u[1][1] = cmul(u[1][1], w1);
+    u[1][2] = cmul(u[1][2], w2);
+    u[1][3] = cmul(u[1][3], w3);
+    u[2][1] = cmul(u[2][1], w2);
+    u[2][2] = mul_j<INV>(u[2][2]);
+    u[2][3] = cmul(u[2][3], w6);
+    u[3][1] = cmul(u[3][1], w3);
+    u[3][2] = cmul(u[3][2], w6);
+    u[3][3] = cmul(u[3][3], w9);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+        float2 w[4] = {u[0][k1], u[1][k1], u[2][k1], u[3][k1]};
+        dft4<INV>(w);
+#pragma unroll
+        for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = w[k2];
+    }
+}
+
+template <int N, bool INV>
+__device__ __forceinline__ void sdft(float2 (&a)[N])
+{
+    if constexpr (N == 4) dft4<INV>(a);
+    else if constexpr (N == 6) dft6<INV>(a);
+    else if constexpr (N == 8) dft8<INV>(a);
+    else if constexpr (N == 12) dft12<INV>(a);
+    else dft16<INV>(a);
+}
+
+constexpr int kTColT = 16;   // phase-2 length
+constexpr int kTColNP = 16;  // columns per tile
+
+template <int V, int MODE>
+__global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst, const float2 *__restrict__ Kh,
+                                                  int Hx, long long estride, long long ostride, long long Pc,
+                                                  const float2 *__restrict__ twg)
+{
+    constexpr int T = kTColT, NP = kTColNP, n = V * T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *A = reinterpret_cast<float2 *>(smem_raw);  // [n][NP]
+    float2 *tw = A + n * NP;                            // [n]: exp(-2 pi i j / n)
+    for (int i = threadIdx.x; i < n; i += 256) tw[i] = __ldg(&twg[i]);
+    const int x0 = blockIdx.x * NP;
+    const long long base = (long long)blockIdx.y * ostride + x0;
+    src += (long long)blockIdx.z * Pc;
+    dst += (long long)blockIdx.z * Pc;
+    const int np = min(NP, Hx - x0);
+    constexpr int tot = n * NP;
+    constexpr int step = 256 * kLoadBatch;
+    for (int t0 = threadIdx.x; t0 < tot; t0 += step) {
+        float2 r[kLoadBatch];
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            const int e = t0 + u * 256;
+            const int p = e % NP, i = e / NP;
+            r[u] = (e < tot && p < np) ? src[base + i * estride + p] : make_float2(0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int u = 0; u < kLoadBatch; ++u) {
+            const int e = t0 + u * 256;
+            if (e < tot) A[e] = r[u];
+        }
+    }
+    __syncthreads();
+    const int c = threadIdx.x % NP;
+    if (MODE != 1) {  // phase 1 forward: item (c, t)
+        const int t = threadIdx.x / NP;
+        float2 a[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) a[v] = A[(t + T * v) * NP + c];
+        sdft<V, false>(a);
+#pragma unroll
+        for (int k1 = 1; k1 < V; ++k1) a[k1] = cmul(a[k1], tw[t * k1]);
+#pragma unroll
+        for (int k1 = 0; k1 < V; ++k1) A[(t + T * k1) * NP + c] = a[k1];
+        __syncthreads();
+    }
+    {  // phase 2: item (c, k1)
+        const int k1 = threadIdx.x / NP;
+        if (k1 < V) {
+            float2 b[T];
+#pragma unroll
+            for (int t = 0; t < T; ++t) b[t] = A[(t + T * k1) * NP + c];
+            if (MODE != 1) sdft<T, false>(b);
+            if (MODE == 2) {
+                float2 kk[T];
+#pragma unroll
+                for (int k2 = 0; k2 < T; ++k2)
+                    kk[k2] = c < np ? __ldg(&Kh[base + (k2 + T * k1) * estride + c]) : make_float2(0.0f, 0.0f);
+#pragma unroll
+                for (int k2 = 0; k2 < T; ++k2) b[k2] = cmul(b[k2], kk[k2]);
+            }
+            if (MODE != 0) sdft<T, true>(b);
+#pragma unroll
+            for (int t = 0; t < T; ++t) A[(t + T * k1) * NP + c] = b[t];
+        }
+        __syncthreads();
+    }
+    if (MODE != 0) {  // phase 1 inverse: item (c, t)
+        const int t = threadIdx.x / NP;
+        float2 a[V];
+#pragma unroll
+        for (int k1 = 0; k1 < V; ++k1) a[k1] = A[(t + T * k1) * NP + c];
+#pragma unroll
+        for (int k1 = 1; k1 < V; ++k1) a[k1] = cmul(a[k1], cconj(tw[t * k1]));
+        sdft<V, true>(a);
+#pragma unroll
+        for (int v = 0; v < V; ++v) A[(t + T * v) * NP + c] = a[v];
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < tot; e += 256) {
+        const int p = e % NP, i = e / NP;
+        if (p < np) dst[base + i * estride + p] = A[e];
+    }
+}
+
+inline size_t tcols_smem(int V) { return sizeof(float2) * (size_t)(V * kTColT) * (kTColNP + 1); }
+
+}  // namespace mvr

@@ -2,6 +2,7 @@
 #include "engine.cuh"
 #include "rows_warp.cuh"
 #include "cols_warp.cuh"
+#include "cols_tile.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -147,6 +148,33 @@ int Engine<T>::cuda_check(cudaError_t e, const char *what)
         }                                     \
     } while (0)
 
+// Launches the kernel expression with V_ = the tile column length (n = 16 V_).
+#define TILE_COLS(tc, ...)                    \
+    do {                                      \
+        switch (tc) {                         \
+        case 4: {                             \
+            constexpr int V_ = 4;             \
+            __VA_ARGS__;                      \
+        } break;                              \
+        case 6: {                             \
+            constexpr int V_ = 6;             \
+            __VA_ARGS__;                      \
+        } break;                              \
+        case 8: {                             \
+            constexpr int V_ = 8;             \
+            __VA_ARGS__;                      \
+        } break;                              \
+        case 12: {                            \
+            constexpr int V_ = 12;            \
+            __VA_ARGS__;                      \
+        } break;                              \
+        default: {                            \
+            constexpr int V_ = 16;            \
+            __VA_ARGS__;                      \
+        } break;                              \
+        }                                     \
+    } while (0)
+
 namespace {
 template <typename V>
 V *dev_twiddles_impl(int n, cudaStream_t s, std::string &err)
@@ -193,6 +221,14 @@ void set_smem_limits_wcols(int m)
     cudaFuncSetAttribute(k_wcols<R, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
 }
 
+template <int V>
+void set_smem_limits_tcols(int m)
+{
+    cudaFuncSetAttribute(k_tcols<V, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_tcols<V, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_tcols<V, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+}
+
 template <typename T>
 void set_smem_limits()
 {
@@ -208,7 +244,21 @@ void set_smem_limits()
         set_smem_limits_wcols<5>(m);
         set_smem_limits_wcols<6>(m);
         set_smem_limits_wcols<8>(m);
+        set_smem_limits_tcols<4>(m);
+        set_smem_limits_tcols<6>(m);
+        set_smem_limits_tcols<8>(m);
+        set_smem_limits_tcols<12>(m);
+        set_smem_limits_tcols<16>(m);
     });
+}
+
+// Two-phase tile column length V (n = 16 V) for an FP32 axis of length n (0: none).
+template <typename T>
+int tile_col_v(int n)
+{
+    if (sizeof(T) != sizeof(float) || n % 16) return 0;
+    const int v = n / 16;
+    return (v == 4 || v == 6 || v == 8 || v == 12 || v == 16) ? v : 0;
 }
 
 // Warp-shuffle column radix for an FP32 axis of length n (0: shared-memory kernels).
@@ -398,8 +448,10 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
     pl.RP = RP;
     pl.smem_row = tws + RP * per_row;
     pl.wr = (sizeof(T) == sizeof(float) && (pl.P[0] == 128 || pl.P[0] == 192 || pl.P[0] == 256)) ? pl.P[0] / 64 : 0;
-    pl.wcy = warp_col_radix<T>(pl.P[1]);
-    pl.wcz = warp_col_radix<T>(pl.P[2]);
+    pl.tcy = tile_col_v<T>(pl.P[1]);
+    pl.tcz = tile_col_v<T>(pl.P[2]);
+    pl.wcy = pl.tcy ? 0 : warp_col_radix<T>(pl.P[1]);
+    pl.wcz = pl.tcz ? 0 : warp_col_radix<T>(pl.P[2]);
     auto col_np = [&](int n, int &NP, size_t &smem) -> bool {
         NP = 16;
         while (NP > 1 && sizeof(V) * (size_t)n * (1 + 2 * NP) > kColSmemTarget) NP >>= 1;
@@ -479,7 +531,22 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
     MVR_TRY(prof_begin(kind, mode == 2 ? 3.0 * cb : 2.0 * cb));
     const long long Pc = pl.Pc;
     const int wc = axis == 1 ? pl.wcy : pl.wcz;
+    const int tc = axis == 1 ? pl.tcy : pl.tcz;
     if constexpr (sizeof(T) == sizeof(float)) {
+        if (tc) {
+            const dim3 tgrid((unsigned)((Hx + kTColNP - 1) / kTColNP), (unsigned)nother, (unsigned)nb);
+            const size_t ts = tcols_smem(tc);
+            TILE_COLS(tc, {
+                if (mode == 0)
+                    k_tcols<V_, 0><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw);
+                else if (mode == 1)
+                    k_tcols<V_, 1><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw);
+                else
+                    k_tcols<V_, 2><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw);
+            });
+            MVR_LAUNCHED("k_tcols");
+            return prof_end();
+        }
         if (wc) {
             const dim3 wgrid((unsigned)((Hx + kWColNP - 1) / kWColNP), (unsigned)nother, (unsigned)nb);
             const size_t ws = wcols_smem(wc, mode);
@@ -539,8 +606,7 @@ int Engine<T>::launch_fwd_mirror(const Plan<T> &pl, const BlockMaps &bms, int nb
     MVR_TRY(prof_begin(KK_ROWS_FWD, nb * (sizeof(T) * nv + sizeof(V) * (double)pl.Pc)));
     if constexpr (sizeof(T) == sizeof(float)) {
         if (pl.wr) {
-            WARP_ROWS(pl.wr, (k_wrows_fwd<R_, SrcMirror<T>><<<grid, kThreads, 0, stream_>>>(SrcMirror<T>{src}, S, bms,
-                                                                                            pl.Pc, pl.twx)));
+            WARP_ROWS(pl.wr, (k_wrows_fwd<R_><<<grid, kThreads, 0, stream_>>>(src, S, bms, pl.Pc, pl.twx)));
             MVR_LAUNCHED("k_wrows_fwd");
             return prof_end();
         }

@@ -117,10 +117,30 @@ __device__ __forceinline__ void warp_c2r_pre(const float2 *__restrict__ in, floa
     }
 }
 
-// ---- forward: extract + R2C ----------------------------------------------------------
-template <int R, class Src>
-__global__ void __launch_bounds__(256) k_wrows_fwd(Src src, float2 *__restrict__ S, const BlockMaps bms, long long Pc,
-                                                   const float2 *__restrict__ twg)
+// Row-invariant x mappings, computed once per CTA into shared memory: the volume x of
+// every domain x depends on the block only, not on the row.
+struct RowX {
+    int mir[256];  // psi: volume x under the mirror mapping
+    int zx[256];   // img / weight: volume x of a block voxel inside the volume, else -1
+};
+
+// domain_ext: x is a domain index (extension wraps to negative block x); otherwise a
+// block index.  Ends with a CTA barrier.
+__device__ __forceinline__ void row_x_init(RowX &rx, const BlockMap &bm, int Px, bool domain_ext)
+{
+    for (int x = threadIdx.x; x < Px; x += blockDim.x) {
+        rx.mir[x] = (int)mirror_x(bm, x);
+        const int bx = domain_ext ? ext_e(x, bm.P[0], bm.L[0]) : x;
+        const long long gx = bm.off[0] + bx;
+        rx.zx[x] = (bx >= 0 && bx < bm.b[0] && gx >= 0 && gx < bm.D[0]) ? (int)gx : -1;
+    }
+    __syncthreads();
+}
+
+// ---- forward: extract psi (mirror-single) + R2C -----------------------------------------
+template <int R>
+__global__ void __launch_bounds__(256) k_wrows_fwd(const float *__restrict__ psi, float2 *__restrict__ S,
+                                                   const BlockMaps bms, long long Pc, const float2 *__restrict__ twg)
 {
     constexpr int m = 32 * R;
     __shared__ float2 srow[8][m + 1];
@@ -129,15 +149,17 @@ __global__ void __launch_bounds__(256) k_wrows_fwd(Src src, float2 *__restrict__
     float2 *Sb = S + (long long)blockIdx.y * Pc;
     WarpTw<R> t;
     warp_tw_init<R>(t, twg, 2 * m, lane);
+    __shared__ RowX rx;
+    row_x_init(rx, bm, 2 * m, true);
     const long long nrows = (long long)bm.P[1] * bm.P[2];
     for (long long row = (long long)blockIdx.x * 8 + wib; row < nrows; row += (long long)gridDim.x * 8) {
         const int y = (int)(row % bm.P[1]), z = (int)(row / bm.P[1]);
-        const typename Src::Row Rw = src.row(bm, y, z);
+        const float *pr = psi + mirror_row(bm, y, z).base;
         float2 a[R];
 #pragma unroll
         for (int s = 0; s < R; ++s) {
-            const int q = lane + 32 * s;
-            a[s] = make_float2(src.template at<float>(Rw, bm, 2 * q), src.template at<float>(Rw, bm, 2 * q + 1));
+            const int x = 2 * (lane + 32 * s);
+            a[s] = make_float2(__ldg(pr + rx.mir[x]), __ldg(pr + rx.mir[x + 1]));
         }
         warp_fft<R, false>(a, t, lane);
         warp_store_natural<R>(a, srow[wib], lane);
@@ -146,6 +168,9 @@ __global__ void __launch_bounds__(256) k_wrows_fwd(Src src, float2 *__restrict__
 }
 
 // ---- C2R -> quotient -> R2C ----------------------------------------------------------
+// DeconvolutionMethods.java:71-74: img > 0 ? img / conv1 : 1.  Voxels outside the
+// block (the value-1 extension) and outside the volume (img zero-extended) both give 1,
+// so they are read as img = 0.
 template <int R>
 __global__ void __launch_bounds__(256) k_wrows_ratio(float2 *__restrict__ S, const float *__restrict__ img,
                                                      const BlockMaps bms, long long Pc, const float2 *__restrict__ twg)
@@ -157,32 +182,31 @@ __global__ void __launch_bounds__(256) k_wrows_ratio(float2 *__restrict__ S, con
     float2 *Sb = S + (long long)blockIdx.y * Pc;
     WarpTw<R> t;
     warp_tw_init<R>(t, twg, 2 * m, lane);
+    __shared__ RowX rx;
+    row_x_init(rx, bm, 2 * m, true);
     const long long nrows = (long long)bm.P[1] * bm.P[2];
     for (long long row = (long long)blockIdx.x * 8 + wib; row < nrows; row += (long long)gridDim.x * 8) {
         float2 *Srow = Sb + row * (m + 1);
         float2 a[R];
         warp_c2r_pre<R>(Srow, a, t, lane);
-        warp_fft<R, true>(a, t, lane);
-        warp_store_natural<R>(a, srow[wib], lane);
         const int y = (int)(row % bm.P[1]), z = (int)(row / bm.P[1]);
         const int ey = ext_e(y, bm.P[1], bm.L[1]), ez = ext_e(z, bm.P[2], bm.L[2]);
         const bool rin = ey >= 0 && ey < bm.b[1] && ez >= 0 && ez < bm.b[2];
-        const ZeroRow zr = rin ? zero_row(bm, ey, ez) : ZeroRow{-1};
+        const long long zb = rin ? zero_row(bm, ey, ez).base : -1;
         float im[R][2];
 #pragma unroll
-        for (int s = 0; s < R; ++s) {
-            const int q = lane + 32 * s;
+        for (int s = 0; s < R; ++s)
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int ex = ext_e(2 * q + h, bm.P[0], bm.L[0]);
-                im[s][h] = (rin && ex >= 0 && ex < bm.b[0]) ? zero_at(img, bm, zr, ex) : -1.0f;
+                const int gx = rx.zx[2 * (lane + 32 * s) + h];
+                im[s][h] = (zb >= 0 && gx >= 0) ? __ldg(img + zb + gx) : 0.0f;
             }
-        }
+        warp_fft<R, true>(a, t, lane);
+        warp_store_natural<R>(a, srow[wib], lane);
 #pragma unroll
         for (int s = 0; s < R; ++s) {
             const float2 c = srow[wib][lane + 32 * s];  // conv1 at x = 2q, 2q+1
-            a[s] = make_float2(im[s][0] < 0.0f ? 1.0f : quotient(im[s][0], c.x),
-                               im[s][1] < 0.0f ? 1.0f : quotient(im[s][1], c.y));
+            a[s] = make_float2(quotient(im[s][0], c.x), quotient(im[s][1], c.y));
         }
         __syncwarp();
         warp_fft<R, false>(a, t, lane);
@@ -204,8 +228,21 @@ __global__ void __launch_bounds__(256) k_wrows_update(float2 *__restrict__ S, Up
     float2 *Sb = S + (long long)blockIdx.y * Pc;
     WarpTw<R> t;
     warp_tw_init<R>(t, twg, 2 * m, lane);
+    __shared__ RowX rx;
+    row_x_init(rx, bm, 2 * m, false);
+    unsigned inb = 0, wr = 0;  // bit (2s+h): x inside the block / inside the written region
+#pragma unroll
+    for (int s = 0; s < R; ++s)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int x = 2 * (lane + 32 * s) + h;
+            if (x < bm.b[0]) inb |= 1u << (2 * s + h);
+            if (x < bm.b[0] && x >= bm.wlo[0] && x < bm.whi[0]) wr |= 1u << (2 * s + h);
+        }
     const float *psrc = reinterpret_cast<const float *>(ua.psi_src);
     float *pdst = reinterpret_cast<float *>(ua.psi_dst);
+    const float *wgt = ua.weight[0];
+    const float minI = ua.minI, maxI = ua.maxI;
     float ksum = 0.0f, kcomp = 0.0f, kmax = -1.0f;
     const long long nrows = (long long)bm.P[1] * bm.P[2];
     for (long long row = (long long)blockIdx.x * 8 + wib; row < nrows; row += (long long)gridDim.x * 8) {
@@ -213,42 +250,39 @@ __global__ void __launch_bounds__(256) k_wrows_update(float2 *__restrict__ S, Up
         if (y >= bm.b[1] || z >= bm.b[2]) continue;  // extension rows carry no block voxels
         float2 a[R];
         warp_c2r_pre<R>(Sb + row * (m + 1), a, t, lane);
-        warp_fft<R, true>(a, t, lane);
-        warp_store_natural<R>(a, srow[wib], lane);
-        const ZeroRow zr = zero_row(bm, y, z);
-        const MirrorRow mr = mirror_row(bm, y, z);
-        const bool wrow = y >= bm.wlo[1] && y < bm.whi[1] && z >= bm.wlo[2] && z < bm.whi[2];
-        const long long orow = ((bm.ooff[2] + z) * bm.OD[1] + (bm.ooff[1] + y)) * bm.OD[0] + bm.ooff[0];
+        const float *pr = psrc + mirror_row(bm, y, z).base;
+        const long long zb = zero_row(bm, y, z).base;
         float lastv[R][2], wv[R][2];
 #pragma unroll
-        for (int s = 0; s < R; ++s) {
-            const int q = lane + 32 * s;
+        for (int s = 0; s < R; ++s)
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int x = 2 * q + h;
-                const bool ok = x < bm.b[0];
-                lastv[s][h] = ok ? psrc[mr.base + mirror_x(bm, x)] : 0.0f;
-                wv[s][h] = ok ? zero_at(ua.weight[0], bm, zr, x) : 0.0f;
+                const int x = 2 * (lane + 32 * s) + h;
+                const bool ok = (inb >> (2 * s + h)) & 1u;
+                const int gx = rx.zx[x];
+                lastv[s][h] = ok ? __ldg(pr + rx.mir[x]) : 0.0f;
+                wv[s][h] = (ok && zb >= 0 && gx >= 0) ? __ldg(wgt + zb + gx) : 0.0f;
             }
-        }
+        warp_fft<R, true>(a, t, lane);
+        warp_store_natural<R>(a, srow[wib], lane);
+        const bool wrow = y >= bm.wlo[1] && y < bm.whi[1] && z >= bm.wlo[2] && z < bm.whi[2];
+        float *orow = pdst + ((bm.ooff[2] + z) * bm.OD[1] + (bm.ooff[1] + y)) * bm.OD[0] + bm.ooff[0];
 #pragma unroll
         for (int s = 0; s < R; ++s) {
-            const int q = lane + 32 * s;
-            const float2 c = srow[wib][q];
+            const float2 c = srow[wib][lane + 32 * s];
             const float cv[2] = {c.x, c.y};
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int x = 2 * q + h;
-                if (x >= bm.b[0]) continue;
+                if (!((inb >> (2 * s + h)) & 1u)) continue;
                 const float last = lastv[s][h];
-                const float next = next_value(last, cv[h], wv[s][h], ua.lambda, ua.minI, ua.maxI);
-                const float ch = next - last;
+                const float next = next_value(last, cv[h], wv[s][h], ua.lambda, minI, maxI);
+                const float ch = next - last;  // signed change (DeconvolutionMethods.java:308)
                 const float ky = ch - kcomp;
                 const float kt = ksum + ky;
                 kcomp = (kt - ksum) - ky;
                 ksum = kt;
                 kmax = kmax > ch ? kmax : ch;
-                if (wrow && x >= bm.wlo[0] && x < bm.whi[0]) pdst[orow + x] = next;
+                if (wrow && ((wr >> (2 * s + h)) & 1u)) orow[2 * (lane + 32 * s) + h] = next;
             }
         }
         __syncwarp();
