@@ -63,6 +63,22 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
+def ncu_traffic():
+    """DRAM bytes per launch (read + write) from the committed ncu summary: the lines of
+    its ```traffic block, 'kernel-family bytes'."""
+    path = os.path.join(ROOT, "profiles", "plane_kernels_4view_256cubed.md")
+    out, inside = {}, False
+    if os.path.exists(path):
+        for line in open(path):
+            if line.startswith("```"):
+                inside = line.strip() == "```traffic"
+                continue
+            if inside and line.strip():
+                k, v = line.split()
+                out[k] = float(v)
+    return out
+
+
 def make_data():
     import synthetic
 
@@ -248,7 +264,7 @@ def run_gb300(args, ws, rank, local):
     d_w = [torch.from_numpy(a).to(f"cuda:{dev}") for a in ds.weights]
     dec = M.Deconvolution(DIMS, VIEWS, BLOCK, mul=False, psf_type=M.PSF_OPTIMIZATION_I, psf_norm_threads=0,
                           lam=LAMBDA, boundary=boundary, precision=M.PRECISION_FP32, weight_norm=M.WEIGHTS_HARD,
-                          device=dev)
+                          batch_blocks=args.batch, device=dev)
     for v in range(VIEWS):
         dec.set_view_device(v, d_img[v].data_ptr(), d_w[v].data_ptr(), ds.psfs[v])
     dec.prepare()
@@ -290,11 +306,7 @@ def run_gb300(args, ws, rank, local):
     dname, (dms, dlaunch, dbytes) = dom
     peak, peak_kind = load_peaks()
     achieved = (dbytes / dlaunch) / (dms / dlaunch / 1e3) / 1e9 if dlaunch else 0.0
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", "ncu_traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            traffic = json.load(f).get(dname)
+    traffic = ncu_traffic().get(dname)
     kernels = {k: {"share": v[0] / total_ms, "launches": v[1],
                    "gbs": (v[2] / (v[0] / 1e3) / 1e9) if v[0] > 0 else None} for k, v in prof.items() if v[1]}
     path_bytes = sum(v[2] for v in prof.values())
@@ -385,6 +397,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--boundary", choices=["circular", "reference"], default="circular")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="blocks per batched launch (1..16); 0 = autotuned")
     ap.add_argument("--cpu-blocks", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

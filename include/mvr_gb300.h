@@ -26,6 +26,11 @@
  * used by one host thread at a time (the reference runs one ComputeBlockThread per
  * Java thread).  There is no CPU fallback: without a usable GB300 (sm_103a) the
  * create calls fail with MVR_ERR_CUDA.
+ *
+ * FP32 FFT domains with Px, Py in {128, 192} run on the plane kernels (x and y transforms
+ * fused per z-plane); the environment variable MVR_PLANE_KERNELS=0, read when kernels are
+ * set or a deconvolution is prepared, selects the row / column kernels instead (for
+ * comparisons; results agree to float rounding).
  */
 #ifndef MVR_GB300_H
 #define MVR_GB300_H
@@ -187,7 +192,7 @@ MVR_API void *mvr_decon_stream(mvr_decon *h);
 /* Number of kernel launches the handle has queued so far. */
 MVR_API long long mvr_decon_launch_count(const mvr_decon *h);
 /* Per-kernel-family timing with CUDA events on the handle's stream (off by default). */
-#define MVR_KERNEL_KINDS 8
+#define MVR_KERNEL_KINDS 11
 MVR_API int mvr_decon_set_profiling(mvr_decon *h, int on);
 /* Accumulated {ms, launches, algorithmic bytes} per family (MVR_KERNEL_KINDS entries each);
  * synchronises the stream. */
@@ -195,6 +200,16 @@ MVR_API int mvr_decon_get_profile(mvr_decon *h, double *ms, long long *launches,
 MVR_API const char *mvr_kernel_name(int kind);
 /* Blocks per batched launch in use (chosen by the autotuner unless fixed). */
 MVR_API int mvr_decon_batch(const mvr_decon *h);
+/* Whole iterations of mvr_decon_run as CUDA graphs (on by default; the batched form of
+ * the iteration loop MultiViewDeconvolution.runIterations, MultiViewDeconvolution.java:
+ * 160-200).  An iteration in a new state (psi buffer, statistics slots, batch size,
+ * scratch allocation, image/weight pointers) runs eagerly; the next one in that state is
+ * captured and later ones replay it.  Results are identical to the eager launches.
+ * on = 0 drops the graphs and launches eagerly.  While profiling is on, iterations run
+ * eagerly. */
+MVR_API int mvr_decon_set_graphs(mvr_decon *h, int on);
+/* Number of captured iteration graphs held by the handle. */
+MVR_API int mvr_decon_graphs_captured(const mvr_decon *h);
 /* Data-likelihood residual of the current psi (no reference counterpart; the reference
  * logs only the change statistics): the Poisson negative log-likelihood
  * sum_v sum_x w_v (conv1_v - img_v ln conv1_v) over img_v > 0, each voxel once, reduced

@@ -108,6 +108,7 @@ __global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *A = reinterpret_cast<float2 *>(smem_raw);  // [n][NP]
     float2 *tw = A + n * NP;                            // [n]: exp(-2 pi i j / n)
+    float2 *KA = tw + n;                                // MODE 2: [n][NP] tile of K^
     for (int i = threadIdx.x; i < n; i += 256) tw[i] = __ldg(&twg[i]);
     const int x0 = blockIdx.x * NP;
     const long long base = (long long)blockIdx.y * ostride + x0;
@@ -117,22 +118,29 @@ __global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst
     constexpr int tot = n * NP;
     constexpr int step = 256 * kLoadBatch;
     for (int t0 = threadIdx.x; t0 < tot; t0 += step) {
-        float2 r[kLoadBatch];
+        float2 r[kLoadBatch], q[kLoadBatch];
 #pragma unroll
         for (int u = 0; u < kLoadBatch; ++u) {
             const int e = t0 + u * 256;
             const int p = e % NP, i = e / NP;
             r[u] = (e < tot && p < np) ? src[base + i * estride + p] : make_float2(0.0f, 0.0f);
+            if (MODE == 2) q[u] = (e < tot && p < np) ? __ldg(&Kh[base + i * estride + p]) : make_float2(0.0f, 0.0f);
         }
 #pragma unroll
         for (int u = 0; u < kLoadBatch; ++u) {
             const int e = t0 + u * 256;
-            if (e < tot) A[e] = r[u];
+            if (e < tot) {
+                A[e] = r[u];
+                if (MODE == 2) KA[e] = q[u];
+            }
         }
     }
     __syncthreads();
     const int c = threadIdx.x % NP;
-    if (MODE != 1) {  // phase 1 forward: item (c, t)
+    // items of columns beyond the domain (the last tile of Hx = 16 q + 1 columns holds
+    // one) skip their transforms
+    const bool live = c < np;
+    if (MODE != 1 && live) {  // phase 1 forward: item (c, t)
         const int t = threadIdx.x / NP;
         float2 a[V];
 #pragma unroll
@@ -142,22 +150,18 @@ __global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst
         for (int k1 = 1; k1 < V; ++k1) a[k1] = cmul(a[k1], tw[t * k1]);
 #pragma unroll
         for (int k1 = 0; k1 < V; ++k1) A[(t + T * k1) * NP + c] = a[k1];
-        __syncthreads();
     }
+    if (MODE != 1) __syncthreads();
     {  // phase 2: item (c, k1)
         const int k1 = threadIdx.x / NP;
-        if (k1 < V) {
+        if (k1 < V && live) {
             float2 b[T];
 #pragma unroll
             for (int t = 0; t < T; ++t) b[t] = A[(t + T * k1) * NP + c];
             if (MODE != 1) sdft<T, false>(b);
             if (MODE == 2) {
-                float2 kk[T];
 #pragma unroll
-                for (int k2 = 0; k2 < T; ++k2)
-                    kk[k2] = c < np ? __ldg(&Kh[base + (k2 + T * k1) * estride + c]) : make_float2(0.0f, 0.0f);
-#pragma unroll
-                for (int k2 = 0; k2 < T; ++k2) b[k2] = cmul(b[k2], kk[k2]);
+                for (int k2 = 0; k2 < T; ++k2) b[k2] = cmul(b[k2], KA[(k2 + T * k1) * NP + c]);
             }
             if (MODE != 0) sdft<T, true>(b);
 #pragma unroll
@@ -165,7 +169,7 @@ __global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst
         }
         __syncthreads();
     }
-    if (MODE != 0) {  // phase 1 inverse: item (c, t)
+    if (MODE != 0 && live) {  // phase 1 inverse: item (c, t)
         const int t = threadIdx.x / NP;
         float2 a[V];
 #pragma unroll
@@ -175,14 +179,19 @@ __global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst
         sdft<V, true>(a);
 #pragma unroll
         for (int v = 0; v < V; ++v) A[(t + T * v) * NP + c] = a[v];
-        __syncthreads();
     }
+    if (MODE != 0) __syncthreads();
     for (int e = threadIdx.x; e < tot; e += 256) {
         const int p = e % NP, i = e / NP;
         if (p < np) dst[base + i * estride + p] = A[e];
     }
 }
 
-inline size_t tcols_smem(int V) { return sizeof(float2) * (size_t)(V * kTColT) * (kTColNP + 1); }
+// data tile + twiddles (+ the K^ tile of MODE 2)
+inline size_t tcols_smem(int V, int mode = 2)
+{
+    const size_t n = (size_t)V * kTColT;
+    return sizeof(float2) * (n * kTColNP + n + (mode == 2 ? n * kTColNP : 0));
+}
 
 }  // namespace mvr

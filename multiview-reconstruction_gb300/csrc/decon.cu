@@ -344,6 +344,8 @@ public:
     virtual int profile(KernelProfile &out) = 0;
     virtual int batch() const = 0;
     virtual int likelihood(double *total, double *per_view) = 0;
+    virtual int set_graphs(bool on) = 0;
+    virtual int graphs_captured() const = 0;
 };
 
 template <typename T>
@@ -403,7 +405,44 @@ private:
     int conv_zero(const float *in, const int id[3], const float *k, const int kd[3], float *out);
     int psf_init();
     int run_step(int s, double *stats_slot, bool trial, int batch);
+    int run_iteration(double *stats_base, size_t stats_stride);
     int autotune();
+    // Whole iterations captured as CUDA graphs, one per starting state: the psi buffer
+    // (the Jacobi path swaps psi and the staging volume every view-step), the stats
+    // slots, the batch size and the engine's scratch allocation.  The first iteration in
+    // a new state runs eagerly (it may allocate scratch); when the next one starts in the
+    // same state it is captured, and every later one replays the graph.
+    struct IterGraph {
+        const T *psi_start = nullptr;
+        const double *stats = nullptr;
+        int batch = 0;
+        long long epoch = -1;
+        long long inputs = -1;
+        cudaGraphExec_t exec = nullptr;
+        T *psi_end = nullptr, *stage_end = nullptr;
+        long long launches = 0;
+        bool same(const IterGraph &o) const
+        {
+            return psi_start == o.psi_start && stats == o.stats && batch == o.batch && epoch == o.epoch &&
+                   inputs == o.inputs;
+        }
+    };
+    std::vector<IterGraph> graphs_;
+    std::vector<IterGraph> seen_;  // states of recent eager iterations (psi alternates between two buffers)
+    bool graphs_on_ = true;
+    long long inputs_epoch_ = 0;  // bumped when image/weight pointers or the set-up change
+    void drop_graphs();
+
+public:
+    int set_graphs(bool on) override
+    {
+        graphs_on_ = on;
+        if (!on) drop_graphs();
+        return MVR_OK;
+    }
+    int graphs_captured() const override { return (int)graphs_.size(); }
+
+private:
     int normalize_weights();
     int batch_ = 1;
     std::vector<std::pair<int, float>> tune_;  // (blocks per launch, ms per view-step)
@@ -452,6 +491,16 @@ Decon<T>::~Decon()
     cudaFree(d_perm_);
     cudaFree(d_flag_);
     cudaFree(d_stats_);
+    drop_graphs();
+}
+
+template <typename T>
+void Decon<T>::drop_graphs()
+{
+    for (auto &g : graphs_)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    graphs_.clear();
+    seen_.clear();
 }
 
 template <typename T>
@@ -481,6 +530,7 @@ int Decon<T>::set_images(int v, const float *img, const float *w, bool on_device
     D_CUDA(cudaSetDevice(p_.device));
     View &vw = views_[v];
     cudaStream_t s = engine_.stream();
+    ++inputs_epoch_;
     if (on_device) {
         if (vw.own_img) cudaFree(vw.img);
         if (vw.own_w) cudaFree(vw.w_raw);
@@ -659,6 +709,8 @@ template <typename T>
 int Decon<T>::prepare()
 {
     D_CUDA(cudaSetDevice(p_.device));
+    ++inputs_epoch_;
+    drop_graphs();
     cudaStream_t s = engine_.stream();
     const int nv = p_.num_views;
     for (int v = 0; v < nv; ++v) {
@@ -941,6 +993,78 @@ int Decon<T>::run_step(int st, double *stats_slot, bool trial, int batch)
     return MVR_OK;
 }
 
+// One iteration (all view-steps): replayed from a captured graph when one exists for
+// the current state, captured when the previous iteration ran in the same state, else
+// run eagerly.  With profiling on, every iteration runs eagerly (the profiler brackets
+// launches with events).
+template <typename T>
+int Decon<T>::run_iteration(double *stats_base, size_t stats_stride)
+{
+    const int steps = num_steps();
+    auto eager = [&]() -> int {
+        for (int st = 0; st < steps; ++st)
+            D_TRY(run_step(st, stats_base ? stats_base + (size_t)st * stats_stride : nullptr, false, batch_));
+        return MVR_OK;
+    };
+    if (!graphs_on_ || engine_.profiling()) return eager();
+    cudaStream_t s = engine_.stream();
+    IterGraph key;
+    key.psi_start = psi_;
+    key.stats = stats_base;
+    key.batch = batch_;
+    key.epoch = engine_.alloc_epoch();
+    key.inputs = inputs_epoch_;
+    for (const auto &g : graphs_) {
+        if (!g.same(key)) continue;
+        D_CUDA(cudaGraphLaunch(g.exec, s));
+        psi_ = g.psi_end;
+        stage_ = g.stage_end;
+        engine_.count_replayed(g.launches);
+        return MVR_OK;
+    }
+    bool seen = false;
+    for (const auto &k : seen_) seen = seen || k.same(key);
+    if (!seen) {
+        D_TRY(eager());
+        if (seen_.size() >= 4) seen_.erase(seen_.begin());
+        seen_.push_back(key);
+        return MVR_OK;
+    }
+    // capture this iteration; the captured work runs when the graph is launched
+    T *psi0 = psi_, *stage0 = stage_;
+    const long long l0 = engine_.launches();
+    D_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int rc = eager();
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (rc != MVR_OK || ce != cudaSuccess || graph == nullptr) {
+        if (graph) cudaGraphDestroy(graph);
+        psi_ = psi0;
+        stage_ = stage0;
+        if (rc != MVR_OK) return rc;
+        return cuda(ce == cudaSuccess ? cudaErrorStreamCaptureInvalidated : ce, "cudaStreamEndCapture");
+    }
+    key.psi_end = psi_;
+    key.stage_end = stage_;
+    key.launches = engine_.launches() - l0;
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) {
+        psi_ = psi0;
+        stage_ = stage0;
+        return cuda(ie, "cudaGraphInstantiate");
+    }
+    key.exec = exec;
+    if (graphs_.size() >= 8) {  // keep the most recent states
+        cudaGraphExecDestroy(graphs_.front().exec);
+        graphs_.erase(graphs_.begin());
+    }
+    graphs_.push_back(key);
+    D_CUDA(cudaGraphLaunch(exec, s));
+    return MVR_OK;
+}
+
 // Batch size per launch: the fastest of 1, 2, 4, 8, 16 blocks on one view-step
 // (CUDA events on the engine stream), unless fixed by the parameters.
 template <typename T>
@@ -1000,8 +1124,7 @@ int Decon<T>::run(int iterations, double *stats)
     }
     std::vector<double> hs;
     for (int it = 0; it < iterations; ++it) {
-        for (int st = 0; st < steps; ++st)
-            D_TRY(run_step(st, stats ? d_stats_ + (size_t)st * maxb * 2 : nullptr, false, batch_));
+        D_TRY(run_iteration(stats ? d_stats_ : nullptr, maxb * 2));
         if (stats) {
             hs.resize((size_t)need);
             D_CUDA(cudaMemcpyAsync(hs.data(), d_stats_, sizeof(double) * (size_t)need, cudaMemcpyDeviceToHost,
@@ -1200,6 +1323,8 @@ extern "C" int mvr_decon_get_profile(mvr_decon *h, double *ms, long long *launch
 }
 extern "C" const char *mvr_kernel_name(int kind) { return mvr::kernel_kind_name(kind); }
 extern "C" int mvr_decon_batch(const mvr_decon *h) { return h ? h->impl->batch() : -1; }
+extern "C" int mvr_decon_set_graphs(mvr_decon *h, int on) { return h ? h->impl->set_graphs(on != 0) : MVR_ERR_ARG; }
+extern "C" int mvr_decon_graphs_captured(const mvr_decon *h) { return h ? h->impl->graphs_captured() : -1; }
 extern "C" int mvr_decon_likelihood(mvr_decon *h, double *total, double *per_view)
 {
     return h ? h->impl->likelihood(total, per_view) : MVR_ERR_ARG;

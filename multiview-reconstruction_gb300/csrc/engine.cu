@@ -3,10 +3,12 @@
 #include "rows_warp.cuh"
 #include "cols_warp.cuh"
 #include "cols_tile.cuh"
+#include "xy.cuh"
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -23,7 +25,8 @@ constexpr size_t kSmemMax = 227 * 1024;
 const char *kernel_kind_name(int k)
 {
     static const char *names[KK_COUNT] = {"rows_fwd_extract", "cols_y_fwd", "cols_y_inv", "cols_z_fwd_mul_inv",
-                                          "rows_c2r_ratio_r2c", "rows_c2r_update", "reduce_stats", "paste"};
+                                          "rows_c2r_ratio_r2c", "rows_c2r_update", "reduce_stats", "paste",
+                                          "xy_fwd_extract", "xy_c2r_ratio_r2c", "xy_c2r_update"};
     return (k >= 0 && k < KK_COUNT) ? names[k] : "?";
 }
 
@@ -211,6 +214,7 @@ void set_smem_limits_big(int m)
     cudaFuncSetAttribute(k_rows_update<T, EPI_MUL_ACC, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     cudaFuncSetAttribute(k_rows_update<T, EPI_MUL_FINAL, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     cudaFuncSetAttribute(k_rows_update<T, EPI_STORE, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_rows_update<T, EPI_NLL, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
 }
 
 template <int R>
@@ -361,6 +365,7 @@ int Engine<T>::reserve(long long Pc, long long nvox_block, long long rows, int n
         MVR_CUDA(cudaMalloc(&S0_, sizeof(V) * (size_t)(Pc * nb)));
         MVR_CUDA(cudaMalloc(&S1_, sizeof(V) * (size_t)(Pc * nb)));
         Scap_ = Pc * nb;
+        ++alloc_epoch_;
     }
     if (rows * nb > partcap_) {
         cudaFree(partials_);
@@ -368,6 +373,7 @@ int Engine<T>::reserve(long long Pc, long long nvox_block, long long rows, int n
         partcap_ = 0;
         MVR_CUDA(cudaMalloc(&partials_, sizeof(double) * 2 * (size_t)(rows * nb)));
         partcap_ = rows * nb;
+        ++alloc_epoch_;
     }
     (void)nvox_block;
     return OK;
@@ -382,6 +388,7 @@ int Engine<T>::reserve_prod(long long n)
         prodcap_ = 0;
         MVR_CUDA(cudaMalloc(&prod_, sizeof(double) * (size_t)n));
         prodcap_ = n;
+        ++alloc_epoch_;
     }
     return OK;
 }
@@ -450,6 +457,12 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
     pl.wr = (sizeof(T) == sizeof(float) && (pl.P[0] == 128 || pl.P[0] == 192 || pl.P[0] == 256)) ? pl.P[0] / 64 : 0;
     pl.tcy = tile_col_v<T>(pl.P[1]);
     pl.tcz = tile_col_v<T>(pl.P[2]);
+    {
+        // plane kernels: FP32, z along the tile column kernels; MVR_PLANE_KERNELS=0 turns them off
+        const char *env = std::getenv("MVR_PLANE_KERNELS");
+        const bool allow = !(env && env[0] == '0');
+        pl.xy = (allow && sizeof(T) == sizeof(float) && pl.tcz) ? xy_combo(pl.P) : 0;
+    }
     pl.wcy = pl.tcy ? 0 : warp_col_radix<T>(pl.P[1]);
     pl.wcz = pl.tcz ? 0 : warp_col_radix<T>(pl.P[2]);
     auto col_np = [&](int n, int &NP, size_t &smem) -> bool {
@@ -490,6 +503,14 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
             kdev = kbuf_;
         }
         SrcKernel src{kdev, {kd1[0], kd1[1], kd1[2]}, scale};
+        if constexpr (sizeof(T) == sizeof(float)) {
+            if (pl.xy) {
+                ++launches_;
+                MVR_CUDA(xy_fwd_kernel(pl.xy, src, S0_, bms, 1, pl.P[2], pl.Pc, pl.twx, pl.twy, stream_));
+                MVR_TRY(launch_cols(pl, 2, 0, S0_, which == 0 ? pl.k1h : pl.k2h, nullptr, 1));
+                continue;
+            }
+        }
         const dim3 grid((unsigned)((nrows + pl.RP - 1) / pl.RP), 1);
         MVR_WITH_BIG(pl.big, (k_rows_fwd<T, SrcKernel, B><<<grid, kThreads, pl.smem_row, stream_>>>(
                                  src, S0_, bms, pl.Pc, pl.dx, pl.twx, pl.RP)));
@@ -535,7 +556,7 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
     if constexpr (sizeof(T) == sizeof(float)) {
         if (tc) {
             const dim3 tgrid((unsigned)((Hx + kTColNP - 1) / kTColNP), (unsigned)nother, (unsigned)nb);
-            const size_t ts = tcols_smem(tc);
+            const size_t ts = tcols_smem(tc, mode);
             TILE_COLS(tc, {
                 if (mode == 0)
                     k_tcols<V_, 0><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw);
@@ -691,6 +712,50 @@ int Engine<T>::launch_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V 
     return OK;
 }
 
+// ---- plane kernels (FP32 plans with pl.xy) ---------------------------------------------
+template <typename T>
+int Engine<T>::launch_xy_fwd(const Plan<T> &pl, const BlockMaps &bms, int nb, const T *src, V *S)
+{
+    if constexpr (sizeof(T) == sizeof(float)) {
+        const double nv = (double)pl.b[0] * pl.b[1] * pl.b[2];
+        MVR_TRY(prof_begin(KK_XY_FWD, nb * (sizeof(T) * nv + sizeof(V) * (double)pl.Pc)));
+        MVR_CUDA(xy_fwd_mirror(pl.xy, src, S, bms, nb, pl.P[2], pl.Pc, pl.twx, pl.twy, stream_));
+        return prof_end();
+    }
+    return fail(ERR_STATE, "plane kernels are FP32 only");
+}
+
+template <typename T>
+int Engine<T>::launch_xy_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img)
+{
+    if constexpr (sizeof(T) == sizeof(float)) {
+        const double nv = (double)pl.b[0] * pl.b[1] * pl.b[2];
+        MVR_TRY(prof_begin(KK_XY_RATIO, nb * (2.0 * sizeof(V) * (double)pl.Pc + 4.0 * nv)));
+        MVR_CUDA(xy_ratio(pl.xy, S, img, bms, nb, pl.P[2], pl.Pc, pl.twx, pl.twy, stream_));
+        return prof_end();
+    }
+    return fail(ERR_STATE, "plane kernels are FP32 only");
+}
+
+template <typename T>
+int Engine<T>::launch_xy_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const UpdateArgs &ua, int epi,
+                                double bytes, double *stats_dev)
+{
+    if constexpr (sizeof(T) == sizeof(float)) {
+        MVR_TRY(prof_begin(KK_XY_UPDATE, bytes));
+        MVR_CUDA(xy_update(pl.xy, epi, S, ua, bms, nb, pl.P[2], pl.Pc, pl.twx, pl.twy, stream_));
+        MVR_TRY(prof_end());
+        if (stats_dev && (epi == EPI_SEQ || epi == EPI_MUL_FINAL || epi == EPI_NLL)) {
+            MVR_TRY(prof_begin(KK_REDUCE, 16.0 * pl.P[2] * nb));
+            k_reduce_stats<double><<<nb, 1024, 0, stream_>>>(partials_, pl.P[2], stats_dev);
+            MVR_LAUNCHED("k_reduce_stats");
+            MVR_TRY(prof_end());
+        }
+        return OK;
+    }
+    return fail(ERR_STATE, "plane kernels are FP32 only");
+}
+
 template <typename T>
 int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const float *img, const float *w, float maxI,
                        double *stats_dev)
@@ -700,14 +765,21 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const f
     const long long nrows = (long long)pl.P[1] * pl.P[2];
     MVR_TRY(reserve(pl.Pc, (long long)pl.b[0] * pl.b[1] * pl.b[2], (nrows + pl.RP - 1) / pl.RP, nb));
     const BlockMaps bms = block_maps(pl, bps, nb);
-    MVR_TRY(launch_fwd_mirror(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
-    MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
-    MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb));
-    MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr, nb));
-    MVR_TRY(launch_ratio(pl, bms, nb, S0_, img));
-    MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
-    MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k2h, nb));
-    MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr, nb));
+    if (pl.xy) {
+        MVR_TRY(launch_xy_fwd(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb));
+        MVR_TRY(launch_xy_ratio(pl, bms, nb, S0_, img));
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k2h, nb));
+    } else {
+        MVR_TRY(launch_fwd_mirror(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
+        MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb));
+        MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr, nb));
+        MVR_TRY(launch_ratio(pl, bms, nb, S0_, img));
+        MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k2h, nb));
+        MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr, nb));
+    }
     UpdateArgs ua{};
     ua.psi_src = bps[0].psi_src;
     ua.psi_dst = bps[0].psi_dst;
@@ -724,6 +796,7 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const f
         const double neff = (double)(bp.whi[0] - bp.wlo[0]) * (bp.whi[1] - bp.wlo[1]) * (bp.whi[2] - bp.wlo[2]);
         bytes += sizeof(V) * (double)pl.Pc + (sizeof(T) + 4.0) * nv + sizeof(T) * neff;
     }
+    if (pl.xy) return launch_xy_update(pl, bms, nb, S0_, ua, EPI_SEQ, bytes, stats_dev);
     return launch_update(pl, bms, nb, S0_, ua, EPI_SEQ, bytes, stats_dev);
 }
 
@@ -753,23 +826,34 @@ int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace
         ua.prod = prod_;
         ua.partials = partials_;
         const BlockMaps bms = block_maps(pl, bps, nb);
-        if (!prev || std::memcmp(prev->P, pl.P, sizeof(pl.P)) != 0 || std::memcmp(prev->L, pl.L, sizeof(pl.L)) != 0) {
+        if (!prev || std::memcmp(prev->P, pl.P, sizeof(pl.P)) != 0 || std::memcmp(prev->L, pl.L, sizeof(pl.L)) != 0 ||
+            prev->xy != pl.xy) {
             // FFT of psi along x and y, shared by every view with this domain
-            MVR_TRY(launch_fwd_mirror(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
-            MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
+            if (pl.xy) {
+                MVR_TRY(launch_xy_fwd(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
+            } else {
+                MVR_TRY(launch_fwd_mirror(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
+                MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
+            }
         }
         prev = &pl;
         MVR_TRY(launch_cols(pl, 2, 2, S0_, S1_, pl.k1h, nb));
-        MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr, nb));
-        MVR_TRY(launch_ratio(pl, bms, nb, S1_, imgs[v]));
-        MVR_TRY(launch_cols(pl, 1, 0, S1_, S1_, nullptr, nb));
-        MVR_TRY(launch_cols(pl, 2, 2, S1_, S1_, pl.k2h, nb));
-        MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr, nb));
+        if (pl.xy) {
+            MVR_TRY(launch_xy_ratio(pl, bms, nb, S1_, imgs[v]));
+            MVR_TRY(launch_cols(pl, 2, 2, S1_, S1_, pl.k2h, nb));
+        } else {
+            MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr, nb));
+            MVR_TRY(launch_ratio(pl, bms, nb, S1_, imgs[v]));
+            MVR_TRY(launch_cols(pl, 1, 0, S1_, S1_, nullptr, nb));
+            MVR_TRY(launch_cols(pl, 2, 2, S1_, S1_, pl.k2h, nb));
+            MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr, nb));
+        }
         const double sb = (double)sizeof(V) * (double)pl.Pc;
         const double bytes = nb * (v == nv - 1 ? sb + (sizeof(T) + 12.0 + 4.0 * nv) * bvox + sizeof(T) * bvox
                                                : sb + (v == 0 ? 8.0 : 16.0) * bvox);
         const int epi = v == nv - 1 ? EPI_MUL_FINAL : (v == 0 ? EPI_MUL_FIRST : EPI_MUL_ACC);
-        MVR_TRY(launch_update(pl, bms, nb, S1_, ua, epi, bytes, stats_dev));
+        if (pl.xy) MVR_TRY(launch_xy_update(pl, bms, nb, S1_, ua, epi, bytes, stats_dev));
+        else MVR_TRY(launch_update(pl, bms, nb, S1_, ua, epi, bytes, stats_dev));
     }
     return OK;
 }
@@ -783,10 +867,15 @@ int Engine<T>::likelihood(const Plan<T> &pl, const BlockPlace *bps, int nb, cons
     const long long nrows = (long long)pl.P[1] * pl.P[2];
     MVR_TRY(reserve(pl.Pc, (long long)pl.b[0] * pl.b[1] * pl.b[2], (nrows + pl.RP - 1) / pl.RP, nb));
     const BlockMaps bms = block_maps(pl, bps, nb);
-    MVR_TRY(launch_fwd_mirror(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
-    MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
-    MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb));
-    MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr, nb));
+    if (pl.xy) {
+        MVR_TRY(launch_xy_fwd(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb));
+    } else {
+        MVR_TRY(launch_fwd_mirror(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
+        MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb));
+        MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr, nb));
+    }
     UpdateArgs ua{};
     ua.psi_src = bps[0].psi_src;
     ua.img = img;
@@ -794,7 +883,9 @@ int Engine<T>::likelihood(const Plan<T> &pl, const BlockPlace *bps, int nb, cons
     ua.nviews = 1;
     ua.partials = partials_;
     const double nv = (double)pl.b[0] * pl.b[1] * pl.b[2];
-    return launch_update(pl, bms, nb, S0_, ua, EPI_NLL, nb * (sizeof(V) * (double)pl.Pc + 8.0 * nv), stats_dev);
+    const double bytes = nb * (sizeof(V) * (double)pl.Pc + 8.0 * nv);
+    if (pl.xy) return launch_xy_update(pl, bms, nb, S0_, ua, EPI_NLL, bytes, stats_dev);
+    return launch_update(pl, bms, nb, S0_, ua, EPI_NLL, bytes, stats_dev);
 }
 
 template <typename T>
@@ -811,6 +902,19 @@ int Engine<T>::convolve(const Plan<T> &pl, const T *blk, int src_kind, float *ou
         bm.whi[d] = pl.b[d];
     }
     bm.fast_x = block_fast_x(bm);
+    if constexpr (sizeof(T) == sizeof(float)) {
+        if (pl.xy) {
+            ++launches_;
+            if (src_kind == SRC_ZERO)
+                MVR_CUDA(xy_fwd_zero(pl.xy, blk, S0_, bms, 1, pl.P[2], pl.Pc, pl.twx, pl.twy, stream_));
+            else MVR_CUDA(xy_fwd_mirror(pl.xy, blk, S0_, bms, 1, pl.P[2], pl.Pc, pl.twx, pl.twy, stream_));
+            MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, 1));
+            UpdateArgs ua{};
+            ua.store = out;
+            ua.partials = partials_;
+            return launch_xy_update(pl, bms, 1, S0_, ua, EPI_STORE, 0.0, nullptr);
+        }
+    }
     const long long nrows = (long long)pl.P[1] * pl.P[2];
     const dim3 grid((unsigned)((nrows + pl.RP - 1) / pl.RP), 1);
     if (src_kind == SRC_ZERO)

@@ -24,6 +24,9 @@ enum KernelKind {
     KK_ROWS_UPDATE,    // C2R, update, stats partials
     KK_REDUCE,         // stats reduction
     KK_PASTE,          // effective-region copy
+    KK_XY_FWD,         // plane: extract + R2C along x + FFT along y
+    KK_XY_RATIO,       // plane: inverse y, C2R, quotient, R2C, FFT y
+    KK_XY_UPDATE,      // plane: inverse y, C2R, update, stats partials
     KK_COUNT
 };
 const char *kernel_kind_name(int k);
@@ -56,6 +59,7 @@ struct Plan {
     int wr = 0;        // FP32 rows of Px = 64 wr reals (wr = 2, 3, 4) take the warp-shuffle row kernels
     int wcy = 0, wcz = 0;  // FP32 columns of 32 wc (wc = 2, 3, 4, 5, 6, 8) take the warp-shuffle column kernels
     int tcy = 0, tcz = 0;  // FP32 columns of 16 tc (tc = 4, 6, 8, 12, 16) take the two-phase tile kernels (preferred)
+    int xy = 0;            // plane kernels (x and y fused per z-plane): shape code, 0 = row / column kernels
     size_t smem_row = 0, smem_coly = 0, smem_colz = 0;
 };
 
@@ -108,6 +112,12 @@ public:
     // launch accounting: every kernel launch of the engine (and of its owner through
     // count_launch) is counted; with profiling on, each is bracketed by CUDA events
     long long launches() const { return launches_; }
+    // adds launches replayed from a captured graph to the count
+    void count_replayed(long long n) { launches_ += n; }
+    // changes whenever the engine's scratch buffers are reallocated (captured graphs
+    // that use them are then stale)
+    long long alloc_epoch() const { return alloc_epoch_; }
+    bool profiling() const { return prof_on_; }
     void set_profiling(bool on) { prof_on_ = on; }
     int prof_begin(int kind, double bytes);
     int prof_end();
@@ -121,6 +131,10 @@ public:
 
 private:
     int launch_fwd_mirror(const Plan<T> &pl, const BlockMaps &bms, int nb, const T *src, V *S);
+    int launch_xy_fwd(const Plan<T> &pl, const BlockMaps &bms, int nb, const T *src, V *S);
+    int launch_xy_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img);
+    int launch_xy_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const UpdateArgs &ua, int epi,
+                         double bytes, double *stats_dev);
     int launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh, int nb);
     int launch_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img);
     int launch_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const UpdateArgs &ua, int epi,
@@ -142,6 +156,7 @@ private:
     long long kcap_ = 0;
     std::string err_;
     long long launches_ = 0;
+    long long alloc_epoch_ = 0;
     bool prof_on_ = false;
     struct Pending {
         int kind;

@@ -363,6 +363,38 @@ __device__ __forceinline__ float next_value(float last, float integral, float we
     const float next = isnan(adjusted) ? minI : (minI >= adjusted ? minI : adjusted);
     return __fadd_rn(last, __fmul_rn(__fsub_rn(next, last), weight));
 }
+// The plane kernels' form of the same rule: the division by maxI becomes a product with
+// its reciprocal, the Tikhonov factor takes the hardware reciprocal square root and the
+// approximate division (each within 2 ulp), the rest is as above.  The difference to
+// the IEEE form is a few float ulp per voxel, far inside the FFT rounding.
+struct UpdConst {
+    float minI, maxI, inv_maxI, two_lambda;
+    bool tik;
+};
+__device__ __forceinline__ float next_value_fast(float last, float integral, float weight, const UpdConst &c)
+{
+    const float value = __fmul_rn(last, integral);
+    float adjusted;
+    if (value > 0.0f) {
+        if (c.tik) {
+            const float v = value * c.inv_maxI;
+            const float s = fmaf(c.two_lambda, v, 1.0f);
+            const float r = s * rsqrtf(s);
+            adjusted = __fdividef(2.0f * v, r + 1.0f) * c.maxI;
+        } else {
+            adjusted = value;
+        }
+    } else {
+        adjusted = c.minI;
+    }
+    const float next = isnan(adjusted) ? c.minI : (c.minI >= adjusted ? c.minI : adjusted);
+    return __fadd_rn(last, __fmul_rn(__fsub_rn(next, last), weight));
+}
+// Quotient with the approximate division (within 2 ulp of img / blurred).
+__device__ __forceinline__ float quotient_fast(float img, float blurred)
+{
+    return img > 0.0f ? __fdividef(img, blurred) : 1.0f;
+}
 // The same rule in double (FP64 run).
 __device__ __forceinline__ double next_value(double last, double integral, double weight, double lambda, double minI,
                                              double maxI)
@@ -451,6 +483,120 @@ struct UpdateArgs {
     double *partials;     // per CTA {sum, max}
 };
 
+// The update epilogue of one block row (C2R result zz: natural-order packed values,
+// zz[q] = (x = 2q, x = 2q + 1)), shared by the row kernels and the plane kernels.
+// ua.prod / ua.store are already offset to the block.  One warp per row, lanes over x.
+template <typename T, int EPI>
+__device__ __forceinline__ void update_row(const typename Cx<T>::t *zz, int m, const BlockMap &bm,
+                                           const UpdateArgs &ua, int y, int z, int lane, T &ksum, T &kcomp, T &kmax)
+{
+    typedef typename Cx<T>::t V;
+    const T *psrc = reinterpret_cast<const T *>(ua.psi_src);
+    T *pdst = reinterpret_cast<T *>(ua.psi_dst);
+    const ZeroRow zr = zero_row(bm, y, z);
+    const MirrorRow mr = mirror_row(bm, y, z);
+    const bool wrow = y >= bm.wlo[1] && y < bm.whi[1] && z >= bm.wlo[2] && z < bm.whi[2];
+    const long long orow = ((bm.ooff[2] + z) * bm.OD[1] + (bm.ooff[1] + y)) * bm.OD[0] + bm.ooff[0];
+    const long long brow = ((long long)z * bm.b[1] + y) * bm.b[0];
+    constexpr int UB = kRowBatch / 2;
+    for (int c0 = 0; c0 < m; c0 += 32 * UB) {
+        T lastv[UB][2];
+        float wv[UB][2];
+        if (EPI == EPI_SEQ || EPI == EPI_MUL_FINAL) {  // psi and the first weight, batched
+#pragma unroll
+            for (int u = 0; u < UB; ++u) {
+                const int q = c0 + lane + 32 * u;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int x = 2 * q + h;
+                    const bool ok = q < m && x < bm.b[0];
+                    lastv[u][h] = ok ? psrc[mr.base + mirror_x(bm, x)] : (T)0;
+                    wv[u][h] = (ok && EPI == EPI_SEQ) ? zero_at(ua.weight[0], bm, zr, x) : 0.0f;
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < UB; ++u) {
+            const int q = c0 + lane + 32 * u;
+            if (q >= m) continue;
+            const V c = zz[q];
+            const T cv[2] = {c.x, c.y};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int x = 2 * q + h;
+                if (x >= bm.b[0]) continue;
+                const T integral = cv[h];
+                if (EPI == EPI_STORE) {
+                    ua.store[brow + x] = (float)integral;
+                    continue;
+                }
+                if (EPI == EPI_MUL_FIRST) { ua.prod[brow + x] = (double)integral; continue; }
+                if (EPI == EPI_NLL) {
+                    // Poisson negative log-likelihood w * (conv1 - img ln conv1) over img > 0,
+                    // each volume voxel once (write region of its block)
+                    if (!(wrow && x >= bm.wlo[0] && x < bm.whi[0])) continue;
+                    const float im = zero_at(ua.img, bm, zr, x);
+                    const float wt = zero_at(ua.weight[0], bm, zr, x);
+                    if (!(im > 0.0f) || !(integral > (T)0)) continue;
+                    const T lg = sizeof(T) == sizeof(float) ? (T)logf((float)integral) : (T)log((double)integral);
+                    const T term = (T)wt * (integral - (T)im * lg);
+                    const T ky = term - kcomp;
+                    const T kt = ksum + ky;
+                    kcomp = (kt - ksum) - ky;
+                    ksum = kt;
+                    continue;
+                }
+                if (EPI == EPI_MUL_ACC) { ua.prod[brow + x] *= (double)integral; continue; }
+                const T last = lastv[u][h];
+                T next;
+                if (EPI == EPI_SEQ) {
+                    next = next_value(last, integral, (T)wv[u][h], ua.lambda, (T)ua.minI, (T)ua.maxI);
+                } else {  // EPI_MUL_FINAL: DeconvolutionMethods.computeNextValueMul 370-419
+                    double prod = (ua.nviews == 1 ? 1.0 : ua.prod[brow + x]) * (double)integral;
+                    double sumW = 0.0;
+                    for (int v = 0; v < ua.nviews; ++v) sumW += (double)zero_at(ua.weight[v], bm, zr, x);
+                    T root;
+                    if (sizeof(T) == sizeof(double)) root = (T)pow(prod, 1.0 / ua.nviews);
+                    else if (ua.nviews == 1) root = (T)prod;
+                    else if (ua.nviews == 2) root = (T)__fsqrt_rn((float)prod);
+                    else root = (T)powf((float)prod, 1.0f / (float)ua.nviews);  // float rate, see tikhonov_f
+                    sumW = sumW < 1.0 ? sumW : 1.0;
+                    next = next_value(last, root, (T)sumW, ua.lambda, (T)ua.minI, (T)ua.maxI);
+                }
+                const T ch = next - last;  // signed change (DeconvolutionMethods.java:308)
+                const T ky = ch - kcomp;
+                const T kt = ksum + ky;
+                kcomp = (kt - ksum) - ky;
+                ksum = kt;
+                kmax = kmax > ch ? kmax : ch;
+                if (wrow && x >= bm.wlo[0] && x < bm.whi[0]) pdst[orow + x] = next;
+            }
+        }
+    }
+}
+
+// Deterministic CTA reduction of the per-thread statistics into ua.partials[slot]
+// (sum in double from the compensated float sums, max).  Every thread must call it.
+template <typename T>
+__device__ __forceinline__ void stats_to_partials(T ksum, T kcomp, T kmax, double *red_s, double *red_m,
+                                                  double *partials, long long slot)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    double lsum = (double)ksum - (double)kcomp, lmax = (double)kmax;
+    for (int o = 16; o > 0; o >>= 1) {
+        lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+        lmax = fmax(lmax, __shfl_down_sync(0xffffffffu, lmax, o));
+    }
+    if (lane == 0) { red_s[warp] = lsum; red_m[warp] = lmax; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0, mx = -1.0;
+        for (int w = 0; w < nw; ++w) { s += red_s[w]; mx = fmax(mx, red_m[w]); }
+        partials[2 * slot] = s;
+        partials[2 * slot + 1] = mx;
+    }
+}
+
 template <typename T, int EPI, bool BIG>
 __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restrict__ S, UpdateArgs ua,
                                                      const BlockMaps bms, long long Pc, FftDesc d,
@@ -476,8 +622,6 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
     c2r_pre_load(S, A, ps, row0, nr, m, tw);
     __syncthreads();
     V *Z = fft_run<true, false, BIG>(A, B, nr, ps, 1, d, tw, 2);
-    const T *psrc = reinterpret_cast<const T *>(ua.psi_src);
-    T *pdst = reinterpret_cast<T *>(ua.psi_dst);
     // signed-change statistics: per thread in T with Kahan compensation (T = float:
     // the double rate is a small fraction of the float rate), per block in double
     T ksum = 0, kcomp = 0, kmax = (T)-1;
@@ -486,105 +630,10 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
         const long long row = row0 + r;
         const int y = (int)(row % bm.P[1]), z = (int)(row / bm.P[1]);
         if (y >= bm.b[1] || z >= bm.b[2]) continue;  // extension rows carry no block voxels
-        const ZeroRow zr = zero_row(bm, y, z);
-        const MirrorRow mr = mirror_row(bm, y, z);
-        const bool wrow = y >= bm.wlo[1] && y < bm.whi[1] && z >= bm.wlo[2] && z < bm.whi[2];
-        const long long orow = ((bm.ooff[2] + z) * bm.OD[1] + (bm.ooff[1] + y)) * bm.OD[0] + bm.ooff[0];
-        const long long brow = ((long long)z * bm.b[1] + y) * bm.b[0];
-        const V *zz = Z + r * ps;
-        constexpr int UB = kRowBatch / 2;
-        for (int c0 = 0; c0 < m; c0 += 32 * UB) {
-            T lastv[UB][2];
-            float wv[UB][2];
-            if (EPI == EPI_SEQ || EPI == EPI_MUL_FINAL) {  // psi and the first weight, batched
-#pragma unroll
-                for (int u = 0; u < UB; ++u) {
-                    const int q = c0 + lane + 32 * u;
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const int x = 2 * q + h;
-                        const bool ok = q < m && x < bm.b[0];
-                        lastv[u][h] = ok ? psrc[mr.base + mirror_x(bm, x)] : (T)0;
-                        wv[u][h] = (ok && EPI == EPI_SEQ) ? zero_at(ua.weight[0], bm, zr, x) : 0.0f;
-                    }
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < UB; ++u) {
-                const int q = c0 + lane + 32 * u;
-                if (q >= m) continue;
-                const V c = zz[q];
-                const T cv[2] = {c.x, c.y};
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int x = 2 * q + h;
-                    if (x >= bm.b[0]) continue;
-                    const T integral = cv[h];
-                    if (EPI == EPI_STORE) {
-                        ua.store[brow + x] = (float)integral;
-                        continue;
-                    }
-                    if (EPI == EPI_MUL_FIRST) { ua.prod[brow + x] = (double)integral; continue; }
-                    if (EPI == EPI_NLL) {
-                        // Poisson negative log-likelihood w * (conv1 - img ln conv1) over img > 0,
-                        // each volume voxel once (write region of its block)
-                        if (!(wrow && x >= bm.wlo[0] && x < bm.whi[0])) continue;
-                        const float im = zero_at(ua.img, bm, zr, x);
-                        const float wt = zero_at(ua.weight[0], bm, zr, x);
-                        if (!(im > 0.0f) || !(integral > (T)0)) continue;
-                        const T lg = sizeof(T) == sizeof(float) ? (T)logf((float)integral) : (T)log((double)integral);
-                        const T term = (T)wt * (integral - (T)im * lg);
-                        const T ky = term - kcomp;
-                        const T kt = ksum + ky;
-                        kcomp = (kt - ksum) - ky;
-                        ksum = kt;
-                        continue;
-                    }
-                    if (EPI == EPI_MUL_ACC) { ua.prod[brow + x] *= (double)integral; continue; }
-                    const T last = lastv[u][h];
-                    T next;
-                    if (EPI == EPI_SEQ) {
-                        next = next_value(last, integral, (T)wv[u][h], ua.lambda, (T)ua.minI, (T)ua.maxI);
-                    } else {  // EPI_MUL_FINAL: DeconvolutionMethods.computeNextValueMul 370-419
-                        double prod = (ua.nviews == 1 ? 1.0 : ua.prod[brow + x]) * (double)integral;
-                        double sumW = 0.0;
-                        for (int v = 0; v < ua.nviews; ++v) sumW += (double)zero_at(ua.weight[v], bm, zr, x);
-                        T root;
-                        if (sizeof(T) == sizeof(double)) root = (T)pow(prod, 1.0 / ua.nviews);
-                        else if (ua.nviews == 1) root = (T)prod;
-                        else if (ua.nviews == 2) root = (T)__fsqrt_rn((float)prod);
-                        else root = (T)powf((float)prod, 1.0f / (float)ua.nviews);  // float rate, see tikhonov_f
-                        sumW = sumW < 1.0 ? sumW : 1.0;
-                        next = next_value(last, root, (T)sumW, ua.lambda, (T)ua.minI, (T)ua.maxI);
-                    }
-                    const T ch = next - last;  // signed change (DeconvolutionMethods.java:308)
-                    const T ky = ch - kcomp;
-                    const T kt = ksum + ky;
-                    kcomp = (kt - ksum) - ky;
-                    ksum = kt;
-                    kmax = kmax > ch ? kmax : ch;
-                    if (wrow && x >= bm.wlo[0] && x < bm.whi[0]) pdst[orow + x] = next;
-                }
-            }
-        }
+        update_row<T, EPI>(Z + r * ps, m, bm, ua, y, z, lane, ksum, kcomp, kmax);
     }
-    if (EPI == EPI_SEQ || EPI == EPI_MUL_FINAL || EPI == EPI_NLL) {
-        // deterministic block reduction -> partials[blockIdx.x]
-        double lsum = (double)ksum - (double)kcomp, lmax = (double)kmax;
-        for (int o = 16; o > 0; o >>= 1) {
-            lsum += __shfl_down_sync(0xffffffffu, lsum, o);
-            lmax = fmax(lmax, __shfl_down_sync(0xffffffffu, lmax, o));
-        }
-        if (lane == 0) { red_s[warp] = lsum; red_m[warp] = lmax; }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double s = 0.0, mx = -1.0;
-            for (int w = 0; w < nw; ++w) { s += red_s[w]; mx = fmax(mx, red_m[w]); }
-            const long long slot = (long long)blockIdx.y * gridDim.x + blockIdx.x;
-            ua.partials[2 * slot] = s;
-            ua.partials[2 * slot + 1] = mx;
-        }
-    }
+    if (EPI == EPI_SEQ || EPI == EPI_MUL_FINAL || EPI == EPI_NLL)
+        stats_to_partials(ksum, kcomp, kmax, red_s, red_m, ua.partials, (long long)blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 // Sum / max of per-CTA partials in a fixed order (one CTA), into out[0..1].

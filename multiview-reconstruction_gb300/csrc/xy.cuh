@@ -1,0 +1,26 @@
+// Host launchers of the plane kernels (xy_plane.cuh), compiled in their own
+// translation unit.  combo = 100 VX + VY for FFT domains Px = 32 VX, Py = 16 VY.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+
+namespace mvr {
+
+// The plane-kernel shape for an FP32 FFT domain P (x, y), or 0 when none exists.
+int xy_combo(const int P[3]);
+size_t xy_smem(int combo);
+
+// One CTA per z-plane (grid Pz x nb); every call returns the launch status.
+cudaError_t xy_fwd_mirror(int combo, const float *psi, float2 *S, const BlockMaps &bms, int nb, int Pz, long long Pc,
+                          const float2 *twx, const float2 *twy, cudaStream_t s);
+cudaError_t xy_fwd_zero(int combo, const float *blk, float2 *S, const BlockMaps &bms, int nb, int Pz, long long Pc,
+                        const float2 *twx, const float2 *twy, cudaStream_t s);
+cudaError_t xy_fwd_kernel(int combo, const SrcKernel &src, float2 *S, const BlockMaps &bms, int nb, int Pz,
+                          long long Pc, const float2 *twx, const float2 *twy, cudaStream_t s);
+cudaError_t xy_ratio(int combo, float2 *S, const float *img, const BlockMaps &bms, int nb, int Pz, long long Pc,
+                     const float2 *twx, const float2 *twy, cudaStream_t s);
+cudaError_t xy_update(int combo, int epi, float2 *S, const UpdateArgs &ua, const BlockMaps &bms, int nb, int Pz,
+                      long long Pc, const float2 *twx, const float2 *twy, cudaStream_t s);
+
+}  // namespace mvr

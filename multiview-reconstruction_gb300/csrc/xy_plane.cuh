@@ -1,0 +1,499 @@
+// Plane kernels: the x and y transforms of one z-plane of a block, fused with the
+// extract / quotient / update work of the iteration, with the whole plane spectrum
+// held in shared memory.
+//
+// For FFT domains Px = 32 VX (real x rows of m = 16 VX packed complex values) and
+// Py = 16 VY, one CTA takes one z-plane of one block:
+//   k_xy_fwd     rows from the source (psi under the mirror mapping, a zero-extended
+//                block, or a wrapped kernel) -> R2C along x -> FFT along y -> plane of S
+//   k_xy_ratio   plane of S -> inverse y -> C2R along x -> quotient img / conv1
+//                (DeconvolutionMethods.java:71-74) -> R2C along x -> FFT along y -> S
+//   k_xy_update  plane of S -> inverse y -> C2R along x -> the row epilogue of the
+//                update (update_row: Seq / Mul update, FP64-reduced statistics,
+//                likelihood, or a plain store)
+// so one view-step is fwd, Z (x K1^), ratio, Z (x K2^), update: five passes over the
+// spectra instead of nine.
+//
+// Both axes use the two-phase register FFT of the tile column kernels (n = 16 V):
+// phase 1, item (pencil, t): V-point DFT of elements t + 16 v, twiddle W_n^(t k1),
+// written back to t + 16 k1; phase 2, item (pencil, k1): 16-point DFT of elements
+// t + 16 k1, written back in place, so position k2 + 16 k1 holds frequency k1 + V k2
+// ("tile order").  The x spectrum of a real row (m + 1 values) therefore sits in tile
+// order too: frequency f < m at position pos(f) = f / VX + 16 (f % VX), the Nyquist
+// value at position m.  Every spectrum the products use (data, K1^, K2^) comes from the
+// same forward kernels, so the spectral product is taken position by position; the
+// inverse phases undo the forward ones exactly and return natural order (times n).
+//
+// Shared memory: the plane as [y][c] with row stride m + 1 (odd: pencil-fastest
+// items touch distinct banks both along rows and along columns), which is also the
+// layout of the plane in S ([z][y][c], c < m + 1), so the plane moves between HBM and
+// shared memory as one contiguous 16-byte-vectorised copy.
+#pragma once
+#include "rows_warp.cuh"
+#include "cols_tile.cuh"
+
+namespace mvr {
+
+constexpr int kXYThreads = 1024;
+constexpr long long kNoRow = -(1LL << 62);
+
+template <int VX, int VY>
+struct XYShape {
+    static constexpr int m = 16 * VX;     // packed complex values per real x row
+    static constexpr int Px = 2 * m;      // real x length
+    static constexpr int Py = 16 * VY;
+    static constexpr int SR = m + 1;      // row stride (x spectrum incl. Nyquist)
+    static constexpr int plane = Py * SR; // complex values per plane
+};
+
+// Bytes of dynamic shared memory of the plane kernels of shape (VX, VY).
+template <int VX, int VY>
+constexpr size_t xy_smem_bytes()
+{
+    typedef XYShape<VX, VY> S;
+    return sizeof(float2) * (size_t)(S::plane + S::Px + S::Py) + 3 * sizeof(long long) * S::Py +
+           sizeof(int) * (size_t)(3 * S::Px + S::m);
+}
+
+// ---- two-phase FFT on pencils in shared memory -------------------------------------
+// Element i of pencil p at A[p * PS + i * ES]; tw[j * TWM] = exp(-2 pi i j / (16 V)).
+template <int V, int NPEN, int PS, int ES, bool INV>
+__device__ __forceinline__ void tp_phase1(float2 *A, const float2 *tw, int twm)
+{
+    constexpr int T = 16, items = NPEN * T;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+        const int t = it / NPEN, p = it - t * NPEN;
+        float2 *a0 = A + p * PS + t * ES;
+        float2 a[V];
+        if (!INV) {
+#pragma unroll
+            for (int v = 0; v < V; ++v) a[v] = a0[T * v * ES];
+            sdft<V, false>(a);
+#pragma unroll
+            for (int k1 = 1; k1 < V; ++k1) a[k1] = cmul(a[k1], tw[t * k1 * twm]);
+        } else {
+#pragma unroll
+            for (int k1 = 0; k1 < V; ++k1) a[k1] = a0[T * k1 * ES];
+#pragma unroll
+            for (int k1 = 1; k1 < V; ++k1) a[k1] = cmul(a[k1], cconj(tw[t * k1 * twm]));
+            sdft<V, true>(a);
+        }
+#pragma unroll
+        for (int v = 0; v < V; ++v) a0[T * v * ES] = a[v];
+    }
+}
+
+template <int V, int NPEN, int PS, int ES, bool INV>
+__device__ __forceinline__ void tp_phase2(float2 *A)
+{
+    constexpr int T = 16, items = NPEN * V;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+        const int k1 = it / NPEN, p = it - k1 * NPEN;
+        float2 *b0 = A + p * PS + T * k1 * ES;
+        float2 b[T];
+#pragma unroll
+        for (int t = 0; t < T; ++t) b[t] = b0[t * ES];
+        sdft<T, INV>(b);
+#pragma unroll
+        for (int t = 0; t < T; ++t) b0[t * ES] = b[t];
+    }
+}
+
+// Forward x FFT of all rows, then the packed-real split in tile order.
+template <int VX, int VY>
+__device__ __forceinline__ void xy_x_forward(float2 *A, const float2 *twx, const int *posx)
+{
+    typedef XYShape<VX, VY> S;
+    constexpr int m = S::m, half = m / 2, items = S::Py * (half + 1);
+    tp_phase1<VX, S::Py, S::SR, 1, false>(A, twx, 2);
+    __syncthreads();
+    tp_phase2<VX, S::Py, S::SR, 1, false>(A);
+    __syncthreads();
+    // X[f] = E[f] + W_Px^f O[f], E = (Z[f] + conj Z[m-f]) / 2, O = -i (Z[f] - conj Z[m-f]) / 2
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+        const int f = it / S::Py, y = it - f * S::Py;
+        float2 *row = A + y * S::SR;
+        if (f == 0) {
+            const float2 z0 = row[0];
+            row[0] = make_float2(z0.x + z0.y, 0.0f);
+            row[m] = make_float2(z0.x - z0.y, 0.0f);
+            continue;
+        }
+        const int g = m - f, pf = posx[f], pg = posx[g];
+        const float2 zf = row[pf], zg = row[pg];
+        {
+            const float2 zc = cconj(zg);
+            const float2 e = cscale(cadd(zf, zc), 0.5f), dd = cscale(csub(zf, zc), 0.5f);
+            row[pf] = cadd(e, cmul(twx[f], make_float2(dd.y, -dd.x)));
+        }
+        if (g != f) {
+            const float2 zc = cconj(zf);
+            const float2 e = cscale(cadd(zg, zc), 0.5f), dd = cscale(csub(zg, zc), 0.5f);
+            row[pg] = cadd(e, cmul(twx[g], make_float2(dd.y, -dd.x)));
+        }
+    }
+    __syncthreads();
+}
+
+// Packed-real merge in tile order, then the inverse x FFT: natural-order packed rows
+// times Px (the kernel spectra carry 1 / (Px Py Pz)).
+template <int VX, int VY>
+__device__ __forceinline__ void xy_x_inverse(float2 *A, const float2 *twx, const int *posx)
+{
+    typedef XYShape<VX, VY> S;
+    constexpr int m = S::m, half = m / 2, items = S::Py * (half + 1);
+    // a[k] = e + i o, e = X[k] + conj X[m-k], o = (X[k] - conj X[m-k]) conj(W_Px^k)
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+        const int f = it / S::Py, y = it - f * S::Py;
+        float2 *row = A + y * S::SR;
+        const int g = m - f, pf = posx[f], pg = f == 0 ? m : posx[g];
+        const float2 xf = row[pf], xg = row[pg];
+        {
+            const float2 c = cconj(xg);
+            const float2 e = cadd(xf, c), o = cmul(csub(xf, c), cconj(twx[f]));
+            row[pf] = make_float2(e.x - o.y, e.y + o.x);
+        }
+        if (f != 0 && g != f) {
+            const float2 c = cconj(xf);
+            const float2 e = cadd(xg, c), o = cmul(csub(xg, c), cconj(twx[g]));
+            row[pg] = make_float2(e.x - o.y, e.y + o.x);
+        }
+    }
+    __syncthreads();
+    tp_phase2<VX, S::Py, S::SR, 1, true>(A);
+    __syncthreads();
+    tp_phase1<VX, S::Py, S::SR, 1, true>(A, twx, 2);
+    __syncthreads();
+}
+
+template <int VX, int VY, bool INV>
+__device__ __forceinline__ void xy_y(float2 *A, const float2 *twy)
+{
+    typedef XYShape<VX, VY> S;
+    if (!INV) {
+        tp_phase1<VY, S::SR, 1, S::SR, false>(A, twy, 1);
+        __syncthreads();
+        tp_phase2<VY, S::SR, 1, S::SR, false>(A);
+    } else {
+        tp_phase2<VY, S::SR, 1, S::SR, true>(A);
+        __syncthreads();
+        tp_phase1<VY, S::SR, 1, S::SR, true>(A, twy, 1);
+    }
+    __syncthreads();
+}
+
+// Shared-memory carve-up and the per-CTA tables.
+template <int VX, int VY>
+struct XYSmem {
+    typedef XYShape<VX, VY> S;
+    float2 *A, *twx, *twy;
+    long long *rowb, *rowb2, *rowb3;  // per domain row: volume / block row bases (or -1)
+    int *colx, *colx2, *colx3;        // per domain x: volume x of the row's voxel (or -1)
+    int *posx;                        // tile position of x frequency f < m
+    __device__ __forceinline__ XYSmem(unsigned char *raw)
+    {
+        A = reinterpret_cast<float2 *>(raw);
+        twx = A + S::plane;
+        twy = twx + S::Px;
+        rowb = reinterpret_cast<long long *>(twy + S::Py);
+        rowb2 = rowb + S::Py;
+        rowb3 = rowb2 + S::Py;
+        colx = reinterpret_cast<int *>(rowb3 + S::Py);
+        colx2 = colx + S::Px;
+        colx3 = colx2 + S::Px;
+        posx = colx3 + S::Px;
+    }
+    __device__ __forceinline__ void load_tables(const float2 *__restrict__ gtwx, const float2 *__restrict__ gtwy)
+    {
+        for (int i = threadIdx.x; i < S::Px; i += blockDim.x) twx[i] = __ldg(&gtwx[i]);
+        for (int i = threadIdx.x; i < S::Py; i += blockDim.x) twy[i] = __ldg(&gtwy[i]);
+        for (int f = threadIdx.x; f < S::m; f += blockDim.x) posx[f] = f / VX + 16 * (f % VX);
+    }
+};
+
+template <int VX, int VY>
+__device__ __forceinline__ void xy_load_plane(float2 *A, const float2 *__restrict__ Sp)
+{
+    constexpr int n4 = XYShape<VX, VY>::plane / 2;
+    const float4 *src = reinterpret_cast<const float4 *>(Sp);
+    float4 *dst = reinterpret_cast<float4 *>(A);
+    constexpr int U = 4;
+    for (int i0 = threadIdx.x; i0 < n4; i0 += blockDim.x * U) {
+        float4 r[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = i0 + u * blockDim.x;
+            if (i < n4) r[u] = src[i];
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int i = i0 + u * blockDim.x;
+            if (i < n4) dst[i] = r[u];
+        }
+    }
+}
+
+template <int VX, int VY>
+__device__ __forceinline__ void xy_store_plane(float2 *__restrict__ Sp, const float2 *A)
+{
+    constexpr int n4 = XYShape<VX, VY>::plane / 2;
+    const float4 *src = reinterpret_cast<const float4 *>(A);
+    float4 *dst = reinterpret_cast<float4 *>(Sp);
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) dst[i] = src[i];
+}
+
+// ---- forward: source rows -> R2C x -> FFT y ---------------------------------------------
+template <typename Src>
+struct XYSrcTraits { static constexpr bool mirror = false; };
+template <>
+struct XYSrcTraits<SrcMirror<float>> { static constexpr bool mirror = true; };
+
+template <int VX, int VY, class Src>
+__global__ void __launch_bounds__(kXYThreads, 1) k_xy_fwd(Src src, float2 *__restrict__ S, const BlockMaps bms,
+                                                          long long Pc, const float2 *__restrict__ gtwx,
+                                                          const float2 *__restrict__ gtwy)
+{
+    typedef XYShape<VX, VY> SH;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    XYSmem<VX, VY> sm(smem_raw);
+    const BlockMap &bm = bms.m[blockIdx.y];
+    const int z = blockIdx.x;
+    float2 *Sp = S + (long long)blockIdx.y * Pc + (long long)z * SH::plane;
+    sm.load_tables(gtwx, gtwy);
+    constexpr bool MIR = XYSrcTraits<Src>::mirror;
+    for (int y = threadIdx.x; y < SH::Py; y += blockDim.x) {
+        const typename Src::Row r = src.row(bm, y, z);
+        sm.rowb[y] = r.base;
+    }
+    if (MIR)
+        for (int x = threadIdx.x; x < SH::Px; x += blockDim.x) sm.colx[x] = (int)mirror_x(bm, x);
+    __syncthreads();
+    // every thread keeps U pairs of loads in flight (the CTA is alone on its SM, so
+    // the load phase is latency-bound otherwise)
+    constexpr int items = SH::Py * SH::m, U = kXYThreads >= 1024 ? 6 : 12;
+    for (int i0 = threadIdx.x; i0 < items; i0 += blockDim.x * U) {
+        float v[U][2];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int it = i0 + u * blockDim.x;
+            const int y = it / SH::m, j = it - y * SH::m;
+            if (it < items) {
+                if constexpr (MIR) {
+                    const float *pr = src.vol + sm.rowb[y];
+                    v[u][0] = __ldg(pr + sm.colx[2 * j]);
+                    v[u][1] = __ldg(pr + sm.colx[2 * j + 1]);
+                } else {
+                    typename Src::Row r;
+                    r.base = sm.rowb[y];
+                    v[u][0] = src.template at<float>(r, bm, 2 * j);
+                    v[u][1] = src.template at<float>(r, bm, 2 * j + 1);
+                }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int it = i0 + u * blockDim.x;
+            const int y = it / SH::m, j = it - y * SH::m;
+            if (it < items) sm.A[y * SH::SR + j] = make_float2(v[u][0], v[u][1]);
+        }
+    }
+    __syncthreads();
+    xy_x_forward<VX, VY>(sm.A, sm.twx, sm.posx);
+    xy_y<VX, VY, false>(sm.A, sm.twy);
+    xy_store_plane<VX, VY>(Sp, sm.A);
+}
+
+// ---- C2R -> quotient -> R2C ----------------------------------------------------------
+// DeconvolutionMethods.java:71-74: img > 0 ? img / conv1 : 1.  Domain voxels outside the
+// block (the value-1 extension) and outside the volume (img zero-extended) read img = 0.
+template <int VX, int VY>
+__global__ void __launch_bounds__(kXYThreads, 1) k_xy_ratio(float2 *__restrict__ S, const float *__restrict__ img,
+                                                            const BlockMaps bms, long long Pc,
+                                                            const float2 *__restrict__ gtwx,
+                                                            const float2 *__restrict__ gtwy)
+{
+    typedef XYShape<VX, VY> SH;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    XYSmem<VX, VY> sm(smem_raw);
+    const BlockMap &bm = bms.m[blockIdx.y];
+    const int z = blockIdx.x;
+    float2 *Sp = S + (long long)blockIdx.y * Pc + (long long)z * SH::plane;
+    sm.load_tables(gtwx, gtwy);
+    const int ez = ext_e(z, bm.P[2], bm.L[2]);
+    for (int y = threadIdx.x; y < SH::Py; y += blockDim.x) {
+        const int ey = ext_e(y, bm.P[1], bm.L[1]);
+        const bool rin = ey >= 0 && ey < bm.b[1] && ez >= 0 && ez < bm.b[2];
+        sm.rowb[y] = rin ? zero_row(bm, ey, ez).base : -1;
+    }
+    for (int x = threadIdx.x; x < SH::Px; x += blockDim.x) {
+        const int bx = ext_e(x, bm.P[0], bm.L[0]);
+        const long long gx = bm.off[0] + bx;
+        sm.colx[x] = (bx >= 0 && bx < bm.b[0] && gx >= 0 && gx < bm.D[0]) ? (int)gx : -1;
+    }
+    __syncthreads();
+    // image pairs (x = 2j, 2j + 1 of row y) in batches of U per thread, double-buffered
+    // in registers; the first batch is in flight while the plane loads and transforms
+    constexpr int items = SH::Py * SH::m, U = 4, STEP = kXYThreads * U;
+    auto load_img = [&](int i0, float (&r)[U][2]) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int it = i0 + u * kXYThreads;
+            const int y = it / SH::m, j = it - y * SH::m;
+            const long long rb = it < items ? sm.rowb[y] : -1;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int gx = sm.colx[2 * j + h];
+                r[u][h] = (rb >= 0 && gx >= 0) ? __ldg(img + rb + gx) : 0.0f;
+            }
+        }
+    };
+    auto apply = [&](int i0, const float (&r)[U][2]) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int it = i0 + u * kXYThreads;
+            const int y = it / SH::m, j = it - y * SH::m;
+            if (it < items) {
+                float2 &c = sm.A[y * SH::SR + j];
+                c = make_float2(quotient_fast(r[u][0], c.x), quotient_fast(r[u][1], c.y));
+            }
+        }
+    };
+    float ia[U][2], ib[U][2];
+    load_img(threadIdx.x, ia);
+    xy_load_plane<VX, VY>(sm.A, Sp);
+    __syncthreads();
+    xy_y<VX, VY, true>(sm.A, sm.twy);
+    xy_x_inverse<VX, VY>(sm.A, sm.twx, sm.posx);
+    for (int i0 = threadIdx.x; i0 < items; i0 += 2 * STEP) {
+        load_img(i0 + STEP, ib);
+        apply(i0, ia);
+        load_img(i0 + 2 * STEP, ia);
+        apply(i0 + STEP, ib);
+    }
+    __syncthreads();
+    xy_x_forward<VX, VY>(sm.A, sm.twx, sm.posx);
+    xy_y<VX, VY, false>(sm.A, sm.twy);
+    xy_store_plane<VX, VY>(Sp, sm.A);
+}
+
+// ---- C2R -> update epilogue --------------------------------------------------------------
+template <int VX, int VY, int EPI>
+__global__ void __launch_bounds__(kXYThreads, 1) k_xy_update(float2 *__restrict__ S, UpdateArgs ua,
+                                                             const BlockMaps bms, long long Pc,
+                                                             const float2 *__restrict__ gtwx,
+                                                             const float2 *__restrict__ gtwy)
+{
+    typedef XYShape<VX, VY> SH;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double red_s[32], red_m[32];
+    XYSmem<VX, VY> sm(smem_raw);
+    const BlockMap &bm = bms.m[blockIdx.y];
+    const int z = blockIdx.x;
+    float2 *Sp = S + (long long)blockIdx.y * Pc + (long long)z * SH::plane;
+    const long long bvox = (long long)bm.b[0] * bm.b[1] * bm.b[2];
+    if (ua.prod) ua.prod += (long long)blockIdx.y * bvox;
+    if (ua.store) ua.store += (long long)blockIdx.y * bvox;
+    sm.load_tables(gtwx, gtwy);
+    float ksum = 0.0f, kcomp = 0.0f, kmax = -1.0f;
+    if constexpr (EPI == EPI_SEQ) {
+        // lean Seq epilogue (computeFinalValues / computeNextValue, DeconvolutionMethods.java
+        // 103-182, 320-358) over the pairs (x = 2j, 2j + 1) of the block rows, with psi and
+        // the weight double-buffered in registers; the first batch is in flight while the
+        // plane loads and transforms
+        const bool zin = z < bm.b[2];  // extension planes carry no block voxels
+        const bool zw = z >= bm.wlo[2] && z < bm.whi[2];
+        for (int y = threadIdx.x; y < SH::Py; y += blockDim.x) {
+            const bool in = zin && y < bm.b[1];
+            sm.rowb[y] = in ? mirror_row(bm, y, z).base : -1;
+            sm.rowb2[y] = in ? zero_row(bm, y, z).base : -1;
+            // output row base (negative for blocks left of the volume; rows outside the
+            // write region carry kNoRow)
+            sm.rowb3[y] = (in && zw && y >= bm.wlo[1] && y < bm.whi[1])
+                              ? ((bm.ooff[2] + z) * bm.OD[1] + (bm.ooff[1] + y)) * bm.OD[0] + bm.ooff[0]
+                              : kNoRow;
+        }
+        for (int x = threadIdx.x; x < SH::Px; x += blockDim.x) {
+            const bool in = x < bm.b[0];
+            const long long gx = bm.off[0] + x;
+            sm.colx[x] = in ? (int)mirror_x(bm, x) : -1;
+            sm.colx2[x] = (in && gx >= 0 && gx < bm.D[0]) ? (int)gx : -1;
+            sm.colx3[x] = (in && x >= bm.wlo[0] && x < bm.whi[0]) ? x : -1;
+        }
+        __syncthreads();
+        const float *psrc = reinterpret_cast<const float *>(ua.psi_src);
+        float *pdst = reinterpret_cast<float *>(ua.psi_dst);
+        const float *wgt = ua.weight[0];
+        UpdConst uc;
+        uc.minI = ua.minI;
+        uc.maxI = ua.maxI;
+        uc.inv_maxI = 1.0f / ua.maxI;
+        uc.two_lambda = (float)(2.0 * ua.lambda);
+        uc.tik = ua.lambda > 0.0;
+        constexpr int items = SH::Py * SH::m, U = 4, STEP = kXYThreads * U;
+        auto load = [&](int i0, float (&pv)[U][2], float (&wv)[U][2]) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int it = i0 + u * kXYThreads;
+                const int y = it / SH::m, j = it - y * SH::m;
+                const long long pb = it < items ? sm.rowb[y] : -1;
+                const long long wb = it < items ? sm.rowb2[y] : -1;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int mx = sm.colx[2 * j + h], gx = sm.colx2[2 * j + h];
+                    pv[u][h] = (pb >= 0 && mx >= 0) ? __ldg(psrc + pb + mx) : 0.0f;
+                    wv[u][h] = (wb >= 0 && gx >= 0) ? __ldg(wgt + wb + gx) : 0.0f;
+                }
+            }
+        };
+        auto apply = [&](int i0, const float (&pv)[U][2], const float (&wv)[U][2]) {
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int it = i0 + u * kXYThreads;
+                const int y = it / SH::m, j = it - y * SH::m;
+                if (it >= items || sm.rowb[y] < 0) continue;
+                const long long ob = sm.rowb3[y];
+                const float2 c = sm.A[y * SH::SR + j];
+                const float cv[2] = {c.x, c.y};
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int x = 2 * j + h;
+                    if (sm.colx[x] < 0) continue;  // beyond the block
+                    const float last = pv[u][h];
+                    const float next = next_value_fast(last, cv[h], wv[u][h], uc);
+                    const float ch = next - last;  // signed change (DeconvolutionMethods.java:308)
+                    const float ky = ch - kcomp;
+                    const float kt = ksum + ky;
+                    kcomp = (kt - ksum) - ky;
+                    ksum = kt;
+                    kmax = kmax > ch ? kmax : ch;
+                    if (ob != kNoRow && sm.colx3[x] >= 0) pdst[ob + x] = next;
+                }
+            }
+        };
+        float pa[U][2], wa[U][2], pb[U][2], wb[U][2];
+        load(threadIdx.x, pa, wa);
+        xy_load_plane<VX, VY>(sm.A, Sp);
+        __syncthreads();
+        xy_y<VX, VY, true>(sm.A, sm.twy);
+        xy_x_inverse<VX, VY>(sm.A, sm.twx, sm.posx);
+        for (int i0 = threadIdx.x; i0 < items; i0 += 2 * STEP) {
+            load(i0 + STEP, pb, wb);
+            apply(i0, pa, wa);
+            load(i0 + 2 * STEP, pa, wa);
+            apply(i0 + STEP, pb, wb);
+        }
+    } else {
+        xy_load_plane<VX, VY>(sm.A, Sp);
+        __syncthreads();
+        xy_y<VX, VY, true>(sm.A, sm.twy);
+        xy_x_inverse<VX, VY>(sm.A, sm.twx, sm.posx);
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+        if (z < bm.b[2])  // extension planes carry no block voxels
+            for (int y = warp; y < bm.b[1] && y < SH::Py; y += nw)
+                update_row<float, EPI>(sm.A + y * SH::SR, SH::m, bm, ua, y, z, lane, ksum, kcomp, kmax);
+    }
+    if (EPI == EPI_SEQ || EPI == EPI_MUL_FINAL || EPI == EPI_NLL)
+        stats_to_partials(ksum, kcomp, kmax, red_s, red_m, ua.partials, (long long)blockIdx.y * gridDim.x + blockIdx.x);
+}
+
+}  // namespace mvr

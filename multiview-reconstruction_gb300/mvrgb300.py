@@ -30,7 +30,7 @@ LIB_PATH = os.path.join(HERE, "libmvrgb300.so")
 OK, ERR_ARG, ERR_CUDA, ERR_OOM, ERR_UNSUPPORTED, ERR_STATE = 0, 1, 2, 3, 4, 5
 PRECISION_FP32, PRECISION_FP64 = 0, 1
 WEIGHTS_AS_GIVEN, WEIGHTS_HARD, WEIGHTS_SMOOTH = 0, 1, 2
-KERNEL_KINDS = 8
+KERNEL_KINDS = 11
 BOUNDARY_REFERENCE, BOUNDARY_CIRCULAR = 0, 1
 PSF_OPTIMIZATION_II, PSF_OPTIMIZATION_I, PSF_EFFICIENT_BAYESIAN, PSF_INDEPENDENT = 0, 1, 2, 3
 
@@ -44,6 +44,7 @@ EXPORTS = [
     "mvr_decon_get_max", "mvr_decon_get_weights", "mvr_decon_psi_device", "mvr_decon_synchronize",
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
     "mvr_kernel_name", "mvr_convolve_static", "mvr_decon_batch", "mvr_decon_likelihood",
+    "mvr_decon_set_graphs", "mvr_decon_graphs_captured",
     "mvr_unet_create", "mvr_unet_destroy", "mvr_unet_last_error", "mvr_unet_num_params", "mvr_unet_get_params",
     "mvr_unet_set_params", "mvr_unet_get_grads", "mvr_unet_set_input", "mvr_unet_forward", "mvr_unet_train_step",
     "mvr_unet_propose", "mvr_conv3d_tc", "mvr_conv3d_tc_wgrad", "mvr_conv3d_tc_last_error",
@@ -140,6 +141,8 @@ def load() -> C.CDLL:
     L.mvr_kernel_name.restype = C.c_char_p
     L.mvr_convolve_static.argtypes = [P, P, P, P, P, P, C.c_char_p, C.c_int]
     L.mvr_decon_batch.argtypes = [P]
+    L.mvr_decon_set_graphs.argtypes = [P, C.c_int]
+    L.mvr_decon_graphs_captured.argtypes = [P]
     L.mvr_decon_likelihood.argtypes = [P, P, P]
     L.mvr_unet_create.argtypes = [C.c_int, P, C.c_uint, C.c_int, C.POINTER(P)]
     L.mvr_unet_destroy.argtypes = [P]
@@ -387,6 +390,13 @@ class Deconvolution:
     def batch(self) -> int:
         """Blocks per batched launch in use."""
         return int(self._lib.mvr_decon_batch(self._h))
+
+    def set_graphs(self, on: bool):
+        """Whole iterations as CUDA graphs (default on); off launches eagerly."""
+        self._check(self._lib.mvr_decon_set_graphs(self._h, int(on)))
+
+    def graphs_captured(self) -> int:
+        return int(self._lib.mvr_decon_graphs_captured(self._h))
 
     def launch_count(self) -> int:
         return int(self._lib.mvr_decon_launch_count(self._h))
