@@ -15,7 +15,10 @@
 //
 // A CTA of 256 threads takes 16 consecutive x' columns at one index of the other axis;
 // the tile moves between HBM and shared memory in coalesced 16-wide row segments.
-// MODE 2 reads K^ straight from HBM in phase 2, in the same 16-wide segments.
+// MODE 2 stages the same tile of K^ in shared memory.  A gathered tile (pstride > 1)
+// takes one x' column at 16 consecutive indices of the other axis instead: the last
+// column of a spectrum with Hx = 16 q + 1 (the Nyquist column) goes that way, so no
+// CTA works on a tile with a single live column.
 #pragma once
 #include "cols_warp.cuh"
 
@@ -102,7 +105,7 @@ constexpr int kTColNP = 16;  // columns per tile
 template <int V, int MODE>
 __global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst, const float2 *__restrict__ Kh,
                                                   int Hx, long long estride, long long ostride, long long Pc,
-                                                  const float2 *__restrict__ twg)
+                                                  const float2 *__restrict__ twg, long long pstride, int nother)
 {
     constexpr int T = kTColT, NP = kTColNP, n = V * T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -110,21 +113,35 @@ __global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst
     float2 *tw = A + n * NP;                            // [n]: exp(-2 pi i j / n)
     float2 *KA = tw + n;                                // MODE 2: [n][NP] tile of K^
     for (int i = threadIdx.x; i < n; i += 256) tw[i] = __ldg(&twg[i]);
-    const int x0 = blockIdx.x * NP;
-    const long long base = (long long)blockIdx.y * ostride + x0;
+    // tile column p of row i at base + i * estride + p * pstride
+    long long base;
+    int np;
+    if (pstride == 1) {
+        const int x0 = blockIdx.x * NP;
+        base = (long long)blockIdx.y * ostride + x0;
+        np = min(NP, Hx - x0);
+    } else {
+        const int o0 = blockIdx.y * NP;
+        base = (long long)o0 * ostride + (Hx - 1);
+        np = min(NP, nother - o0);
+    }
     src += (long long)blockIdx.z * Pc;
     dst += (long long)blockIdx.z * Pc;
-    const int np = min(NP, Hx - x0);
     constexpr int tot = n * NP;
     constexpr int step = 256 * kLoadBatch;
+    // every thread keeps one column p = threadIdx % 16 and rows threadIdx / 16 + 16 u
+    const int pc = threadIdx.x % NP;
+    const bool plive = pc < np;
+    const long long coff = base + (long long)pc * pstride + (long long)(threadIdx.x / NP) * estride;
+    const long long rstep = (long long)(256 / NP) * estride;
     for (int t0 = threadIdx.x; t0 < tot; t0 += step) {
         float2 r[kLoadBatch], q[kLoadBatch];
+        const long long o0 = coff + (long long)((t0 - threadIdx.x) / 256) * rstep;
 #pragma unroll
         for (int u = 0; u < kLoadBatch; ++u) {
-            const int e = t0 + u * 256;
-            const int p = e % NP, i = e / NP;
-            r[u] = (e < tot && p < np) ? src[base + i * estride + p] : make_float2(0.0f, 0.0f);
-            if (MODE == 2) q[u] = (e < tot && p < np) ? __ldg(&Kh[base + i * estride + p]) : make_float2(0.0f, 0.0f);
+            const bool ok = t0 + u * 256 < tot && plive;
+            r[u] = ok ? src[o0 + u * rstep] : make_float2(0.0f, 0.0f);
+            if (MODE == 2) q[u] = ok ? __ldg(&Kh[o0 + u * rstep]) : make_float2(0.0f, 0.0f);
         }
 #pragma unroll
         for (int u = 0; u < kLoadBatch; ++u) {
@@ -181,10 +198,8 @@ __global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst
         for (int v = 0; v < V; ++v) A[(t + T * v) * NP + c] = a[v];
     }
     if (MODE != 0) __syncthreads();
-    for (int e = threadIdx.x; e < tot; e += 256) {
-        const int p = e % NP, i = e / NP;
-        if (p < np) dst[base + i * estride + p] = A[e];
-    }
+    if (plive)
+        for (int e = threadIdx.x; e < tot; e += 256) dst[coff + (long long)((e - threadIdx.x) / 256) * rstep] = A[e];
 }
 
 // data tile + twiddles (+ the K^ tile of MODE 2)

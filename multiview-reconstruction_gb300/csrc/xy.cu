@@ -81,7 +81,7 @@ cudaError_t fwd(int combo, const Src &src, float2 *S, const BlockMaps &bms, int 
 {
     set_limits();
     const dim3 grid((unsigned)Pz, (unsigned)nb);
-    XY_DISPATCH(combo, (k_xy_fwd<VX_, VY_, Src><<<grid, kXYThreads, xy_smem_bytes<VX_, VY_>(), s>>>(
+    XY_DISPATCH(combo, (k_xy_fwd<VX_, VY_, Src><<<grid, XYShape<VX_, VY_>::NT, xy_smem_bytes<VX_, VY_>(), s>>>(
                            src, S, bms, Pc, twx, twy)));
     return cudaGetLastError();
 }
@@ -111,7 +111,7 @@ cudaError_t xy_ratio(int combo, float2 *S, const float *img, const BlockMaps &bm
 {
     set_limits();
     const dim3 grid((unsigned)Pz, (unsigned)nb);
-    XY_DISPATCH(combo, (k_xy_ratio<VX_, VY_><<<grid, kXYThreads, xy_smem_bytes<VX_, VY_>(), s>>>(S, img, bms, Pc, twx,
+    XY_DISPATCH(combo, (k_xy_ratio<VX_, VY_><<<grid, XYShape<VX_, VY_>::NT, xy_smem_bytes<VX_, VY_>(), s>>>(S, img, bms, Pc, twx,
                                                                                                  twy)));
     return cudaGetLastError();
 }
@@ -122,7 +122,7 @@ cudaError_t xy_update(int combo, int epi, float2 *S, const UpdateArgs &ua, const
     set_limits();
     const dim3 grid((unsigned)Pz, (unsigned)nb);
 #define XY_UPD(E)                                                                                               \
-    XY_DISPATCH(combo, (k_xy_update<VX_, VY_, E><<<grid, kXYThreads, xy_smem_bytes<VX_, VY_>(), s>>>(S, ua, bms, \
+    XY_DISPATCH(combo, (k_xy_update<VX_, VY_, E><<<grid, XYShape<VX_, VY_>::NT, xy_smem_bytes<VX_, VY_>(), s>>>(S, ua, bms, \
                                                                                                     Pc, twx, twy)))
     switch (epi) {
     case EPI_SEQ: XY_UPD(EPI_SEQ); break;

@@ -34,7 +34,6 @@
 
 namespace mvr {
 
-constexpr int kXYThreads = 1024;
 constexpr long long kNoRow = -(1LL << 62);
 
 template <int VX, int VY>
@@ -44,6 +43,14 @@ struct XYShape {
     static constexpr int Py = 16 * VY;
     static constexpr int SR = m + 1;      // row stride (x spectrum incl. Nyquist)
     static constexpr int plane = Py * SR; // complex values per plane
+    // threads per CTA and CTAs per SM: 1024 x 1 for the 155 KB plane of 192 x 192,
+    // 512 x 2 for the planes of at most 100 KB (the latency of the shared-memory FFT
+    // phases is hidden by warps, not by per-thread interleaving)
+    static constexpr int NT = (VX == 6 && VY == 12) ? 1024 : 512;
+    static constexpr int MINB = (VX == 6 && VY == 12) ? 1 : 2;
+    // rounds of the row items (y, t) of the fused x phase 1
+    static constexpr int RX = Py * 16 / NT;
+    static_assert((Py * 16) % NT == 0, "row items must fill whole rounds");
 };
 
 // Bytes of dynamic shared memory of the plane kernels of shape (VX, VY).
@@ -52,28 +59,27 @@ constexpr size_t xy_smem_bytes()
 {
     typedef XYShape<VX, VY> S;
     return sizeof(float2) * (size_t)(S::plane + S::Px + S::Py) + 3 * sizeof(long long) * S::Py +
-           sizeof(int) * (size_t)(3 * S::Px + S::m);
+           sizeof(int) * (size_t)(3 * S::Px + S::m + S::Py);
 }
 
 // ---- two-phase FFT on pencils in shared memory -------------------------------------
 // Element i of pencil p at A[p * PS + i * ES]; tw[j * TWM] = exp(-2 pi i j / (16 V)).
-template <int V, int NPEN, int PS, int ES, bool INV>
+// Items run pencil-fastest so that a warp touches consecutive pencils.
+template <int V, int NPEN, int PS, int ES, bool INV, int NT>
 __device__ __forceinline__ void tp_phase1(float2 *A, const float2 *tw, int twm)
 {
     constexpr int T = 16, items = NPEN * T;
-    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    for (int it = threadIdx.x; it < items; it += NT) {
         const int t = it / NPEN, p = it - t * NPEN;
         float2 *a0 = A + p * PS + t * ES;
         float2 a[V];
-        if (!INV) {
 #pragma unroll
-            for (int v = 0; v < V; ++v) a[v] = a0[T * v * ES];
+        for (int v = 0; v < V; ++v) a[v] = a0[T * v * ES];
+        if (!INV) {
             sdft<V, false>(a);
 #pragma unroll
             for (int k1 = 1; k1 < V; ++k1) a[k1] = cmul(a[k1], tw[t * k1 * twm]);
         } else {
-#pragma unroll
-            for (int k1 = 0; k1 < V; ++k1) a[k1] = a0[T * k1 * ES];
 #pragma unroll
             for (int k1 = 1; k1 < V; ++k1) a[k1] = cmul(a[k1], cconj(tw[t * k1 * twm]));
             sdft<V, true>(a);
@@ -83,11 +89,11 @@ __device__ __forceinline__ void tp_phase1(float2 *A, const float2 *tw, int twm)
     }
 }
 
-template <int V, int NPEN, int PS, int ES, bool INV>
+template <int V, int NPEN, int PS, int ES, bool INV, int NT>
 __device__ __forceinline__ void tp_phase2(float2 *A)
 {
     constexpr int T = 16, items = NPEN * V;
-    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    for (int it = threadIdx.x; it < items; it += NT) {
         const int k1 = it / NPEN, p = it - k1 * NPEN;
         float2 *b0 = A + p * PS + T * k1 * ES;
         float2 b[T];
@@ -99,24 +105,39 @@ __device__ __forceinline__ void tp_phase2(float2 *A)
     }
 }
 
-// Forward x FFT of all rows, then the packed-real split in tile order.
+// x phase 1 of one row item (y, t) on registers: a[v] <-> positions t + 16 v of row y.
+// Forward: natural-order values in, twiddled phase-1 output out; inverse the reverse.
+template <int VX, bool INV>
+__device__ __forceinline__ void xrow_p1(float2 (&a)[VX], const float2 *twx, int t)
+{
+    if (!INV) {
+        sdft<VX, false>(a);
+#pragma unroll
+        for (int k1 = 1; k1 < VX; ++k1) a[k1] = cmul(a[k1], twx[2 * t * k1]);
+    } else {
+#pragma unroll
+        for (int k1 = 1; k1 < VX; ++k1) a[k1] = cmul(a[k1], cconj(twx[2 * t * k1]));
+        sdft<VX, true>(a);
+    }
+}
+
+// x phase 2 (forward), then the packed-real split in tile order.  The DC and Nyquist
+// values of a row (both real) are packed as one complex value at position 0, so that the
+// y transforms run on m columns.
 template <int VX, int VY>
-__device__ __forceinline__ void xy_x_forward(float2 *A, const float2 *twx, const int *posx)
+__device__ __forceinline__ void xy_x_forward_p2(float2 *A, const float2 *twx, const int *posx)
 {
     typedef XYShape<VX, VY> S;
-    constexpr int m = S::m, half = m / 2, items = S::Py * (half + 1);
-    tp_phase1<VX, S::Py, S::SR, 1, false>(A, twx, 2);
-    __syncthreads();
-    tp_phase2<VX, S::Py, S::SR, 1, false>(A);
+    constexpr int m = S::m, half = m / 2, items = S::Py * (half + 1), NT = S::NT;
+    tp_phase2<VX, S::Py, S::SR, 1, false, NT>(A);
     __syncthreads();
     // X[f] = E[f] + W_Px^f O[f], E = (Z[f] + conj Z[m-f]) / 2, O = -i (Z[f] - conj Z[m-f]) / 2
-    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    for (int it = threadIdx.x; it < items; it += NT) {
         const int f = it / S::Py, y = it - f * S::Py;
         float2 *row = A + y * S::SR;
         if (f == 0) {
             const float2 z0 = row[0];
-            row[0] = make_float2(z0.x + z0.y, 0.0f);
-            row[m] = make_float2(z0.x - z0.y, 0.0f);
+            row[0] = make_float2(z0.x + z0.y, z0.x - z0.y);  // (X[0], X[m]), both real
             continue;
         }
         const int g = m - f, pf = posx[f], pg = posx[g];
@@ -135,49 +156,76 @@ __device__ __forceinline__ void xy_x_forward(float2 *A, const float2 *twx, const
     __syncthreads();
 }
 
-// Packed-real merge in tile order, then the inverse x FFT: natural-order packed rows
-// times Px (the kernel spectra carry 1 / (Px Py Pz)).
+// Packed-real merge in tile order, then x phase 2 inverse (x phase 1 inverse follows in
+// the caller).  Position 0 holds (X[0], X[m]).
 template <int VX, int VY>
-__device__ __forceinline__ void xy_x_inverse(float2 *A, const float2 *twx, const int *posx)
+__device__ __forceinline__ void xy_x_inverse_p2(float2 *A, const float2 *twx, const int *posx)
 {
     typedef XYShape<VX, VY> S;
-    constexpr int m = S::m, half = m / 2, items = S::Py * (half + 1);
+    constexpr int m = S::m, half = m / 2, items = S::Py * (half + 1), NT = S::NT;
     // a[k] = e + i o, e = X[k] + conj X[m-k], o = (X[k] - conj X[m-k]) conj(W_Px^k)
-    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    for (int it = threadIdx.x; it < items; it += NT) {
         const int f = it / S::Py, y = it - f * S::Py;
         float2 *row = A + y * S::SR;
-        const int g = m - f, pf = posx[f], pg = f == 0 ? m : posx[g];
+        if (f == 0) {
+            const float2 p = row[0];
+            row[0] = make_float2(p.x + p.y, p.x - p.y);
+            continue;
+        }
+        const int g = m - f, pf = posx[f], pg = posx[g];
         const float2 xf = row[pf], xg = row[pg];
         {
             const float2 c = cconj(xg);
             const float2 e = cadd(xf, c), o = cmul(csub(xf, c), cconj(twx[f]));
             row[pf] = make_float2(e.x - o.y, e.y + o.x);
         }
-        if (f != 0 && g != f) {
+        if (g != f) {
             const float2 c = cconj(xf);
             const float2 e = cadd(xg, c), o = cmul(csub(xg, c), cconj(twx[g]));
             row[pg] = make_float2(e.x - o.y, e.y + o.x);
         }
     }
     __syncthreads();
-    tp_phase2<VX, S::Py, S::SR, 1, true>(A);
-    __syncthreads();
-    tp_phase1<VX, S::Py, S::SR, 1, true>(A, twx, 2);
+    tp_phase2<VX, S::Py, S::SR, 1, true, NT>(A);
     __syncthreads();
 }
 
+// y transforms of the m columns.  Forward: column 0 holds X[0] + i X[m] per row (two real
+// sequences); afterwards it is split into the spectra of both (Hermitian in y), X[0]'s
+// to column 0 and X[m]'s to column m.  Inverse: the two columns are recombined as
+// Y0 + i Ym before the transform, and column 0 returns X[0] + i X[m] per row.
 template <int VX, int VY, bool INV>
-__device__ __forceinline__ void xy_y(float2 *A, const float2 *twy)
+__device__ __forceinline__ void xy_y(float2 *A, const float2 *twy, const int *posy)
 {
     typedef XYShape<VX, VY> S;
+    constexpr int m = S::m, Py = S::Py, NT = S::NT;
     if (!INV) {
-        tp_phase1<VY, S::SR, 1, S::SR, false>(A, twy, 1);
+        tp_phase1<VY, m, 1, S::SR, false, NT>(A, twy, 1);
         __syncthreads();
-        tp_phase2<VY, S::SR, 1, S::SR, false>(A);
+        tp_phase2<VY, m, 1, S::SR, false, NT>(A);
+        __syncthreads();
+        for (int k = threadIdx.x; k <= Py / 2; k += NT) {
+            const int g = (Py - k) % Py, pk = posy[k], pg = posy[g];
+            const float2 P = A[pk * S::SR], Q = A[pg * S::SR];
+            // Y0[k] = (P + conj Q) / 2, Ym[k] = -i (P - conj Q) / 2, and the same for g
+            const float2 y0k = cscale(cadd(P, cconj(Q)), 0.5f), dk = cscale(csub(P, cconj(Q)), 0.5f);
+            const float2 y0g = cscale(cadd(Q, cconj(P)), 0.5f), dg = cscale(csub(Q, cconj(P)), 0.5f);
+            A[pk * S::SR] = y0k;
+            A[pk * S::SR + m] = make_float2(dk.y, -dk.x);
+            if (g != k) {
+                A[pg * S::SR] = y0g;
+                A[pg * S::SR + m] = make_float2(dg.y, -dg.x);
+            }
+        }
     } else {
-        tp_phase2<VY, S::SR, 1, S::SR, true>(A);
+        for (int q = threadIdx.x; q < Py; q += NT) {
+            const float2 a = A[q * S::SR], b = A[q * S::SR + m];
+            A[q * S::SR] = make_float2(a.x - b.y, a.y + b.x);
+        }
         __syncthreads();
-        tp_phase1<VY, S::SR, 1, S::SR, true>(A, twy, 1);
+        tp_phase2<VY, m, 1, S::SR, true, NT>(A);
+        __syncthreads();
+        tp_phase1<VY, m, 1, S::SR, true, NT>(A, twy, 1);
     }
     __syncthreads();
 }
@@ -190,6 +238,7 @@ struct XYSmem {
     long long *rowb, *rowb2, *rowb3;  // per domain row: volume / block row bases (or -1)
     int *colx, *colx2, *colx3;        // per domain x: volume x of the row's voxel (or -1)
     int *posx;                        // tile position of x frequency f < m
+    int *posy;                        // tile position of y frequency k < Py
     __device__ __forceinline__ XYSmem(unsigned char *raw)
     {
         A = reinterpret_cast<float2 *>(raw);
@@ -202,12 +251,14 @@ struct XYSmem {
         colx2 = colx + S::Px;
         colx3 = colx2 + S::Px;
         posx = colx3 + S::Px;
+        posy = posx + S::m;
     }
     __device__ __forceinline__ void load_tables(const float2 *__restrict__ gtwx, const float2 *__restrict__ gtwy)
     {
         for (int i = threadIdx.x; i < S::Px; i += blockDim.x) twx[i] = __ldg(&gtwx[i]);
         for (int i = threadIdx.x; i < S::Py; i += blockDim.x) twy[i] = __ldg(&gtwy[i]);
         for (int f = threadIdx.x; f < S::m; f += blockDim.x) posx[f] = f / VX + 16 * (f % VX);
+        for (int k = threadIdx.x; k < S::Py; k += blockDim.x) posy[k] = k / VY + 16 * (k % VY);
     }
 };
 
@@ -248,12 +299,15 @@ struct XYSrcTraits { static constexpr bool mirror = false; };
 template <>
 struct XYSrcTraits<SrcMirror<float>> { static constexpr bool mirror = true; };
 
+// Row items (y, t) of the fused x phase 1: thread k of the CTA takes item
+// it = k + r NT (r < RX), t = it % 16 (a half-warp covers 32 consecutive x of one row).
 template <int VX, int VY, class Src>
-__global__ void __launch_bounds__(kXYThreads, 1) k_xy_fwd(Src src, float2 *__restrict__ S, const BlockMaps bms,
-                                                          long long Pc, const float2 *__restrict__ gtwx,
-                                                          const float2 *__restrict__ gtwy)
+__global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
+    k_xy_fwd(Src src, float2 *__restrict__ S, const BlockMaps bms, long long Pc, const float2 *__restrict__ gtwx,
+             const float2 *__restrict__ gtwy)
 {
     typedef XYShape<VX, VY> SH;
+    constexpr int NT = SH::NT, RX = SH::RX;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     XYSmem<VX, VY> sm(smem_raw);
     const BlockMap &bm = bms.m[blockIdx.y];
@@ -261,58 +315,55 @@ __global__ void __launch_bounds__(kXYThreads, 1) k_xy_fwd(Src src, float2 *__res
     float2 *Sp = S + (long long)blockIdx.y * Pc + (long long)z * SH::plane;
     sm.load_tables(gtwx, gtwy);
     constexpr bool MIR = XYSrcTraits<Src>::mirror;
-    for (int y = threadIdx.x; y < SH::Py; y += blockDim.x) {
+    for (int y = threadIdx.x; y < SH::Py; y += NT) {
         const typename Src::Row r = src.row(bm, y, z);
         sm.rowb[y] = r.base;
     }
     if (MIR)
-        for (int x = threadIdx.x; x < SH::Px; x += blockDim.x) sm.colx[x] = (int)mirror_x(bm, x);
+        for (int x = threadIdx.x; x < SH::Px; x += NT) sm.colx[x] = (int)mirror_x(bm, x);
     __syncthreads();
-    // every thread keeps U pairs of loads in flight (the CTA is alone on its SM, so
-    // the load phase is latency-bound otherwise)
-    constexpr int items = SH::Py * SH::m, U = kXYThreads >= 1024 ? 6 : 12;
-    for (int i0 = threadIdx.x; i0 < items; i0 += blockDim.x * U) {
-        float v[U][2];
+    // all loads of the thread's row items first, then their x phase 1
+    float2 a[RX][VX];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int it = i0 + u * blockDim.x;
-            const int y = it / SH::m, j = it - y * SH::m;
-            if (it < items) {
-                if constexpr (MIR) {
-                    const float *pr = src.vol + sm.rowb[y];
-                    v[u][0] = __ldg(pr + sm.colx[2 * j]);
-                    v[u][1] = __ldg(pr + sm.colx[2 * j + 1]);
-                } else {
-                    typename Src::Row r;
-                    r.base = sm.rowb[y];
-                    v[u][0] = src.template at<float>(r, bm, 2 * j);
-                    v[u][1] = src.template at<float>(r, bm, 2 * j + 1);
-                }
+    for (int r = 0; r < RX; ++r) {
+        const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;
+#pragma unroll
+        for (int v = 0; v < VX; ++v) {
+            const int x = 2 * (t + 16 * v);
+            if constexpr (MIR) {
+                const float *pr = src.vol + sm.rowb[y];
+                a[r][v] = make_float2(__ldg(pr + sm.colx[x]), __ldg(pr + sm.colx[x + 1]));
+            } else {
+                typename Src::Row row;
+                row.base = sm.rowb[y];
+                a[r][v] = make_float2(src.template at<float>(row, bm, x), src.template at<float>(row, bm, x + 1));
             }
         }
+    }
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int it = i0 + u * blockDim.x;
-            const int y = it / SH::m, j = it - y * SH::m;
-            if (it < items) sm.A[y * SH::SR + j] = make_float2(v[u][0], v[u][1]);
-        }
+    for (int r = 0; r < RX; ++r) {
+        const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;
+        xrow_p1<VX, false>(a[r], sm.twx, t);
+#pragma unroll
+        for (int v = 0; v < VX; ++v) sm.A[y * SH::SR + t + 16 * v] = a[r][v];
     }
     __syncthreads();
-    xy_x_forward<VX, VY>(sm.A, sm.twx, sm.posx);
-    xy_y<VX, VY, false>(sm.A, sm.twy);
+    xy_x_forward_p2<VX, VY>(sm.A, sm.twx, sm.posx);
+    xy_y<VX, VY, false>(sm.A, sm.twy, sm.posy);
     xy_store_plane<VX, VY>(Sp, sm.A);
 }
 
 // ---- C2R -> quotient -> R2C ----------------------------------------------------------
 // DeconvolutionMethods.java:71-74: img > 0 ? img / conv1 : 1.  Domain voxels outside the
 // block (the value-1 extension) and outside the volume (img zero-extended) read img = 0.
+// x phase 1 inverse, the quotient and x phase 1 forward run on registers per row item.
 template <int VX, int VY>
-__global__ void __launch_bounds__(kXYThreads, 1) k_xy_ratio(float2 *__restrict__ S, const float *__restrict__ img,
-                                                            const BlockMaps bms, long long Pc,
-                                                            const float2 *__restrict__ gtwx,
-                                                            const float2 *__restrict__ gtwy)
+__global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
+    k_xy_ratio(float2 *__restrict__ S, const float *__restrict__ img, const BlockMaps bms, long long Pc,
+               const float2 *__restrict__ gtwx, const float2 *__restrict__ gtwy)
 {
     typedef XYShape<VX, VY> SH;
+    constexpr int NT = SH::NT, RX = SH::RX;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     XYSmem<VX, VY> sm(smem_raw);
     const BlockMap &bm = bms.m[blockIdx.y];
@@ -320,70 +371,57 @@ __global__ void __launch_bounds__(kXYThreads, 1) k_xy_ratio(float2 *__restrict__
     float2 *Sp = S + (long long)blockIdx.y * Pc + (long long)z * SH::plane;
     sm.load_tables(gtwx, gtwy);
     const int ez = ext_e(z, bm.P[2], bm.L[2]);
-    for (int y = threadIdx.x; y < SH::Py; y += blockDim.x) {
+    for (int y = threadIdx.x; y < SH::Py; y += NT) {
         const int ey = ext_e(y, bm.P[1], bm.L[1]);
         const bool rin = ey >= 0 && ey < bm.b[1] && ez >= 0 && ez < bm.b[2];
         sm.rowb[y] = rin ? zero_row(bm, ey, ez).base : -1;
     }
-    for (int x = threadIdx.x; x < SH::Px; x += blockDim.x) {
+    for (int x = threadIdx.x; x < SH::Px; x += NT) {
         const int bx = ext_e(x, bm.P[0], bm.L[0]);
         const long long gx = bm.off[0] + bx;
         sm.colx[x] = (bx >= 0 && bx < bm.b[0] && gx >= 0 && gx < bm.D[0]) ? (int)gx : -1;
     }
-    __syncthreads();
-    // image pairs (x = 2j, 2j + 1 of row y) in batches of U per thread, double-buffered
-    // in registers; the first batch is in flight while the plane loads and transforms
-    constexpr int items = SH::Py * SH::m, U = 4, STEP = kXYThreads * U;
-    auto load_img = [&](int i0, float (&r)[U][2]) {
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int it = i0 + u * kXYThreads;
-            const int y = it / SH::m, j = it - y * SH::m;
-            const long long rb = it < items ? sm.rowb[y] : -1;
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int gx = sm.colx[2 * j + h];
-                r[u][h] = (rb >= 0 && gx >= 0) ? __ldg(img + rb + gx) : 0.0f;
-            }
-        }
-    };
-    auto apply = [&](int i0, const float (&r)[U][2]) {
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int it = i0 + u * kXYThreads;
-            const int y = it / SH::m, j = it - y * SH::m;
-            if (it < items) {
-                float2 &c = sm.A[y * SH::SR + j];
-                c = make_float2(quotient_fast(r[u][0], c.x), quotient_fast(r[u][1], c.y));
-            }
-        }
-    };
-    float ia[U][2], ib[U][2];
-    load_img(threadIdx.x, ia);
     xy_load_plane<VX, VY>(sm.A, Sp);
     __syncthreads();
-    xy_y<VX, VY, true>(sm.A, sm.twy);
-    xy_x_inverse<VX, VY>(sm.A, sm.twx, sm.posx);
-    for (int i0 = threadIdx.x; i0 < items; i0 += 2 * STEP) {
-        load_img(i0 + STEP, ib);
-        apply(i0, ia);
-        load_img(i0 + 2 * STEP, ia);
-        apply(i0 + STEP, ib);
+    xy_y<VX, VY, true>(sm.A, sm.twy, sm.posy);
+    xy_x_inverse_p2<VX, VY>(sm.A, sm.twx, sm.posx);
+#pragma unroll 1
+    for (int r = 0; r < RX; ++r) {
+        const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;
+        const long long rb = sm.rowb[y];
+        float im[VX][2];
+#pragma unroll
+        for (int v = 0; v < VX; ++v)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int gx = sm.colx[2 * (t + 16 * v) + h];
+                im[v][h] = (rb >= 0 && gx >= 0) ? __ldg(img + rb + gx) : 0.0f;
+            }
+        float2 a[VX];
+        float2 *row = sm.A + y * SH::SR + t;
+#pragma unroll
+        for (int v = 0; v < VX; ++v) a[v] = row[16 * v];
+        xrow_p1<VX, true>(a, sm.twx, t);  // natural order: a[v] = conv1 at x = 2 (t + 16 v) + {0, 1}
+#pragma unroll
+        for (int v = 0; v < VX; ++v) a[v] = make_float2(quotient_fast(im[v][0], a[v].x), quotient_fast(im[v][1], a[v].y));
+        xrow_p1<VX, false>(a, sm.twx, t);
+#pragma unroll
+        for (int v = 0; v < VX; ++v) row[16 * v] = a[v];
     }
     __syncthreads();
-    xy_x_forward<VX, VY>(sm.A, sm.twx, sm.posx);
-    xy_y<VX, VY, false>(sm.A, sm.twy);
+    xy_x_forward_p2<VX, VY>(sm.A, sm.twx, sm.posx);
+    xy_y<VX, VY, false>(sm.A, sm.twy, sm.posy);
     xy_store_plane<VX, VY>(Sp, sm.A);
 }
 
 // ---- C2R -> update epilogue --------------------------------------------------------------
 template <int VX, int VY, int EPI>
-__global__ void __launch_bounds__(kXYThreads, 1) k_xy_update(float2 *__restrict__ S, UpdateArgs ua,
-                                                             const BlockMaps bms, long long Pc,
-                                                             const float2 *__restrict__ gtwx,
-                                                             const float2 *__restrict__ gtwy)
+__global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
+    k_xy_update(float2 *__restrict__ S, UpdateArgs ua, const BlockMaps bms, long long Pc,
+                const float2 *__restrict__ gtwx, const float2 *__restrict__ gtwy)
 {
     typedef XYShape<VX, VY> SH;
+    constexpr int NT = SH::NT, RX = SH::RX;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double red_s[32], red_m[32];
     XYSmem<VX, VY> sm(smem_raw);
@@ -396,13 +434,11 @@ __global__ void __launch_bounds__(kXYThreads, 1) k_xy_update(float2 *__restrict_
     sm.load_tables(gtwx, gtwy);
     float ksum = 0.0f, kcomp = 0.0f, kmax = -1.0f;
     if constexpr (EPI == EPI_SEQ) {
-        // lean Seq epilogue (computeFinalValues / computeNextValue, DeconvolutionMethods.java
-        // 103-182, 320-358) over the pairs (x = 2j, 2j + 1) of the block rows, with psi and
-        // the weight double-buffered in registers; the first batch is in flight while the
-        // plane loads and transforms
+        // Seq epilogue (computeFinalValues / computeNextValue, DeconvolutionMethods.java
+        // 103-182, 320-358) fused with x phase 1 inverse on the row items
         const bool zin = z < bm.b[2];  // extension planes carry no block voxels
         const bool zw = z >= bm.wlo[2] && z < bm.whi[2];
-        for (int y = threadIdx.x; y < SH::Py; y += blockDim.x) {
+        for (int y = threadIdx.x; y < SH::Py; y += NT) {
             const bool in = zin && y < bm.b[1];
             sm.rowb[y] = in ? mirror_row(bm, y, z).base : -1;
             sm.rowb2[y] = in ? zero_row(bm, y, z).base : -1;
@@ -412,14 +448,17 @@ __global__ void __launch_bounds__(kXYThreads, 1) k_xy_update(float2 *__restrict_
                               ? ((bm.ooff[2] + z) * bm.OD[1] + (bm.ooff[1] + y)) * bm.OD[0] + bm.ooff[0]
                               : kNoRow;
         }
-        for (int x = threadIdx.x; x < SH::Px; x += blockDim.x) {
+        for (int x = threadIdx.x; x < SH::Px; x += NT) {
             const bool in = x < bm.b[0];
             const long long gx = bm.off[0] + x;
             sm.colx[x] = in ? (int)mirror_x(bm, x) : -1;
             sm.colx2[x] = (in && gx >= 0 && gx < bm.D[0]) ? (int)gx : -1;
             sm.colx3[x] = (in && x >= bm.wlo[0] && x < bm.whi[0]) ? x : -1;
         }
+        xy_load_plane<VX, VY>(sm.A, Sp);
         __syncthreads();
+        xy_y<VX, VY, true>(sm.A, sm.twy, sm.posy);
+        xy_x_inverse_p2<VX, VY>(sm.A, sm.twx, sm.posx);
         const float *psrc = reinterpret_cast<const float *>(ua.psi_src);
         float *pdst = reinterpret_cast<float *>(ua.psi_dst);
         const float *wgt = ua.weight[0];
@@ -429,37 +468,35 @@ __global__ void __launch_bounds__(kXYThreads, 1) k_xy_update(float2 *__restrict_
         uc.inv_maxI = 1.0f / ua.maxI;
         uc.two_lambda = (float)(2.0 * ua.lambda);
         uc.tik = ua.lambda > 0.0;
-        constexpr int items = SH::Py * SH::m, U = 4, STEP = kXYThreads * U;
-        auto load = [&](int i0, float (&pv)[U][2], float (&wv)[U][2]) {
+#pragma unroll 1
+        for (int r = 0; r < RX; ++r) {
+            const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;
+            const long long pb = sm.rowb[y], wb = sm.rowb2[y], ob = sm.rowb3[y];
+            if (pb < 0) continue;  // not a block row
+            float pv[VX][2], wv[VX][2];
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int it = i0 + u * kXYThreads;
-                const int y = it / SH::m, j = it - y * SH::m;
-                const long long pb = it < items ? sm.rowb[y] : -1;
-                const long long wb = it < items ? sm.rowb2[y] : -1;
+            for (int v = 0; v < VX; ++v)
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    const int mx = sm.colx[2 * j + h], gx = sm.colx2[2 * j + h];
-                    pv[u][h] = (pb >= 0 && mx >= 0) ? __ldg(psrc + pb + mx) : 0.0f;
-                    wv[u][h] = (wb >= 0 && gx >= 0) ? __ldg(wgt + wb + gx) : 0.0f;
+                    const int x = 2 * (t + 16 * v) + h;
+                    const int mx = sm.colx[x], gx = sm.colx2[x];
+                    pv[v][h] = mx >= 0 ? __ldg(psrc + pb + mx) : 0.0f;
+                    wv[v][h] = (wb >= 0 && gx >= 0) ? __ldg(wgt + wb + gx) : 0.0f;
                 }
-            }
-        };
-        auto apply = [&](int i0, const float (&pv)[U][2], const float (&wv)[U][2]) {
+            float2 a[VX];
+            const float2 *row = sm.A + y * SH::SR + t;
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int it = i0 + u * kXYThreads;
-                const int y = it / SH::m, j = it - y * SH::m;
-                if (it >= items || sm.rowb[y] < 0) continue;
-                const long long ob = sm.rowb3[y];
-                const float2 c = sm.A[y * SH::SR + j];
-                const float cv[2] = {c.x, c.y};
+            for (int v = 0; v < VX; ++v) a[v] = row[16 * v];
+            xrow_p1<VX, true>(a, sm.twx, t);  // natural order: conv2 at x = 2 (t + 16 v) + {0, 1}
+#pragma unroll
+            for (int v = 0; v < VX; ++v) {
+                const float cv[2] = {a[v].x, a[v].y};
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    const int x = 2 * j + h;
+                    const int x = 2 * (t + 16 * v) + h;
                     if (sm.colx[x] < 0) continue;  // beyond the block
-                    const float last = pv[u][h];
-                    const float next = next_value_fast(last, cv[h], wv[u][h], uc);
+                    const float last = pv[v][h];
+                    const float next = next_value_fast(last, cv[h], wv[v][h], uc);
                     const float ch = next - last;  // signed change (DeconvolutionMethods.java:308)
                     const float ky = ch - kcomp;
                     const float kt = ksum + ky;
@@ -469,25 +506,15 @@ __global__ void __launch_bounds__(kXYThreads, 1) k_xy_update(float2 *__restrict_
                     if (ob != kNoRow && sm.colx3[x] >= 0) pdst[ob + x] = next;
                 }
             }
-        };
-        float pa[U][2], wa[U][2], pb[U][2], wb[U][2];
-        load(threadIdx.x, pa, wa);
-        xy_load_plane<VX, VY>(sm.A, Sp);
-        __syncthreads();
-        xy_y<VX, VY, true>(sm.A, sm.twy);
-        xy_x_inverse<VX, VY>(sm.A, sm.twx, sm.posx);
-        for (int i0 = threadIdx.x; i0 < items; i0 += 2 * STEP) {
-            load(i0 + STEP, pb, wb);
-            apply(i0, pa, wa);
-            load(i0 + 2 * STEP, pa, wa);
-            apply(i0 + STEP, pb, wb);
         }
     } else {
         xy_load_plane<VX, VY>(sm.A, Sp);
         __syncthreads();
-        xy_y<VX, VY, true>(sm.A, sm.twy);
-        xy_x_inverse<VX, VY>(sm.A, sm.twx, sm.posx);
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+        xy_y<VX, VY, true>(sm.A, sm.twy, sm.posy);
+        xy_x_inverse_p2<VX, VY>(sm.A, sm.twx, sm.posx);
+        tp_phase1<VX, SH::Py, SH::SR, 1, true, NT>(sm.A, sm.twx, 2);
+        __syncthreads();
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = NT >> 5;
         if (z < bm.b[2])  // extension planes carry no block voxels
             for (int y = warp; y < bm.b[1] && y < SH::Py; y += nw)
                 update_row<float, EPI>(sm.A + y * SH::SR, SH::m, bm, ua, y, z, lane, ksum, kcomp, kmax);
