@@ -35,23 +35,63 @@ for _p in (PKG, os.path.join(ROOT, "oracle")):
 
 import numpy as np  # noqa: E402
 
-DIMS = (256, 256, 256)
-VIEWS = 4
-BLOCK = (192, 192, 192)
-PSF = (31, 31, 61)
-LAMBDA = 0.006
-METRIC = "voxel-iterations/s (4 views)"
 UNIT = "voxel-iterations/s"
-NVOX = DIMS[0] * DIMS[1] * DIMS[2]
-VIEW_BLOCKS_PER_ITER = 16 * VIEWS  # 2 x 2 x 4 blocks of 192^3 per view
 
 
-def workload_config(boundary):
-    return {"workload": "4 views 256^3 float32, PSF 31x31x61 Optimization-I, blocks 192^3, Seq (OSEM-like)",
-            "views": VIEWS, "dims": list(DIMS), "block": list(BLOCK), "psf": list(PSF), "lambda": LAMBDA,
-            "iterations_per_step": 1, "boundary": boundary,
-            "l2": "inputs larger than L2 (4 images + 4 weights + psi = 576 MiB)",
-            "data": "seeded synthetic beads + ellipsoid, Poisson, background 10"}
+class Workload:
+    """A named deconvolution workload: volume, views, compute block, PSF sizes per view."""
+
+    def __init__(self, name, dims, views, block, psfs, lam, make, desc):
+        self.name, self.dims, self.views, self.block, self.psfs, self.lam = name, dims, views, block, psfs, lam
+        self.make, self.desc = make, desc
+        self.nvox = dims[0] * dims[1] * dims[2]
+        self.metric = f"voxel-iterations/s ({views} views)"
+
+    def blocks(self, v):
+        import oracle
+
+        kk = tuple(2 * k - 1 for k in self.psfs[v])
+        return oracle.divide_into_blocks(self.dims, kk, self.block)
+
+    def view_blocks_per_iter(self):
+        return sum(len(self.blocks(v)) for v in range(self.views))
+
+    def config(self, boundary):
+        return {"workload": self.desc, "views": self.views, "dims": list(self.dims), "block": list(self.block),
+                "psf": [list(p) for p in self.psfs] if len(set(self.psfs)) > 1 else list(self.psfs[0]),
+                "lambda": self.lam, "iterations_per_step": 1, "boundary": boundary,
+                "l2": f"inputs larger than L2 ({self.views} images + {self.views} weights + psi = "
+                      f"{(2 * self.views + 1) * self.nvox * 4 / 2**20:.0f} MiB)",
+                "data": "seeded synthetic beads + ellipsoid, Poisson, background 10"}
+
+
+def _make256():
+    import synthetic
+
+    return synthetic.config_256()
+
+
+def _make512():
+    import synthetic
+
+    return synthetic.config_512()
+
+
+def _psf_sizes_6():
+    import synthetic
+
+    return [tuple(p) for p in synthetic.PSF_SIZES_6]
+
+
+WORKLOADS = {
+    "4view256": lambda: Workload("4view256", (256, 256, 256), 4, (192, 192, 192), [(31, 31, 61)] * 4, 0.006, _make256,
+                                 "4 views 256^3 float32, PSF 31x31x61 Optimization-I, blocks 192^3, Seq (OSEM-like)"),
+    "6view512": lambda: Workload("6view512", (512, 512, 256), 6, (192, 192, 256), _psf_sizes_6(), 0.006, _make512,
+                                 "6 views 512x512x256 float32, PSFs 21x21x41 ... 41x41x81 per view, "
+                                 "Optimization-I, compute blocks 192x192x256 (effective 112-152 x 112-152 x 96-176, "
+                                 "uneven edge blocks), Seq"),
+}
+W = None  # the workload of this run (set in main)
 
 
 def load_peaks():
@@ -80,9 +120,7 @@ def ncu_traffic():
 
 
 def make_data():
-    import synthetic
-
-    return synthetic.config_256()
+    return W.make()
 
 
 class ClockSampler:
@@ -179,16 +217,16 @@ def cpu_block_sample(ds, k1s, k2s, mx, n_blocks):
     of the workload; returns (seconds per view-block, threads)."""
     import oracle
 
-    D = DIMS
-    kk = tuple(2 * k - 1 for k in PSF)
-    blocks = oracle.divide_into_blocks(D, kk, BLOCK)
+    D = W.dims
+    B = W.block
     times = []
     for i in range(n_blocks):
-        v = i % VIEWS
+        v = i % W.views
+        blocks = W.blocks(v)
         bl = blocks[(5 + i) % len(blocks)]
         off = bl["offset"]
-        idx = [np.arange(off[d], off[d] + BLOCK[d]) for d in range(3)]
-        psi = np.full((BLOCK[2], BLOCK[1], BLOCK[0]), 50.0, np.float32)
+        idx = [np.arange(off[d], off[d] + B[d]) for d in range(3)]
+        psi = np.full((B[2], B[1], B[0]), 50.0, np.float32)
         img = np.zeros_like(psi)
         w = np.zeros_like(psi)
         ok = [(idx[d] >= 0) & (idx[d] < D[d]) for d in range(3)]
@@ -197,9 +235,15 @@ def cpu_block_sample(ds, k1s, k2s, mx, n_blocks):
         img[dst] = ds.images[v][sub]
         w[dst] = ds.weights[v][sub]
         t0 = time.perf_counter()
-        oracle.block_seq(psi, img, w, k1s[v], k2s[v], LAMBDA, 1e-4, float(mx[v]))
+        oracle.block_seq(psi, img, w, k1s[v], k2s[v], W.lam, 1e-4, float(mx[v]))
         times.append(time.perf_counter() - t0)
     return float(np.mean(times)), oracle.num_threads()
+
+
+def cpu_sample_text(n):
+    dom = "x".join(str(W.block[d] + W.psfs[0][d] - 1) for d in range(3))
+    return (f"{n} view-block(s) of {W.block[0]}x{W.block[1]}x{W.block[2]} (reference boundary, FFT domain about "
+            f"{dom}), extrapolated to the {W.view_blocks_per_iter()} view-blocks of one iteration")
 
 
 def prepare_reference_inputs(ds):
@@ -230,13 +274,13 @@ def run_reference(args, ws, rank):
         per_vb.append(t)
     wall = time.perf_counter() - t0
     t_vb = float(np.mean(per_vb))
-    value = NVOX / (t_vb * VIEW_BLOCKS_PER_ITER)
-    sample = (f"1 view-block (192^3, reference boundary, FFT domain 222x222x252) per step, "
-              f"extrapolated to the {VIEW_BLOCKS_PER_ITER} view-blocks of one 256^3 iteration")
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_vb * VIEW_BLOCKS_PER_ITER,
+    nvb = W.view_blocks_per_iter()
+    value = W.nvox / (t_vb * nvb)
+    sample = cpu_sample_text(1) + " (one view-block per step)"
+    line = {"impl": "reference", "metric": W.metric, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_vb * nvb,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": workload_config("reference (mirror-single / value-1 extension)"),
+            "data": "synthetic", "config": W.config("reference (mirror-single / value-1 extension)"),
             "wall_s": wall,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -258,14 +302,14 @@ def run_gb300(args, ws, rank, local):
     torch.cuda.set_device(local)
     dev = local
     ds = make_data()
-    shape = (DIMS[2], DIMS[1], DIMS[0])
+    shape = (W.dims[2], W.dims[1], W.dims[0])
     boundary = M.BOUNDARY_CIRCULAR if args.boundary == "circular" else M.BOUNDARY_REFERENCE
     d_img = [torch.from_numpy(a).to(f"cuda:{dev}") for a in ds.images]
     d_w = [torch.from_numpy(a).to(f"cuda:{dev}") for a in ds.weights]
-    dec = M.Deconvolution(DIMS, VIEWS, BLOCK, mul=False, psf_type=M.PSF_OPTIMIZATION_I, psf_norm_threads=0,
-                          lam=LAMBDA, boundary=boundary, precision=M.PRECISION_FP32, weight_norm=M.WEIGHTS_HARD,
+    dec = M.Deconvolution(W.dims, W.views, W.block, mul=False, psf_type=M.PSF_OPTIMIZATION_I, psf_norm_threads=0,
+                          lam=W.lam, boundary=boundary, precision=M.PRECISION_FP32, weight_norm=M.WEIGHTS_HARD,
                           batch_blocks=args.batch, device=dev)
-    for v in range(VIEWS):
+    for v in range(W.views):
         dec.set_view_device(v, d_img[v].data_ptr(), d_w[v].data_ptr(), ds.psfs[v])
     dec.prepare()
     stream = torch.cuda.ExternalStream(dec.stream_ptr(), device=f"cuda:{dev}")
@@ -292,7 +336,7 @@ def run_gb300(args, ws, rank, local):
     barrier(ws)
     ms = max_over_ranks(ms, ws)
     clocks = clk.summary()
-    value = ws * NVOX * args.steps / (ms / 1e3)
+    value = ws * W.nvox * args.steps / (ms / 1e3)
 
     # ---- roofline: per-kernel CUDA events on the library stream, same workload ----
     dec.set_profiling(True)
@@ -306,7 +350,8 @@ def run_gb300(args, ws, rank, local):
     dname, (dms, dlaunch, dbytes) = dom
     peak, peak_kind = load_peaks()
     achieved = (dbytes / dlaunch) / (dms / dlaunch / 1e3) / 1e9 if dlaunch else 0.0
-    traffic = ncu_traffic().get(dname)
+    # the committed ncu capture is of the 4-view 256^3 workload
+    traffic = ncu_traffic().get(dname) if W.name == "4view256" else None
     kernels = {k: {"share": v[0] / total_ms, "launches": v[1],
                    "gbs": (v[2] / (v[0] / 1e3) / 1e9) if v[0] > 0 else None} for k, v in prof.items() if v[1]}
     path_bytes = sum(v[2] for v in prof.values())
@@ -327,21 +372,20 @@ def run_gb300(args, ws, rank, local):
         oracle.build()
         k1s, k2s, mx = prepare_reference_inputs(ds)
         t_vb, threads = cpu_block_sample(ds, k1s, k2s, mx, args.cpu_blocks)
-        cpu = {"value": NVOX / (t_vb * VIEW_BLOCKS_PER_ITER), "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_blocks} view-block(s) of 192^3 (reference boundary, FFT domain "
-                         f"222x222x252), extrapolated to the {VIEW_BLOCKS_PER_ITER} view-blocks of one iteration"}
+        cpu = {"value": W.nvox / (t_vb * W.view_blocks_per_iter()), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": cpu_sample_text(args.cpu_blocks)}
     dec.close()
     learned_res = None
     if args.learned and rank == 0:
         import learned
 
-        learned_res = learned.experiment(ds, DIMS, BLOCK, n_objects=args.learned_objects, device=dev,
+        learned_res = learned.experiment(ds, W.dims, W.block, n_objects=args.learned_objects, device=dev,
                                          datasets=pre_datasets)
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        line = {"metric": W.metric, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": dict(workload_config(args.boundary), batch_blocks=batch), "clocks": clocks,
+                "config": dict(W.config(args.boundary), batch_blocks=batch), "clocks": clocks,
                 "gpu_launches": launches, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu}
         if learned_res is not None:
             line["learned"] = learned_res
@@ -359,16 +403,16 @@ def run_e2e(args, ws, dev, ds, dec, shape, boundary):
     h_w = [torch.from_numpy(a).pin_memory() for a in ds.weights]
     h_psi = torch.empty(shape, dtype=torch.float32).pin_memory()
     h_psi.copy_(torch.from_numpy(dec.get_psi()))
-    e2e_dec = M.Deconvolution(DIMS, VIEWS, BLOCK, mul=False, psf_type=M.PSF_OPTIMIZATION_I, psf_norm_threads=0,
-                              lam=LAMBDA, boundary=boundary, precision=M.PRECISION_FP32, weight_norm=M.WEIGHTS_HARD,
+    e2e_dec = M.Deconvolution(W.dims, W.views, W.block, mul=False, psf_type=M.PSF_OPTIMIZATION_I,
+                              psf_norm_threads=0, lam=W.lam, boundary=boundary, precision=M.PRECISION_FP32, weight_norm=M.WEIGHTS_HARD,
                               device=dev)
-    for v in range(VIEWS):
+    for v in range(W.views):
         e2e_dec.set_view(v, h_img[v].numpy(), h_w[v].numpy(), ds.psfs[v])
     e2e_dec.prepare()
     out = h_psi.numpy()
     e2e_steps = max(1, min(args.steps, 10))
     for _ in range(min(2, args.warmup)):
-        for v in range(VIEWS):
+        for v in range(W.views):
             e2e_dec.update_images(v, h_img[v].numpy(), h_w[v].numpy())
         e2e_dec.set_psi(out)
         e2e_dec.run_iterations(1)
@@ -376,15 +420,15 @@ def run_e2e(args, ws, dev, ds, dec, shape, boundary):
     barrier(ws)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        for v in range(VIEWS):
+        for v in range(W.views):
             e2e_dec.update_images(v, h_img[v].numpy(), h_w[v].numpy())
         e2e_dec.set_psi(out)
         e2e_dec.run_iterations(1)
         e2e_dec.get_psi(out)
     e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
-    e2e_value = ws * NVOX * e2e_steps / e2e_s
-    h2d = VIEWS * 2 * NVOX * 4 + NVOX * 4
-    d2h = NVOX * 4
+    e2e_value = ws * W.nvox * e2e_steps / e2e_s
+    h2d = W.views * 2 * W.nvox * 4 + W.nvox * 4
+    d2h = W.nvox * 4
     e2e_dec.close()
     return {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "steps": e2e_steps}
@@ -396,6 +440,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="4view256",
+                    help="4view256: 4 views 256^3 (the headline case); 6view512: 6 views 512x512x256 with "
+                         "per-view PSF sizes and uneven edge blocks")
     ap.add_argument("--boundary", choices=["circular", "reference"], default="circular")
     ap.add_argument("--batch", type=int, default=0,
                     help="blocks per batched launch (1..16); 0 = autotuned")
@@ -406,6 +453,8 @@ def main():
                     help="also run the learned-proposal experiment (training + gated run vs plain)")
     ap.add_argument("--learned-objects", type=int, default=50)
     args = ap.parse_args()
+    global W
+    W = WORKLOADS[args.workload]()
     ws, rank, local = dist_setup(args)
     if args.impl == "reference":
         run_reference(args, ws, rank)

@@ -210,6 +210,19 @@ MVR_API int mvr_decon_batch(const mvr_decon *h);
 MVR_API int mvr_decon_set_graphs(mvr_decon *h, int on);
 /* Number of captured iteration graphs held by the handle. */
 MVR_API int mvr_decon_graphs_captured(const mvr_decon *h);
+
+/* PsiInit (MV/deconvolution/init/): re-initialise psi and the per-view maxima on the
+ * device after mvr_decon_prepare (which runs MVR_PSI_INIT_AVG_PRECISE).
+ *   MVR_PSI_INIT_AVG_PRECISE   PsiInitAvgPrecise.java:52-110
+ *   MVR_PSI_INIT_AVG_APPROX    PsiInitAvgApprox.java:49-106, PsiInitAvgApproxThread.java:57-84
+ *   MVR_PSI_INIT_BLURRED_FUSED PsiInitBlurredFused.java:66-127 (non-zero weighted fusion with
+ *                              the normalised weights, then a Gaussian of `sigma` on every
+ *                              axis, mirror-single extension; the reference default is 5)
+ * avg (or NULL) receives the average intensity (PsiInit.getAvg). */
+#define MVR_PSI_INIT_AVG_PRECISE 0
+#define MVR_PSI_INIT_AVG_APPROX 1
+#define MVR_PSI_INIT_BLURRED_FUSED 2
+MVR_API int mvr_decon_init_psi(mvr_decon *h, int method, double sigma, double *avg);
 /* Data-likelihood residual of the current psi (no reference counterpart; the reference
  * logs only the change statistics): the Poisson negative log-likelihood
  * sum_v sum_x w_v (conv1_v - img_v ln conv1_v) over img_v > 0, each voxel once, reduced

@@ -132,8 +132,19 @@ struct ImgPtrs {
     const float *img[kMaxViews];
 };
 
-// PsiInitAvgPreciseThread.compatibleLoop 127-160, per-CTA partials
-__global__ void k_psi_avg_partials(ImgPtrs ip, int nv, long long n, double *psum, long long *pcnt, float *pmax)
+// Optional fused output of PsiInitBlurredFused: the weighted average over the views with
+// data, FusedNonZeroRandomAccess.get (deconvolution/util/FusedNonZeroRandomAccess.java
+// 63-102): sum(I w) / sum(w) over I > 0, 0 where no weight.
+struct FusePtrs {
+    const float *w[kMaxViews];
+    void *out;  // T volume, or NULL
+};
+
+// PsiInitAvgPreciseThread.compatibleLoop 127-160 (and the statistics of
+// FusedNonZeroRandomAccess, which are the same), per-CTA partials
+template <typename T>
+__global__ void k_psi_avg_partials(ImgPtrs ip, FusePtrs fp, int nv, long long n, double *psum, long long *pcnt,
+                                   float *pmax)
 {
     __shared__ double ss[256];
     __shared__ long long sc[256];
@@ -143,7 +154,7 @@ __global__ void k_psi_avg_partials(ImgPtrs ip, int nv, long long n, double *psum
     float mx[kMaxViews];
     for (int v = 0; v < nv; ++v) mx[v] = 0.0f;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        double sum = 0.0;
+        double sum = 0.0, sumI = 0.0, sumW = 0.0;
         int cnt = 0;
         for (int v = 0; v < nv; ++v) {
             const float x = ip.img[v][i];
@@ -151,8 +162,14 @@ __global__ void k_psi_avg_partials(ImgPtrs ip, int nv, long long n, double *psum
                 mx[v] = fmaxf(mx[v], x);
                 sum += x;
                 ++cnt;
+                if (fp.out) {
+                    const double wv = (double)fp.w[v][i];
+                    sumI += (double)x * wv;
+                    sumW += wv;
+                }
             }
         }
+        if (fp.out) reinterpret_cast<T *>(fp.out)[i] = sumW > 0.0 ? (T)(float)(sumI / sumW) : (T)0;
         if (cnt > 0) {
             s += sum / cnt;
             ++c;
@@ -210,6 +227,59 @@ __global__ void k_fill_avg(T *psi, long long n, const double *avg)
     const T v = (T)(float)(*avg);
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         psi[i] = v;
+}
+
+// One separable pass of Gauss3.gauss (imglib2-algorithm, net.imglib2.algorithm.gauss3,
+// called by PsiInitBlurredFused.java:117): out = sum_k h[|k|] in[mirror-single(i + k)]
+// along `axis`, h the normalised half kernel of length hs.
+template <typename T>
+__global__ void k_gauss_axis(const T *__restrict__ in, T *__restrict__ out, long long D0, long long D1, long long D2,
+                             int axis, const double *__restrict__ h, int hs)
+{
+    const long long n = D0 * D1 * D2;
+    const long long len = axis == 0 ? D0 : (axis == 1 ? D1 : D2);
+    const long long stride = axis == 0 ? 1 : (axis == 1 ? D0 : D0 * D1);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long c = (i / stride) % len;
+        const long long base = i - c * stride;
+        double acc = h[0] * (double)in[i];
+        for (int k = 1; k < hs; ++k)
+            acc += h[k] * ((double)in[base + mirror1(c - k, len) * stride] + (double)in[base + mirror1(c + k, len) * stride]);
+        out[i] = (T)acc;
+    }
+}
+
+// PsiInitAvgApproxThread.call 57-84: min / max / mean of each view's y-z slice at
+// x = D0 / 2 (the reference iterates that same slice once per dimension, which leaves
+// the mean unchanged).  One CTA per view: out[3 v .. 3 v + 2] = {sum, max, count}.
+__global__ void k_slice_stats(ImgPtrs ip, long long D0, long long D1, long long D2, double *out)
+{
+    __shared__ double ss[256];
+    __shared__ float sm[256];
+    const float *img = ip.img[blockIdx.x];
+    const long long x0 = D0 / 2, n = D1 * D2;
+    double s = 0.0;
+    float mx = -3.402823466e38f;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        const float v = img[i * D0 + x0];
+        s += (double)v;
+        mx = fmaxf(mx, v);
+    }
+    ss[threadIdx.x] = s;
+    sm[threadIdx.x] = mx;
+    __syncthreads();
+    for (int h = blockDim.x >> 1; h > 0; h >>= 1) {
+        if (threadIdx.x < h) {
+            ss[threadIdx.x] += ss[threadIdx.x + h];
+            sm[threadIdx.x] = fmaxf(sm[threadIdx.x], sm[threadIdx.x + h]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[3 * blockIdx.x] = ss[0];
+        out[3 * blockIdx.x + 1] = (double)sm[0];
+        out[3 * blockIdx.x + 2] = (double)n;
+    }
 }
 
 template <typename A, typename B>
@@ -345,6 +415,7 @@ public:
     virtual int batch() const = 0;
     virtual int likelihood(double *total, double *per_view) = 0;
     virtual int set_graphs(bool on) = 0;
+    virtual int psi_init(int method, double sigma, double *avg) = 0;
     virtual int graphs_captured() const = 0;
 };
 
@@ -406,6 +477,7 @@ private:
     int psf_init();
     int run_step(int s, double *stats_slot, bool trial, int batch);
     int run_iteration(double *stats_base, size_t stats_stride);
+    int init_psi(int method, double sigma, double *avg_out);
     int autotune();
     // Whole iterations captured as CUDA graphs, one per starting state: the psi buffer
     // (the Jacobi path swaps psi and the staging volume every view-step), the stats
@@ -441,6 +513,7 @@ public:
         return MVR_OK;
     }
     int graphs_captured() const override { return (int)graphs_.size(); }
+    int psi_init(int method, double sigma, double *avg) override;
 
 private:
     int normalize_weights();
@@ -772,27 +845,116 @@ int Decon<T>::prepare()
         jacobi_[st] = (eff >= vw.kd[sd] - 1 && blocks_[st].size() == all.size()) ? 1 : 0;
     }
     // psi init: PsiInitAvgPrecise (average over views with data) and max per view
-    {
-        ImgPtrs ip{};
-        for (int v = 0; v < nv; ++v) ip.img[v] = views_[v].img;
+    D_TRY(init_psi(MVR_PSI_INIT_AVG_PRECISE, 0.0, nullptr));
+    D_CUDA(cudaStreamSynchronize(s));
+    D_TRY(autotune());
+    prepared_ = true;
+    return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::psi_init(int method, double sigma, double *avg)
+{
+    if (!prepared_) return fail(MVR_ERR_STATE, "mvr_decon_prepare was not called");
+    D_CUDA(cudaSetDevice(p_.device));
+    if (weights_dirty_) D_TRY(normalize_weights());
+    return init_psi(method, sigma, avg);
+}
+
+// PsiInit (deconvolution/init/): psi and the per-view maxima used by the update.
+//   AVG_PRECISE    PsiInitAvgPrecise.java:52-110: psi = mean over voxels with data of the
+//                  mean of the views with data; max = per-view maximum
+//   AVG_APPROX     PsiInitAvgApprox.java:49-106 with PsiInitAvgApproxThread.java:57-84:
+//                  psi = mean over views of the mean of the y-z slice at x = D0 / 2; max =
+//                  that slice's maximum
+//   BLURRED_FUSED  PsiInitBlurredFused.java:66-127: psi = the non-zero weighted fusion
+//                  (normalised weights), then Gauss3 with sigma on all axes and mirror-single
+//                  extension; avg / max as AVG_PRECISE
+template <typename T>
+int Decon<T>::init_psi(int method, double sigma, double *avg_out)
+{
+    cudaStream_t s = engine_.stream();
+    const int nv = p_.num_views;
+    ImgPtrs ip{};
+    for (int v = 0; v < nv; ++v) ip.img[v] = views_[v].img;
+    double avg_h = 0.0;
+    if (method == MVR_PSI_INIT_AVG_PRECISE || method == MVR_PSI_INIT_BLURRED_FUSED) {
         const int parts = 1024;
         double *psum = d_scratch_;
         long long *pcnt = reinterpret_cast<long long *>(d_scratch_ + 2 * 4096);
         float *pmax = reinterpret_cast<float *>(pcnt + 4096);
-        k_psi_avg_partials<<<parts, 256, 0, s>>>(ip, nv, n_, psum, pcnt, pmax);
+        FusePtrs fp{};
+        if (method == MVR_PSI_INIT_BLURRED_FUSED) {
+            for (int v = 0; v < nv; ++v) fp.w[v] = views_[v].w;
+            fp.out = psi_;
+        }
+        k_psi_avg_partials<T><<<parts, 256, 0, s>>>(ip, fp, nv, n_, psum, pcnt, pmax);
         D_CUDA(cudaGetLastError());
         double *avg = d_scratch_ + 4096;
         float *mx = reinterpret_cast<float *>(d_scratch_ + 4097);
         k_psi_avg_final<<<1, 1, 0, s>>>(psum, pcnt, pmax, parts, nv, avg, mx);
         D_CUDA(cudaGetLastError());
-        k_fill_avg<T><<<grid_for(n_), 256, 0, s>>>(psi_, n_, avg);
-        D_CUDA(cudaGetLastError());
+        if (method == MVR_PSI_INIT_AVG_PRECISE) {
+            k_fill_avg<T><<<grid_for(n_), 256, 0, s>>>(psi_, n_, avg);
+            D_CUDA(cudaGetLastError());
+        } else {
+            // Gauss3.halfkernel: h[0] = 1, h[x] = exp(-x^2 / (2 sigma^2)) for x < hs =
+            // max(2, (int)(3 sigma + 0.5) + 1), normalised so that h[0] + 2 sum h[x>0] = 1
+            if (!(sigma > 0.0) || sigma > 1000.0) return fail(MVR_ERR_ARG, "sigma must be in (0, 1000]");
+            const int hs = std::max(2, (int)(3.0 * sigma + 0.5) + 1);
+            std::vector<double> h(hs);
+            h[0] = 1.0;
+            double sum = 0.5;
+            for (int x = 1; x < hs; ++x) {
+                h[x] = std::exp(-(double)(x * x) / (2.0 * sigma * sigma));
+                sum += h[x];
+            }
+            sum *= 2.0;
+            for (double &v : h) v /= sum;
+            double *dh = nullptr;
+            D_CUDA(cudaMalloc(&dh, sizeof(double) * hs));
+            int rc = cuda(cudaMemcpyAsync(dh, h.data(), sizeof(double) * hs, cudaMemcpyHostToDevice, s), "gauss kernel");
+            const long long D0 = p_.dims[0], D1 = p_.dims[1], D2 = p_.dims[2];
+            T *a = psi_, *b = stage_;
+            for (int axis = 0; axis < 3 && rc == MVR_OK; ++axis) {
+                k_gauss_axis<T><<<grid_for(n_), 256, 0, s>>>(a, b, D0, D1, D2, axis, dh, hs);
+                rc = cuda(cudaGetLastError(), "k_gauss_axis");
+                std::swap(a, b);
+            }
+            if (rc == MVR_OK) rc = cuda(cudaStreamSynchronize(s), "gauss");
+            cudaFree(dh);
+            D_TRY(rc);
+            psi_ = a;  // the result of the third pass
+            stage_ = b;
+        }
         max_.assign(nv, 0.0f);
         D_CUDA(cudaMemcpyAsync(max_.data(), mx, sizeof(float) * nv, cudaMemcpyDeviceToHost, s));
+        D_CUDA(cudaMemcpyAsync(&avg_h, avg, sizeof(double), cudaMemcpyDeviceToHost, s));
+    } else if (method == MVR_PSI_INIT_AVG_APPROX) {
+        double *st = d_scratch_;
+        k_slice_stats<<<nv, 256, 0, s>>>(ip, p_.dims[0], p_.dims[1], p_.dims[2], st);
+        D_CUDA(cudaGetLastError());
+        std::vector<double> hs(3 * nv);
+        D_CUDA(cudaMemcpyAsync(hs.data(), st, sizeof(double) * 3 * nv, cudaMemcpyDeviceToHost, s));
+        D_CUDA(cudaStreamSynchronize(s));
+        max_.assign(nv, 0.0f);
+        for (int v = 0; v < nv; ++v) {
+            avg_h += hs[3 * v] / hs[3 * v + 2];
+            max_[v] = (float)hs[3 * v + 1];
+        }
+        avg_h /= (double)nv;
+        if (std::isnan(avg_h)) avg_h = 1.0;
+        double *avg = d_scratch_ + 4096;
+        D_CUDA(cudaMemcpyAsync(avg, &avg_h, sizeof(double), cudaMemcpyHostToDevice, s));
+        k_fill_avg<T><<<grid_for(n_), 256, 0, s>>>(psi_, n_, avg);
+        D_CUDA(cudaGetLastError());
+    } else {
+        return fail(MVR_ERR_ARG, "unknown psi initialisation");
     }
     D_CUDA(cudaStreamSynchronize(s));
-    D_TRY(autotune());
-    prepared_ = true;
+    if (avg_out) *avg_out = avg_h;
+    ++inputs_epoch_;  // max_ and possibly the psi buffer changed: captured graphs are stale
+    drop_graphs();
     return MVR_OK;
 }
 
@@ -1325,6 +1487,10 @@ extern "C" const char *mvr_kernel_name(int kind) { return mvr::kernel_kind_name(
 extern "C" int mvr_decon_batch(const mvr_decon *h) { return h ? h->impl->batch() : -1; }
 extern "C" int mvr_decon_set_graphs(mvr_decon *h, int on) { return h ? h->impl->set_graphs(on != 0) : MVR_ERR_ARG; }
 extern "C" int mvr_decon_graphs_captured(const mvr_decon *h) { return h ? h->impl->graphs_captured() : -1; }
+extern "C" int mvr_decon_init_psi(mvr_decon *h, int method, double sigma, double *avg)
+{
+    return h ? h->impl->psi_init(method, sigma, avg) : MVR_ERR_ARG;
+}
 extern "C" int mvr_decon_likelihood(mvr_decon *h, double *total, double *per_view)
 {
     return h ? h->impl->likelihood(total, per_view) : MVR_ERR_ARG;

@@ -142,9 +142,11 @@ def train(pairs, crop=(64, 64, 64), steps=1500, batch=4, lr=1e-3, seed=0, device
 
 
 class GatedProposer:
-    """Likelihood-gated learned proposals on a whole volume."""
+    """Likelihood-gated learned proposals on a whole volume.  Every `every`-th step
+    proposes (the others are plain iterations); the seconds spent in the network and in
+    the gate's likelihood evaluations are accumulated in `timing`."""
 
-    def __init__(self, params, dims, cap=1.0, device=0):
+    def __init__(self, params, dims, cap=1.0, device=0, every=1):
         import torch
 
         self.net = M.UNet(1, dims, seed=0, device=device)
@@ -154,24 +156,44 @@ class GatedProposer:
         self.nxt = torch.empty_like(self.psi)
         self.prop = torch.empty_like(self.psi)
         self.cap = cap
+        self.every = max(1, int(every))
+        self.count = 0
+        self.timing = {"plain_s": 0.0, "network_s": 0.0, "gate_s": 0.0}
 
     def close(self):
         self.net.close()
 
     def step(self, dec):
-        """One gated step on dec; returns (accepted, nll_plain, nll_proposal)."""
+        """One step on dec; returns (accepted, nll_plain, nll_proposal) (NaNs for a plain step)."""
+        import torch
+
+        self.count += 1
+        t0 = time.perf_counter()
+        if self.count % self.every:
+            dec.run_iterations(1)
+            dec.synchronize()
+            self.timing["plain_s"] += time.perf_counter() - t0
+            return False, float("nan"), float("nan")
         dec.get_psi_device(self.psi.data_ptr())
         dec.run_iterations(1)
         dec.get_psi_device(self.nxt.data_ptr())
+        t1 = time.perf_counter()
         self.net.set_input(self.psi.data_ptr(), self.nxt.data_ptr())
         self.net.propose(self.psi.data_ptr(), self.prop.data_ptr(), self.cap)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
         l_plain = dec.likelihood()[0]
         dec.set_psi_device(self.prop.data_ptr())
         l_prop = dec.likelihood()[0]
-        if l_prop < l_plain:
-            return True, l_plain, l_prop
-        dec.set_psi_device(self.nxt.data_ptr())
-        return False, l_plain, l_prop
+        accepted = l_prop < l_plain
+        if not accepted:
+            dec.set_psi_device(self.nxt.data_ptr())
+        dec.synchronize()
+        t3 = time.perf_counter()
+        self.timing["plain_s"] += t1 - t0
+        self.timing["network_s"] += t2 - t1
+        self.timing["gate_s"] += t3 - t2
+        return accepted, l_plain, l_prop
 
 
 def convergence(dec, n_steps, ref=None, proposer=None):
@@ -214,7 +236,7 @@ def first_time(hist, pred):
 
 def experiment(ds, dims, block, n_objects=50, train_dims=(128, 128, 128), crop=(64, 64, 64), iters=45, m=5,
                pairs_per_object=40, train_steps=1500, batch=4, lr=1e-3, eval_iters=20, tol=1e-3, device=0,
-               datasets=None):
+               datasets=None, everies=(1, 3)):
     """Learned + gated vs plain GPU RL on ds: wall time to relative L2 <= tol against the
     FP64 plain result after eval_iters iterations, and to that result's likelihood."""
     import torch
@@ -241,24 +263,30 @@ def experiment(ds, dims, block, n_objects=50, train_dims=(128, 128, 128), crop=(
     plain = make_decon(ds, dims, block, device)
     h_plain = convergence(plain, eval_iters, ref)
     plain.close()
-    gated = make_decon(ds, dims, block, device)
-    prop = GatedProposer(params, dims, device=device)
-    h_gated = convergence(gated, eval_iters, ref, prop)
-    prop.close()
-    gated.close()
+    runs = {}
+    for every in everies:
+        gated = make_decon(ds, dims, block, device)
+        prop = GatedProposer(params, dims, device=device, every=every)
+        h = convergence(gated, eval_iters + 10, ref, prop)
+        runs[every] = (h, dict(prop.timing))
+        prop.close()
+        gated.close()
 
     def summary(h):
         return {"t_err": first_time(h, lambda e, n: e <= tol), "t_nll": first_time(h, lambda e, n: n <= nll_ref),
                 "final_err": h[-1][1], "final_nll": h[-1][2], "seconds": h[-1][0],
                 "accepted": int(sum(1 for x in h if x[3]))}
 
-    sp, sg = summary(h_plain), summary(h_gated)
-    speed = None
-    if sp["t_err"] and sg["t_err"]:
-        speed = sp["t_err"] / sg["t_err"]
-    return {"pairs": n_objects * pairs_per_object, "objects": n_objects, "m": m, "train_steps": train_steps,
-            "train_loss_first": float(np.mean(losses[:20])), "train_loss_last": float(np.mean(losses[-20:])),
-            "no_change_loss": base, "gen_s": gen_s, "train_s": train_s, "eval_iters": eval_iters, "tol": tol,
-            "nll_fp64_ref": nll_ref, "plain": sp, "learned": sg, "speedup_to_tol": speed,
-            "trace_plain": [(round(t, 5), e, n) for t, e, n, _ in h_plain],
-            "trace_learned": [(round(t, 5), e, n, a) for t, e, n, a in h_gated]}
+    sp = summary(h_plain)
+    out = {"pairs": n_objects * pairs_per_object, "objects": n_objects, "m": m, "train_steps": train_steps,
+           "train_loss_first": float(np.mean(losses[:20])), "train_loss_last": float(np.mean(losses[-20:])),
+           "no_change_loss": base, "gen_s": gen_s, "train_s": train_s, "eval_iters": eval_iters, "tol": tol,
+           "nll_fp64_ref": nll_ref, "plain": sp, "trace_plain": [(round(t, 5), e, n) for t, e, n, _ in h_plain]}
+    for every, (h, timing) in runs.items():
+        sg = summary(h)
+        sg["timing"] = timing
+        sg["speedup_to_tol"] = sp["t_err"] / sg["t_err"] if sp["t_err"] and sg["t_err"] else None
+        sg["speedup_to_nll"] = sp["t_nll"] / sg["t_nll"] if sp["t_nll"] and sg["t_nll"] else None
+        sg["trace"] = [(round(t, 5), e, n, a) for t, e, n, a in h]
+        out[f"learned_every{every}"] = sg
+    return out

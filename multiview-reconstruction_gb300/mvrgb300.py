@@ -33,6 +33,7 @@ WEIGHTS_AS_GIVEN, WEIGHTS_HARD, WEIGHTS_SMOOTH = 0, 1, 2
 KERNEL_KINDS = 11
 BOUNDARY_REFERENCE, BOUNDARY_CIRCULAR = 0, 1
 PSF_OPTIMIZATION_II, PSF_OPTIMIZATION_I, PSF_EFFICIENT_BAYESIAN, PSF_INDEPENDENT = 0, 1, 2, 3
+PSI_INIT_AVG_PRECISE, PSI_INIT_AVG_APPROX, PSI_INIT_BLURRED_FUSED = 0, 1, 2
 
 # every symbol include/mvr_gb300.h declares
 EXPORTS = [
@@ -44,7 +45,7 @@ EXPORTS = [
     "mvr_decon_get_max", "mvr_decon_get_weights", "mvr_decon_psi_device", "mvr_decon_synchronize",
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
     "mvr_kernel_name", "mvr_convolve_static", "mvr_decon_batch", "mvr_decon_likelihood",
-    "mvr_decon_set_graphs", "mvr_decon_graphs_captured",
+    "mvr_decon_set_graphs", "mvr_decon_graphs_captured", "mvr_decon_init_psi",
     "mvr_unet_create", "mvr_unet_destroy", "mvr_unet_last_error", "mvr_unet_num_params", "mvr_unet_get_params",
     "mvr_unet_set_params", "mvr_unet_get_grads", "mvr_unet_set_input", "mvr_unet_forward", "mvr_unet_train_step",
     "mvr_unet_propose", "mvr_conv3d_tc", "mvr_conv3d_tc_wgrad", "mvr_conv3d_tc_last_error",
@@ -142,6 +143,7 @@ def load() -> C.CDLL:
     L.mvr_convolve_static.argtypes = [P, P, P, P, P, P, C.c_char_p, C.c_int]
     L.mvr_decon_batch.argtypes = [P]
     L.mvr_decon_set_graphs.argtypes = [P, C.c_int]
+    L.mvr_decon_init_psi.argtypes = [P, C.c_int, C.c_double, P]
     L.mvr_decon_graphs_captured.argtypes = [P]
     L.mvr_decon_likelihood.argtypes = [P, P, P]
     L.mvr_unet_create.argtypes = [C.c_int, P, C.c_uint, C.c_int, C.POINTER(P)]
@@ -390,6 +392,13 @@ class Deconvolution:
     def batch(self) -> int:
         """Blocks per batched launch in use."""
         return int(self._lib.mvr_decon_batch(self._h))
+
+    def init_psi(self, method=PSI_INIT_BLURRED_FUSED, sigma: float = 5.0) -> float:
+        """PsiInit on the device (PsiInitAvgPrecise / PsiInitAvgApprox / PsiInitBlurredFused);
+        returns the average intensity (PsiInit.getAvg)."""
+        avg = np.zeros(1, np.float64)
+        self._check(self._lib.mvr_decon_init_psi(self._h, int(method), float(sigma), _p(avg)))
+        return float(avg[0])
 
     def set_graphs(self, on: bool):
         """Whole iterations as CUDA graphs (default on); off launches eagerly."""

@@ -148,9 +148,11 @@ class MultiviewData:
 
 def make_dataset(dims_xyz, angles, psf_size_xyz, n_beads=200, seed=1001, sigma_xy=1.5, sigma_z=4.5,
                  side_lobes=False, weights="ones", background=10.0, bead_sigma=(1.0, 2.0)):
+    """psf_size_xyz: one size for every view, or a list with one size per view."""
     rng = np.random.Generator(np.random.PCG64(seed))
     obj = make_object(dims_xyz, n_beads, rng, sigma=bead_sigma)
-    psfs = [make_psf(psf_size_xyz, sigma_xy, sigma_z, a, side_lobes) for a in angles]
+    sizes = psf_size_xyz if isinstance(psf_size_xyz[0], (tuple, list)) else [psf_size_xyz] * len(angles)
+    psfs = [make_psf(sz, sigma_xy, sigma_z, a, side_lobes) for sz, a in zip(sizes, angles)]
     imgs, ws = [], []
     for a, p in zip(angles, psfs):
         b = blur(obj, p) + background
@@ -172,4 +174,15 @@ def config_256(seed=1002):
     """4 views, 256^3, 31x31x61 Gaussian-plus-side-lobe PSFs at 0/45/90/135 degrees,
     cosine-blended weights (raw; normalise with the reference's hard rule)."""
     return make_dataset((256, 256, 256), (0.0, 45.0, 90.0, 135.0), (31, 31, 61), n_beads=200,
+                        seed=seed, side_lobes=True, weights="cosine")
+
+
+# per-view PSF sizes of the 6-view workload: 21 ... 41 voxels in x/y, 41 ... 81 in z
+PSF_SIZES_6 = [(21, 21, 41), (25, 25, 49), (29, 29, 57), (33, 33, 65), (37, 37, 73), (41, 41, 81)]
+
+
+def config_512(seed=1003):
+    """6 views, 512 x 512 x 256, Gaussian-plus-side-lobe PSFs of different sizes per view
+    (21-41 voxels in x/y, 41-81 in z) at 0/30/.../150 degrees, cosine-blended weights."""
+    return make_dataset((512, 512, 256), (0.0, 30.0, 60.0, 90.0, 120.0, 150.0), PSF_SIZES_6, n_beads=800,
                         seed=seed, side_lobes=True, weights="cosine")

@@ -208,6 +208,84 @@ def psi_init_avg(imgs):
     return psi, mx, avg
 
 
+def gauss3_half_kernel(sigma: float) -> np.ndarray:
+    """Gauss3.halfkernel of imglib2-algorithm (net.imglib2.algorithm.gauss3, the version
+    pom-scijava 43.0.0 manages; not vendored in the reference): size max(2, (int)(3 sigma +
+    0.5) + 1), h[0] = 1, h[x] = exp(-x^2 / (2 sigma^2)), normalised so that
+    h[0] + 2 sum_{x>0} h[x] = 1."""
+    hs = max(2, int(3.0 * sigma + 0.5) + 1)
+    x = np.arange(hs, dtype=np.float64)
+    h = np.exp(-(x * x) / (2.0 * sigma * sigma))
+    h[0] = 1.0
+    return h / (2.0 * (0.5 + h[1:].sum()))
+
+
+def gauss3(vol: np.ndarray, sigma: float) -> np.ndarray:
+    """Gauss3.gauss(sigma on every axis, Views.extendMirrorSingle(vol), vol): separable
+    symmetric convolution along x, then y, then z, mirror-single extension, float64."""
+    h = gauss3_half_kernel(sigma)
+    hs = len(h)
+    full = np.concatenate([h[:0:-1], h])
+    out = np.asarray(vol, dtype=np.float64)
+    for axis in (2, 1, 0):  # x, y, z of a [z][y][x] array
+        n = out.shape[axis]
+        idx = np.arange(-(hs - 1), n + hs - 1)
+        if n > 1:
+            p = 2 * n - 2
+            idx = np.mod(idx, p)
+            idx = np.where(idx >= n, p - idx, idx)
+        else:
+            idx = np.zeros_like(idx)
+        ext = np.take(out, idx, axis=axis)
+        acc = np.zeros_like(out)
+        for k in range(2 * hs - 1):
+            sl = [slice(None)] * 3
+            sl[axis] = slice(k, k + n)
+            acc += full[k] * ext[tuple(sl)]
+        out = acc
+    return out
+
+
+def psi_init_blurred_fused(imgs, weights, sigma: float = 5.0):
+    """PsiInitBlurredFused.runInitialization (deconvolution/init/PsiInitBlurredFused.java
+    66-127) with FusedNonZeroRandomAccess.get (deconvolution/util/
+    FusedNonZeroRandomAccess.java 63-102): psi = sum(I w) / sum(w) over the views with
+    I > 0 (0 where the weights sum to 0), then Gauss3 with sigma; avg = the mean over voxels
+    with data of the mean of those views; max = per-view maximum.  Returns (psi float32,
+    max float32[views], avg)."""
+    I = np.stack([np.asarray(a, dtype=np.float64) for a in imgs])
+    Wt = np.stack([np.asarray(a, dtype=np.float64) for a in weights])
+    pos = I > 0
+    sumI = np.where(pos, I * Wt, 0.0).sum(0)
+    sumW = np.where(pos, Wt, 0.0).sum(0)
+    fused = np.where(sumW > 0, sumI / np.where(sumW > 0, sumW, 1.0), 0.0).astype(np.float32)
+    cnt = pos.sum(0)
+    tot = np.where(pos, I, 0.0).sum(0)
+    has = cnt > 0
+    avg = float((tot[has] / cnt[has]).sum() / has.sum()) if has.any() else float("nan")
+    if np.isnan(avg):
+        avg = 1.0
+    mx = np.array([np.where(pos[v], I[v], 0.0).max() for v in range(len(imgs))], dtype=np.float32)
+    return gauss3(fused, sigma).astype(np.float32), mx, avg
+
+
+def psi_init_avg_approx(imgs):
+    """PsiInitAvgApprox.runInitialization (deconvolution/init/PsiInitAvgApprox.java
+    49-106) with PsiInitAvgApproxThread.call (57-84): per view the mean and maximum of the
+    y-z slice at x = nx / 2; avg = mean of the views' slice means, psi = avg.  Returns
+    (psi, max, avg)."""
+    means, mx = [], []
+    for a in imgs:
+        sl = np.asarray(a, dtype=np.float64)[:, :, a.shape[2] // 2]
+        means.append(sl.mean())
+        mx.append(sl.max())
+    avg = float(np.mean(means))
+    if np.isnan(avg):
+        avg = 1.0
+    psi = np.full(imgs[0].shape, np.float32(avg), dtype=np.float32)
+    return psi, np.array(mx, dtype=np.float32), avg
+
+
 def decon_run(psi, imgs, ws, k1s, k2s, block_size, iters, mul=False, lam=0.0, min_value=1e-4,
               max_intensities=None, filter_blocks=True, fp64=False):
     """MultiViewDeconvolution{Seq,Mul}.runIterations with the reference's block order.

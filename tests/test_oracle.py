@@ -207,3 +207,53 @@ def test_seq_equals_mul_for_one_view():
     m, sm = O.block_mul(b["psi"], [b["img0"]], [b["w0"]], [b["k1_0"]], [b["k2_0"]], 0.0, 1e-4, [b["max"][0]])
     assert np.array_equal(a, m)
     assert np.allclose(sa, sm)
+
+
+def test_gauss3_kernel_and_known_answers():
+    # Gauss3 half kernel: size max(2, (int)(3 sigma + 0.5) + 1), normalised to sum 1
+    for sigma in (0.5, 1.0, 2.0, 5.0):
+        h = O.gauss3_half_kernel(sigma)
+        assert len(h) == max(2, int(3 * sigma + 0.5) + 1)
+        assert abs(h[0] + 2 * h[1:].sum() - 1.0) < 1e-14
+    # a constant volume is a fixed point, an interior delta gives the separable kernel
+    assert np.abs(O.gauss3(np.full((7, 9, 11), 4.0), 1.5) - 4.0).max() < 1e-12
+    v = np.zeros((31, 31, 31))
+    v[15, 15, 15] = 1.0
+    h = O.gauss3_half_kernel(2.0)
+    full = np.concatenate([h[:0:-1], h])
+    g = O.gauss3(v, 2.0)
+    c = len(h) - 1
+    assert np.allclose(g[15, 15, 15 - c:15 + c + 1], full * full[c] * full[c], atol=1e-15)
+    # mirror-single at the border (period 2n - 2, the edge voxel not repeated): a delta at
+    # x = 1 is seen twice from x = 0 (offsets -1 and +1) and at x = 1 also through x = -1 -> 1;
+    # a delta at x = 0 is seen once from x = 1
+    h = O.gauss3_half_kernel(1.0)
+    v = np.zeros((1, 1, 12))
+    v[0, 0, 1] = 1.0
+    g = O.gauss3(v, 1.0)
+    assert abs(g[0, 0, 0] - 2 * h[1]) < 1e-15 and abs(g[0, 0, 1] - (h[0] + h[2])) < 1e-15
+    v = np.zeros((1, 1, 12))
+    v[0, 0, 0] = 1.0
+    g = O.gauss3(v, 1.0)
+    assert abs(g[0, 0, 1] - h[1]) < 1e-15 and abs(g[0, 0, 0] - h[0]) < 1e-15
+
+
+def test_psi_init_known_answers():
+    rng = np.random.default_rng(3)
+    shape = (8, 10, 12)
+    a = rng.uniform(1, 5, shape).astype(np.float32)
+    # one view with weight 1: the fusion is the image itself, blurred
+    psi, mx, avg = O.psi_init_blurred_fused([a], [np.ones(shape, np.float32)], 1.0)
+    assert np.allclose(psi, O.gauss3(a, 1.0), rtol=1e-6)
+    assert mx[0] == a.max() and abs(avg - a.astype(np.float64).mean()) < 1e-9
+    # views without data (0) do not count; zero weight everywhere gives 0
+    z = np.zeros(shape, np.float32)
+    psi, mx, avg = O.psi_init_blurred_fused([a, z], [np.ones(shape, np.float32)] * 2, 1.0)
+    assert mx[1] == 0.0 and abs(avg - a.astype(np.float64).mean()) < 1e-9
+    psi, _, _ = O.psi_init_blurred_fused([a], [z], 1.0)
+    assert np.all(psi == 0.0)
+    # approximate average: the y-z slice at x = nx / 2
+    psi, mx, avg = O.psi_init_avg_approx([a, 2 * a])
+    sl = a[:, :, 6].astype(np.float64)
+    assert abs(avg - 1.5 * sl.mean()) < 1e-9 and mx[1] == np.float32(2 * sl.max())
+    assert np.all(psi == np.float32(avg))
