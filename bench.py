@@ -77,6 +77,14 @@ def _make512():
     return synthetic.config_512()
 
 
+def _make_large():
+    import torch
+
+    import synthetic
+
+    return synthetic.config_large(torch.cuda.current_device() if torch.cuda.is_available() else "cpu")
+
+
 def _psf_sizes_6():
     import synthetic
 
@@ -90,6 +98,10 @@ WORKLOADS = {
                                  "6 views 512x512x256 float32, PSFs 21x21x41 ... 41x41x81 per view, "
                                  "Optimization-I, compute blocks 192x192x256 (effective 112-152 x 112-152 x 96-176, "
                                  "uneven edge blocks), Seq"),
+    "8view1024": lambda: Workload("8view1024", (1024, 1024, 512), 8, (256, 256, 256), [(41, 41, 81)] * 8, 0.006,
+                                  _make_large,
+                                  "8 views 1024x1024x512 (uint16 recorded, converted to float32), 20000 nuclei-like "
+                                  "blobs, PSF 41x41x81 at 45 degree steps, compute blocks 256^3 (216 per view), Seq"),
 }
 W = None  # the workload of this run (set in main)
 
@@ -232,8 +244,12 @@ def cpu_block_sample(ds, k1s, k2s, mx, n_blocks):
         ok = [(idx[d] >= 0) & (idx[d] < D[d]) for d in range(3)]
         sub = np.ix_(idx[2][ok[2]], idx[1][ok[1]], idx[0][ok[0]])
         dst = np.ix_(np.nonzero(ok[2])[0], np.nonzero(ok[1])[0], np.nonzero(ok[0])[0])
-        img[dst] = ds.images[v][sub]
-        w[dst] = ds.weights[v][sub]
+        img[dst] = _region(ds.images[v], sub)
+        if isinstance(ds.weights[v], np.ndarray):
+            w[dst] = ds.weights[v][sub]
+        else:  # raw device weights: normalise this region with the hard rule
+            raw = [_region(ds.weights[u], sub) for u in range(W.views)]
+            w[dst] = oracle.normalize_weights(raw)[v]
         t0 = time.perf_counter()
         oracle.block_seq(psi, img, w, k1s[v], k2s[v], W.lam, 1e-4, float(mx[v]))
         times.append(time.perf_counter() - t0)
@@ -246,14 +262,28 @@ def cpu_sample_text(n):
             f"{dom}), extrapolated to the {W.view_blocks_per_iter()} view-blocks of one iteration")
 
 
-def prepare_reference_inputs(ds):
+def prepare_reference_inputs(ds, mx=None):
+    """Kernels, normalised weights and per-view maxima for the CPU sample.  For device
+    volumes (the large workload) the weights are normalised per sampled block (the hard
+    rule is per voxel) and the maxima come from the GPU run (mx)."""
     import oracle
 
     k1s, k2s = oracle.psf_init(ds.psfs, oracle.PSF_OPTIMIZATION_I, 0)
-    ws = oracle.normalize_weights(ds.weights)
-    _, mx, _ = oracle.psi_init_avg(ds.images)
-    ds.weights = ws
+    if mx is None:
+        ws = oracle.normalize_weights(ds.weights)
+        _, mx, _ = oracle.psi_init_avg(ds.images)
+        ds.weights = ws
     return k1s, k2s, mx
+
+
+def _region(vol, sub, normalise_with=None):
+    """vol[sub] as a host array (vol a host array or a device tensor)."""
+    if isinstance(vol, np.ndarray):
+        return vol[sub]
+    import torch
+
+    idx = [torch.as_tensor(np.asarray(i).reshape(-1), device=vol.device) for i in sub]
+    return vol.index_select(0, idx[0]).index_select(1, idx[1]).index_select(2, idx[2]).cpu().numpy()
 
 
 def run_reference(args, ws, rank):
@@ -304,14 +334,16 @@ def run_gb300(args, ws, rank, local):
     ds = make_data()
     shape = (W.dims[2], W.dims[1], W.dims[0])
     boundary = M.BOUNDARY_CIRCULAR if args.boundary == "circular" else M.BOUNDARY_REFERENCE
-    d_img = [torch.from_numpy(a).to(f"cuda:{dev}") for a in ds.images]
-    d_w = [torch.from_numpy(a).to(f"cuda:{dev}") for a in ds.weights]
+    on_dev = torch.is_tensor(ds.images[0])  # synthesised on the device (large workload)
+    d_img = ds.images if on_dev else [torch.from_numpy(a).to(f"cuda:{dev}") for a in ds.images]
+    d_w = ds.weights if on_dev else [torch.from_numpy(a).to(f"cuda:{dev}") for a in ds.weights]
     dec = M.Deconvolution(W.dims, W.views, W.block, mul=False, psf_type=M.PSF_OPTIMIZATION_I, psf_norm_threads=0,
                           lam=W.lam, boundary=boundary, precision=M.PRECISION_FP32, weight_norm=M.WEIGHTS_HARD,
                           batch_blocks=args.batch, device=dev)
     for v in range(W.views):
         dec.set_view_device(v, d_img[v].data_ptr(), d_w[v].data_ptr(), ds.psfs[v])
     dec.prepare()
+    dec_max = dec.max_intensities()
     stream = torch.cuda.ExternalStream(dec.stream_ptr(), device=f"cuda:{dev}")
     batch = dec.batch()
     for _ in range(args.warmup):
@@ -361,8 +393,8 @@ def run_gb300(args, ws, rank, local):
                 "path_achieved": path_bytes / (total_ms / 1e3) / 1e9, "kernels": kernels}
 
     # ---- e2e: public C ABI with pinned host buffers, copies inside the timed region ----
-    if args.no_e2e:
-        e2e = None
+    if args.no_e2e or on_dev:
+        e2e = None  # the large workload keeps its volumes on the device only
     else:
         e2e = run_e2e(args, ws, dev, ds, dec, shape, boundary)
     cpu = None
@@ -370,7 +402,7 @@ def run_gb300(args, ws, rank, local):
         import oracle
 
         oracle.build()
-        k1s, k2s, mx = prepare_reference_inputs(ds)
+        k1s, k2s, mx = prepare_reference_inputs(ds, dec_max if on_dev else None)
         t_vb, threads = cpu_block_sample(ds, k1s, k2s, mx, args.cpu_blocks)
         cpu = {"value": W.nvox / (t_vb * W.view_blocks_per_iter()), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": cpu_sample_text(args.cpu_blocks)}
@@ -442,7 +474,8 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="4view256",
                     help="4view256: 4 views 256^3 (the headline case); 6view512: 6 views 512x512x256 with "
-                         "per-view PSF sizes and uneven edge blocks")
+                         "per-view PSF sizes and uneven edge blocks; 8view1024: 8 views 1024x1024x512, 256^3 "
+                         "blocks (volumes synthesised on the device, no e2e line)")
     ap.add_argument("--boundary", choices=["circular", "reference"], default="circular")
     ap.add_argument("--batch", type=int, default=0,
                     help="blocks per batched launch (1..16); 0 = autotuned")

@@ -186,3 +186,81 @@ def config_512(seed=1003):
     (21-41 voxels in x/y, 41-81 in z) at 0/30/.../150 degrees, cosine-blended weights."""
     return make_dataset((512, 512, 256), (0.0, 30.0, 60.0, 90.0, 120.0, 150.0), PSF_SIZES_6, n_beads=800,
                         seed=seed, side_lobes=True, weights="cosine")
+
+
+def config_large(device=0, seed=1005, dims_xyz=(1024, 1024, 512), n_views=8, n_objects=20000,
+                 psf_size_xyz=(41, 41, 81)):
+    """The large-volume stress case: 8 views of 1024 x 1024 x 512 recorded as uint16 and
+    converted to float32, dense nuclei-like blobs (sigma U[3, 6], amplitude U[100, 1000]),
+    Gaussian-plus-side-lobe PSFs 41 x 41 x 81 rotated in 45 degree steps, background 10,
+    Poisson noise, cosine-blended weights.  Synthesised on the GPU with torch (at this size
+    the host generator above would take minutes per view); returns images and weights as
+    device tensors [z][y][x] and the PSFs as host arrays."""
+    import torch
+
+    dev = device if isinstance(device, str) else f"cuda:{device}"
+    nx, ny, nz = dims_xyz
+    rng = np.random.Generator(np.random.PCG64(seed))
+    cx, cy, cz = rng.uniform(0, nx, n_objects), rng.uniform(0, ny, n_objects), rng.uniform(0, nz, n_objects)
+    sg = rng.uniform(3.0, 6.0, n_objects)
+    amp = rng.uniform(100, 1000, n_objects)
+    # blobs in four sigma classes: amplitudes scattered at their centres, blurred by the
+    # class's Gaussian in Fourier space (periodic; the objects keep 3 sigma from the border)
+    fz = torch.fft.fftfreq(nz, device=dev).view(-1, 1, 1)
+    fy = torch.fft.fftfreq(ny, device=dev).view(1, -1, 1)
+    fx = torch.fft.rfftfreq(nx, device=dev).view(1, 1, -1)
+    f2 = fz * fz + fy * fy + fx * fx
+    obj = torch.zeros((nz, ny, nx), dtype=torch.float32, device=dev)
+    edges = np.linspace(3.0, 6.0, 5)
+    for c in range(4):
+        sel = (sg >= edges[c]) & (sg <= edges[c + 1] if c == 3 else sg < edges[c + 1])
+        s = float(0.5 * (edges[c] + edges[c + 1]))
+        m = 3 * s
+        ix = np.clip(cx[sel], m, nx - 1 - m).astype(np.int64)
+        iy = np.clip(cy[sel], m, ny - 1 - m).astype(np.int64)
+        iz = np.clip(cz[sel], m, nz - 1 - m).astype(np.int64)
+        # peak amplitude a: a Gaussian of volume a (2 pi s^2)^(3/2)
+        a = torch.from_numpy(amp[sel] * (2 * math.pi * s * s) ** 1.5).to(dev, torch.float32)
+        spikes = torch.zeros_like(obj)
+        flat = torch.from_numpy((iz * ny + iy) * nx + ix).to(dev)
+        spikes.view(-1).index_add_(0, flat, a)
+        spec = torch.fft.rfftn(spikes) * torch.exp(-2 * math.pi ** 2 * s * s * f2)
+        obj += torch.fft.irfftn(spec, s=(nz, ny, nx))
+        del spikes, spec
+    obj.clamp_(min=0)
+    angles = [45.0 * v for v in range(n_views)]
+    psfs = [make_psf(psf_size_xyz, 1.5, 4.5, a, side_lobes=True) for a in angles]
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    imgs, ws = [], []
+    pad = [obj.shape[d] + psfs[0].shape[d] - 1 for d in range(3)]
+    ospec = torch.fft.rfftn(obj, s=pad)
+    for a, p in zip(angles, psfs):
+        pk = torch.from_numpy(p.astype(np.float32)).to(dev)
+        b = torch.fft.irfftn(ospec * torch.fft.rfftn(pk, s=pad), s=pad)
+        c = [p.shape[d] // 2 for d in range(3)]
+        b = b[c[0]:c[0] + nz, c[1]:c[1] + ny, c[2]:c[2] + nx] + 10.0
+        counts = torch.poisson(b.clamp(min=0), generator=gen).clamp_(1, 65535).to(torch.int32)
+        del b
+        img_u16 = counts.to(torch.int16)  # the recorded uint16 values (bit pattern)
+        del counts
+        imgs.append((img_u16.to(torch.int32) & 0xFFFF).to(torch.float32))  # uint16 -> float32
+        del img_u16
+        ws.append(_cosine_weight_torch(dims_xyz, a, dev))
+    del ospec, obj
+    return MultiviewData(images=imgs, weights=ws, psfs=psfs, obj=None)
+
+
+def _cosine_weight_torch(dims_xyz, angle_deg, dev, blend=12.0):
+    """cosine_weight on the GPU (the weight depends on x and z only)."""
+    import torch
+
+    nx, ny, nz = dims_xyz
+    a = math.radians(angle_deg)
+    x = torch.arange(nx, device=dev, dtype=torch.float64).view(1, -1)
+    z = torch.arange(nz, device=dev, dtype=torch.float64).view(-1, 1)
+    u = (x - (nx - 1) / 2) * math.cos(a) + (z - (nz - 1) / 2) * math.sin(a)
+    half = 0.5 * (abs(nx * math.cos(a)) + abs(nz * math.sin(a)))
+    d = half - u.abs()
+    w = torch.where(d >= blend, torch.ones_like(d), 0.5 * (1 - torch.cos(math.pi * d.clamp(0, blend) / blend)))
+    return w.to(torch.float32).view(nz, 1, nx).expand(nz, ny, nx).contiguous()
