@@ -556,30 +556,23 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
     if constexpr (sizeof(T) == sizeof(float)) {
         if (tc) {
             // Hx = 16 q + 1: q full tiles, and the last column in gathered tiles of 16
-            // other-axis indices (a second, small launch)
-            const bool gather = Hx > 1 && Hx % kTColNP == 1;
+            // other-axis indices (an extra x tile of the same grid)
+            const int gather = (Hx > 1 && Hx % kTColNP == 1) ? 1 : 0;
             const int hmain = gather ? Hx - 1 : Hx;
             const size_t ts = tcols_smem(tc, mode);
-            for (int part = 0; part < (gather ? 2 : 1); ++part) {
-                const dim3 tgrid(part == 0 ? (unsigned)((hmain + kTColNP - 1) / kTColNP) : 1u,
-                                 part == 0 ? (unsigned)nother : (unsigned)((nother + kTColNP - 1) / kTColNP),
-                                 (unsigned)nb);
-                const long long ps = part == 0 ? 1 : ostride;
-                const int hx = part == 0 ? hmain : Hx;
-                TILE_COLS(tc, {
-                    if (mode == 0)
-                        k_tcols<V_, 0><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, hx, estride, ostride, Pc, tw,
-                                                                          ps, nother);
-                    else if (mode == 1)
-                        k_tcols<V_, 1><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, hx, estride, ostride, Pc, tw,
-                                                                          ps, nother);
-                    else
-                        k_tcols<V_, 2><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, hx, estride, ostride, Pc, tw,
-                                                                          ps, nother);
-                });
-                MVR_LAUNCHED("k_tcols");
-                if (part == 1) ++launches_;
-            }
+            const dim3 tgrid((unsigned)((hmain + kTColNP - 1) / kTColNP + gather), (unsigned)nother, (unsigned)nb);
+            TILE_COLS(tc, {
+                if (mode == 0)
+                    k_tcols<V_, 0><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw, gather,
+                                                                      nother);
+                else if (mode == 1)
+                    k_tcols<V_, 1><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw, gather,
+                                                                      nother);
+                else
+                    k_tcols<V_, 2><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw, gather,
+                                                                      nother);
+            });
+            MVR_LAUNCHED("k_tcols");
             return prof_end();
         }
         if (wc) {

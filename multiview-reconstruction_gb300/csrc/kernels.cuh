@@ -575,25 +575,67 @@ __device__ __forceinline__ void update_row(const typename Cx<T>::t *zz, int m, c
     }
 }
 
+// Sum of two float-pair values (hi + lo) without losing the low part (Knuth's TwoSum on
+// the high parts, the low parts and the rounding error added, then renormalised).  The
+// pair carries about 48 significant bits, which is what the CTA reduction needs: the
+// GPU's double rate is so low that a few double additions per thread at the end of every
+// CTA cost a large part of the kernel.
+__device__ __forceinline__ void pair_add(float &hi, float &lo, float bhi, float blo)
+{
+    const float s = hi + bhi;
+    const float v = s - hi;
+    float e = (hi - (s - v)) + (bhi - v);
+    e += lo + blo;
+    hi = s + e;
+    lo = e - (hi - s);
+}
+
 // Deterministic CTA reduction of the per-thread statistics into ua.partials[slot]
-// (sum in double from the compensated float sums, max).  Every thread must call it.
+// (sum from the compensated per-thread sums as float pairs, converted to double once per
+// CTA; max).  Every thread must call it.
 template <typename T>
 __device__ __forceinline__ void stats_to_partials(T ksum, T kcomp, T kmax, double *red_s, double *red_m,
                                                   double *partials, long long slot)
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    double lsum = (double)ksum - (double)kcomp, lmax = (double)kmax;
-    for (int o = 16; o > 0; o >>= 1) {
-        lsum += __shfl_down_sync(0xffffffffu, lsum, o);
-        lmax = fmax(lmax, __shfl_down_sync(0xffffffffu, lmax, o));
-    }
-    if (lane == 0) { red_s[warp] = lsum; red_m[warp] = lmax; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0, mx = -1.0;
-        for (int w = 0; w < nw; ++w) { s += red_s[w]; mx = fmax(mx, red_m[w]); }
-        partials[2 * slot] = s;
-        partials[2 * slot + 1] = mx;
+    if constexpr (sizeof(T) == sizeof(float)) {
+        float hi = ksum, lo = -kcomp, mx = kmax;
+        for (int o = 16; o > 0; o >>= 1) {
+            const float bh = __shfl_down_sync(0xffffffffu, hi, o), bl = __shfl_down_sync(0xffffffffu, lo, o);
+            pair_add(hi, lo, bh, bl);
+            mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        }
+        float *rs = reinterpret_cast<float *>(red_s);  // [hi, lo] per warp
+        float *rm = reinterpret_cast<float *>(red_m);
+        if (lane == 0) {
+            rs[2 * warp] = hi;
+            rs[2 * warp + 1] = lo;
+            rm[warp] = mx;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float sh = 0.0f, sl = 0.0f, m = -1.0f;
+            for (int w = 0; w < nw; ++w) {
+                pair_add(sh, sl, rs[2 * w], rs[2 * w + 1]);
+                m = fmaxf(m, rm[w]);
+            }
+            partials[2 * slot] = (double)sh + (double)sl;
+            partials[2 * slot + 1] = (double)m;
+        }
+    } else {
+        double lsum = (double)ksum - (double)kcomp, lmax = (double)kmax;
+        for (int o = 16; o > 0; o >>= 1) {
+            lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+            lmax = fmax(lmax, __shfl_down_sync(0xffffffffu, lmax, o));
+        }
+        if (lane == 0) { red_s[warp] = lsum; red_m[warp] = lmax; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0, mx = -1.0;
+            for (int w = 0; w < nw; ++w) { s += red_s[w]; mx = fmax(mx, red_m[w]); }
+            partials[2 * slot] = s;
+            partials[2 * slot + 1] = mx;
+        }
     }
 }
 

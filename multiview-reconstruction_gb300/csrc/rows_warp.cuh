@@ -287,26 +287,7 @@ __global__ void __launch_bounds__(256) k_wrows_update(float2 *__restrict__ S, Up
         }
         __syncwarp();
     }
-    double lsum = (double)ksum - (double)kcomp, lmax = (double)kmax;
-    for (int o = 16; o > 0; o >>= 1) {
-        lsum += __shfl_down_sync(0xffffffffu, lsum, o);
-        lmax = fmax(lmax, __shfl_down_sync(0xffffffffu, lmax, o));
-    }
-    if (lane == 0) {
-        red_s[wib] = lsum;
-        red_m[wib] = lmax;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0, mx = -1.0;
-        for (int w = 0; w < 8; ++w) {
-            s += red_s[w];
-            mx = fmax(mx, red_m[w]);
-        }
-        const long long slot = (long long)blockIdx.y * gridDim.x + blockIdx.x;
-        ua.partials[2 * slot] = s;
-        ua.partials[2 * slot + 1] = mx;
-    }
+    stats_to_partials(ksum, kcomp, kmax, red_s, red_m, ua.partials, (long long)blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 }  // namespace mvr
