@@ -34,7 +34,10 @@ def _stale() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    if not force and not _stale():
+    # MVR_NVCC_DEFINES: extra -D tuning definitions (e.g. -DMVR_XY_THREADS_192=768); any
+    # value forces a rebuild
+    defines = os.environ.get("MVR_NVCC_DEFINES", "").split()
+    if not force and not defines and not _stale():
         return LIB
     nvcc = _nvcc()
     objdir = os.path.join(HERE, "_build")
@@ -43,7 +46,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src):
         obj = os.path.join(objdir, src.replace(".cu", ".o"))
-        cmd = [nvcc, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc, *NVCC_FLAGS, *defines, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")

@@ -474,7 +474,7 @@ struct UpdateArgs {
     void *psi_dst;        // T output volume (write region only)
     const float *weight[kMaxViews];
     int nviews;
-    double *prod;         // Mul: running product over views, block layout [bz][by][bx]
+    void *prod;           // Mul: running product over views (T), block layout [bz][by][bx]
     float *store;         // EPI_STORE: conv result, block layout
     const float *img;     // EPI_NLL: the view's image (zero outside the volume)
     double lambda;
@@ -530,7 +530,7 @@ __device__ __forceinline__ void update_row(const typename Cx<T>::t *zz, int m, c
                     ua.store[brow + x] = (float)integral;
                     continue;
                 }
-                if (EPI == EPI_MUL_FIRST) { ua.prod[brow + x] = (double)integral; continue; }
+                if (EPI == EPI_MUL_FIRST) { reinterpret_cast<T *>(ua.prod)[brow + x] = integral; continue; }
                 if (EPI == EPI_NLL) {
                     // Poisson negative log-likelihood w * (conv1 - img ln conv1) over img > 0,
                     // each volume voxel once (write region of its block)
@@ -546,22 +546,25 @@ __device__ __forceinline__ void update_row(const typename Cx<T>::t *zz, int m, c
                     ksum = kt;
                     continue;
                 }
-                if (EPI == EPI_MUL_ACC) { ua.prod[brow + x] *= (double)integral; continue; }
+                if (EPI == EPI_MUL_ACC) { reinterpret_cast<T *>(ua.prod)[brow + x] *= integral; continue; }
                 const T last = lastv[u][h];
                 T next;
                 if (EPI == EPI_SEQ) {
                     next = next_value(last, integral, (T)wv[u][h], ua.lambda, (T)ua.minI, (T)ua.maxI);
                 } else {  // EPI_MUL_FINAL: DeconvolutionMethods.computeNextValueMul 370-419
-                    double prod = (ua.nviews == 1 ? 1.0 : ua.prod[brow + x]) * (double)integral;
-                    double sumW = 0.0;
-                    for (int v = 0; v < ua.nviews; ++v) sumW += (double)zero_at(ua.weight[v], bm, zr, x);
+                    // the product and the weight sum in T (the reference uses double; on this
+                    // GPU the double rate is a small fraction of the float rate, and the float
+                    // product of V factors near 1 stays within a few ulp)
+                    const T prod = (ua.nviews == 1 ? (T)1 : reinterpret_cast<const T *>(ua.prod)[brow + x]) * integral;
+                    T sumW = 0;
+                    for (int v = 0; v < ua.nviews; ++v) sumW += (T)zero_at(ua.weight[v], bm, zr, x);
                     T root;
-                    if (sizeof(T) == sizeof(double)) root = (T)pow(prod, 1.0 / ua.nviews);
-                    else if (ua.nviews == 1) root = (T)prod;
+                    if (sizeof(T) == sizeof(double)) root = (T)pow((double)prod, 1.0 / ua.nviews);
+                    else if (ua.nviews == 1) root = prod;
                     else if (ua.nviews == 2) root = (T)__fsqrt_rn((float)prod);
-                    else root = (T)powf((float)prod, 1.0f / (float)ua.nviews);  // float rate, see tikhonov_f
-                    sumW = sumW < 1.0 ? sumW : 1.0;
-                    next = next_value(last, root, (T)sumW, ua.lambda, (T)ua.minI, (T)ua.maxI);
+                    else root = (T)powf((float)prod, 1.0f / (float)ua.nviews);
+                    sumW = sumW < (T)1 ? sumW : (T)1;
+                    next = next_value(last, root, sumW, ua.lambda, (T)ua.minI, (T)ua.maxI);
                 }
                 const T ch = next - last;  // signed change (DeconvolutionMethods.java:308)
                 const T ky = ch - kcomp;
@@ -648,7 +651,7 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
     const BlockMap &bm = bms.m[blockIdx.y];
     S += (long long)blockIdx.y * Pc;
     const long long bvox = (long long)bm.b[0] * bm.b[1] * bm.b[2];
-    if (ua.prod) ua.prod += (long long)blockIdx.y * bvox;
+    if (ua.prod) ua.prod = reinterpret_cast<T *>(ua.prod) + (long long)blockIdx.y * bvox;
     if (ua.store) ua.store += (long long)blockIdx.y * bvox;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double red_s[32], red_m[32];

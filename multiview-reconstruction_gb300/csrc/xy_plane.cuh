@@ -36,6 +36,11 @@ namespace mvr {
 
 constexpr long long kNoRow = -(1LL << 62);
 
+// CTA size of the 192 x 192 plane kernels (a build-time tuning knob; 1024 measured best)
+#ifndef MVR_XY_THREADS_192
+#define MVR_XY_THREADS_192 1024
+#endif
+
 template <int VX, int VY>
 struct XYShape {
     static constexpr int m = 16 * VX;     // packed complex values per real x row
@@ -46,7 +51,7 @@ struct XYShape {
     // threads per CTA and CTAs per SM: 1024 x 1 for the 155 KB plane of 192 x 192,
     // 512 x 2 for the planes of at most 100 KB (the latency of the shared-memory FFT
     // phases is hidden by warps, not by per-thread interleaving)
-    static constexpr int NT = (VX == 6 && VY == 12) ? 1024 : 512;
+    static constexpr int NT = (VX == 6 && VY == 12) ? MVR_XY_THREADS_192 : 512;
     static constexpr int MINB = (VX == 6 && VY == 12) ? 1 : 2;
     // rounds of the row items (y, t) of the fused x phase 1
     static constexpr int RX = Py * 16 / NT;
@@ -429,7 +434,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
     const int z = blockIdx.x;
     float2 *Sp = S + (long long)blockIdx.y * Pc + (long long)z * SH::plane;
     const long long bvox = (long long)bm.b[0] * bm.b[1] * bm.b[2];
-    if (ua.prod) ua.prod += (long long)blockIdx.y * bvox;
+    if (ua.prod) ua.prod = reinterpret_cast<float *>(ua.prod) + (long long)blockIdx.y * bvox;
     if (ua.store) ua.store += (long long)blockIdx.y * bvox;
     sm.load_tables(gtwx, gtwy);
     float ksum = 0.0f, kcomp = 0.0f, kmax = -1.0f;
