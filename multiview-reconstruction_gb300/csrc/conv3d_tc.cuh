@@ -152,6 +152,145 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(const __nv_bfloat16 *__restri
     if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
+// The same convolution on output bricks of 8 x 4 x 4 voxels (x, y, z): the brick's
+// input halo (10 x 6 x 6 voxels, zero outside the volume) is loaded into shared memory
+// once, and the A operand of every tap is copied from it (shared to shared) instead of
+// being gathered 27 times from L1/L2.  Row r of the 128-row tile is voxel
+// (r % 8, (r / 8) % 4, r / 32) of the brick.  Shared memory: halo, two A stages, two B
+// stages.
+constexpr int kBrickX = 8, kBrickY = 4, kBrickZ = 4;
+constexpr int kHaloX = kBrickX + 2, kHaloY = kBrickY + 2, kHaloZ = kBrickZ + 2;
+constexpr int kHaloVox = kHaloX * kHaloY * kHaloZ;
+
+template <int N, int C>
+constexpr size_t conv_brick_smem()
+{
+    return (size_t)kHaloVox * C * 2 + 2 * (128 * C * 2 + N * C * 2);
+}
+
+template <int N, int C, int OUT_MODE>
+__global__ void __launch_bounds__(128) k_conv3d_brick(const __nv_bfloat16 *__restrict__ act,
+                                                      const __nv_bfloat16 *__restrict__ wk,
+                                                      const float *__restrict__ bias, void *out, ConvGeom g, int sign,
+                                                      int relu, int *err)
+{
+    static_assert(N % 16 == 0 && N <= 256 && C % 16 == 0 && C <= 128, "tile shape");
+    constexpr int A_BYTES = 128 * C * 2, B_BYTES = N * C * 2, H_BYTES = kHaloVox * C * 2;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *sA[2] = {smem, smem + A_BYTES};
+    uint8_t *sB[2] = {smem + 2 * A_BYTES, smem + 2 * A_BYTES + B_BYTES};
+    uint8_t *halo = smem + 2 * A_BYTES + 2 * B_BYTES;
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    constexpr uint32_t ncols = TmemCols<N>::value;
+    if (warp == 0) tc::tmem_alloc(&tbase, ncols);
+    if (tid == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // brick coordinates
+    const int nbx = (g.W + kBrickX - 1) / kBrickX, nby = (g.H + kBrickY - 1) / kBrickY,
+              nbz = (g.D + kBrickZ - 1) / kBrickZ;
+    long long q = blockIdx.x;
+    const int ibx = (int)(q % nbx);
+    q /= nbx;
+    const int iby = (int)(q % nby);
+    q /= nby;
+    const int ibz = (int)(q % nbz);
+    const int b = (int)(q / nbz);
+    const int x0 = ibx * kBrickX, y0 = iby * kBrickY, z0 = ibz * kBrickZ;
+    // halo: C / 8 chunks of 16 bytes per voxel, zero outside the volume
+    constexpr int CH = C / 8;
+    for (int k = tid; k < kHaloVox * CH; k += 128) {
+        const int hv = k / CH, j = k - hv * CH;
+        const int hx = hv % kHaloX, hy = (hv / kHaloX) % kHaloY, hz = hv / (kHaloX * kHaloY);
+        const int xx = x0 - 1 + hx, yy = y0 - 1 + hy, zz = z0 - 1 + hz;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (xx >= 0 && yy >= 0 && zz >= 0 && xx < g.W && yy < g.H && zz < g.D)
+            v = __ldg(reinterpret_cast<const uint4 *>(act + ((((long long)b * g.D + zz) * g.H + yy) * g.W + xx) * C) + j);
+        *reinterpret_cast<uint4 *>(halo + (size_t)hv * C * 2 + 16 * j) = v;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tbase;
+    const int lx = tid & 7, ly = (tid >> 3) & 3, lz = tid >> 5;
+    const int x = x0 + lx, y = y0 + ly, z = z0 + lz;
+    const bool rv = x < g.W && y < g.H && z < g.D;
+    const long long n = rv ? (((long long)b * g.D + z) * g.H + y) * g.W + x : 0;
+    const uint32_t idesc = tc::idesc_bf16(128, N);
+    bool ok = true;
+    uint32_t uses[2] = {0, 0};
+    for (int t = 0; t < 27; ++t) {
+        const int buf = t & 1;
+        if (t >= 2) {  // the MMAs that last read this buffer must be done
+            ok = ok && tc::mbar_wait(&mbar[buf], (uses[buf] - 1) & 1, kTcWaitIter);
+        }
+        // A: this thread's row from the halo at tap t
+        const int dz = (t / 9 - 1) * sign, dy = ((t / 3) % 3 - 1) * sign, dx = (t % 3 - 1) * sign;
+        const int hv = ((lz + 1 + dz) * kHaloY + (ly + 1 + dy)) * kHaloX + (lx + 1 + dx);
+        const uint4 *hp = reinterpret_cast<const uint4 *>(halo + (size_t)hv * C * 2);
+#pragma unroll
+        for (int j = 0; j < CH; ++j)
+            *reinterpret_cast<uint4 *>(sA[buf] + tc::core_offset(tid, 8 * j, C)) = hp[j];
+        // B: N rows of K = (t, 0..C-1)
+        for (int s = tid; s < N * CH; s += 128) {
+            const int r = s / CH, j = s % CH;
+            const uint4 v = __ldg(reinterpret_cast<const uint4 *>(wk + ((long long)r * 27 + t) * C) + j);
+            *reinterpret_cast<uint4 *>(sB[buf] + tc::core_offset(r, 8 * j, C)) = v;
+        }
+        tc::fence_proxy_async();
+        __syncthreads();
+        if (tid == 0 && ok) {
+            tc::fence_after_sync();
+#pragma unroll
+            for (int c = 0; c < C / 16; ++c) {
+                const uint64_t ad = tc::smem_desc(tc::smem_u32(sA[buf]) + c * 256, 128, C * 16);
+                const uint64_t bd = tc::smem_desc(tc::smem_u32(sB[buf]) + c * 256, 128, C * 16);
+                tc::mma_bf16(tmem, ad, bd, idesc, (t > 0 || c > 0) ? 1 : 0);
+            }
+            tc::mma_commit(&mbar[buf]);
+        }
+        ++uses[buf];
+    }
+    for (int bb = 0; bb < 2; ++bb)
+        if (uses[bb]) ok = tc::mbar_wait(&mbar[bb], (uses[bb] - 1) & 1, kTcWaitIter) && ok;
+    tc::fence_after_sync();
+    __syncthreads();
+    if (!ok) {
+        if (tid == 0) atomicExch(err, 1);
+    } else {
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            float v[16];
+            tc::tmem_ld16(trow + c0, v);
+            if (!rv) continue;
+            if (OUT_MODE == 0) {
+                __align__(16) __nv_bfloat16 o[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    float a = v[j] + (bias ? bias[c0 + j] : 0.0f);
+                    if (relu) a = fmaxf(a, 0.0f);
+                    o[j] = __float2bfloat16(a);
+                }
+                uint4 *op = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(out) + n * N + c0);
+                op[0] = reinterpret_cast<const uint4 *>(o)[0];
+                op[1] = reinterpret_cast<const uint4 *>(o)[1];
+            } else {
+                float4 *op = reinterpret_cast<float4 *>(reinterpret_cast<float *>(out) + n * N + c0);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) op[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
 // wgrad: D[(t,ci) rows][co] over the voxels [blockIdx.y * vpc, +vpc), atomically added
 // to dW[co][t][ci] (FP32).
 template <int N, int C>

@@ -41,15 +41,20 @@ size_t conv_smem() { return 2 * (128 * C * 2 + N * C * 2); }
 template <int N>
 size_t wgrad_smem() { return 2 * (128 * 64 * 2 + N * 64 * 2); }
 
+// Forward and data-gradient convolutions run on 8 x 4 x 4 output bricks with the input
+// halo staged in shared memory (k_conv3d_brick); k_conv3d_tc (128 consecutive voxels,
+// gathered per tap) remains the reference form of the same product.
 template <int N, int C, int OUT>
 cudaError_t launch_conv(const bf16 *act, const bf16 *w, const float *bias, void *out, const ConvGeom &g, int sign,
                         int relu, int *err, cudaStream_t s)
 {
-    const size_t sm = conv_smem<N, C>();
-    cudaError_t e = cudaFuncSetAttribute(k_conv3d_tc<N, C, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    const size_t sm = conv_brick_smem<N, C>();
+    cudaError_t e =
+        cudaFuncSetAttribute(k_conv3d_brick<N, C, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    const unsigned grid = (unsigned)((g.nvox + 127) / 128);
-    k_conv3d_tc<N, C, OUT><<<grid, 128, sm, s>>>(act, w, bias, out, g, sign, relu, err);
+    const long long bricks = (long long)((g.W + kBrickX - 1) / kBrickX) * ((g.H + kBrickY - 1) / kBrickY) *
+                             ((g.D + kBrickZ - 1) / kBrickZ) * g.B;
+    k_conv3d_brick<N, C, OUT><<<(unsigned)bricks, 128, sm, s>>>(act, w, bias, out, g, sign, relu, err);
     return cudaGetLastError();
 }
 

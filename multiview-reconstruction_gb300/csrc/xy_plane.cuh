@@ -267,23 +267,26 @@ struct XYSmem {
     }
 };
 
+// The plane from HBM: every thread issues all its (at most 12) 16-byte loads before the
+// first store, so the copy costs one memory latency.
 template <int VX, int VY>
 __device__ __forceinline__ void xy_load_plane(float2 *A, const float2 *__restrict__ Sp)
 {
-    constexpr int n4 = XYShape<VX, VY>::plane / 2;
+    typedef XYShape<VX, VY> SH;
+    constexpr int n4 = SH::plane / 2, NT = SH::NT;
+    constexpr int U = (n4 + NT - 1) / NT < 12 ? (n4 + NT - 1) / NT : 12;
     const float4 *src = reinterpret_cast<const float4 *>(Sp);
     float4 *dst = reinterpret_cast<float4 *>(A);
-    constexpr int U = 4;
-    for (int i0 = threadIdx.x; i0 < n4; i0 += blockDim.x * U) {
+    for (int i0 = threadIdx.x; i0 < n4; i0 += NT * U) {
         float4 r[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            const int i = i0 + u * blockDim.x;
-            if (i < n4) r[u] = src[i];
+            const int i = i0 + u * NT;
+            if (i < n4) r[u] = __ldg(src + i);
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-            const int i = i0 + u * blockDim.x;
+            const int i = i0 + u * NT;
             if (i < n4) dst[i] = r[u];
         }
     }

@@ -1,0 +1,29 @@
+"""bench.py workload definitions (CPU): block grids of the three workloads follow the
+reference's DeconView / BlockGeneratorFixedSizePrecise geometry (the doubled kernel 2k-1)."""
+import os
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+
+
+def test_workload_block_grids():
+    w = bench.WORKLOADS["4view256"]()
+    assert [len(w.blocks(v)) for v in range(4)] == [16] * 4  # 2 x 2 x 4 blocks of 192^3
+    assert w.view_blocks_per_iter() == 64 and w.metric == "voxel-iterations/s (4 views)"
+    w = bench.WORKLOADS["6view512"]()
+    # effective sizes 192 - 2(k-1): 152 ... 112 in x/y, 256 - 2(k-1): 176 ... 96 in z
+    assert [len(w.blocks(v)) for v in range(6)] == [32, 32, 32, 32, 75, 75]
+    w = bench.WORKLOADS["8view1024"]()
+    assert [len(w.blocks(v)) for v in range(8)] == [216] * 8
+
+
+def test_workload_config_fields():
+    for name, make in bench.WORKLOADS.items():
+        w = make()
+        c = w.config("circular")
+        assert c["views"] == w.views and c["dims"] == list(w.dims) and c["block"] == list(w.block)
+        assert "inputs larger than L2" in c["l2"]
