@@ -229,6 +229,32 @@ MVR_API int mvr_decon_init_psi(mvr_decon *h, int method, double sigma, double *a
  * in FP64.  per_view (or NULL) receives num_views partial sums. */
 MVR_API int mvr_decon_likelihood(mvr_decon *h, double *total, double *per_view);
 
+/* ---- input preparation: transformed, fused views (device) ------------------------------
+ * ProcessInputImages.fuseGroups (MV/deconvolution/util/ProcessInputImages.java:279-399) for
+ * one group: every view is transformed into the bounding box with linear interpolation
+ * (TransformView.transformView with minValueImg 1 inside and 0 outside the view,
+ * TransformedInputRandomAccess.get), weighted by its cosine blending
+ * (TransformWeight.transformBlending, BlendingRealRandomAccess.computeWeight) and averaged
+ * (FusedRandomAccess, Fusion.AVG); the deconvolution weight is the sum of the views'
+ * deconvolution blendings (CombineWeightsSumRandomAccess).  The result is the image and the
+ * raw weight of one DeconView (mvr_decon_set_view_device). */
+typedef struct mvr_fuse_view {
+    const float *img;         /* device pointer: the view's image, x fastest */
+    int dims[3];              /* its size {x, y, z} */
+    double model[12];         /* view pixel -> world, row-packed 3 x 4 (AffineTransform3D.getRowPackedCopy) */
+    int fusion_blend;         /* 0: fusion weight 1 (no blending), 1: blending with the two arrays below */
+    float fusion_border[3];   /* pixels skipped at each face before blending (x, y, z) */
+    float fusion_range[3];    /* pixels over which the weight rises from 0 to 1 */
+    int decon_blend;          /* the same for the deconvolution weight */
+    float decon_border[3];
+    float decon_range[3];
+} mvr_fuse_view;
+/* bb_min: world coordinate of the box's first voxel; bb_dims {x, y, z}; image_out and
+ * weight_out: device float volumes of the box.  Synchronous on `stream`. */
+MVR_API int mvr_fuse_group(const mvr_fuse_view *views, int num_views, const long long bb_min[3], const int bb_dims[3],
+                           float *image_out, float *weight_out, int device, void *stream);
+MVR_API const char *mvr_fuse_last_error(void);
+
 /* ---- learned multi-iteration proposal (no counterpart in the reference) ---------------
  * A 3-level 3D U-Net (16/32/64 channels, 3x3x3 convolutions, BF16 weights and
  * activations, FP32 accumulation on the tcgen05 tensor cores) with its own forward and

@@ -168,12 +168,16 @@ constexpr size_t conv_brick_smem()
     return (size_t)kHaloVox * C * 2 + 2 * (128 * C * 2 + N * C * 2);
 }
 
-template <int N, int C, int OUT_MODE>
+// CU > 0: the input is the concatenation [nearest x2 upsampling of `act` (CU channels,
+// a volume of half the size), act2 (C - CU channels)] read straight into the halo, so the
+// decoder layers need no concatenated copy.
+template <int N, int C, int OUT_MODE, int CU = 0>
 __global__ void __launch_bounds__(128) k_conv3d_brick(const __nv_bfloat16 *__restrict__ act,
                                                       const __nv_bfloat16 *__restrict__ wk,
                                                       const float *__restrict__ bias, void *out, ConvGeom g, int sign,
-                                                      int relu, int *err)
+                                                      int relu, int *err, const __nv_bfloat16 *__restrict__ act2 = nullptr)
 {
+    static_assert(CU % 8 == 0 && CU < C, "concatenated channel split");
     static_assert(N % 16 == 0 && N <= 256 && C % 16 == 0 && C <= 128, "tile shape");
     constexpr int A_BYTES = 128 * C * 2, B_BYTES = N * C * 2, H_BYTES = kHaloVox * C * 2;
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -208,8 +212,17 @@ __global__ void __launch_bounds__(128) k_conv3d_brick(const __nv_bfloat16 *__res
         const int hx = hv % kHaloX, hy = (hv / kHaloX) % kHaloY, hz = hv / (kHaloX * kHaloY);
         const int xx = x0 - 1 + hx, yy = y0 - 1 + hy, zz = z0 - 1 + hz;
         uint4 v = make_uint4(0, 0, 0, 0);
-        if (xx >= 0 && yy >= 0 && zz >= 0 && xx < g.W && yy < g.H && zz < g.D)
-            v = __ldg(reinterpret_cast<const uint4 *>(act + ((((long long)b * g.D + zz) * g.H + yy) * g.W + xx) * C) + j);
+        if (xx >= 0 && yy >= 0 && zz >= 0 && xx < g.W && yy < g.H && zz < g.D) {
+            if constexpr (CU == 0) {
+                v = __ldg(reinterpret_cast<const uint4 *>(act + ((((long long)b * g.D + zz) * g.H + yy) * g.W + xx) * C) + j);
+            } else if (j < CU / 8) {
+                const long long lv = (((long long)b * (g.D / 2) + zz / 2) * (g.H / 2) + yy / 2) * (g.W / 2) + xx / 2;
+                v = __ldg(reinterpret_cast<const uint4 *>(act + lv * CU) + j);
+            } else {
+                const long long hv2 = (((long long)b * g.D + zz) * g.H + yy) * g.W + xx;
+                v = __ldg(reinterpret_cast<const uint4 *>(act2 + hv2 * (C - CU)) + (j - CU / 8));
+            }
+        }
         *reinterpret_cast<uint4 *>(halo + (size_t)hv * C * 2 + 16 * j) = v;
     }
     tc::fence_before_sync();

@@ -1,0 +1,202 @@
+// Input preparation on the device: the views of one group transformed into the
+// deconvolution bounding box and fused, with the fusion and deconvolution blending weights
+// (ProcessInputImages.fuseGroups, deconvolution/util/ProcessInputImages.java:279-399).
+//
+// Per output voxel p of the bounding box (world coordinate s = p + bb_min) and view v:
+//   t = model_v^-1 s                                  (double, AffineTransform3D.applyInverse)
+//   image  I_v = max(1, linear interpolation of the view at t) when t lies strictly inside
+//                the view (min < t < max on every axis), else 0
+//                (TransformView.transformView with minValueImg 1 / outsideValueImg 0,
+//                 TransformedInputRandomAccess.get, AbstractTransformedImgRandomAccess)
+//   weights wf_v, wd_v = the cosine blending of the view's interval at t (as float) with the
+//                fusion / deconvolution border and range, or 1 without blending
+//                (TransformWeight.transformBlending, TransformedRasteredRandomAccess.applyInverse,
+//                 BlendingRealRandomAccess.computeWeight)
+//   fused image = sum(I_v wf_v) / sum(wf_v) over wf_v != 0, 0 when the sum is 0
+//                (FusedRandomAccess.get, Fusion.AVG)
+//   deconvolution weight = sum(wd_v) (CombineWeightsSumRandomAccess.get)
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mvr_gb300.h"
+
+namespace mvr {
+namespace {
+
+constexpr int kFuseMaxViews = 16;
+
+struct FuseView {
+    const float *img;
+    int dims[3];
+    double inv[12];  // world -> view pixel, row-packed 3 x 4
+    float fb[3], fr[3], db[3], dr[3];
+    int fblend, dblend;
+};
+
+struct FuseViews {
+    FuseView v[kFuseMaxViews];
+    int n;
+};
+
+// BlendingRealRandomAccess.computeWeight on an interval [0, dims - 1] at a float location
+// (float arithmetic as in the reference, the look-up table product in double).
+__device__ __forceinline__ float blend_weight(const float *loc, const int *dims, const float *border,
+                                              const float *range, const double *lut)
+{
+    float tmp[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float l = loc[d];
+        const float a = __fsub_rn(l, border[d]);
+        const float b = __fsub_rn(__fsub_rn((float)(dims[d] - 1), l), border[d]);
+        tmp[d] = a < b ? a : b;
+        if (tmp[d] <= 0.0f) return 0.0f;
+    }
+    float w = 1.0f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float rel = __fdiv_rn(tmp[d], range[d]);
+        if (rel < 1.0f) w = (float)((double)w * lut[(int)((double)rel * 1000.0 + 0.5)]);
+    }
+    return w;
+}
+
+// Linear interpolation of a float volume at t (all eight neighbours exist: t is strictly
+// inside).  Weights in double, the value accumulated in float (the interpolator's FloatType
+// arithmetic).
+__device__ __forceinline__ float trilinear(const float *__restrict__ img, const int *dims, const double *t)
+{
+    const int x0 = (int)floor(t[0]), y0 = (int)floor(t[1]), z0 = (int)floor(t[2]);
+    const double fx = t[0] - x0, fy = t[1] - y0, fz = t[2] - z0;
+    const long long sx = 1, sy = dims[0], sz = (long long)dims[0] * dims[1];
+    const long long base = z0 * sz + y0 * sy + x0;
+    float acc = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int dx = c & 1, dy = (c >> 1) & 1, dz = c >> 2;
+        const double w = (dx ? fx : 1.0 - fx) * (dy ? fy : 1.0 - fy) * (dz ? fz : 1.0 - fz);
+        const float v = __ldg(img + base + dz * sz + dy * sy + dx * sx);
+        acc = __fadd_rn(acc, (float)((double)v * w));
+    }
+    return acc;
+}
+
+__global__ void k_fuse_group(FuseViews fv, long long bx, long long by, long long bz, int nx, int ny, int nz,
+                             float *__restrict__ out_img, float *__restrict__ out_w, const double *__restrict__ lut)
+{
+    const long long n = (long long)nx * ny * nz;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % nx);
+        const int y = (int)((i / nx) % ny);
+        const int z = (int)(i / ((long long)nx * ny));
+        const double s0 = (double)(x + bx), s1 = (double)(y + by), s2 = (double)(z + bz);
+        double sumI = 0.0, sumW = 0.0, sumD = 0.0;
+        for (int k = 0; k < fv.n; ++k) {
+            const FuseView &v = fv.v[k];
+            const double *m = v.inv;
+            const double t[3] = {s0 * m[0] + s1 * m[1] + s2 * m[2] + m[3], s0 * m[4] + s1 * m[5] + s2 * m[6] + m[7],
+                                 s0 * m[8] + s1 * m[9] + s2 * m[10] + m[11]};
+            const float tf[3] = {(float)t[0], (float)t[1], (float)t[2]};
+            const float wf = v.fblend ? blend_weight(tf, v.dims, v.fb, v.fr, lut) : 1.0f;
+            const float wd = v.dblend ? blend_weight(tf, v.dims, v.db, v.dr, lut) : 1.0f;
+            sumD += (double)wd;
+            if (wf == 0.0f) continue;
+            float val = 0.0f;  // outsideValueImg
+            if (t[0] > 0.0 && t[1] > 0.0 && t[2] > 0.0 && t[0] < v.dims[0] - 1 && t[1] < v.dims[1] - 1 &&
+                t[2] < v.dims[2] - 1)
+                val = fmaxf(1.0f, trilinear(v.img, v.dims, t));  // minValueImg
+            sumI += (double)val * (double)wf;
+            sumW += (double)wf;
+        }
+        out_img[i] = sumW > 0.0 ? (float)(sumI / sumW) : 0.0f;
+        out_w[i] = (float)sumD;
+    }
+}
+
+bool invert_affine(const double *m, double *inv)
+{
+    const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9], k = m[10];
+    const double det = a * (e * k - f * h) - b * (d * k - f * g) + c * (d * h - e * g);
+    if (det == 0.0 || !std::isfinite(det)) return false;
+    const double r = 1.0 / det;
+    const double i00 = (e * k - f * h) * r, i01 = (c * h - b * k) * r, i02 = (b * f - c * e) * r;
+    const double i10 = (f * g - d * k) * r, i11 = (a * k - c * g) * r, i12 = (c * d - a * f) * r;
+    const double i20 = (d * h - e * g) * r, i21 = (b * g - a * h) * r, i22 = (a * e - b * d) * r;
+    inv[0] = i00, inv[1] = i01, inv[2] = i02;
+    inv[4] = i10, inv[5] = i11, inv[6] = i12;
+    inv[8] = i20, inv[9] = i21, inv[10] = i22;
+    inv[3] = -(i00 * m[3] + i01 * m[7] + i02 * m[11]);
+    inv[7] = -(i10 * m[3] + i11 * m[7] + i12 * m[11]);
+    inv[11] = -(i20 * m[3] + i21 * m[7] + i22 * m[11]);
+    return true;
+}
+
+thread_local std::string g_fuse_err;
+
+int fuse_fail(int code, const std::string &m)
+{
+    g_fuse_err = m;
+    return code;
+}
+
+}  // namespace
+}  // namespace mvr
+
+using namespace mvr;
+
+extern "C" MVR_API const char *mvr_fuse_last_error(void) { return g_fuse_err.c_str(); }
+
+extern "C" MVR_API int mvr_fuse_group(const mvr_fuse_view *views, int num_views, const long long bb_min[3],
+                                      const int bb_dims[3], float *image_out, float *weight_out, int device,
+                                      void *stream)
+{
+    if (!views || num_views < 1 || num_views > kFuseMaxViews || !bb_min || !bb_dims || !image_out || !weight_out)
+        return fuse_fail(MVR_ERR_ARG, "mvr_fuse_group: 1..16 views, bounding box and outputs are required");
+    for (int d = 0; d < 3; ++d)
+        if (bb_dims[d] < 1) return fuse_fail(MVR_ERR_ARG, "mvr_fuse_group: empty bounding box");
+    FuseViews fv{};
+    fv.n = num_views;
+    for (int k = 0; k < num_views; ++k) {
+        const mvr_fuse_view &s = views[k];
+        FuseView &v = fv.v[k];
+        if (!s.img) return fuse_fail(MVR_ERR_ARG, "mvr_fuse_group: a view image is NULL");
+        for (int d = 0; d < 3; ++d) {
+            if (s.dims[d] < 2) return fuse_fail(MVR_ERR_ARG, "mvr_fuse_group: view sizes must be >= 2");
+            v.dims[d] = s.dims[d];
+            v.fb[d] = s.fusion_border[d];
+            v.fr[d] = s.fusion_range[d];
+            v.db[d] = s.decon_border[d];
+            v.dr[d] = s.decon_range[d];
+        }
+        v.fblend = s.fusion_blend;
+        v.dblend = s.decon_blend;
+        v.img = s.img;
+        if (!invert_affine(s.model, v.inv)) return fuse_fail(MVR_ERR_ARG, "mvr_fuse_group: a view model is singular");
+    }
+    // the blending look-up table of BlendingRealRandomAccess: d runs from 0 in steps of 0.001
+    // (accumulated in double, as there), entry (int)(d * 1000 + 0.5) = (cos((1 - d) pi) + 1) / 2
+    std::vector<double> lut(1001, 0.0);
+    for (double d = 0; d <= 1.0001; d = d + 0.001) lut[(int)(d * 1000.0 + 0.5)] = (std::cos((1 - d) * M_PI) + 1) / 2;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return fuse_fail(MVR_ERR_CUDA, cudaGetErrorString(e));
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    double *dlut = nullptr;
+    e = cudaMalloc(&dlut, sizeof(double) * lut.size());
+    if (e != cudaSuccess) return fuse_fail(e == cudaErrorMemoryAllocation ? MVR_ERR_OOM : MVR_ERR_CUDA, cudaGetErrorString(e));
+    e = cudaMemcpyAsync(dlut, lut.data(), sizeof(double) * lut.size(), cudaMemcpyHostToDevice, s);
+    const long long n = (long long)bb_dims[0] * bb_dims[1] * bb_dims[2];
+    if (e == cudaSuccess) {
+        const int grid = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+        k_fuse_group<<<grid, 256, 0, s>>>(fv, bb_min[0], bb_min[1], bb_min[2], bb_dims[0], bb_dims[1], bb_dims[2],
+                                          image_out, weight_out, dlut);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(dlut);
+    if (e != cudaSuccess) return fuse_fail(MVR_ERR_CUDA, std::string("mvr_fuse_group: ") + cudaGetErrorString(e));
+    return MVR_OK;
+}

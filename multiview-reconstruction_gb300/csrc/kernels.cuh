@@ -21,6 +21,7 @@
 //              (Views.extendMirrorSingle(psi)), img/weight zero-extended (:122-123)
 #pragma once
 #include "fft_device.cuh"
+#include "fsum.cuh"
 
 namespace mvr {
 
@@ -576,21 +577,6 @@ __device__ __forceinline__ void update_row(const typename Cx<T>::t *zz, int m, c
             }
         }
     }
-}
-
-// Sum of two float-pair values (hi + lo) without losing the low part (Knuth's TwoSum on
-// the high parts, the low parts and the rounding error added, then renormalised).  The
-// pair carries about 48 significant bits, which is what the CTA reduction needs: the
-// GPU's double rate is so low that a few double additions per thread at the end of every
-// CTA cost a large part of the kernel.
-__device__ __forceinline__ void pair_add(float &hi, float &lo, float bhi, float blo)
-{
-    const float s = hi + bhi;
-    const float v = s - hi;
-    float e = (hi - (s - v)) + (bhi - v);
-    e += lo + blo;
-    hi = s + e;
-    lo = e - (hi - s);
 }
 
 // Deterministic CTA reduction of the per-thread statistics into ua.partials[slot]

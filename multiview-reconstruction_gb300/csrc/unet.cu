@@ -27,6 +27,7 @@
 
 #include "../../include/mvr_gb300.h"
 #include "conv3d_tc.cuh"
+#include "fsum.cuh"
 
 namespace mvr {
 namespace {
@@ -55,6 +56,22 @@ cudaError_t launch_conv(const bf16 *act, const bf16 *w, const float *bias, void 
     const long long bricks = (long long)((g.W + kBrickX - 1) / kBrickX) * ((g.H + kBrickY - 1) / kBrickY) *
                              ((g.D + kBrickZ - 1) / kBrickZ) * g.B;
     k_conv3d_brick<N, C, OUT><<<(unsigned)bricks, 128, sm, s>>>(act, w, bias, out, g, sign, relu, err);
+    return cudaGetLastError();
+}
+
+// Decoder convolution (bias, ReLU, BF16 out) on the concatenation [up(low) (CU channels),
+// skip (C - CU channels)] without materialising it.
+template <int N, int C, int CU>
+cudaError_t launch_conv_concat(const bf16 *low, const bf16 *skip, const bf16 *w, const float *bias, void *out,
+                               const ConvGeom &g, int *err, cudaStream_t s)
+{
+    const size_t sm = conv_brick_smem<N, C>();
+    cudaError_t e =
+        cudaFuncSetAttribute(k_conv3d_brick<N, C, 0, CU>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    const long long bricks = (long long)((g.W + kBrickX - 1) / kBrickX) * ((g.H + kBrickY - 1) / kBrickY) *
+                             ((g.D + kBrickZ - 1) / kBrickZ) * g.B;
+    k_conv3d_brick<N, C, 0, CU><<<(unsigned)bricks, 128, sm, s>>>(low, w, bias, out, g, 1, 1, err, skip);
     return cudaGetLastError();
 }
 
@@ -107,20 +124,40 @@ cudaError_t wgrad_any(int N, int C, const bf16 *X, const bf16 *G, float *dW, con
 }
 
 // ---- elementwise kernels ------------------------------------------------------------
-// per-patch mean of psi (FP64), one CTA per patch
-__global__ void k_patch_mean(const float *psi, long long per, double *mean)
+// per-patch mean of psi: kMeanParts CTAs per patch sum their slices as compensated float
+// pairs (one double per CTA), then one thread per patch adds the parts in FP64
+constexpr int kMeanParts = 256;
+
+__global__ void k_patch_partials(const float *psi, long long per, double *parts)
 {
-    __shared__ double sm[256];
-    const float *p = psi + (long long)blockIdx.x * per;
-    double s = 0.0;
-    for (long long i = threadIdx.x; i < per; i += blockDim.x) s += p[i];
-    sm[threadIdx.x] = s;
+    __shared__ float sh[256], sl[256];
+    const float *p = psi + (long long)blockIdx.y * per;
+    const long long chunk = (per + kMeanParts - 1) / kMeanParts;
+    const long long i0 = (long long)blockIdx.x * chunk, i1 = min(per, i0 + chunk);
+    float hi = 0.0f, lo = 0.0f;
+    for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) pair_add(hi, lo, p[i], 0.0f);
+    sh[threadIdx.x] = hi;
+    sl[threadIdx.x] = lo;
     __syncthreads();
     for (int h = blockDim.x >> 1; h > 0; h >>= 1) {
-        if (threadIdx.x < h) sm[threadIdx.x] += sm[threadIdx.x + h];
+        if (threadIdx.x < h) {
+            float a = sh[threadIdx.x], b = sl[threadIdx.x];
+            pair_add(a, b, sh[threadIdx.x + h], sl[threadIdx.x + h]);
+            sh[threadIdx.x] = a;
+            sl[threadIdx.x] = b;
+        }
         __syncthreads();
     }
-    if (threadIdx.x == 0) mean[blockIdx.x] = sm[0] / (double)per;
+    if (threadIdx.x == 0) parts[(long long)blockIdx.y * kMeanParts + blockIdx.x] = (double)sh[0] + (double)sl[0];
+}
+
+__global__ void k_patch_mean(const double *parts, long long per, int B, double *mean)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    double s = 0.0;
+    for (int k = 0; k < kMeanParts; ++k) s += parts[(long long)b * kMeanParts + k];
+    mean[b] = s / (double)per;
 }
 
 // features: [log(psi / mean), log(psi_next / psi), 0 x 14] as BF16; target log(psi_m / psi)
@@ -160,22 +197,25 @@ __global__ void k_pool(const bf16 *in, bf16 *out, ConvGeom lo, int C)
     }
 }
 
-// out[n] = [up(low)[n] (Cu channels), skip[n] (Cs channels)], nearest upsampling x2
+// out[n] = [up(low)[n] (Cu channels), skip[n] (Cs channels)], nearest upsampling x2, in
+// chunks of 8 channels (16 bytes); Cu and Cs are multiples of 8
 __global__ void k_up_concat(const bf16 *low, const bf16 *skip, bf16 *out, ConvGeom hi, int Cu, int Cs)
 {
-    const int Ct = Cu + Cs;
-    const long long n = hi.nvox * Ct;
+    const int Ct = Cu + Cs, K = Ct / 8, Ku = Cu / 8;
+    const long long n = hi.nvox * K;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % Ct);
-        const long long v = i / Ct;
-        if (c < Cu) {
+        const int c8 = (int)(i % K);
+        const long long v = i / K;
+        uint4 val;
+        if (c8 < Ku) {
             int x, y, z, b;
             vox_coords(hi, v, x, y, z, b);
             const long long lv = (((long long)b * (hi.D / 2) + z / 2) * (hi.H / 2) + y / 2) * (hi.W / 2) + x / 2;
-            out[i] = low[lv * Cu + c];
+            val = reinterpret_cast<const uint4 *>(low + lv * Cu)[c8];
         } else {
-            out[i] = skip[v * Cs + (c - Cu)];
+            val = reinterpret_cast<const uint4 *>(skip + v * Cs)[c8 - Ku];
         }
+        reinterpret_cast<uint4 *>(out + v * Ct)[c8] = val;
     }
 }
 
@@ -335,7 +375,7 @@ public:
     ~UNet();
     int init();
     int set_input(const float *psi, const float *psi_next, const float *psi_target);
-    int forward(float *pred);
+    int forward(float *pred, bool fused = false);
     int train_step(float lr, double *loss);
     int propose(const float *psi, float *out, float cap);
     long long num_params() const { return nparams_; }
@@ -382,7 +422,7 @@ private:
     bf16 *G_ = nullptr;  // BF16 gradient scratch (largest: level 1 x 16 or level 2 x 32)
     float *out_ = nullptr, *target_ = nullptr;
     float *gc1_ = nullptr, *gc2_ = nullptr, *gd2_ = nullptr, *gb3_ = nullptr, *gp2_ = nullptr, *gp1_ = nullptr;
-    double *mean_ = nullptr, *loss_ = nullptr;
+    double *mean_ = nullptr, *meanp_ = nullptr, *loss_ = nullptr;
     int *err_dev_ = nullptr;
     int step_ = 0;
     bool weights_fresh_ = false;
@@ -434,7 +474,7 @@ int UNet::init()
     A_(c2_, n2 * 96) A_(d2_, n2 * 32) A_(c1_, n1 * 48) A_(d1_, n1 * 16)
     A_(G_, std::max(n1 * 16, n2 * 32)) A_(out_, n1) A_(target_, n1)
     A_(gc1_, n1 * 48) A_(gc2_, n2 * 96) A_(gd2_, n2 * 32) A_(gb3_, n3 * 64) A_(gp2_, n3 * 32) A_(gp1_, n2 * 16)
-    A_(mean_, B_) A_(loss_, 1) A_(err_dev_, 1)
+    A_(mean_, B_) A_(meanp_, (long long)B_ * kMeanParts) A_(loss_, 1) A_(err_dev_, 1)
 #undef A_
     // He initialisation from a seeded generator (host), zero biases
     std::vector<float> h((size_t)nparams_, 0.0f);
@@ -481,13 +521,14 @@ int UNet::set_input(const float *psi, const float *psi_next, const float *psi_ta
     if (!psi) return fail(MVR_ERR_ARG, "psi must not be NULL");
     cudaSetDevice(dev_);
     const long long per = g1_.nvox / B_;
-    k_patch_mean<<<B_, 256, 0, s_>>>(psi, per, mean_);
+    k_patch_partials<<<dim3(kMeanParts, B_), 256, 0, s_>>>(psi, per, meanp_);
+    k_patch_mean<<<(B_ + 127) / 128, 128, 0, s_>>>(meanp_, per, B_, mean_);
     k_features<<<gsize(g1_.nvox), 256, 0, s_>>>(psi, psi_next, psi_target, g1_.nvox, per, mean_, in16_,
                                                 psi_target ? target_ : nullptr);
     return cuda(cudaGetLastError(), "k_features");
 }
 
-int UNet::forward(float *pred)
+int UNet::forward(float *pred, bool fused)
 {
     cudaSetDevice(dev_);
     int rc = refresh_weights();
@@ -500,10 +541,15 @@ int UNet::forward(float *pred)
     C_(conv_any(32, 16, 0, p1_, wt_[1], params_ + boff_[1], e2_, g2_, 1, 1, err_dev_, s_))
     k_pool<<<gsize(g3_.nvox * 32), 256, 0, s_>>>(e2_, p2_, g3_, 32);
     C_(conv_any(64, 32, 0, p2_, wt_[2], params_ + boff_[2], b3_, g3_, 1, 1, err_dev_, s_))
-    k_up_concat<<<gsize(n2 * 96), 256, 0, s_>>>(b3_, e2_, c2_, g2_, 64, 32);
-    C_(conv_any(32, 96, 0, c2_, wt_[3], params_ + boff_[3], d2_, g2_, 1, 1, err_dev_, s_))
-    k_up_concat<<<gsize(n1 * 48), 256, 0, s_>>>(d2_, e1_, c1_, g1_, 32, 16);
-    C_(conv_any(16, 48, 0, c1_, wt_[4], params_ + boff_[4], d1_, g1_, 1, 1, err_dev_, s_))
+    if (fused) {  // inference: the decoder convolutions read [up(low), skip] directly
+        C_((launch_conv_concat<32, 96, 64>(b3_, e2_, wt_[3], params_ + boff_[3], d2_, g2_, err_dev_, s_)))
+        C_((launch_conv_concat<16, 48, 32>(d2_, e1_, wt_[4], params_ + boff_[4], d1_, g1_, err_dev_, s_)))
+    } else {  // training: the concatenations are kept for the backward pass
+        k_up_concat<<<gsize(n2 * 12), 256, 0, s_>>>(b3_, e2_, c2_, g2_, 64, 32);
+        C_(conv_any(32, 96, 0, c2_, wt_[3], params_ + boff_[3], d2_, g2_, 1, 1, err_dev_, s_))
+        k_up_concat<<<gsize(n1 * 6), 256, 0, s_>>>(d2_, e1_, c1_, g1_, 32, 16);
+        C_(conv_any(16, 48, 0, c1_, wt_[4], params_ + boff_[4], d1_, g1_, 1, 1, err_dev_, s_))
+    }
     k_head<<<gsize(n1), 256, 0, s_>>>(d1_, params_ + whoff_, params_ + bhoff_, out_, n1);
     C_(cudaGetLastError())
     if (pred) C_(cudaMemcpyAsync(pred, out_, sizeof(float) * (size_t)n1, cudaMemcpyDeviceToDevice, s_))
@@ -572,7 +618,7 @@ int UNet::train_step(float lr, double *loss)
 
 int UNet::propose(const float *psi, float *out, float cap)
 {
-    int rc = forward(nullptr);
+    int rc = forward(nullptr, true);
     if (rc != MVR_OK) return rc;
     k_propose<<<gsize(g1_.nvox), 256, 0, s_>>>(psi, out_, out, g1_.nvox, cap);
     if ((rc = cuda(cudaGetLastError(), "k_propose")) != MVR_OK) return rc;

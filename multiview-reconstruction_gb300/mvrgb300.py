@@ -45,7 +45,8 @@ EXPORTS = [
     "mvr_decon_get_max", "mvr_decon_get_weights", "mvr_decon_psi_device", "mvr_decon_synchronize",
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
     "mvr_kernel_name", "mvr_convolve_static", "mvr_decon_batch", "mvr_decon_likelihood",
-    "mvr_decon_set_graphs", "mvr_decon_graphs_captured", "mvr_decon_init_psi",
+    "mvr_decon_set_graphs", "mvr_decon_graphs_captured", "mvr_decon_init_psi", "mvr_fuse_group",
+    "mvr_fuse_last_error",
     "mvr_unet_create", "mvr_unet_destroy", "mvr_unet_last_error", "mvr_unet_num_params", "mvr_unet_get_params",
     "mvr_unet_set_params", "mvr_unet_get_grads", "mvr_unet_set_input", "mvr_unet_forward", "mvr_unet_train_step",
     "mvr_unet_propose", "mvr_conv3d_tc", "mvr_conv3d_tc_wgrad", "mvr_conv3d_tc_last_error",
@@ -144,6 +145,8 @@ def load() -> C.CDLL:
     L.mvr_decon_batch.argtypes = [P]
     L.mvr_decon_set_graphs.argtypes = [P, C.c_int]
     L.mvr_decon_init_psi.argtypes = [P, C.c_int, C.c_double, P]
+    L.mvr_fuse_group.argtypes = [P, C.c_int, P, P, P, P, C.c_int, P]
+    L.mvr_fuse_last_error.restype = C.c_char_p
     L.mvr_decon_graphs_captured.argtypes = [P]
     L.mvr_decon_likelihood.argtypes = [P, P, P]
     L.mvr_unet_create.argtypes = [C.c_int, P, C.c_uint, C.c_int, C.POINTER(P)]
@@ -539,3 +542,35 @@ def device_info(device: int = 0) -> dict:
     return dict(count=L.getNumDevicesCUDA(), name=name.value.decode(), mem=L.getMemDeviceCUDA(device),
                 free=L.getFreeMemDeviceCUDA(device), major=L.getCUDAcomputeCapabilityMajorVersion(device),
                 minor=L.getCUDAcomputeCapabilityMinorVersion(device))
+
+
+class _FuseView(C.Structure):
+    _fields_ = [("img", C.c_void_p), ("dims", C.c_int * 3), ("model", C.c_double * 12), ("fusion_blend", C.c_int),
+                ("fusion_border", C.c_float * 3), ("fusion_range", C.c_float * 3), ("decon_blend", C.c_int),
+                ("decon_border", C.c_float * 3), ("decon_range", C.c_float * 3)]
+
+
+def fuse_group(views, bb_min, bb_dims, image_out_ptr: int, weight_out_ptr: int, device: int = 0, stream: int = 0):
+    """ProcessInputImages.fuseGroups for one group on the device.  views: dicts with
+    'img_ptr' (device float volume), 'dims' (x, y, z), 'model' (3 x 4 view -> world) and
+    optional 'fusion' / 'decon' blendings as (border xyz, range xyz).  Writes the fused image
+    and the summed deconvolution weight of the bounding box (device float volumes)."""
+    L = load()
+    arr = (_FuseView * len(views))()
+    for k, v in enumerate(views):
+        a = arr[k]
+        a.img = v["img_ptr"]
+        a.dims = (C.c_int * 3)(*v["dims"])
+        a.model = (C.c_double * 12)(*np.asarray(v["model"], dtype=np.float64).reshape(12))
+        for key, flag, border, rng in (("fusion", "fusion_blend", "fusion_border", "fusion_range"),
+                                       ("decon", "decon_blend", "decon_border", "decon_range")):
+            b = v.get(key)
+            setattr(a, flag, 0 if b is None else 1)
+            if b is not None:
+                setattr(a, border, (C.c_float * 3)(*b[0]))
+                setattr(a, rng, (C.c_float * 3)(*b[1]))
+    rc = L.mvr_fuse_group(C.cast(arr, C.c_void_p), len(views), (C.c_longlong * 3)(*bb_min), (C.c_int * 3)(*bb_dims),
+                          C.c_void_p(image_out_ptr), C.c_void_p(weight_out_ptr), device,
+                          C.c_void_p(stream) if stream else None)
+    if rc != OK:
+        raise MvrError(rc, L.mvr_fuse_last_error().decode())

@@ -315,3 +315,93 @@ def decon_run(psi, imgs, ws, k1s, k2s, block_size, iters, mul=False, lam=0.0, mi
     if rc != 0:
         raise ValueError("block size smaller than the doubled kernel")
     return (p64 if fp64 else p32), st
+
+
+# ---- input preparation (ProcessInputImages.fuseGroups) ----------------------------------
+
+def blending_lut():
+    """BlendingRealRandomAccess's static table (fusion/transformed/weights/
+    BlendingRealRandomAccess.java:38-47): d from 0 in steps of 0.001 accumulated in double,
+    entry (int)(d * 1000 + 0.5) = (cos((1 - d) pi) + 1) / 2."""
+    import math
+
+    lut = np.zeros(1001)
+    d = 0.0
+    while d <= 1.0001:
+        lut[int(d * 1000.0 + 0.5)] = (math.cos((1 - d) * math.pi) + 1) / 2
+        d = d + 0.001
+    return lut
+
+
+def blending_weight(loc, dims_xyz, border, rng, lut=None):
+    """BlendingRealRandomAccess.computeWeight (:96-125) on [0, dims - 1] at float32
+    locations loc[..., 3] (x, y, z), float arithmetic, the table product in double."""
+    lut = blending_lut() if lut is None else lut
+    loc = np.asarray(loc, dtype=np.float32)
+    w = np.ones(loc.shape[:-1], dtype=np.float32)
+    zero = np.zeros(loc.shape[:-1], dtype=bool)
+    tmps = []
+    for d in range(3):
+        l = loc[..., d]
+        a = l - np.float32(border[d])
+        b = (np.float32(dims_xyz[d] - 1) - l) - np.float32(border[d])
+        t = np.minimum(a, b)
+        zero |= t <= 0
+        tmps.append(t)
+    for d in range(3):
+        rel = tmps[d] / np.float32(rng[d])
+        use = rel < 1
+        idx = np.clip((rel.astype(np.float64) * 1000.0 + 0.5).astype(np.int64), 0, 1000)
+        w = np.where(use, (w.astype(np.float64) * lut[idx]).astype(np.float32), w)
+    return np.where(zero, np.float32(0), w)
+
+
+def _invert_affine(m):
+    m = np.asarray(m, dtype=np.float64).reshape(3, 4)
+    A = np.linalg.inv(m[:, :3])
+    return np.concatenate([A, -(A @ m[:, 3:4])], axis=1)
+
+
+def fuse_group(views, bb_min, bb_dims):
+    """ProcessInputImages.fuseGroups (deconvolution/util/ProcessInputImages.java:279-399)
+    for one group: each view (dict: img [z][y][x], model 3 x 4 view -> world, optional
+    'fusion' / 'decon' = (border xyz, range xyz)) is transformed into the bounding box with
+    linear interpolation, max(1, .) strictly inside the view and 0 outside
+    (TransformedInputRandomAccess.get, AbstractTransformedIntervalRandomAccess
+    .intersectsLinearInterpolation), weighted by its blending and averaged (FusedRandomAccess
+    .get); the deconvolution weight is the sum of the views' deconvolution blendings
+    (CombineWeightsSumRandomAccess.get).  Returns (image, weight) float32 [z][y][x]."""
+    nx, ny, nz = bb_dims
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    s = np.stack([x + bb_min[0], y + bb_min[1], z + bb_min[2]], axis=-1).astype(np.float64)
+    lut = blending_lut()
+    sumI = np.zeros(s.shape[:-1])
+    sumW = np.zeros(s.shape[:-1])
+    sumD = np.zeros(s.shape[:-1])
+    for v in views:
+        img = np.asarray(v["img"], dtype=np.float32)
+        dims = (img.shape[2], img.shape[1], img.shape[0])
+        inv = _invert_affine(v["model"])
+        t = s @ inv[:, :3].T + inv[:, 3]
+        tf = t.astype(np.float32)
+        wf = blending_weight(tf, dims, *v["fusion"], lut=lut) if v.get("fusion") else np.ones(s.shape[:-1], np.float32)
+        wd = blending_weight(tf, dims, *v["decon"], lut=lut) if v.get("decon") else np.ones(s.shape[:-1], np.float32)
+        sumD += wd.astype(np.float64)
+        inside = np.all((t > 0) & (t < np.array(dims, dtype=np.float64) - 1), axis=-1)
+        val = np.zeros(s.shape[:-1], dtype=np.float32)
+        ti = t[inside]
+        f0 = np.floor(ti).astype(np.int64)
+        fr = ti - f0
+        acc = np.zeros(len(ti), dtype=np.float32)
+        for c in range(8):
+            dx, dy, dz = c & 1, (c >> 1) & 1, c >> 2
+            wgt = ((fr[:, 0] if dx else 1 - fr[:, 0]) * (fr[:, 1] if dy else 1 - fr[:, 1]) *
+                   (fr[:, 2] if dz else 1 - fr[:, 2]))
+            vv = img[f0[:, 2] + dz, f0[:, 1] + dy, f0[:, 0] + dx].astype(np.float64)
+            acc = acc + (vv * wgt).astype(np.float32)
+        val[inside] = np.maximum(np.float32(1), acc)
+        use = wf != 0
+        sumI += np.where(use, val.astype(np.float64) * wf.astype(np.float64), 0.0)
+        sumW += np.where(use, wf.astype(np.float64), 0.0)
+    image = np.where(sumW > 0, sumI / np.where(sumW > 0, sumW, 1.0), 0.0).astype(np.float32)
+    return image, sumD.astype(np.float32)

@@ -102,3 +102,25 @@ def test_unet_training_lowers_the_loss():
         net.set_input(pd.data_ptr(), rd.data_ptr(), td.data_ptr())
         losses = [net.train_step(2e-3) for _ in range(60)]
     assert losses[-1] < 0.3 * losses[0], (losses[0], losses[-1])
+
+
+def test_fused_decoder_inference_equals_materialised_concat():
+    # propose() runs the decoder convolutions straight from [up(low), skip]; forward() builds
+    # the concatenated volumes first (as training needs them): the predictions agree exactly
+    rng = np.random.default_rng(5)
+    dims = (32, 24, 16)
+    net = M.UNet(2, dims, seed=3)
+    try:
+        shape = (2, dims[2], dims[1], dims[0])
+        psi = torch.from_numpy(rng.uniform(1, 50, shape).astype(np.float32)).cuda()
+        nxt = psi * torch.from_numpy(rng.uniform(0.9, 1.1, shape).astype(np.float32)).cuda()
+        pred = torch.empty_like(psi)
+        out = torch.empty_like(psi)
+        net.set_input(psi.data_ptr(), nxt.data_ptr())
+        net.forward(pred.data_ptr())
+        net.propose(psi.data_ptr(), out.data_ptr(), 0.5)
+        ref = psi * torch.exp(torch.clamp(pred, -0.5, 0.5))
+        assert torch.allclose(out, ref, rtol=1e-6, atol=0)
+        assert float(pred.abs().max()) > 0
+    finally:
+        net.close()

@@ -257,3 +257,32 @@ def test_psi_init_known_answers():
     sl = a[:, :, 6].astype(np.float64)
     assert abs(avg - 1.5 * sl.mean()) < 1e-9 and mx[1] == np.float32(2 * sl.max())
     assert np.all(psi == np.float32(avg))
+
+
+def test_fusion_known_answers():
+    # identity model, no blending: interior voxels are max(1, img); the view's border voxels
+    # are not strictly inside it and read the outside value 0 (intersectsLinearInterpolation)
+    rng = np.random.default_rng(0)
+    img = rng.uniform(0, 5, (6, 7, 8)).astype(np.float32)
+    ident = np.hstack([np.eye(3), np.zeros((3, 1))])
+    im, w = O.fuse_group([{"img": img, "model": ident}], (0, 0, 0), (8, 7, 6))
+    assert np.array_equal(im[1:-1, 1:-1, 1:-1], np.maximum(1, img[1:-1, 1:-1, 1:-1]))
+    assert im[0].max() == 0 and im[:, :, -1].max() == 0 and np.all(w == 1)
+    # a half-voxel shift interpolates linearly between neighbours
+    shift = ident.copy()
+    shift[0, 3] = -0.5
+    im, _ = O.fuse_group([{"img": img, "model": shift}], (0, 0, 0), (8, 7, 6))
+    mid = 0.5 * (img[2, 3, 3].astype(np.float64) + img[2, 3, 4])
+    assert abs(im[2, 3, 3] - max(1.0, mid)) < 1e-6
+    # blending: 0 within the border, (cos((1 - d) pi) + 1) / 2 over the range, 1 beyond
+    lut = O.blending_lut()
+    assert lut[0] == 0 and abs(lut[500] - 0.5) < 1e-12 and lut[1000] == 1
+    loc = np.array([[1.0, 20, 20], [2.0 + 5.0, 20, 20], [20, 20, 20]], dtype=np.float32)
+    wts = O.blending_weight(loc, (41, 41, 41), (2, 2, 2), (10, 10, 10))
+    assert wts[0] == 0 and abs(wts[1] - 0.5) < 1e-6 and wts[2] == 1
+    # two views with complementary blending average with their weights; the deconvolution
+    # weight is the plain sum
+    im, w = O.fuse_group([{"img": img, "model": ident}, {"img": 3 * img, "model": ident}], (0, 0, 0), (8, 7, 6))
+    assert np.allclose(im[1:-1, 1:-1, 1:-1], 0.5 * (np.maximum(1, img) + np.maximum(1, 3 * img))[1:-1, 1:-1, 1:-1],
+                       rtol=1e-6)
+    assert np.all(w == 2)
