@@ -102,11 +102,18 @@ struct WeightPtrs {
 __global__ void k_normalize_weights(WeightPtrs wp, int nv, long long n, double osem, int smooth, float maxDiffRange,
                                     float scalingRange)
 {
+    // the double operations of the reference are kept where they round (the sum and the
+    // division); min(1, w) is exact in float, and the OSEM factor 1 needs no product
+    const bool osem_one = osem == 1.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         double sumW = 0.0;
-        for (int v = 0; v < nv; ++v) sumW += fmin(1.0, (double)wp.raw[v][i]);
+        for (int v = 0; v < nv; ++v) sumW += (double)fminf(1.0f, wp.raw[v][i]);
         for (int v = 0; v < nv; ++v) {
-            const float my = (float)fmin(1.0, (double)wp.raw[v][i]);
+            const float my = fminf(1.0f, wp.raw[v][i]);
+            if (!smooth && osem_one) {
+                wp.out[v][i] = sumW > 1 ? (float)((double)my / sumW) : my;
+                continue;
+            }
             double r;
             if (smooth) {
                 float s;
