@@ -304,6 +304,183 @@ __global__ void __launch_bounds__(128) k_conv3d_brick(const __nv_bfloat16 *__res
     if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
+// The same convolution with no per-tap copies at all: the output tile is a brick of 8 x 16 x 1
+// voxels (x, y, z), row r = x + 8 y, and the input halo (10 x 18 x 3 voxels) is stored in
+// shared memory "K-group major": the 16-byte chunk of channels 8j..8j+7 of halo voxel
+// h = hx + 10 hy + 180 hz at byte j * LBO + 16 h.  Eight x-consecutive halo voxels then form
+// one canonical core matrix (8 rows x 16 bytes), the next y line of the brick is 10 rows
+// (160 bytes) further, and the A operand of tap (dx, dy, dz) is the same layout started
+// 16 ((1 + dx) + 10 (1 + dy) + 180 (1 + dz)) bytes later: one shared-memory descriptor per
+// tap over the halo loaded once.  B (all taps of the weights, canonical K-major per tap) is
+// staged in chunks of G taps through two buffers.
+constexpr int kShX = 8, kShY = 16;                     // brick
+constexpr int kShHX = kShX + 2, kShHY = kShY + 2, kShHZ = 3;
+constexpr int kShRows = kShHX * kShHY * kShHZ;         // 540 halo voxels
+constexpr int kShLbo = (kShRows + 1) * 16;             // K-group stride (one padding row: distinct banks)
+
+template <int N, int C>
+__host__ __device__ constexpr size_t shift_halo_bytes()
+{
+    return ((size_t)C / 8 * kShLbo + 1023) / 1024 * 1024;  // B starts 1 KB aligned
+}
+
+// taps of B per staged chunk: all 27 in one buffer when they fit next to the halo in
+// 220 KB, else chunks of 9, else of 3, through two buffers
+template <int N, int C>
+__host__ __device__ constexpr int shift_taps_per_chunk()
+{
+    return (shift_halo_bytes<N, C>() + 27 * (size_t)N * C * 2 <= 220 * 1024)      ? 27
+           : (shift_halo_bytes<N, C>() + 2 * 9 * (size_t)N * C * 2 <= 220 * 1024) ? 9
+                                                                                   : 3;
+}
+
+template <int N, int C>
+__host__ __device__ constexpr size_t conv_shift_smem()
+{
+    constexpr int G = shift_taps_per_chunk<N, C>();
+    return shift_halo_bytes<N, C>() + (G == 27 ? 1 : 2) * (size_t)G * N * C * 2;
+}
+
+template <int N, int C, int OUT_MODE, int CU = 0>
+__global__ void __launch_bounds__(128) k_conv3d_shift(const __nv_bfloat16 *__restrict__ act,
+                                                      const __nv_bfloat16 *__restrict__ wk,
+                                                      const float *__restrict__ bias, void *out, ConvGeom g, int sign,
+                                                      int relu, int *err, const __nv_bfloat16 *__restrict__ act2 = nullptr)
+{
+    static_assert(N % 16 == 0 && N <= 256 && C % 16 == 0 && C <= 128, "tile shape");
+    static_assert(CU % 8 == 0 && CU < C, "concatenated channel split");
+    constexpr int G = shift_taps_per_chunk<N, C>(), NCH = 27 / G;
+    constexpr int B_TAP = N * C * 2, B_BYTES = G * B_TAP;
+    constexpr size_t H_BYTES = shift_halo_bytes<N, C>();
+    constexpr int CH = C / 8;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *halo = smem;
+    uint8_t *sB[2] = {smem + H_BYTES, smem + H_BYTES + (NCH > 1 ? B_BYTES : 0)};
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tbase;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    constexpr uint32_t ncols = TmemCols<N>::value;
+    if (warp == 0) tc::tmem_alloc(&tbase, ncols);
+    if (tid == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    const int nbx = (g.W + kShX - 1) / kShX, nby = (g.H + kShY - 1) / kShY;
+    long long q = blockIdx.x;
+    const int ibx = (int)(q % nbx);
+    q /= nbx;
+    const int iby = (int)(q % nby);
+    q /= nby;
+    const int z0 = (int)(q % g.D);
+    const int b = (int)(q / g.D);
+    const int x0 = ibx * kShX, y0 = iby * kShY;
+    // halo, channel chunk fastest (coalesced reads), zero outside the volume
+    for (int k = tid; k < kShRows * CH; k += 128) {
+        const int h = k / CH, j = k - h * CH;
+        const int hx = h % kShHX, hy = (h / kShHX) % kShHY, hz = h / (kShHX * kShHY);
+        const int xx = x0 - 1 + hx, yy = y0 - 1 + hy, zz = z0 - 1 + hz;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (xx >= 0 && yy >= 0 && zz >= 0 && xx < g.W && yy < g.H && zz < g.D) {
+            if constexpr (CU == 0) {
+                v = __ldg(reinterpret_cast<const uint4 *>(act + ((((long long)b * g.D + zz) * g.H + yy) * g.W + xx) * C) + j);
+            } else if (j < CU / 8) {
+                const long long lv = (((long long)b * (g.D / 2) + zz / 2) * (g.H / 2) + yy / 2) * (g.W / 2) + xx / 2;
+                v = __ldg(reinterpret_cast<const uint4 *>(act + lv * CU) + j);
+            } else {
+                const long long hv2 = (((long long)b * g.D + zz) * g.H + yy) * g.W + xx;
+                v = __ldg(reinterpret_cast<const uint4 *>(act2 + hv2 * (C - CU)) + (j - CU / 8));
+            }
+        }
+        *reinterpret_cast<uint4 *>(halo + (size_t)j * kShLbo + 16 * h) = v;
+    }
+    // B chunk c (taps G c .. G c + G - 1) into buffer `buf`, canonical K-major per tap
+    auto load_b = [&](int c, int buf) {
+        for (int s = tid; s < G * N * CH; s += 128) {
+            const int tt = s / (N * CH), rem = s - tt * (N * CH), r = rem / CH, j = rem - r * CH;
+            const uint4 v = __ldg(reinterpret_cast<const uint4 *>(wk + ((long long)r * 27 + G * c + tt) * C) + j);
+            *reinterpret_cast<uint4 *>(sB[buf] + tt * B_TAP + tc::core_offset(r, 8 * j, C)) = v;
+        }
+    };
+    load_b(0, 0);
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tbase;
+    const uint32_t idesc = tc::idesc_bf16(128, N);
+    const uint32_t hbase = tc::smem_u32(halo);
+    bool ok = true;
+    uint32_t uses[2] = {0, 0};
+    for (int c = 0; c < NCH; ++c) {
+        const int buf = c & 1;
+        if (tid == 0 && ok) {
+            tc::fence_after_sync();
+            for (int tt = 0; tt < G; ++tt) {
+                const int t = G * c + tt;
+                const int dz = (t / 9 - 1) * sign, dy = ((t / 3) % 3 - 1) * sign, dx = (t % 3 - 1) * sign;
+                const uint32_t a0 = hbase + 16u * (uint32_t)((1 + dx) + kShHX * (1 + dy) + kShHX * kShHY * (1 + dz));
+                const uint32_t b0 = tc::smem_u32(sB[buf] + tt * B_TAP);
+#pragma unroll
+                for (int k = 0; k < C / 16; ++k) {
+                    const uint64_t ad = tc::smem_desc(a0 + (uint32_t)(2 * k) * kShLbo, kShLbo, kShHX * 16);
+                    const uint64_t bd = tc::smem_desc(b0 + k * 256, 128, C * 16);
+                    tc::mma_bf16(tmem, ad, bd, idesc, (t > 0 || k > 0) ? 1 : 0);
+                }
+            }
+            tc::mma_commit(&mbar[buf]);
+        }
+        ++uses[buf];
+        if (c + 1 < NCH) {
+            const int nb = (c + 1) & 1;
+            if (c + 1 >= 2) ok = ok && tc::mbar_wait(&mbar[nb], (uses[nb] - 1) & 1, kTcWaitIter);
+            load_b(c + 1, nb);
+            tc::fence_proxy_async();
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+        }
+    }
+    for (int bb = 0; bb < 2; ++bb)
+        if (uses[bb]) ok = tc::mbar_wait(&mbar[bb], (uses[bb] - 1) & 1, kTcWaitIter) && ok;
+    tc::fence_after_sync();
+    __syncthreads();
+    const int lx = tid & 7, ly = tid >> 3;
+    const int x = x0 + lx, y = y0 + ly;
+    const bool rv = x < g.W && y < g.H;
+    const long long n = rv ? (((long long)b * g.D + z0) * g.H + y) * g.W + x : 0;
+    if (!ok) {
+        if (tid == 0) atomicExch(err, 1);
+    } else {
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+        for (int c0 = 0; c0 < N; c0 += 16) {
+            float v[16];
+            tc::tmem_ld16(trow + c0, v);
+            if (!rv) continue;
+            if (OUT_MODE == 0) {
+                __align__(16) __nv_bfloat16 o[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    float a = v[j] + (bias ? bias[c0 + j] : 0.0f);
+                    if (relu) a = fmaxf(a, 0.0f);
+                    o[j] = __float2bfloat16(a);
+                }
+                uint4 *op = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(out) + n * N + c0);
+                op[0] = reinterpret_cast<const uint4 *>(o)[0];
+                op[1] = reinterpret_cast<const uint4 *>(o)[1];
+            } else {
+                float4 *op = reinterpret_cast<float4 *>(reinterpret_cast<float *>(out) + n * N + c0);
+#pragma unroll
+                for (int j = 0; j < 4; ++j) op[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
 // wgrad: D[(t,ci) rows][co] over the voxels [blockIdx.y * vpc, +vpc), atomically added
 // to dW[co][t][ci] (FP32).
 template <int N, int C>

@@ -42,20 +42,21 @@ size_t conv_smem() { return 2 * (128 * C * 2 + N * C * 2); }
 template <int N>
 size_t wgrad_smem() { return 2 * (128 * 64 * 2 + N * 64 * 2); }
 
-// Forward and data-gradient convolutions run on 8 x 4 x 4 output bricks with the input
-// halo staged in shared memory (k_conv3d_brick); k_conv3d_tc (128 consecutive voxels,
-// gathered per tap) remains the reference form of the same product.
+// Forward and data-gradient convolutions run on 8 x 16 x 1 output bricks with the input
+// halo staged once in shared memory and one descriptor per tap (k_conv3d_shift);
+// k_conv3d_brick (halo, per-tap copies) and k_conv3d_tc (gathered per tap) are earlier
+// forms of the same product.
 template <int N, int C, int OUT>
 cudaError_t launch_conv(const bf16 *act, const bf16 *w, const float *bias, void *out, const ConvGeom &g, int sign,
                         int relu, int *err, cudaStream_t s)
 {
-    const size_t sm = conv_brick_smem<N, C>();
+    const size_t sm = conv_shift_smem<N, C>();
     cudaError_t e =
-        cudaFuncSetAttribute(k_conv3d_brick<N, C, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_conv3d_shift<N, C, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    const long long bricks = (long long)((g.W + kBrickX - 1) / kBrickX) * ((g.H + kBrickY - 1) / kBrickY) *
-                             ((g.D + kBrickZ - 1) / kBrickZ) * g.B;
-    k_conv3d_brick<N, C, OUT><<<(unsigned)bricks, 128, sm, s>>>(act, w, bias, out, g, sign, relu, err);
+    const long long bricks =
+        (long long)((g.W + kShX - 1) / kShX) * ((g.H + kShY - 1) / kShY) * g.D * g.B;
+    k_conv3d_shift<N, C, OUT><<<(unsigned)bricks, 128, sm, s>>>(act, w, bias, out, g, sign, relu, err);
     return cudaGetLastError();
 }
 
@@ -65,13 +66,13 @@ template <int N, int C, int CU>
 cudaError_t launch_conv_concat(const bf16 *low, const bf16 *skip, const bf16 *w, const float *bias, void *out,
                                const ConvGeom &g, int *err, cudaStream_t s)
 {
-    const size_t sm = conv_brick_smem<N, C>();
+    const size_t sm = conv_shift_smem<N, C>();
     cudaError_t e =
-        cudaFuncSetAttribute(k_conv3d_brick<N, C, 0, CU>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_conv3d_shift<N, C, 0, CU>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    const long long bricks = (long long)((g.W + kBrickX - 1) / kBrickX) * ((g.H + kBrickY - 1) / kBrickY) *
-                             ((g.D + kBrickZ - 1) / kBrickZ) * g.B;
-    k_conv3d_brick<N, C, 0, CU><<<(unsigned)bricks, 128, sm, s>>>(low, w, bias, out, g, 1, 1, err, skip);
+    const long long bricks =
+        (long long)((g.W + kShX - 1) / kShX) * ((g.H + kShY - 1) / kShY) * g.D * g.B;
+    k_conv3d_shift<N, C, 0, CU><<<(unsigned)bricks, 128, sm, s>>>(low, w, bias, out, g, 1, 1, err, skip);
     return cudaGetLastError();
 }
 
