@@ -796,12 +796,19 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const f
     ua.minI = min_value_;
     ua.maxI = maxI;
     ua.partials = partials_;
+    // without statistics the voxels outside the write region are not needed: the plane
+    // kernels skip their planes and rows
+    ua.prune = (!stats_dev && pl.xy) ? 1 : 0;
     const double nv = (double)pl.b[0] * pl.b[1] * pl.b[2];
     double bytes = 0.0;
     for (int i = 0; i < nb; ++i) {
         const BlockPlace &bp = bps[i];
-        const double neff = (double)(bp.whi[0] - bp.wlo[0]) * (bp.whi[1] - bp.wlo[1]) * (bp.whi[2] - bp.wlo[2]);
-        bytes += sizeof(V) * (double)pl.Pc + (sizeof(T) + 4.0) * nv + sizeof(T) * neff;
+        const double ez = bp.whi[2] - bp.wlo[2], ey = bp.whi[1] - bp.wlo[1];
+        const double neff = (double)(bp.whi[0] - bp.wlo[0]) * ey * ez;
+        if (ua.prune)
+            bytes += sizeof(V) * (double)pl.Pc * ez / pl.P[2] + (sizeof(T) + 4.0) * pl.b[0] * ey * ez + sizeof(T) * neff;
+        else
+            bytes += sizeof(V) * (double)pl.Pc + (sizeof(T) + 4.0) * nv + sizeof(T) * neff;
     }
     if (pl.xy) return launch_xy_update(pl, bms, nb, S0_, ua, EPI_SEQ, bytes, stats_dev);
     return launch_update(pl, bms, nb, S0_, ua, EPI_SEQ, bytes, stats_dev);
@@ -832,6 +839,7 @@ int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace
         if (nv > 1) MVR_TRY(reserve_prod(bvox * nb));
         ua.prod = prod_;
         ua.partials = partials_;
+        ua.prune = (!stats_dev && pl.xy) ? 1 : 0;
         const BlockMaps bms = block_maps(pl, bps, nb);
         if (!prev || std::memcmp(prev->P, pl.P, sizeof(pl.P)) != 0 || std::memcmp(prev->L, pl.L, sizeof(pl.L)) != 0 ||
             prev->xy != pl.xy) {

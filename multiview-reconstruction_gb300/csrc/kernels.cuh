@@ -482,6 +482,8 @@ struct UpdateArgs {
     float minI;
     float maxI;
     double *partials;     // per CTA {sum, max}
+    int prune;            // plane kernels: only the planes and rows of the write region, no
+                          // statistics (voxels outside the write region are discarded)
 };
 
 // The update epilogue of one block row (C2R result zz: natural-order packed values,

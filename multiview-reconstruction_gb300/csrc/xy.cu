@@ -2,6 +2,7 @@
 #include "xy.cuh"
 #include "xy_plane.cuh"
 
+#include <algorithm>
 #include <mutex>
 
 namespace mvr {
@@ -120,7 +121,14 @@ cudaError_t xy_update(int combo, int epi, float2 *S, const UpdateArgs &ua, const
                       long long Pc, const float2 *twx, const float2 *twy, cudaStream_t s)
 {
     set_limits();
-    const dim3 grid((unsigned)Pz, (unsigned)nb);
+    int planes = Pz;
+    if (ua.prune) {
+        if (epi == EPI_NLL || epi == EPI_STORE) return cudaErrorInvalidValue;
+        planes = 0;
+        for (int i = 0; i < nb; ++i) planes = std::max(planes, bms.m[i].whi[2] - bms.m[i].wlo[2]);
+        if (planes < 1) return cudaSuccess;
+    }
+    const dim3 grid((unsigned)planes, (unsigned)nb);
 #define XY_UPD(E)                                                                                               \
     XY_DISPATCH(combo, (k_xy_update<VX_, VY_, E><<<grid, XYShape<VX_, VY_>::NT, xy_smem_bytes<VX_, VY_>(), s>>>(S, ua, bms, \
                                                                                                     Pc, twx, twy)))

@@ -434,7 +434,11 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
     __shared__ double red_s[32], red_m[32];
     XYSmem<VX, VY> sm(smem_raw);
     const BlockMap &bm = bms.m[blockIdx.y];
-    const int z = blockIdx.x;
+    int z = blockIdx.x;
+    if (ua.prune) {  // the grid covers the deepest write region of the batch
+        z += bm.wlo[2];
+        if (z >= bm.whi[2]) return;
+    }
     float2 *Sp = S + (long long)blockIdx.y * Pc + (long long)z * SH::plane;
     const long long bvox = (long long)bm.b[0] * bm.b[1] * bm.b[2];
     if (ua.prod) ua.prod = reinterpret_cast<float *>(ua.prod) + (long long)blockIdx.y * bvox;
@@ -480,7 +484,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
         for (int r = 0; r < RX; ++r) {
             const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;
             const long long pb = sm.rowb[y], wb = sm.rowb2[y], ob = sm.rowb3[y];
-            if (pb < 0) continue;  // not a block row
+            if (pb < 0 || (ua.prune && ob == kNoRow)) continue;  // not a block row / not written
             float pv[VX][2], wv[VX][2];
 #pragma unroll
             for (int v = 0; v < VX; ++v)
@@ -523,11 +527,12 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
         tp_phase1<VX, SH::Py, SH::SR, 1, true, NT>(sm.A, sm.twx, 2);
         __syncthreads();
         const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = NT >> 5;
+        const int ylo = ua.prune ? bm.wlo[1] : 0, yhi = ua.prune ? bm.whi[1] : bm.b[1];
         if (z < bm.b[2])  // extension planes carry no block voxels
-            for (int y = warp; y < bm.b[1] && y < SH::Py; y += nw)
+            for (int y = ylo + warp; y < yhi && y < SH::Py; y += nw)
                 update_row<float, EPI>(sm.A + y * SH::SR, SH::m, bm, ua, y, z, lane, ksum, kcomp, kmax);
     }
-    if (EPI == EPI_SEQ || EPI == EPI_MUL_FINAL || EPI == EPI_NLL)
+    if ((EPI == EPI_SEQ || EPI == EPI_MUL_FINAL || EPI == EPI_NLL) && !ua.prune)
         stats_to_partials(ksum, kcomp, kmax, red_s, red_m, ua.partials, (long long)blockIdx.y * gridDim.x + blockIdx.x);
 }
 

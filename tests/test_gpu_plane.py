@@ -133,3 +133,24 @@ def test_volume_run_and_likelihood_plane_kernels():
     assert rel(res[True][0], res[False][0]) <= 1e-5
     assert np.allclose(res[True][1][:, 1], res[False][1][:, 1], rtol=1e-4, atol=1e-4)
     assert res[True][2] == pytest.approx(res[False][2], rel=1e-6)
+
+
+@pytest.mark.parametrize("mul", [False, True])
+def test_runs_without_statistics_write_the_same_volume(mul):
+    # without statistics the plane kernels update only the planes and rows of each
+    # block's write region; the volume they leave is bit-identical to the run that
+    # updates (and reduces) every block voxel
+    dims, kd = (200, 180, 150), (9, 9, 15)
+    ds = synthetic.make_dataset(dims, (0.0, 90.0), kd, n_beads=60, seed=9, side_lobes=False, weights="cosine")
+    res = {}
+    for stats in (True, False):
+        with plane_kernels(True):
+            d = M.Deconvolution(dims, 2, (128, 128, 64), mul=mul, psf_type=M.PSF_OPTIMIZATION_I, lam=0.006,
+                                weight_norm=M.WEIGHTS_HARD)
+            for v in range(2):
+                d.set_view(v, ds.images[v], ds.weights[v], ds.psfs[v])
+            d.prepare()
+            d.run_iterations(3, stats=stats)
+            res[stats] = d.get_psi()
+            d.close()
+    assert np.array_equal(res[True], res[False])
