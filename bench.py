@@ -391,6 +391,14 @@ def run_gb300(args, ws, rank, local):
                 "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
                 "traffic": traffic, "bytes_per_launch": dbytes / max(1, dlaunch),
                 "path_achieved": path_bytes / (total_ms / 1e3) / 1e9, "kernels": kernels}
+    # the whole path against the algorithmic byte model of one view-block, 28 N + 48 Pc
+    # (N block voxels, Pc = (bx / 2 + 1) by bz spectrum values), over the timed steps
+    bn = W.block[0] * W.block[1] * W.block[2]
+    bpc = (W.block[0] // 2 + 1) * W.block[1] * W.block[2]
+    b_it = W.view_blocks_per_iter() * (28.0 * bn + 48.0 * bpc)
+    roofline["model_bytes_per_iteration"] = b_it
+    roofline["model_achieved"] = b_it * args.steps / (ms / 1e3) / 1e9
+    roofline["model_frac"] = roofline["model_achieved"] / peak
 
     # ---- e2e: public C ABI with pinned host buffers, copies inside the timed region ----
     if args.no_e2e or on_dev:

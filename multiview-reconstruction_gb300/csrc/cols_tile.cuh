@@ -105,7 +105,8 @@ constexpr int kTColNP = 16;  // columns per tile
 template <int V, int MODE>
 __global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst, const float2 *__restrict__ Kh,
                                                   int Hx, long long estride, long long ostride, long long Pc,
-                                                  const float2 *__restrict__ twg, int gather, int nother)
+                                                  const float2 *__restrict__ twg, int gather, int nother, int rlo,
+                                                  int rhi)
 {
     constexpr int T = kTColT, NP = kTColNP, n = V * T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -204,8 +205,12 @@ __global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst
         for (int v = 0; v < V; ++v) A[(t + T * v) * NP + c] = a[v];
     }
     if (MODE != 0) __syncthreads();
-    if (plive)
-        for (int e = threadIdx.x; e < tot; e += 256) dst[coff + (long long)((e - threadIdx.x) / 256) * rstep] = A[e];
+    // rows [rlo, rhi) of the transformed axis are stored (all of them unless the caller
+    // reads only a sub-range)
+    if (plive) {
+        const long long cb = base + (long long)pc * pstride;
+        for (int e = threadIdx.x + rlo * NP; e < rhi * NP; e += 256) dst[cb + (long long)(e / NP) * estride] = A[e];
+    }
 }
 
 // data tile + twiddles (+ the K^ tile of MODE 2)

@@ -523,7 +523,8 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
 }
 
 template <typename T>
-int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh, int nb)
+int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh, int nb, int rlo,
+                           int rhi)
 {
     const int Hx = pl.Hx;
     long long estride, ostride;
@@ -549,7 +550,11 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
     const dim3 grid((unsigned)((Hx + NP - 1) / NP), (unsigned)nother, (unsigned)nb);
     const double cb = (double)sizeof(V) * (double)pl.Pc * nb;
     const int kind = mode == 2 ? KK_COLS_ZMUL : (mode == 1 ? KK_COLS_INV : KK_COLS_FWD);
-    MVR_TRY(prof_begin(kind, mode == 2 ? 3.0 * cb : 2.0 * cb));
+    const int nax = pl.P[axis];
+    if (rhi < 0 || rhi > nax || sizeof(T) != sizeof(float) || !(axis == 1 ? pl.tcy : pl.tcz)) rhi = nax;
+    if (rlo < 0 || rlo > rhi || rhi == nax) rlo = 0;
+    const double stored = (double)(rhi - rlo) / nax;
+    MVR_TRY(prof_begin(kind, mode == 2 ? (2.0 + stored) * cb : (1.0 + stored) * cb));
     const long long Pc = pl.Pc;
     const int wc = axis == 1 ? pl.wcy : pl.wcz;
     const int tc = axis == 1 ? pl.tcy : pl.tcz;
@@ -564,13 +569,13 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
             TILE_COLS(tc, {
                 if (mode == 0)
                     k_tcols<V_, 0><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw, gather,
-                                                                      nother);
+                                                                      nother, rlo, rhi);
                 else if (mode == 1)
                     k_tcols<V_, 1><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw, gather,
-                                                                      nother);
+                                                                      nother, rlo, rhi);
                 else
                     k_tcols<V_, 2><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw, gather,
-                                                                      nother);
+                                                                      nother, rlo, rhi);
             });
             MVR_LAUNCHED("k_tcols");
             return prof_end();
@@ -763,6 +768,17 @@ int Engine<T>::launch_xy_update(const Plan<T> &pl, const BlockMaps &bms, int nb,
     return fail(ERR_STATE, "plane kernels are FP32 only");
 }
 
+// The planes [zlo, zhi) holding every write region of a batch.
+inline void write_planes(const BlockPlace *bps, int nb, int &zlo, int &zhi)
+{
+    zlo = bps[0].wlo[2];
+    zhi = bps[0].whi[2];
+    for (int i = 1; i < nb; ++i) {
+        zlo = std::min(zlo, bps[i].wlo[2]);
+        zhi = std::max(zhi, bps[i].whi[2]);
+    }
+}
+
 template <typename T>
 int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const float *img, const float *w, float maxI,
                        double *stats_dev)
@@ -772,11 +788,13 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const f
     const long long nrows = (long long)pl.P[1] * pl.P[2];
     MVR_TRY(reserve(pl.Pc, (long long)pl.b[0] * pl.b[1] * pl.b[2], (nrows + pl.RP - 1) / pl.RP, nb));
     const BlockMaps bms = block_maps(pl, bps, nb);
+    int zlo = 0, zhi = -1;
+    if (!stats_dev && pl.xy) write_planes(bps, nb, zlo, zhi);
     if (pl.xy) {
         MVR_TRY(launch_xy_fwd(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
         MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb));
         MVR_TRY(launch_xy_ratio(pl, bms, nb, S0_, img));
-        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k2h, nb));
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k2h, nb, zlo, zhi));
     } else {
         MVR_TRY(launch_fwd_mirror(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
         MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
@@ -854,8 +872,10 @@ int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace
         prev = &pl;
         MVR_TRY(launch_cols(pl, 2, 2, S0_, S1_, pl.k1h, nb));
         if (pl.xy) {
+            int zlo = 0, zhi = -1;
+            if (!stats_dev) write_planes(bps, nb, zlo, zhi);
             MVR_TRY(launch_xy_ratio(pl, bms, nb, S1_, imgs[v]));
-            MVR_TRY(launch_cols(pl, 2, 2, S1_, S1_, pl.k2h, nb));
+            MVR_TRY(launch_cols(pl, 2, 2, S1_, S1_, pl.k2h, nb, zlo, zhi));
         } else {
             MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr, nb));
             MVR_TRY(launch_ratio(pl, bms, nb, S1_, imgs[v]));

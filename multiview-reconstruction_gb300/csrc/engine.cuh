@@ -135,7 +135,9 @@ private:
     int launch_xy_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img);
     int launch_xy_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const UpdateArgs &ua, int epi,
                          double bytes, double *stats_dev);
-    int launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh, int nb);
+    // rows [rlo, rhi) of the transformed axis are stored (rhi < 0: all; tile kernels only)
+    int launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh, int nb, int rlo = 0,
+                    int rhi = -1);
     int launch_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img);
     int launch_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const UpdateArgs &ua, int epi,
                       double bytes, double *stats_dev);
