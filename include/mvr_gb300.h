@@ -255,6 +255,44 @@ MVR_API int mvr_fuse_group(const mvr_fuse_view *views, int num_views, const long
                            float *image_out, float *weight_out, int device, void *stream);
 MVR_API const char *mvr_fuse_last_error(void);
 
+/* ---- PSF preparation (MV/process/psf, deconvolution/util/PSFPreparation.java:41-91) ------
+ * Device float volumes, x fastest, sizes {x, y, z}; synchronous on `stream`.
+ *
+ * mvr_psf_extract: PSFExtraction.extractPSFLocal (PSFExtraction.java:234-269) on the
+ * periodic extension of the image (the RandomAccessibleInterval constructors, :112-120):
+ * psf(p) = sum over the locations, in their order, of the linear interpolation of the image
+ * at p - psf_dims / 2 + location.  locations: host array of num_locations {x, y, z} doubles
+ * (0 locations: a zero PSF, hadDetections false). */
+MVR_API int mvr_psf_extract(const float *img, const long long img_dims[3], const double *locations, int num_locations,
+                            const int psf_dims[3], float *psf_out, int device, void *stream);
+/* The size of PSFExtraction.transformPSF's output (:367-409): the bounding box of the
+ * transformed PSF, (int) extent + 1, made odd.  model: row-packed 3 x 4. */
+MVR_API int mvr_psf_transformed_dims(const int dims[3], const double model[12], int out_dims[3]);
+/* PSFExtraction.getTransformedNormalizedPSF (:182-188): the PSF normalised to [0, 1]
+ * (normalize, :453-471; the input is not modified) and transformed with the view's model,
+ * its centre voxel dims / 2 kept at the output centre (transform, :411-451; linear
+ * interpolation, zero outside).  out_dims must equal mvr_psf_transformed_dims. */
+MVR_API int mvr_psf_transform_normalized(const float *psf, const int dims[3], const double model[12], float *out,
+                                         const int out_dims[3], int device, void *stream);
+/* PSFCombination.computeAverageImage (PSFCombination.java:74-138): the PSFs (1..64, dims
+ * num_psfs x {x, y, z}) centred and averaged on the largest (max_size 1) or smallest
+ * (max_size 0) size per axis, returned in out_dims; out holds that many voxels (at most the
+ * largest size on every axis). */
+MVR_API int mvr_psf_average(const float *const *psfs, const int *dims, int num_psfs, int max_size, float *out,
+                            int out_dims[3], int device, void *stream);
+/* PSFCombination.makeSameSize (:182-210): the PSF centred in `size`, extended with its minimum. */
+MVR_API int mvr_psf_make_same_size(const float *psf, const int dims[3], const int size[3], float *out, int device,
+                                   void *stream);
+/* PSFCombination.computeMaxProjection (:228-296): max (use_max 1) or min projection along
+ * axis dim (dim < 0: the smallest axis, returned in used_dim); the output keeps the other
+ * two axes in order. */
+MVR_API int mvr_psf_projection(const float *psf, const int dims[3], int dim, int use_max, float *out, int *used_dim,
+                               int device, void *stream);
+/* PSFExtraction.removeMinProjections (:190-229): for axis 0, 1, 2 in turn, subtract the min
+ * projection along that axis (in place). */
+MVR_API int mvr_psf_remove_min_projections(float *psf, const int dims[3], int device, void *stream);
+MVR_API const char *mvr_psf_last_error(void);
+
 /* ---- learned multi-iteration proposal (no counterpart in the reference) ---------------
  * A 3-level 3D U-Net (16/32/64 channels, 3x3x3 convolutions, BF16 weights and
  * activations, FP32 accumulation on the tcgen05 tensor cores) with its own forward and

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "../../include/mvr_gb300.h"
+#include "affine.cuh"
 
 namespace mvr {
 namespace {
@@ -66,23 +67,14 @@ __device__ __forceinline__ float blend_weight(const float *loc, const int *dims,
 }
 
 // Linear interpolation of a float volume at t (all eight neighbours exist: t is strictly
-// inside).  Weights in double, the value accumulated in float (the interpolator's FloatType
-// arithmetic).
+// inside), the interpolator of the reference's views (NLinearInterpolator3D order).
 __device__ __forceinline__ float trilinear(const float *__restrict__ img, const int *dims, const double *t)
 {
-    const int x0 = (int)floor(t[0]), y0 = (int)floor(t[1]), z0 = (int)floor(t[2]);
-    const double fx = t[0] - x0, fy = t[1] - y0, fz = t[2] - z0;
-    const long long sx = 1, sy = dims[0], sz = (long long)dims[0] * dims[1];
-    const long long base = z0 * sz + y0 * sy + x0;
-    float acc = 0.0f;
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-        const int dx = c & 1, dy = (c >> 1) & 1, dz = c >> 2;
-        const double w = (dx ? fx : 1.0 - fx) * (dy ? fy : 1.0 - fy) * (dz ? fz : 1.0 - fz);
-        const float v = __ldg(img + base + dz * sz + dy * sy + dx * sx);
-        acc = __fadd_rn(acc, (float)((double)v * w));
-    }
-    return acc;
+    const double f[3] = {floor(t[0]), floor(t[1]), floor(t[2])};
+    const double w[3] = {__dsub_rn(t[0], f[0]), __dsub_rn(t[1], f[1]), __dsub_rn(t[2], f[2])};
+    const long long sy = dims[0], sz = (long long)dims[0] * dims[1];
+    const float *p = img + (long long)f[2] * sz + (long long)f[1] * sy + (long long)f[0];
+    return nlinear3(w, [&](int dx, int dy, int dz) { return __ldg(p + dz * sz + dy * sy + dx); });
 }
 
 __global__ void k_fuse_group(FuseViews fv, long long bx, long long by, long long bz, int nx, int ny, int nz,
@@ -97,9 +89,9 @@ __global__ void k_fuse_group(FuseViews fv, long long bx, long long by, long long
         double sumI = 0.0, sumW = 0.0, sumD = 0.0;
         for (int k = 0; k < fv.n; ++k) {
             const FuseView &v = fv.v[k];
-            const double *m = v.inv;
-            const double t[3] = {s0 * m[0] + s1 * m[1] + s2 * m[2] + m[3], s0 * m[4] + s1 * m[5] + s2 * m[6] + m[7],
-                                 s0 * m[8] + s1 * m[9] + s2 * m[10] + m[11]};
+            const double sp[3] = {s0, s1, s2};
+            double t[3];
+            apply_affine(v.inv, sp, t);
             const float tf[3] = {(float)t[0], (float)t[1], (float)t[2]};
             const float wf = v.fblend ? blend_weight(tf, v.dims, v.fb, v.fr, lut) : 1.0f;
             const float wd = v.dblend ? blend_weight(tf, v.dims, v.db, v.dr, lut) : 1.0f;
@@ -115,24 +107,6 @@ __global__ void k_fuse_group(FuseViews fv, long long bx, long long by, long long
         out_img[i] = sumW > 0.0 ? (float)(sumI / sumW) : 0.0f;
         out_w[i] = (float)sumD;
     }
-}
-
-bool invert_affine(const double *m, double *inv)
-{
-    const double a = m[0], b = m[1], c = m[2], d = m[4], e = m[5], f = m[6], g = m[8], h = m[9], k = m[10];
-    const double det = a * (e * k - f * h) - b * (d * k - f * g) + c * (d * h - e * g);
-    if (det == 0.0 || !std::isfinite(det)) return false;
-    const double r = 1.0 / det;
-    const double i00 = (e * k - f * h) * r, i01 = (c * h - b * k) * r, i02 = (b * f - c * e) * r;
-    const double i10 = (f * g - d * k) * r, i11 = (a * k - c * g) * r, i12 = (c * d - a * f) * r;
-    const double i20 = (d * h - e * g) * r, i21 = (b * g - a * h) * r, i22 = (a * e - b * d) * r;
-    inv[0] = i00, inv[1] = i01, inv[2] = i02;
-    inv[4] = i10, inv[5] = i11, inv[6] = i12;
-    inv[8] = i20, inv[9] = i21, inv[10] = i22;
-    inv[3] = -(i00 * m[3] + i01 * m[7] + i02 * m[11]);
-    inv[7] = -(i10 * m[3] + i11 * m[7] + i12 * m[11]);
-    inv[11] = -(i20 * m[3] + i21 * m[7] + i22 * m[11]);
-    return true;
 }
 
 thread_local std::string g_fuse_err;

@@ -46,7 +46,9 @@ EXPORTS = [
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
     "mvr_kernel_name", "mvr_convolve_static", "mvr_decon_batch", "mvr_decon_likelihood",
     "mvr_decon_set_graphs", "mvr_decon_graphs_captured", "mvr_decon_init_psi", "mvr_fuse_group",
-    "mvr_fuse_last_error",
+    "mvr_fuse_last_error", "mvr_psf_extract", "mvr_psf_transformed_dims", "mvr_psf_transform_normalized",
+    "mvr_psf_average", "mvr_psf_make_same_size", "mvr_psf_projection", "mvr_psf_remove_min_projections",
+    "mvr_psf_last_error",
     "mvr_unet_create", "mvr_unet_destroy", "mvr_unet_last_error", "mvr_unet_num_params", "mvr_unet_get_params",
     "mvr_unet_set_params", "mvr_unet_get_grads", "mvr_unet_set_input", "mvr_unet_forward", "mvr_unet_train_step",
     "mvr_unet_propose", "mvr_conv3d_tc", "mvr_conv3d_tc_wgrad", "mvr_conv3d_tc_last_error",
@@ -147,6 +149,14 @@ def load() -> C.CDLL:
     L.mvr_decon_init_psi.argtypes = [P, C.c_int, C.c_double, P]
     L.mvr_fuse_group.argtypes = [P, C.c_int, P, P, P, P, C.c_int, P]
     L.mvr_fuse_last_error.restype = C.c_char_p
+    L.mvr_psf_extract.argtypes = [P, P, P, C.c_int, P, P, C.c_int, P]
+    L.mvr_psf_transformed_dims.argtypes = [P, P, P]
+    L.mvr_psf_transform_normalized.argtypes = [P, P, P, P, P, C.c_int, P]
+    L.mvr_psf_average.argtypes = [P, P, C.c_int, C.c_int, P, P, C.c_int, P]
+    L.mvr_psf_make_same_size.argtypes = [P, P, P, P, C.c_int, P]
+    L.mvr_psf_projection.argtypes = [P, P, C.c_int, C.c_int, P, P, C.c_int, P]
+    L.mvr_psf_remove_min_projections.argtypes = [P, P, C.c_int, P]
+    L.mvr_psf_last_error.restype = C.c_char_p
     L.mvr_decon_graphs_captured.argtypes = [P]
     L.mvr_decon_likelihood.argtypes = [P, P, P]
     L.mvr_unet_create.argtypes = [C.c_int, P, C.c_uint, C.c_int, C.POINTER(P)]
@@ -574,3 +584,118 @@ def fuse_group(views, bb_min, bb_dims, image_out_ptr: int, weight_out_ptr: int, 
                           C.c_void_p(stream) if stream else None)
     if rc != OK:
         raise MvrError(rc, L.mvr_fuse_last_error().decode())
+
+
+# ---- PSF preparation (MV/process/psf, deconvolution/util/PSFPreparation.java) -----------
+# Pointer arguments are device float volumes [z][y][x]; sizes are (x, y, z).
+
+def _psf_check(rc):
+    if rc != OK:
+        raise MvrError(rc, load().mvr_psf_last_error().decode())
+
+
+def _sp(stream):
+    return C.c_void_p(stream) if stream else None
+
+
+def psf_extract(img_ptr: int, img_dims, locations, psf_dims, psf_out_ptr: int, device: int = 0, stream: int = 0):
+    """PSFExtraction.extractPSFLocal on the periodic image: the sum over the locations
+    (n x 3 array of x, y, z) of the linearly interpolated neighbourhoods of size psf_dims."""
+    loc = np.ascontiguousarray(np.asarray(locations, dtype=np.float64).reshape(-1, 3))
+    _psf_check(load().mvr_psf_extract(C.c_void_p(img_ptr), (C.c_longlong * 3)(*img_dims), _p(loc) if len(loc) else None,
+                                      len(loc), (C.c_int * 3)(*psf_dims), C.c_void_p(psf_out_ptr), device,
+                                      _sp(stream)))
+
+
+def psf_transformed_dims(dims, model):
+    """Size (x, y, z) of PSFExtraction.transformPSF's output for the 3 x 4 model."""
+    out = (C.c_int * 3)()
+    m = np.ascontiguousarray(np.asarray(model, dtype=np.float64).reshape(12))
+    _psf_check(load().mvr_psf_transformed_dims((C.c_int * 3)(*dims), _p(m), out))
+    return tuple(out)
+
+
+def psf_transform_normalized(psf_ptr: int, dims, model, out_ptr: int, out_dims, device: int = 0, stream: int = 0):
+    """PSFExtraction.getTransformedNormalizedPSF (the input PSF is left unchanged)."""
+    m = np.ascontiguousarray(np.asarray(model, dtype=np.float64).reshape(12))
+    _psf_check(load().mvr_psf_transform_normalized(C.c_void_p(psf_ptr), (C.c_int * 3)(*dims), _p(m),
+                                                   C.c_void_p(out_ptr), (C.c_int * 3)(*out_dims), device,
+                                                   _sp(stream)))
+
+
+def psf_average_dims(dims_list, max_size: bool):
+    f = max if max_size else min
+    return tuple(f(int(d[k]) for d in dims_list) for k in range(3))
+
+
+def psf_average(psf_ptrs, dims_list, max_size: bool, out_ptr: int, device: int = 0, stream: int = 0):
+    """PSFCombination.computeAverageImage; returns the output size (x, y, z)."""
+    n = len(psf_ptrs)
+    ptrs = (C.c_void_p * n)(*psf_ptrs)
+    dims = (C.c_int * (3 * n))(*[int(v) for d in dims_list for v in d])
+    out = (C.c_int * 3)()
+    _psf_check(load().mvr_psf_average(C.cast(ptrs, C.c_void_p), C.cast(dims, C.c_void_p), n, 1 if max_size else 0,
+                                      C.c_void_p(out_ptr), out, device, _sp(stream)))
+    return tuple(out)
+
+
+def psf_make_same_size(psf_ptr: int, dims, size, out_ptr: int, device: int = 0, stream: int = 0):
+    """PSFCombination.makeSameSize."""
+    _psf_check(load().mvr_psf_make_same_size(C.c_void_p(psf_ptr), (C.c_int * 3)(*dims), (C.c_int * 3)(*size),
+                                             C.c_void_p(out_ptr), device, _sp(stream)))
+
+
+def psf_projection(psf_ptr: int, dims, dim: int, use_max: bool, out_ptr: int, device: int = 0, stream: int = 0):
+    """PSFCombination.computeProjection; returns the projected axis."""
+    used = C.c_int(-1)
+    _psf_check(load().mvr_psf_projection(C.c_void_p(psf_ptr), (C.c_int * 3)(*dims), dim, 1 if use_max else 0,
+                                         C.c_void_p(out_ptr), C.byref(used), device, _sp(stream)))
+    return used.value
+
+
+def psf_remove_min_projections(psf_ptr: int, dims, device: int = 0, stream: int = 0):
+    """PSFExtraction.removeMinProjections, in place."""
+    _psf_check(load().mvr_psf_remove_min_projections(C.c_void_p(psf_ptr), (C.c_int * 3)(*dims), device, _sp(stream)))
+
+
+def load_group_transform_psfs(groups, same_size_for_all: bool = True, device: int = 0):
+    """PSFPreparation.loadGroupTransformPSFs (deconvolution/util/PSFPreparation.java:41-91) on
+    the device.  groups: list of groups, each a list of (psf [z][y][x] float array, 3 x 4 model
+    of its view, downsampling included).  Per group the views' normalised transformed PSFs
+    are averaged on their smallest common size; with same_size_for_all every group's PSF
+    is then centred in the largest size (extended with its minimum).  Returns float32
+    arrays [z][y][x], one per group."""
+    import torch
+
+    dev = f"cuda:{device}"
+
+    def vol(d):
+        return torch.empty((d[2], d[1], d[0]), dtype=torch.float32, device=dev)
+
+    out = []
+    for grp in groups:
+        tr, dims = [], []
+        for psf, model in grp:
+            p = torch.from_numpy(np.ascontiguousarray(psf, dtype=np.float32)).to(dev)
+            pd = (p.shape[2], p.shape[1], p.shape[0])
+            td = psf_transformed_dims(pd, model)
+            t = vol(td)
+            psf_transform_normalized(p.data_ptr(), pd, model, t.data_ptr(), td, device)
+            tr.append(t)
+            dims.append(td)
+        ad = psf_average_dims(dims, False)
+        avg = vol(ad)
+        psf_average([t.data_ptr() for t in tr], dims, False, avg.data_ptr(), device)
+        out.append(avg)
+    if same_size_for_all:
+        mx = tuple(max(a.shape[2 - k] for a in out) for k in range(3))
+        res = []
+        for a in out:
+            d = (a.shape[2], a.shape[1], a.shape[0])
+            r = vol(mx)
+            psf_make_same_size(a.data_ptr(), d, mx, r.data_ptr(), device)
+            res.append(r)
+        out = res
+    torch.cuda.synchronize(device)
+    return [a.cpu().numpy() for a in out]
+

@@ -357,9 +357,51 @@ def blending_weight(loc, dims_xyz, border, rng, lut=None):
 
 
 def _invert_affine(m):
+    """Inverse of a 3 x 4 affine transform by the adjugate of its 3 x 3 part."""
     m = np.asarray(m, dtype=np.float64).reshape(3, 4)
-    A = np.linalg.inv(m[:, :3])
-    return np.concatenate([A, -(A @ m[:, 3:4])], axis=1)
+    a, b, c, d = m[0, 0], m[0, 1], m[0, 2], m[0, 3]
+    e, f, g, h = m[1, 0], m[1, 1], m[1, 2], m[1, 3]
+    i, j, k, l = m[2, 0], m[2, 1], m[2, 2], m[2, 3]
+    det = a * (f * k - g * j) - b * (e * k - g * i) + c * (e * j - f * i)
+    r = 1.0 / det
+    A = np.array([[(f * k - g * j) * r, (c * j - b * k) * r, (b * g - c * f) * r],
+                  [(g * i - e * k) * r, (a * k - c * i) * r, (c * e - a * g) * r],
+                  [(e * j - f * i) * r, (b * i - a * j) * r, (a * f - b * e) * r]])
+    t = np.array([-(A[q, 0] * d + A[q, 1] * h + A[q, 2] * l) for q in range(3)])
+    return np.concatenate([A, t.reshape(3, 1)], axis=1)
+
+
+def apply_affine(m, s):
+    """AffineTransform3D.apply (imglib2-realtransform) on s[..., 3] (x, y, z): each output
+    coordinate s0 m0 + s1 m1 + s2 m2 + m3, summed left to right in double."""
+    m = np.asarray(m, dtype=np.float64).reshape(3, 4)
+    s = np.asarray(s, dtype=np.float64)
+    return np.stack([((s[..., 0] * m[r, 0] + s[..., 1] * m[r, 1]) + s[..., 2] * m[r, 2]) + m[r, 3]
+                     for r in range(3)], axis=-1)
+
+
+_GRAY = ((0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 1, 1), (1, 1, 1), (1, 0, 1), (0, 0, 1))
+
+
+def nlinear(get, t):
+    """Linear interpolation as imglib2's NLinearInterpolator3D.get (imglib2 8.0.0, the
+    interpolator of Views.interpolate with NLinearInterpolatorFactory): t[..., 3] double
+    positions (x, y, z); get(ix, iy, iz) returns float32 values of the extended image.
+    Weights in double (t - floor t, products x * y * z), each corner's value times its
+    weight rounded to float, the corners summed in float in the Gray-code order 000, 100,
+    110, 010, 011, 111, 101, 001."""
+    t = np.asarray(t, dtype=np.float64)
+    f = np.floor(t)
+    w = t - f
+    u = 1.0 - w
+    fi = f.astype(np.int64)
+    acc = None
+    for dx, dy, dz in _GRAY:
+        wgt = ((w[..., 0] if dx else u[..., 0]) * (w[..., 1] if dy else u[..., 1])) * (w[..., 2] if dz else u[..., 2])
+        v = np.asarray(get(fi[..., 0] + dx, fi[..., 1] + dy, fi[..., 2] + dz), dtype=np.float32)
+        term = (v.astype(np.float64) * wgt).astype(np.float32)
+        acc = term if acc is None else (acc + term).astype(np.float32)
+    return acc
 
 
 def fuse_group(views, bb_min, bb_dims):
@@ -382,26 +424,166 @@ def fuse_group(views, bb_min, bb_dims):
         img = np.asarray(v["img"], dtype=np.float32)
         dims = (img.shape[2], img.shape[1], img.shape[0])
         inv = _invert_affine(v["model"])
-        t = s @ inv[:, :3].T + inv[:, 3]
+        t = apply_affine(inv, s)
         tf = t.astype(np.float32)
         wf = blending_weight(tf, dims, *v["fusion"], lut=lut) if v.get("fusion") else np.ones(s.shape[:-1], np.float32)
         wd = blending_weight(tf, dims, *v["decon"], lut=lut) if v.get("decon") else np.ones(s.shape[:-1], np.float32)
         sumD += wd.astype(np.float64)
         inside = np.all((t > 0) & (t < np.array(dims, dtype=np.float64) - 1), axis=-1)
         val = np.zeros(s.shape[:-1], dtype=np.float32)
-        ti = t[inside]
-        f0 = np.floor(ti).astype(np.int64)
-        fr = ti - f0
-        acc = np.zeros(len(ti), dtype=np.float32)
-        for c in range(8):
-            dx, dy, dz = c & 1, (c >> 1) & 1, c >> 2
-            wgt = ((fr[:, 0] if dx else 1 - fr[:, 0]) * (fr[:, 1] if dy else 1 - fr[:, 1]) *
-                   (fr[:, 2] if dz else 1 - fr[:, 2]))
-            vv = img[f0[:, 2] + dz, f0[:, 1] + dy, f0[:, 0] + dx].astype(np.float64)
-            acc = acc + (vv * wgt).astype(np.float32)
+        acc = nlinear(lambda ix, iy, iz: img[iz, iy, ix], t[inside])
         val[inside] = np.maximum(np.float32(1), acc)
         use = wf != 0
         sumI += np.where(use, val.astype(np.float64) * wf.astype(np.float64), 0.0)
         sumW += np.where(use, wf.astype(np.float64), 0.0)
     image = np.where(sumW > 0, sumI / np.where(sumW > 0, sumW, 1.0), 0.0).astype(np.float32)
     return image, sumD.astype(np.float32)
+
+
+# ---- PSF preparation (MV/process/psf, deconvolution/util/PSFPreparation.java) -------------
+# Arrays [z][y][x] float32, sizes (x, y, z), models row-packed 3 x 4.
+
+def _xyz(a):
+    return (a.shape[2], a.shape[1], a.shape[0])
+
+
+def _grid(size):
+    z, y, x = np.meshgrid(np.arange(size[2]), np.arange(size[1]), np.arange(size[0]), indexing="ij")
+    return x, y, z
+
+
+def psf_extract(img, locations, size):
+    """PSFExtraction.extractPSFLocal (MV/process/psf/PSFExtraction.java:234-269) on the
+    periodic extension of img (the RandomAccessibleInterval constructors, :112-120): for each
+    location l in order, every PSF voxel p adds the linear interpolation of the image at
+    p - size / 2 + l (psf + value in double, stored as float)."""
+    img = np.asarray(img, dtype=np.float32)
+    D = _xyz(img)
+    x, y, z = _grid(size)
+    rel = np.stack([x - size[0] // 2, y - size[1] // 2, z - size[2] // 2], axis=-1).astype(np.float64)
+
+    def get(ix, iy, iz):
+        return img[np.mod(iz, D[2]), np.mod(iy, D[1]), np.mod(ix, D[0])]
+
+    psf = np.zeros((size[2], size[1], size[0]), dtype=np.float32)
+    for l in np.asarray(locations, dtype=np.float64).reshape(-1, 3):
+        v = nlinear(get, rel + l)
+        psf = (psf.astype(np.float64) + v.astype(np.float64)).astype(np.float32)
+    return psf
+
+
+def psf_normalize(psf):
+    """PSFExtraction.normalize (:453-471): (v - min) / (max - min) in double, stored as float."""
+    a = np.asarray(psf, dtype=np.float32).astype(np.float64)
+    mn, mx = a.min(), a.max()
+    with np.errstate(invalid="ignore", divide="ignore"):
+        return ((a - mn) / (mx - mn)).astype(np.float32)
+
+
+def psf_transformed_geometry(dims, model):
+    """transformPSF's output size and offset (:367-409): the bounding box of the transformed
+    corners of [0, dims - 1] (AffineTransform3D.estimateBounds), size (int) extent + 1 made
+    odd, offset = model(dims / 2) - size / 2."""
+    corners = np.array([[(c & 1) * (dims[0] - 1), ((c >> 1) & 1) * (dims[1] - 1), ((c >> 2) & 1) * (dims[2] - 1)]
+                        for c in range(8)], dtype=np.float64)
+    t = apply_affine(model, corners)
+    lo, hi = t.min(axis=0), t.max(axis=0)
+    center = apply_affine(model, np.array([d // 2 for d in dims], dtype=np.float64))
+    size, off = [], []
+    for d in range(3):
+        n = int(hi[d] - lo[d]) + 1
+        if n % 2 == 0:
+            n += 1
+        size.append(n)
+        off.append(center[d] - (n // 2))
+    return tuple(size), np.array(off)
+
+
+def psf_transform_normalized(psf, model):
+    """PSFExtraction.getTransformedNormalizedPSF (:182-188): normalize, then transform (:411-451):
+    out(p) = linear interpolation of the zero-extended PSF at model^-1 (p + offset)."""
+    p = psf_normalize(psf)
+    dims = _xyz(p)
+    size, off = psf_transformed_geometry(dims, model)
+    inv = _invert_affine(model)
+    x, y, z = _grid(size)
+    s = np.stack([x + off[0], y + off[1], z + off[2]], axis=-1)
+    t = apply_affine(inv, s)
+
+    def get(ix, iy, iz):
+        ok = (ix >= 0) & (iy >= 0) & (iz >= 0) & (ix < dims[0]) & (iy < dims[1]) & (iz < dims[2])
+        v = p[np.clip(iz, 0, dims[2] - 1), np.clip(iy, 0, dims[1] - 1), np.clip(ix, 0, dims[0] - 1)]
+        return np.where(ok, v, np.float32(0))
+
+    return nlinear(get, t)
+
+
+def psf_average(psfs, max_size=True):
+    """PSFCombination.computeAverageImage (MV/process/psf/PSFCombination.java:74-138): the
+    PSFs centred (centre = size / 2) on the largest or smallest size per axis, summed in float
+    in list order, divided by their number (double)."""
+    dl = [_xyz(p) for p in psfs]
+    f = max if max_size else min
+    a = tuple(f(d[k] for d in dl) for k in range(3))
+    acc = np.zeros((a[2], a[1], a[0]), dtype=np.float32)
+    for p, d in zip(psfs, dl):
+        o = [a[k] // 2 - d[k] // 2 for k in range(3)]  # avg index of PSF voxel 0
+        src = [slice(max(0, -o[k]), min(d[k], a[k] - o[k])) for k in range(3)]
+        dst = [slice(max(0, o[k]), max(0, o[k]) + (src[k].stop - src[k].start)) for k in range(3)]
+        acc[dst[2], dst[1], dst[0]] = (acc[dst[2], dst[1], dst[0]] +
+                                       np.asarray(p, np.float32)[src[2], src[1], src[0]]).astype(np.float32)
+    return (acc.astype(np.float64) / len(psfs)).astype(np.float32)
+
+
+def psf_make_same_size(psf, size):
+    """PSFCombination.makeSameSize (:182-210): the PSF centred in size, extended with its
+    minimum."""
+    p = np.asarray(psf, dtype=np.float32)
+    d = _xyz(p)
+    out = np.full((size[2], size[1], size[0]), np.float32(np.float64(p.min())), dtype=np.float32)
+    x, y, z = _grid(size)
+    px, py, pz = x - size[0] // 2 + d[0] // 2, y - size[1] // 2 + d[1] // 2, z - size[2] // 2 + d[2] // 2
+    ok = (px >= 0) & (py >= 0) & (pz >= 0) & (px < d[0]) & (py < d[1]) & (pz < d[2])
+    out[ok] = p[pz[ok], py[ok], px[ok]]
+    return out
+
+
+def psf_projection(psf, dim=-1, use_max=True):
+    """PSFCombination.computeMaxProjection (:228-296): the max or min along axis dim (x = 0;
+    dim < 0: the first smallest axis), the other axes kept in order.  Returns (projection
+    [second kept][first kept], dim)."""
+    p = np.asarray(psf, dtype=np.float32)
+    d = _xyz(p)
+    if dim < 0:
+        dim = 0
+        for k in range(1, 3):
+            if d[k] < d[dim]:
+                dim = k
+    ax = 2 - dim  # numpy axis of (x, y, z) axis dim
+    a = p.astype(np.float64)
+    ext = np.full(np.delete(np.array(p.shape), ax), -np.finfo(np.float64).max if use_max else np.finfo(np.float64).max)
+    for k in range(d[dim]):
+        v = np.take(a, k, axis=ax)
+        ext = np.where(v > ext, v, ext) if use_max else np.where(v < ext, v, ext)
+    return ext.astype(np.float32), dim
+
+
+def psf_remove_min_projections(psf):
+    """PSFExtraction.removeMinProjections / subtractProjection (:190-229): for axis 0, 1, 2 in
+    turn the min projection along it is subtracted (float)."""
+    p = np.array(psf, dtype=np.float32)
+    for dim in range(3):
+        proj, _ = psf_projection(p, dim, use_max=False)
+        p = (p - np.expand_dims(proj, axis=2 - dim)).astype(np.float32)
+    return p
+
+
+def load_group_transform_psfs(groups, same_size_for_all=True):
+    """PSFPreparation.loadGroupTransformPSFs (deconvolution/util/PSFPreparation.java:41-91):
+    per group the average, on the smallest common size, of its views' normalised transformed
+    PSFs; with same_size_for_all each is then centred in the largest size."""
+    out = [psf_average([psf_transform_normalized(p, m) for p, m in grp], max_size=False) for grp in groups]
+    if same_size_for_all:
+        mx = tuple(max(_xyz(a)[k] for a in out) for k in range(3))
+        out = [psf_make_same_size(a, mx) for a in out]
+    return out

@@ -286,3 +286,73 @@ def test_fusion_known_answers():
     assert np.allclose(im[1:-1, 1:-1, 1:-1], 0.5 * (np.maximum(1, img) + np.maximum(1, 3 * img))[1:-1, 1:-1, 1:-1],
                        rtol=1e-6)
     assert np.all(w == 2)
+
+
+def test_psf_extraction_known_answers():
+    # a single bead: at an integer location the neighbourhood is the bead itself; half a voxel
+    # off it splits linearly; several locations add up; the image wraps periodically
+    img = np.zeros((20, 22, 24), np.float32)
+    img[10, 11, 12] = 8
+    p = O.psf_extract(img, [(12, 11, 10)], (5, 5, 5))
+    assert p[2, 2, 2] == 8 and p.sum() == 8
+    p = O.psf_extract(img, [(12.5, 11, 10)], (5, 5, 5))
+    assert p[2, 2, 2] == 4 and p[2, 2, 1] == 4 and p.sum() == 8
+    p = O.psf_extract(img, [(12, 11, 10), (12, 11, 10)], (5, 5, 5))
+    assert p[2, 2, 2] == 16
+    edge = np.zeros((20, 22, 24), np.float32)
+    edge[0, 0, 0] = 3
+    p = O.psf_extract(edge, [(0, 0, 0)], (5, 5, 5))
+    assert p[2, 2, 2] == 3 and p.sum() == 3
+    p = O.psf_extract(edge, [(23, 21, 19)], (5, 5, 5))  # the bead one voxel beyond, wrapped
+    assert p[3, 3, 3] == 3
+    assert not O.psf_extract(img, [], (5, 5, 5)).any()  # no detections: a zero PSF
+
+
+def test_psf_transform_known_answers():
+    rng = np.random.default_rng(0)
+    q = rng.random((7, 5, 9)).astype(np.float32)
+    n = O.psf_normalize(q)
+    assert n.min() == 0 and n.max() == 1
+    # identity: the normalised PSF itself
+    ident = np.hstack([np.eye(3), np.zeros((3, 1))])
+    assert O.psf_transformed_geometry((9, 5, 7), ident)[0] == (9, 5, 7)
+    assert np.array_equal(O.psf_transform_normalized(q, ident), n)
+    # a translation does not move the PSF (its centre stays the centre)
+    shifted = ident.copy()
+    shifted[:, 3] = (10.0, -3.0, 7.0)
+    assert np.array_equal(O.psf_transform_normalized(q, shifted), n)
+    # 90 degrees about z: (x, y, z) -> (-y, x, z); sizes swap, values rotate exactly
+    rot = np.array([[0, -1, 0, 0], [1, 0, 0, 0], [0, 0, 1, 0]], dtype=np.float64)
+    size, off = O.psf_transformed_geometry((9, 5, 7), rot)
+    assert size == (5, 9, 7) and np.array_equal(off, [-4, 0, 0])
+    t = O.psf_transform_normalized(q, rot)
+    z, y, x = np.meshgrid(np.arange(7), np.arange(9), np.arange(5), indexing="ij")
+    assert np.array_equal(t, n[z, 4 - x, y])
+    # an even extent becomes odd: scaling x by 1.5 gives extent 12 -> 13 voxels
+    sc = ident.copy()
+    sc[0, 0] = 1.5
+    assert O.psf_transformed_geometry((9, 5, 7), sc)[0] == (13, 5, 7)
+
+
+def test_psf_combination_known_answers():
+    a = np.arange(27, dtype=np.float32).reshape(3, 3, 3)
+    b = np.ones((5, 3, 1), np.float32)  # x 1, y 3, z 5
+    # centred average on the largest size: b's single x column sits at x = 1
+    avg = O.psf_average([a, b], max_size=True)
+    assert avg.shape == (5, 3, 3)
+    assert avg[0, 1, 1] == np.float32(0.5) and avg[0, 1, 0] == 0
+    assert avg[2, 1, 1] == np.float32((13 + 1) / 2)
+    # smallest size: 1 x 3 x 3 around the centres
+    avg = O.psf_average([a, b], max_size=False)
+    assert avg.shape == (3, 3, 1) and avg[1, 1, 0] == np.float32(7)
+    # make the same size: centred, extended with the minimum
+    s = O.psf_make_same_size(a + 5, (5, 3, 5))
+    assert s.shape == (5, 3, 5) and s[0, 0, 0] == 5 and s[2, 1, 2] == 5 + 13
+    # projections: max along the smallest axis (x for b: size 1), min along y
+    pr, d = O.psf_projection(b, -1, True)
+    assert d == 0 and pr.shape == (5, 3) and np.all(pr == 1)
+    pr, d = O.psf_projection(a, 1, False)
+    assert d == 1 and pr.shape == (3, 3) and np.array_equal(pr, a[:, 0, :])
+    # removing the min projections of a separable ramp leaves zeros
+    r = (np.arange(4)[None, None, :] + 10 * np.arange(3)[None, :, None] + 100 * np.arange(5)[:, None, None])
+    assert not O.psf_remove_min_projections(r.astype(np.float32)).any()
