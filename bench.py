@@ -474,6 +474,64 @@ def run_e2e(args, ws, dev, ds, dec, shape, boundary):
             "steps": e2e_steps}
 
 
+def run_psf(args):
+    """PSF preparation on one GPU: PSFExtraction.extractPSFLocal of 2000 beads (PSF 31x31x61)
+    from one 1024x1024x512 float view on the device, and PSFPreparation.loadGroupTransformPSFs
+    of 8 views in 4 groups.  The oracle's extraction on the host cores is the CPU baseline
+    (a bounded sample of beads, scaled per bead)."""
+    import numpy as np
+    import torch
+
+    import mvrgb300 as M
+
+    dev = 0
+    torch.cuda.set_device(dev)
+    dims, nloc, size = (1024, 1024, 512), 2000, (31, 31, 61)
+    g = torch.Generator(device=f"cuda:{dev}")
+    g.manual_seed(1005)
+    img = torch.rand((dims[2], dims[1], dims[0]), generator=g, device=f"cuda:{dev}", dtype=torch.float32) * 100
+    rng = np.random.default_rng(1005)
+    loc = rng.uniform(0, 1, (nloc, 3)) * np.array(dims, dtype=np.float64)
+    out = torch.empty((size[2], size[1], size[0]), dtype=torch.float32, device=f"cuda:{dev}")
+    for _ in range(args.warmup):
+        M.psf_extract(img.data_ptr(), dims, loc, size, out.data_ptr(), dev)
+    steps = max(1, min(args.steps, 10))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(steps):
+        M.psf_extract(img.data_ptr(), dims, loc, size, out.data_ptr(), dev)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    psf = out.cpu().numpy()
+    views = [(psf, np.hstack([np.eye(3) * (1.0, 1.0, 1.0 + 0.1 * v), np.zeros((3, 1))])) for v in range(8)]
+    groups = [views[2 * k:2 * k + 2] for k in range(4)]
+    M.load_group_transform_psfs(groups, True, dev)
+    t0 = time.perf_counter()
+    M.load_group_transform_psfs(groups, True, dev)
+    prep_ms = (time.perf_counter() - t0) * 1e3
+    cpu = None
+    if not args.no_cpu:
+        import oracle
+
+        himg = img[:128, :128, :128].cpu().numpy()
+        sample = 8
+        sl = rng.uniform(0, 128, (sample, 3))
+        t0 = time.perf_counter()
+        oracle.psf_extract(himg, sl, size)
+        per = (time.perf_counter() - t0) / sample
+        cpu = {"value": 1.0 / per, "unit": "beads/s", "cores": 1, "kind": "port",
+               "sample": f"{sample} beads, PSF 31x31x61, numpy restatement of extractPSFLocal on one core"}
+    line = {"metric": "PSF bead neighbourhoods extracted/s", "value": nloc / (ms / 1e3), "unit": "beads/s",
+            "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "dtype": "f32 data, f64 positions and weights", "data": "synthetic",
+            "config": {"workload": "PSF extraction, 2000 beads, PSF 31x31x61, view 1024x1024x512 float32 on the device",
+                       "group_preparation": "8 views in 4 groups: normalise, transform, average, same size"},
+            "group_preparation_ms": prep_ms, "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -493,7 +551,12 @@ def main():
     ap.add_argument("--learned", action="store_true",
                     help="also run the learned-proposal experiment (training + gated run vs plain)")
     ap.add_argument("--learned-objects", type=int, default=50)
+    ap.add_argument("--psf", action="store_true",
+                    help="time the PSF preparation instead (bead extraction from a 1024x1024x512 view)")
     args = ap.parse_args()
+    if args.psf:
+        run_psf(args)
+        return
     global W
     W = WORKLOADS[args.workload]()
     ws, rank, local = dist_setup(args)
