@@ -106,7 +106,7 @@ template <int V, int MODE>
 __global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst, const float2 *__restrict__ Kh,
                                                   int Hx, long long estride, long long ostride, long long Pc,
                                                   const float2 *__restrict__ twg, int gather, int nother, int rlo,
-                                                  int rhi)
+                                                  int rhi, int olo)
 {
     constexpr int T = kTColT, NP = kTColNP, n = V * T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -114,20 +114,21 @@ __global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst
     float2 *tw = A + n * NP;                            // [n]: exp(-2 pi i j / n)
     float2 *KA = tw + n;                                // MODE 2: [n][NP] tile of K^
     for (int i = threadIdx.x; i < n; i += 256) tw[i] = __ldg(&twg[i]);
-    // tile column p of row i at base + i * estride + p * pstride.  With gather, the last
-    // x tile of the grid is the gathered tile of the last column (Hx - 1) at the
-    // other-axis indices 16 blockIdx.y ...; the other tiles cover columns < Hx - 1.
+    // tile column p of row i at base + i * estride + p * pstride.  The grid covers the
+    // other-axis indices olo + blockIdx.y < nother.  With gather, the last x tile of the grid
+    // is the gathered tile of the last column (Hx - 1) at the other-axis indices
+    // olo + 16 blockIdx.y ...; the other tiles cover columns < Hx - 1.
     const bool gtile = gather && blockIdx.x == gridDim.x - 1;
-    if (gtile && (int)blockIdx.y * NP >= nother) return;  // the whole CTA, before any barrier
+    if (gtile && olo + (int)blockIdx.y * NP >= nother) return;  // the whole CTA, before any barrier
     long long base, pstride;
     int np;
     if (!gtile) {
         const int x0 = blockIdx.x * NP;
-        base = (long long)blockIdx.y * ostride + x0;
+        base = (long long)(olo + blockIdx.y) * ostride + x0;
         np = min(NP, (gather ? Hx - 1 : Hx) - x0);
         pstride = 1;
     } else {
-        const int o0 = blockIdx.y * NP;
+        const int o0 = olo + blockIdx.y * NP;
         base = (long long)o0 * ostride + (Hx - 1);
         np = min(NP, nother - o0);
         pstride = ostride;

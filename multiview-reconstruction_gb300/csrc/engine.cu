@@ -524,7 +524,7 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
 
 template <typename T>
 int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh, int nb, int rlo,
-                           int rhi)
+                           int rhi, int olo, int ohi)
 {
     const int Hx = pl.Hx;
     long long estride, ostride;
@@ -551,10 +551,13 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
     const double cb = (double)sizeof(V) * (double)pl.Pc * nb;
     const int kind = mode == 2 ? KK_COLS_ZMUL : (mode == 1 ? KK_COLS_INV : KK_COLS_FWD);
     const int nax = pl.P[axis];
-    if (rhi < 0 || rhi > nax || sizeof(T) != sizeof(float) || !(axis == 1 ? pl.tcy : pl.tcz)) rhi = nax;
+    const bool tiled = sizeof(T) == sizeof(float) && (axis == 1 ? pl.tcy : pl.tcz);
+    if (rhi < 0 || rhi > nax || !tiled) rhi = nax;
     if (rlo < 0 || rlo > rhi || rhi == nax) rlo = 0;
-    const double stored = (double)(rhi - rlo) / nax;
-    MVR_TRY(prof_begin(kind, mode == 2 ? (2.0 + stored) * cb : (1.0 + stored) * cb));
+    if (ohi < 0 || ohi > nother || !tiled) ohi = nother;
+    if (olo < 0 || olo >= ohi) olo = 0;
+    const double stored = (double)(rhi - rlo) / nax, part = (double)(ohi - olo) / nother;
+    MVR_TRY(prof_begin(kind, part * (mode == 2 ? (2.0 + stored) * cb : (1.0 + stored) * cb)));
     const long long Pc = pl.Pc;
     const int wc = axis == 1 ? pl.wcy : pl.wcz;
     const int tc = axis == 1 ? pl.tcy : pl.tcz;
@@ -565,17 +568,17 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
             const int gather = (Hx > 1 && Hx % kTColNP == 1) ? 1 : 0;
             const int hmain = gather ? Hx - 1 : Hx;
             const size_t ts = tcols_smem(tc, mode);
-            const dim3 tgrid((unsigned)((hmain + kTColNP - 1) / kTColNP + gather), (unsigned)nother, (unsigned)nb);
+            const dim3 tgrid((unsigned)((hmain + kTColNP - 1) / kTColNP + gather), (unsigned)(ohi - olo), (unsigned)nb);
             TILE_COLS(tc, {
                 if (mode == 0)
                     k_tcols<V_, 0><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw, gather,
-                                                                      nother, rlo, rhi);
+                                                                      ohi, rlo, rhi, olo);
                 else if (mode == 1)
                     k_tcols<V_, 1><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw, gather,
-                                                                      nother, rlo, rhi);
+                                                                      ohi, rlo, rhi, olo);
                 else
                     k_tcols<V_, 2><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw, gather,
-                                                                      nother, rlo, rhi);
+                                                                      ohi, rlo, rhi, olo);
             });
             MVR_LAUNCHED("k_tcols");
             return prof_end();
@@ -674,8 +677,14 @@ template <typename T>
 int Engine<T>::launch_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const UpdateArgs &ua, int epi,
                              double bytes, double *stats_dev)
 {
-    const long long nrows = (long long)pl.P[1] * pl.P[2];
-    const unsigned gx = (unsigned)((nrows + pl.RP - 1) / pl.RP);
+    long long nrows = (long long)pl.P[1] * pl.P[2];
+    if (ua.prune) {  // k_wrows_update over the rows of the write regions' planes
+        if (!(sizeof(T) == sizeof(float) && pl.wr && epi == EPI_SEQ)) return fail(ERR_STATE, "pruned update");
+        int depth = 0;
+        for (int i = 0; i < nb; ++i) depth = std::max(depth, bms.m[i].whi[2] - bms.m[i].wlo[2]);
+        nrows = (long long)pl.P[1] * depth;
+    }
+    const unsigned gx = (unsigned)std::max(1LL, (nrows + pl.RP - 1) / pl.RP);
     const dim3 grid(gx, (unsigned)nb);
     MVR_TRY(prof_begin(KK_ROWS_UPDATE, bytes));
     bool warp_done = false;
@@ -768,14 +777,18 @@ int Engine<T>::launch_xy_update(const Plan<T> &pl, const BlockMaps &bms, int nb,
     return fail(ERR_STATE, "plane kernels are FP32 only");
 }
 
-// The planes [zlo, zhi) holding every write region of a batch.
-inline void write_planes(const BlockPlace *bps, int nb, int &zlo, int &zhi)
+// The planes [zlo, zhi) and rows [ylo, yhi) holding every write region of a batch.
+inline void write_region(const BlockPlace *bps, int nb, int &zlo, int &zhi, int &ylo, int &yhi)
 {
     zlo = bps[0].wlo[2];
     zhi = bps[0].whi[2];
+    ylo = bps[0].wlo[1];
+    yhi = bps[0].whi[1];
     for (int i = 1; i < nb; ++i) {
         zlo = std::min(zlo, bps[i].wlo[2]);
         zhi = std::max(zhi, bps[i].whi[2]);
+        ylo = std::min(ylo, bps[i].wlo[1]);
+        yhi = std::max(yhi, bps[i].whi[1]);
     }
 }
 
@@ -788,8 +801,11 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const f
     const long long nrows = (long long)pl.P[1] * pl.P[2];
     MVR_TRY(reserve(pl.Pc, (long long)pl.b[0] * pl.b[1] * pl.b[2], (nrows + pl.RP - 1) / pl.RP, nb));
     const BlockMaps bms = block_maps(pl, bps, nb);
-    int zlo = 0, zhi = -1;
-    if (!stats_dev && pl.xy) write_planes(bps, nb, zlo, zhi);
+    // without statistics only the write regions are needed after the second convolution
+    // (the plane kernels, or the warp-row update of the row / column path)
+    const bool prune = !stats_dev && (pl.xy || (sizeof(T) == sizeof(float) && pl.wr));
+    int zlo = 0, zhi = -1, ylo = 0, yhi = -1;
+    if (prune) write_region(bps, nb, zlo, zhi, ylo, yhi);
     if (pl.xy) {
         MVR_TRY(launch_xy_fwd(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
         MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb));
@@ -802,8 +818,9 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const f
         MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr, nb));
         MVR_TRY(launch_ratio(pl, bms, nb, S0_, img));
         MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
-        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k2h, nb));
-        MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr, nb));
+        // Z: store the write planes; Y inverse: those planes only, storing the write rows
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k2h, nb, zlo, zhi));
+        MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr, nb, ylo, yhi, zlo, zhi < 0 ? -1 : zhi));
     }
     UpdateArgs ua{};
     ua.psi_src = bps[0].psi_src;
@@ -816,7 +833,7 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const f
     ua.partials = partials_;
     // without statistics the voxels outside the write region are not needed: the plane
     // kernels skip their planes and rows
-    ua.prune = (!stats_dev && pl.xy) ? 1 : 0;
+    ua.prune = prune ? 1 : 0;
     const double nv = (double)pl.b[0] * pl.b[1] * pl.b[2];
     double bytes = 0.0;
     for (int i = 0; i < nb; ++i) {
@@ -824,7 +841,8 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const f
         const double ez = bp.whi[2] - bp.wlo[2], ey = bp.whi[1] - bp.wlo[1];
         const double neff = (double)(bp.whi[0] - bp.wlo[0]) * ey * ez;
         if (ua.prune)
-            bytes += sizeof(V) * (double)pl.Pc * ez / pl.P[2] + (sizeof(T) + 4.0) * pl.b[0] * ey * ez + sizeof(T) * neff;
+            bytes += sizeof(V) * (double)pl.Pc * ez / pl.P[2] * (pl.xy ? 1.0 : ey / pl.P[1]) +
+                     (sizeof(T) + 4.0) * pl.b[0] * ey * ez + sizeof(T) * neff;
         else
             bytes += sizeof(V) * (double)pl.Pc + (sizeof(T) + 4.0) * nv + sizeof(T) * neff;
     }
@@ -872,8 +890,8 @@ int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace
         prev = &pl;
         MVR_TRY(launch_cols(pl, 2, 2, S0_, S1_, pl.k1h, nb));
         if (pl.xy) {
-            int zlo = 0, zhi = -1;
-            if (!stats_dev) write_planes(bps, nb, zlo, zhi);
+            int zlo = 0, zhi = -1, ylo, yhi;
+            if (!stats_dev) write_region(bps, nb, zlo, zhi, ylo, yhi);
             MVR_TRY(launch_xy_ratio(pl, bms, nb, S1_, imgs[v]));
             MVR_TRY(launch_cols(pl, 2, 2, S1_, S1_, pl.k2h, nb, zlo, zhi));
         } else {

@@ -135,9 +135,10 @@ private:
     int launch_xy_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img);
     int launch_xy_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const UpdateArgs &ua, int epi,
                          double bytes, double *stats_dev);
-    // rows [rlo, rhi) of the transformed axis are stored (rhi < 0: all; tile kernels only)
+    // rows [rlo, rhi) of the transformed axis are stored, and only the other-axis indices
+    // [olo, ohi) are transformed (negative hi: all; tile kernels only, the others do all)
     int launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh, int nb, int rlo = 0,
-                    int rhi = -1);
+                    int rhi = -1, int olo = 0, int ohi = -1);
     int launch_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img);
     int launch_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const UpdateArgs &ua, int epi,
                       double bytes, double *stats_dev);

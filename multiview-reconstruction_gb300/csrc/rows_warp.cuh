@@ -244,10 +244,14 @@ __global__ void __launch_bounds__(256) k_wrows_update(float2 *__restrict__ S, Up
     const float *wgt = ua.weight[0];
     const float minI = ua.minI, maxI = ua.maxI;
     float ksum = 0.0f, kcomp = 0.0f, kmax = -1.0f;
-    const long long nrows = (long long)bm.P[1] * bm.P[2];
-    for (long long row = (long long)blockIdx.x * 8 + wib; row < nrows; row += (long long)gridDim.x * 8) {
+    // all rows, or (prune) the rows of the write region's planes
+    const long long r0 = ua.prune ? (long long)bm.wlo[2] * bm.P[1] : 0;
+    const long long nrows = ua.prune ? (long long)bm.whi[2] * bm.P[1] : (long long)bm.P[1] * bm.P[2];
+    for (long long row = r0 + (long long)blockIdx.x * 8 + wib; row < nrows; row += (long long)gridDim.x * 8) {
         const int y = (int)(row % bm.P[1]), z = (int)(row / bm.P[1]);
         if (y >= bm.b[1] || z >= bm.b[2]) continue;  // extension rows carry no block voxels
+        const bool wrow = y >= bm.wlo[1] && y < bm.whi[1] && z >= bm.wlo[2] && z < bm.whi[2];
+        if (ua.prune && !wrow) continue;
         float2 a[R];
         warp_c2r_pre<R>(Sb + row * (m + 1), a, t, lane);
         const float *pr = psrc + mirror_row(bm, y, z).base;
@@ -265,7 +269,6 @@ __global__ void __launch_bounds__(256) k_wrows_update(float2 *__restrict__ S, Up
             }
         warp_fft<R, true>(a, t, lane);
         warp_store_natural<R>(a, srow[wib], lane);
-        const bool wrow = y >= bm.wlo[1] && y < bm.whi[1] && z >= bm.wlo[2] && z < bm.whi[2];
         float *orow = pdst + ((bm.ooff[2] + z) * bm.OD[1] + (bm.ooff[1] + y)) * bm.OD[0] + bm.ooff[0];
 #pragma unroll
         for (int s = 0; s < R; ++s) {
@@ -287,7 +290,8 @@ __global__ void __launch_bounds__(256) k_wrows_update(float2 *__restrict__ S, Up
         }
         __syncwarp();
     }
-    stats_to_partials(ksum, kcomp, kmax, red_s, red_m, ua.partials, (long long)blockIdx.y * gridDim.x + blockIdx.x);
+    if (!ua.prune)
+        stats_to_partials(ksum, kcomp, kmax, red_s, red_m, ua.partials, (long long)blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 }  // namespace mvr

@@ -135,17 +135,21 @@ def test_volume_run_and_likelihood_plane_kernels():
     assert res[True][2] == pytest.approx(res[False][2], rel=1e-6)
 
 
-@pytest.mark.parametrize("mul", [False, True])
-def test_runs_without_statistics_write_the_same_volume(mul):
-    # without statistics the plane kernels update only the planes and rows of each
-    # block's write region; the volume they leave is bit-identical to the run that
-    # updates (and reduces) every block voxel
-    dims, kd = (200, 180, 150), (9, 9, 15)
+@pytest.mark.parametrize("mul,plane,block,dims", [(False, True, (128, 128, 64), (200, 180, 150)),
+                                                  (True, True, (128, 128, 64), (200, 180, 150)),
+                                                  (False, False, (128, 128, 64), (200, 180, 150)),
+                                                  (False, False, (256, 256, 256), (300, 280, 270))])
+def test_runs_without_statistics_write_the_same_volume(mul, plane, block, dims):
+    # without statistics the plane kernels (and the row / column path's second Z pass, Y
+    # inverse and update) work only on the planes and rows of each block's write region;
+    # the volume they leave is bit-identical to the run that updates (and reduces) every
+    # block voxel
+    kd = (9, 9, 15)
     ds = synthetic.make_dataset(dims, (0.0, 90.0), kd, n_beads=60, seed=9, side_lobes=False, weights="cosine")
     res = {}
     for stats in (True, False):
-        with plane_kernels(True):
-            d = M.Deconvolution(dims, 2, (128, 128, 64), mul=mul, psf_type=M.PSF_OPTIMIZATION_I, lam=0.006,
+        with plane_kernels(plane):
+            d = M.Deconvolution(dims, 2, block, mul=mul, psf_type=M.PSF_OPTIMIZATION_I, lam=0.006,
                                 weight_norm=M.WEIGHTS_HARD)
             for v in range(2):
                 d.set_view(v, ds.images[v], ds.weights[v], ds.psfs[v])
