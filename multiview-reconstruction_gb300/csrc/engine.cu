@@ -882,6 +882,8 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const f
     ua.weight[0] = w;
     ua.nviews = 1;
     ua.lambda = lambda_;
+    ua.two_lambda = (float)(2.0 * lambda_);
+    ua.tik = lambda_ > 0 ? 1 : 0;
     ua.minI = min_value_;
     ua.maxI = maxI;
     ua.partials = partials_;
@@ -917,6 +919,8 @@ int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace
     for (int v = 0; v < nv; ++v) ua.weight[v] = ws[v];
     ua.nviews = nv;
     ua.lambda = lambda_;
+    ua.two_lambda = (float)(2.0 * lambda_);
+    ua.tik = lambda_ > 0 ? 1 : 0;
     ua.minI = min_value_;
     ua.maxI = maxI;
     const Plan<T> *prev = nullptr;

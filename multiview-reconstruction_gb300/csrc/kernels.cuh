@@ -353,13 +353,14 @@ __device__ __forceinline__ float tikhonov_f(float v, float two_lambda)
 
 // computeNextValue (DeconvolutionMethods.java:320-358) in float: every operation the
 // reference does in float is done in float here with IEEE rounding and no contraction.
-__device__ __forceinline__ float next_value(float last, float integral, float weight, double lambda, float minI,
-                                            float maxI)
+// two_lambda = (float)(2 lambda) and tik = lambda > 0 come from the host (no FP64 here).
+__device__ __forceinline__ float next_value(float last, float integral, float weight, float two_lambda, int tik,
+                                            float minI, float maxI)
 {
     const float value = __fmul_rn(last, integral);
     float adjusted;
     if (value > 0.0f)
-        adjusted = lambda > 0 ? __fmul_rn(tikhonov_f(__fdiv_rn(value, maxI), (float)(2.0 * lambda)), maxI) : value;
+        adjusted = tik ? __fmul_rn(tikhonov_f(__fdiv_rn(value, maxI), two_lambda), maxI) : value;
     else adjusted = minI;
     const float next = isnan(adjusted) ? minI : (minI >= adjusted ? minI : adjusted);
     return __fadd_rn(last, __fmul_rn(__fsub_rn(next, last), weight));
@@ -479,6 +480,8 @@ struct UpdateArgs {
     float *store;         // EPI_STORE: conv result, block layout
     const float *img;     // EPI_NLL: the view's image (zero outside the volume)
     double lambda;
+    float two_lambda;     // (float)(2 lambda), for the float update
+    int tik;              // lambda > 0
     float minI;
     float maxI;
     double *partials;     // per CTA {sum, max}
@@ -553,7 +556,11 @@ __device__ __forceinline__ void update_row(const typename Cx<T>::t *zz, int m, c
                 const T last = lastv[u][h];
                 T next;
                 if (EPI == EPI_SEQ) {
-                    next = next_value(last, integral, (T)wv[u][h], ua.lambda, (T)ua.minI, (T)ua.maxI);
+                    if constexpr (sizeof(T) == sizeof(float))
+                        next = next_value((float)last, (float)integral, (float)wv[u][h], ua.two_lambda, ua.tik, ua.minI,
+                                          ua.maxI);
+                    else
+                        next = next_value(last, integral, (T)wv[u][h], ua.lambda, (T)ua.minI, (T)ua.maxI);
                 } else {  // EPI_MUL_FINAL: DeconvolutionMethods.computeNextValueMul 370-419
                     // the product and the weight sum in T (the reference uses double; on this
                     // GPU the double rate is a small fraction of the float rate, and the float
@@ -567,7 +574,10 @@ __device__ __forceinline__ void update_row(const typename Cx<T>::t *zz, int m, c
                     else if (ua.nviews == 2) root = (T)__fsqrt_rn((float)prod);
                     else root = (T)powf((float)prod, 1.0f / (float)ua.nviews);
                     sumW = sumW < (T)1 ? sumW : (T)1;
-                    next = next_value(last, root, sumW, ua.lambda, (T)ua.minI, (T)ua.maxI);
+                    if constexpr (sizeof(T) == sizeof(float))
+                        next = next_value((float)last, (float)root, (float)sumW, ua.two_lambda, ua.tik, ua.minI, ua.maxI);
+                    else
+                        next = next_value(last, root, sumW, ua.lambda, (T)ua.minI, (T)ua.maxI);
                 }
                 const T ch = next - last;  // signed change (DeconvolutionMethods.java:308)
                 const T ky = ch - kcomp;

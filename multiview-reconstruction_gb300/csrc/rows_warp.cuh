@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(256) k_wrows_update(float2 *__restrict__ S, Up
             for (int h = 0; h < 2; ++h) {
                 if (!((inb >> (2 * s + h)) & 1u)) continue;
                 const float last = lastv[s][h];
-                const float next = next_value(last, cv[h], wv[s][h], ua.lambda, minI, maxI);
+                const float next = next_value(last, cv[h], wv[s][h], ua.two_lambda, ua.tik, minI, maxI);
                 const float ch = next - last;  // signed change (DeconvolutionMethods.java:308)
                 const float ky = ch - kcomp;
                 const float kt = ksum + ky;

@@ -478,8 +478,8 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
         uc.minI = ua.minI;
         uc.maxI = ua.maxI;
         uc.inv_maxI = 1.0f / ua.maxI;
-        uc.two_lambda = (float)(2.0 * ua.lambda);
-        uc.tik = ua.lambda > 0.0;
+        uc.two_lambda = ua.two_lambda;
+        uc.tik = ua.tik != 0;
 #pragma unroll 1
         for (int r = 0; r < RX; ++r) {
             const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;

@@ -63,3 +63,11 @@ def test_fp32_against_fp64_run(data):
     f32, _ = run(data, (192, 192, 192), 2)
     f64, _ = run(data, (192, 192, 192), 2, precision=M.PRECISION_FP64)
     assert rel(f32, f64) <= 1e-5
+
+
+def test_256_blocks_match_192_blocks(data):
+    # 256^3 blocks run the row / column kernels with the persistent Z pass of 256-long
+    # columns; the pasted volume equals the 192^3-block (plane kernel) run
+    a, _ = run(data, (192, 192, 192), 2)
+    b, _ = run(data, (256, 256, 256), 2)
+    assert rel(a, b) <= 1e-5
