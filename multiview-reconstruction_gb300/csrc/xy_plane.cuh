@@ -126,72 +126,128 @@ __device__ __forceinline__ void xrow_p1(float2 (&a)[VX], const float2 *twx, int 
     }
 }
 
+// x phase 2 with the packed-real split (forward) or merge (inverse) fused in registers.
+// Item (row y, k1) holds the frequencies f = k1 + V k2 (k2 < 16) at positions k2 + 16 k1; the
+// split pairs f with m - f, which item (y, V - k1) holds at slot 15 - k2 (k1 = 0: the same
+// item at slot 16 - k2; k1 = V / 2: the same item at slot 15 - k2).  A warp takes 16 rows:
+// lanes 0-15 item k1, lanes 16-31 the partner item V - k1 of the same rows, so the partner
+// values come over one shuffle; the last pair group is (0, V / 2), both self-paired.
+//   forward: X[f] = E + W_Px^f (-i D), E = (Z[f] + conj Z[m-f]) / 2, D = (Z[f] - conj Z[m-f]) / 2,
+//            the DC and Nyquist values (both real) packed as (X[0], X[m]) at position 0;
+//   inverse: a[f] = e + i o, e = X[f] + conj X[m-f], o = (X[f] - conj X[m-f]) conj(W_Px^f),
+//            then the inverse 16-point DFT.
+template <int VX, int VY, bool INV>
+__device__ __forceinline__ float2 xy_split_one(float2 zf, float2 zg, int f, const float2 *twx)
+{
+    const float2 zc = cconj(zg);
+    if (f == 0) return make_float2(zf.x + zf.y, zf.x - zf.y);
+    if (!INV) {
+        const float2 e = cscale(cadd(zf, zc), 0.5f), dd = cscale(csub(zf, zc), 0.5f);
+        return cadd(e, cmul(twx[f], make_float2(dd.y, -dd.x)));
+    }
+    const float2 e = cadd(zf, zc), q = cmul(csub(zf, zc), cconj(twx[f]));
+    return make_float2(e.x - q.y, e.y + q.x);
+}
+
+template <int VX, int VY, bool INV>
+__device__ __forceinline__ void xy_x_p2_split(float2 *A, const float2 *twx)
+{
+    typedef XYShape<VX, VY> S;
+    constexpr int T = 16, Py = S::Py, NT = S::NT, RB = Py / 16, items = Py * VX;
+    static_assert(Py % 16 == 0 && VX % 2 == 0 && items % 32 == 0 && NT % 32 == 0, "whole warps of row pairs");
+    for (int it = threadIdx.x; it < items; it += NT) {
+        const int l = it & 31, grp = it >> 5;
+        const int h = l >> 4, jp = grp / RB;
+        const int y = (grp - jp * RB) * 16 + (l & 15);
+        const bool selfgrp = jp == VX / 2 - 1;  // the same for the whole warp
+        const int k1 = selfgrp ? (h ? VX / 2 : 0) : (h ? VX - 1 - jp : 1 + jp);
+        float2 *b0 = A + y * S::SR + T * k1;
+        float2 b[T];
+#pragma unroll
+        for (int t = 0; t < T; ++t) b[t] = b0[t];
+        if (!INV) sdft<T, false>(b);  // b[k2] = Z[k1 + V k2]
+        if (!selfgrp) {
+            // partner item V - k1 in lane ^ 16: frequency m - f sits at its slot 15 - k2
+#pragma unroll
+            for (int k2 = 0; k2 < T / 2; ++k2) {
+                const int k3 = T - 1 - k2;
+                float2 ga, gb;
+                ga.x = __shfl_xor_sync(0xffffffffu, b[k3].x, 16);
+                ga.y = __shfl_xor_sync(0xffffffffu, b[k3].y, 16);
+                gb.x = __shfl_xor_sync(0xffffffffu, b[k2].x, 16);
+                gb.y = __shfl_xor_sync(0xffffffffu, b[k2].y, 16);
+                const float2 oa = xy_split_one<VX, VY, INV>(b[k2], ga, k1 + VX * k2, twx);
+                const float2 ob = xy_split_one<VX, VY, INV>(b[k3], gb, k1 + VX * k3, twx);
+                if (INV) {
+                    b[k2] = oa;
+                    b[k3] = ob;
+                } else {  // forward: straight back to shared memory
+                    b0[k2] = oa;
+                    b0[k3] = ob;
+                }
+            }
+        } else if (h == 0) {  // k1 = 0: f = V k2 pairs with slot 16 - k2; slot 8 is m / 2
+            const float2 o0 = xy_split_one<VX, VY, INV>(b[0], b[0], 0, twx);
+            const float2 o8 = xy_split_one<VX, VY, INV>(b[8], b[8], VX * 8, twx);
+            if (INV) {
+                b[0] = o0;
+                b[8] = o8;
+            } else {
+                b0[0] = o0;
+                b0[8] = o8;
+            }
+#pragma unroll
+            for (int k2 = 1; k2 < T / 2; ++k2) {
+                const int k3 = T - k2;
+                const float2 oa = xy_split_one<VX, VY, INV>(b[k2], b[k3], VX * k2, twx);
+                const float2 ob = xy_split_one<VX, VY, INV>(b[k3], b[k2], VX * k3, twx);
+                if (INV) {
+                    b[k2] = oa;
+                    b[k3] = ob;
+                } else {  // forward: straight back to shared memory
+                    b0[k2] = oa;
+                    b0[k3] = ob;
+                }
+            }
+        } else {  // k1 = V / 2: slot k2 pairs with slot 15 - k2
+#pragma unroll
+            for (int k2 = 0; k2 < T / 2; ++k2) {
+                const int k3 = T - 1 - k2;
+                const float2 oa = xy_split_one<VX, VY, INV>(b[k2], b[k3], VX / 2 + VX * k2, twx);
+                const float2 ob = xy_split_one<VX, VY, INV>(b[k3], b[k2], VX / 2 + VX * k3, twx);
+                if (INV) {
+                    b[k2] = oa;
+                    b[k3] = ob;
+                } else {  // forward: straight back to shared memory
+                    b0[k2] = oa;
+                    b0[k3] = ob;
+                }
+            }
+        }
+        if (INV) {
+            sdft<T, true>(b);
+#pragma unroll
+            for (int t = 0; t < T; ++t) b0[t] = b[t];
+        }
+    }
+}
+
 // x phase 2 (forward), then the packed-real split in tile order.  The DC and Nyquist
 // values of a row (both real) are packed as one complex value at position 0, so that the
 // y transforms run on m columns.
 template <int VX, int VY>
-__device__ __forceinline__ void xy_x_forward_p2(float2 *A, const float2 *twx, const int *posx)
+__device__ __forceinline__ void xy_x_forward_p2(float2 *A, const float2 *twx, const int *)
 {
-    typedef XYShape<VX, VY> S;
-    constexpr int m = S::m, half = m / 2, items = S::Py * (half + 1), NT = S::NT;
-    tp_phase2<VX, S::Py, S::SR, 1, false, NT>(A);
-    __syncthreads();
-    // X[f] = E[f] + W_Px^f O[f], E = (Z[f] + conj Z[m-f]) / 2, O = -i (Z[f] - conj Z[m-f]) / 2
-    for (int it = threadIdx.x; it < items; it += NT) {
-        const int f = it / S::Py, y = it - f * S::Py;
-        float2 *row = A + y * S::SR;
-        if (f == 0) {
-            const float2 z0 = row[0];
-            row[0] = make_float2(z0.x + z0.y, z0.x - z0.y);  // (X[0], X[m]), both real
-            continue;
-        }
-        const int g = m - f, pf = posx[f], pg = posx[g];
-        const float2 zf = row[pf], zg = row[pg];
-        {
-            const float2 zc = cconj(zg);
-            const float2 e = cscale(cadd(zf, zc), 0.5f), dd = cscale(csub(zf, zc), 0.5f);
-            row[pf] = cadd(e, cmul(twx[f], make_float2(dd.y, -dd.x)));
-        }
-        if (g != f) {
-            const float2 zc = cconj(zf);
-            const float2 e = cscale(cadd(zg, zc), 0.5f), dd = cscale(csub(zg, zc), 0.5f);
-            row[pg] = cadd(e, cmul(twx[g], make_float2(dd.y, -dd.x)));
-        }
-    }
+    xy_x_p2_split<VX, VY, false>(A, twx);
     __syncthreads();
 }
 
 // Packed-real merge in tile order, then x phase 2 inverse (x phase 1 inverse follows in
 // the caller).  Position 0 holds (X[0], X[m]).
 template <int VX, int VY>
-__device__ __forceinline__ void xy_x_inverse_p2(float2 *A, const float2 *twx, const int *posx)
+__device__ __forceinline__ void xy_x_inverse_p2(float2 *A, const float2 *twx, const int *)
 {
-    typedef XYShape<VX, VY> S;
-    constexpr int m = S::m, half = m / 2, items = S::Py * (half + 1), NT = S::NT;
-    // a[k] = e + i o, e = X[k] + conj X[m-k], o = (X[k] - conj X[m-k]) conj(W_Px^k)
-    for (int it = threadIdx.x; it < items; it += NT) {
-        const int f = it / S::Py, y = it - f * S::Py;
-        float2 *row = A + y * S::SR;
-        if (f == 0) {
-            const float2 p = row[0];
-            row[0] = make_float2(p.x + p.y, p.x - p.y);
-            continue;
-        }
-        const int g = m - f, pf = posx[f], pg = posx[g];
-        const float2 xf = row[pf], xg = row[pg];
-        {
-            const float2 c = cconj(xg);
-            const float2 e = cadd(xf, c), o = cmul(csub(xf, c), cconj(twx[f]));
-            row[pf] = make_float2(e.x - o.y, e.y + o.x);
-        }
-        if (g != f) {
-            const float2 c = cconj(xf);
-            const float2 e = cadd(xg, c), o = cmul(csub(xg, c), cconj(twx[g]));
-            row[pg] = make_float2(e.x - o.y, e.y + o.x);
-        }
-    }
-    __syncthreads();
-    tp_phase2<VX, S::Py, S::SR, 1, true, NT>(A);
+    xy_x_p2_split<VX, VY, true>(A, twx);
     __syncthreads();
 }
 
