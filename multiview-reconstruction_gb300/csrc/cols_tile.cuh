@@ -102,18 +102,21 @@ __device__ __forceinline__ void sdft(float2 (&a)[N])
 constexpr int kTColT = 16;   // phase-2 length
 constexpr int kTColNP = 16;  // columns per tile
 
-template <int V, int MODE>
-__global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst, const float2 *__restrict__ Kh,
-                                                  int Hx, long long estride, long long ostride, long long Pc,
-                                                  const float2 *__restrict__ twg, int gather, int nother, int rlo,
-                                                  int rhi, int olo)
+// NP columns per tile with 16 NP threads (NP = 16: 256 threads, 3 CTAs per SM).  Measured on
+// GB300 for the 192-long Z pass: 32-column tiles (512 threads, 256-byte row segments, 2 CTAs
+// per SM) ran at 3.5 TB/s against 4.5 TB/s for 16-column tiles.
+template <int V, int MODE, int NP = kTColNP>
+__global__ void __launch_bounds__(16 * NP, NP == 16 ? 3 : 2)
+    k_tcols(const float2 *src, float2 *dst, const float2 *__restrict__ Kh, int Hx, long long estride,
+            long long ostride, long long Pc, const float2 *__restrict__ twg, int gather, int nother, int rlo, int rhi,
+            int olo)
 {
-    constexpr int T = kTColT, NP = kTColNP, n = V * T;
+    constexpr int T = kTColT, n = V * T, NT = 16 * NP;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *A = reinterpret_cast<float2 *>(smem_raw);  // [n][NP]
     float2 *tw = A + n * NP;                            // [n]: exp(-2 pi i j / n)
     float2 *KA = tw + n;                                // MODE 2: [n][NP] tile of K^
-    for (int i = threadIdx.x; i < n; i += 256) tw[i] = __ldg(&twg[i]);
+    for (int i = threadIdx.x; i < n; i += NT) tw[i] = __ldg(&twg[i]);
     // tile column p of row i at base + i * estride + p * pstride.  The grid covers the
     // other-axis indices olo + blockIdx.y < nother.  With gather, the last x tile of the grid
     // is the gathered tile of the last column (Hx - 1) at the other-axis indices
@@ -136,24 +139,24 @@ __global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst
     src += (long long)blockIdx.z * Pc;
     dst += (long long)blockIdx.z * Pc;
     constexpr int tot = n * NP;
-    constexpr int step = 256 * kLoadBatch;
+    constexpr int step = NT * kLoadBatch;
     // every thread keeps one column p = threadIdx % 16 and rows threadIdx / 16 + 16 u
     const int pc = threadIdx.x % NP;
     const bool plive = pc < np;
     const long long coff = base + (long long)pc * pstride + (long long)(threadIdx.x / NP) * estride;
-    const long long rstep = (long long)(256 / NP) * estride;
+    const long long rstep = (long long)(NT / NP) * estride;
     for (int t0 = threadIdx.x; t0 < tot; t0 += step) {
         float2 r[kLoadBatch], q[kLoadBatch];
-        const long long o0 = coff + (long long)((t0 - threadIdx.x) / 256) * rstep;
+        const long long o0 = coff + (long long)((t0 - threadIdx.x) / NT) * rstep;
 #pragma unroll
         for (int u = 0; u < kLoadBatch; ++u) {
-            const bool ok = t0 + u * 256 < tot && plive;
+            const bool ok = t0 + u * NT < tot && plive;
             r[u] = ok ? src[o0 + u * rstep] : make_float2(0.0f, 0.0f);
             if (MODE == 2) q[u] = ok ? __ldg(&Kh[o0 + u * rstep]) : make_float2(0.0f, 0.0f);
         }
 #pragma unroll
         for (int u = 0; u < kLoadBatch; ++u) {
-            const int e = t0 + u * 256;
+            const int e = t0 + u * NT;
             if (e < tot) {
                 A[e] = r[u];
                 if (MODE == 2) KA[e] = q[u];
@@ -210,15 +213,15 @@ __global__ void __launch_bounds__(256, 3) k_tcols(const float2 *src, float2 *dst
     // reads only a sub-range)
     if (plive) {
         const long long cb = base + (long long)pc * pstride;
-        for (int e = threadIdx.x + rlo * NP; e < rhi * NP; e += 256) dst[cb + (long long)(e / NP) * estride] = A[e];
+        for (int e = threadIdx.x + rlo * NP; e < rhi * NP; e += NT) dst[cb + (long long)(e / NP) * estride] = A[e];
     }
 }
 
 // data tile + twiddles (+ the K^ tile of MODE 2)
-inline size_t tcols_smem(int V, int mode = 2)
+inline size_t tcols_smem(int V, int mode = 2, int np = kTColNP)
 {
     const size_t n = (size_t)V * kTColT;
-    return sizeof(float2) * (n * kTColNP + n + (mode == 2 ? n * kTColNP : 0));
+    return sizeof(float2) * (n * np + n + (mode == 2 ? n * np : 0));
 }
 
 }  // namespace mvr
