@@ -139,27 +139,29 @@ __global__ void __launch_bounds__(16 * NP, NP == 16 ? 3 : 2)
     src += (long long)blockIdx.z * Pc;
     dst += (long long)blockIdx.z * Pc;
     constexpr int tot = n * NP;
-    constexpr int step = NT * kLoadBatch;
-    // every thread keeps one column p = threadIdx % 16 and rows threadIdx / 16 + 16 u
+    // every thread keeps one column p = threadIdx % NP and the rows threadIdx / NP + 16 j,
+    // j < R, loaded in batches of LB with all loads of a batch in flight
+    constexpr int R = tot / NT, LB = (R % 8 == 0) ? 8 : ((R % 6 == 0) ? 6 : 4);
+    static_assert(R % LB == 0, "load batches");
     const int pc = threadIdx.x % NP;
     const bool plive = pc < np;
     const long long coff = base + (long long)pc * pstride + (long long)(threadIdx.x / NP) * estride;
     const long long rstep = (long long)(NT / NP) * estride;
-    for (int t0 = threadIdx.x; t0 < tot; t0 += step) {
-        float2 r[kLoadBatch], q[kLoadBatch];
-        const long long o0 = coff + (long long)((t0 - threadIdx.x) / NT) * rstep;
+    {
+        const float2 *sp = src + coff;
+        const float2 *kp = Kh + coff;
 #pragma unroll
-        for (int u = 0; u < kLoadBatch; ++u) {
-            const bool ok = t0 + u * NT < tot && plive;
-            r[u] = ok ? src[o0 + u * rstep] : make_float2(0.0f, 0.0f);
-            if (MODE == 2) q[u] = ok ? __ldg(&Kh[o0 + u * rstep]) : make_float2(0.0f, 0.0f);
-        }
+        for (int j0 = 0; j0 < R; j0 += LB) {
+            float2 r[LB], q[LB];
 #pragma unroll
-        for (int u = 0; u < kLoadBatch; ++u) {
-            const int e = t0 + u * NT;
-            if (e < tot) {
-                A[e] = r[u];
-                if (MODE == 2) KA[e] = q[u];
+            for (int u = 0; u < LB; ++u) {
+                r[u] = plive ? sp[(j0 + u) * rstep] : make_float2(0.0f, 0.0f);
+                if (MODE == 2) q[u] = plive ? __ldg(kp + (j0 + u) * rstep) : make_float2(0.0f, 0.0f);
+            }
+#pragma unroll
+            for (int u = 0; u < LB; ++u) {
+                A[threadIdx.x + (j0 + u) * NT] = r[u];
+                if (MODE == 2) KA[threadIdx.x + (j0 + u) * NT] = q[u];
             }
         }
     }
@@ -212,8 +214,13 @@ __global__ void __launch_bounds__(16 * NP, NP == 16 ? 3 : 2)
     // rows [rlo, rhi) of the transformed axis are stored (all of them unless the caller
     // reads only a sub-range)
     if (plive) {
-        const long long cb = base + (long long)pc * pstride;
-        for (int e = threadIdx.x + rlo * NP; e < rhi * NP; e += NT) dst[cb + (long long)(e / NP) * estride] = A[e];
+        float2 *dp = dst + coff;
+        const int prow = threadIdx.x / NP;
+#pragma unroll
+        for (int j = 0; j < R; ++j) {
+            const int row = prow + (NT / NP) * j;
+            if (row >= rlo && row < rhi) dp[j * rstep] = A[threadIdx.x + j * NT];
+        }
     }
 }
 
