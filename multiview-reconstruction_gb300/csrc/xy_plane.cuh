@@ -396,7 +396,8 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
             const int x = 2 * (t + 16 * v);
             if constexpr (MIR) {
                 const float *pr = src.vol + sm.rowb[y];
-                a[r][v] = make_float2(__ldg(pr + sm.colx[x]), __ldg(pr + sm.colx[x + 1]));
+                const int2 cx = *reinterpret_cast<const int2 *>(sm.colx + x);  // x even: one 8-byte read
+                a[r][v] = make_float2(__ldg(pr + cx.x), __ldg(pr + cx.y));
             } else {
                 typename Src::Row row;
                 row.base = sm.rowb[y];
@@ -455,12 +456,11 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
         const long long rb = sm.rowb[y];
         float im[VX][2];
 #pragma unroll
-        for (int v = 0; v < VX; ++v)
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int gx = sm.colx[2 * (t + 16 * v) + h];
-                im[v][h] = (rb >= 0 && gx >= 0) ? __ldg(img + rb + gx) : 0.0f;
-            }
+        for (int v = 0; v < VX; ++v) {
+            const int2 cx = *reinterpret_cast<const int2 *>(sm.colx + 2 * (t + 16 * v));
+            im[v][0] = (rb >= 0 && cx.x >= 0) ? __ldg(img + rb + cx.x) : 0.0f;
+            im[v][1] = (rb >= 0 && cx.y >= 0) ? __ldg(img + rb + cx.y) : 0.0f;
+        }
         float2 a[VX];
         float2 *row = sm.A + y * SH::SR + t;
 #pragma unroll
@@ -543,14 +543,15 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
             if (pb < 0 || (ua.prune && ob == kNoRow)) continue;  // not a block row / not written
             float pv[VX][2], wv[VX][2];
 #pragma unroll
-            for (int v = 0; v < VX; ++v)
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int x = 2 * (t + 16 * v) + h;
-                    const int mx = sm.colx[x], gx = sm.colx2[x];
-                    pv[v][h] = mx >= 0 ? __ldg(psrc + pb + mx) : 0.0f;
-                    wv[v][h] = (wb >= 0 && gx >= 0) ? __ldg(wgt + wb + gx) : 0.0f;
-                }
+            for (int v = 0; v < VX; ++v) {
+                const int x = 2 * (t + 16 * v);  // even: the pair of table entries is one 8-byte read
+                const int2 mx = *reinterpret_cast<const int2 *>(sm.colx + x);
+                const int2 gx = *reinterpret_cast<const int2 *>(sm.colx2 + x);
+                pv[v][0] = mx.x >= 0 ? __ldg(psrc + pb + mx.x) : 0.0f;
+                pv[v][1] = mx.y >= 0 ? __ldg(psrc + pb + mx.y) : 0.0f;
+                wv[v][0] = (wb >= 0 && gx.x >= 0) ? __ldg(wgt + wb + gx.x) : 0.0f;
+                wv[v][1] = (wb >= 0 && gx.y >= 0) ? __ldg(wgt + wb + gx.y) : 0.0f;
+            }
             float2 a[VX];
             const float2 *row = sm.A + y * SH::SR + t;
 #pragma unroll
@@ -559,10 +560,12 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
 #pragma unroll
             for (int v = 0; v < VX; ++v) {
                 const float cv[2] = {a[v].x, a[v].y};
+                const int2 cx = *reinterpret_cast<const int2 *>(sm.colx + 2 * (t + 16 * v));
+                const int2 c3 = *reinterpret_cast<const int2 *>(sm.colx3 + 2 * (t + 16 * v));
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const int x = 2 * (t + 16 * v) + h;
-                    if (sm.colx[x] < 0) continue;  // beyond the block
+                    if ((h ? cx.y : cx.x) < 0) continue;  // beyond the block
                     const float last = pv[v][h];
                     const float next = next_value_fast(last, cv[h], wv[v][h], uc);
                     const float ch = next - last;  // signed change (DeconvolutionMethods.java:308)
@@ -571,7 +574,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
                     kcomp = (kt - ksum) - ky;
                     ksum = kt;
                     kmax = kmax > ch ? kmax : ch;
-                    if (ob != kNoRow && sm.colx3[x] >= 0) pdst[ob + x] = next;
+                    if (ob != kNoRow && (h ? c3.y : c3.x) >= 0) pdst[ob + x] = next;
                 }
             }
         }
