@@ -15,7 +15,8 @@
 //
 // A CTA of 256 threads takes 16 consecutive x' columns at one index of the other axis;
 // the tile moves between HBM and shared memory in coalesced 16-wide row segments.
-// MODE 2 stages the same tile of K^ in shared memory.  A gathered tile (pstride > 1)
+// MODE 2 multiplies by K^ in phase 2, reading it from L2 (every block of a batch shares
+// one K^) or, with MVR_TCOLS_KS=1, from a staged shared-memory tile.  A gathered tile (pstride > 1)
 // takes one x' column at 16 consecutive indices of the other axis instead: the last
 // column of a spectrum with Hx = 16 q + 1 (the Nyquist column) goes that way, so no
 // CTA works on a tile with a single live column.
@@ -102,11 +103,22 @@ __device__ __forceinline__ void sdft(float2 (&a)[N])
 constexpr int kTColT = 16;   // phase-2 length
 constexpr int kTColNP = 16;  // columns per tile
 
+// Build-time knobs: MVR_TCOLS_KS=1 stages the K^ tile in shared memory with the data tile
+// (MODE 2) instead of reading K^ from L2 in phase 2, and MVR_TCOLS_MINB sets the register
+// budget (CTAs per SM).  Measured on GB300 for the 192-long Z pass: K^ from L2 at 3 CTAs per
+// SM 4.99 TB/s, staged 4.80 TB/s, from L2 at 4 CTAs per SM (64 registers) 4.54 TB/s.
+#ifndef MVR_TCOLS_KS
+#define MVR_TCOLS_KS 0
+#endif
+#ifndef MVR_TCOLS_MINB
+#define MVR_TCOLS_MINB 3
+#endif
+
 // NP columns per tile with 16 NP threads (NP = 16: 256 threads, 3 CTAs per SM).  Measured on
 // GB300 for the 192-long Z pass: 32-column tiles (512 threads, 256-byte row segments, 2 CTAs
 // per SM) ran at 3.5 TB/s against 4.5 TB/s for 16-column tiles.
 template <int V, int MODE, int NP = kTColNP>
-__global__ void __launch_bounds__(16 * NP, NP == 16 ? 3 : 2)
+__global__ void __launch_bounds__(16 * NP, NP == 16 ? MVR_TCOLS_MINB : 2)
     k_tcols(const float2 *src, float2 *dst, const float2 *__restrict__ Kh, int Hx, long long estride,
             long long ostride, long long Pc, const float2 *__restrict__ twg, int gather, int nother, int rlo, int rhi,
             int olo)
@@ -156,12 +168,12 @@ __global__ void __launch_bounds__(16 * NP, NP == 16 ? 3 : 2)
 #pragma unroll
             for (int u = 0; u < LB; ++u) {
                 r[u] = plive ? sp[(j0 + u) * rstep] : make_float2(0.0f, 0.0f);
-                if (MODE == 2) q[u] = plive ? __ldg(kp + (j0 + u) * rstep) : make_float2(0.0f, 0.0f);
+                if (MODE == 2 && MVR_TCOLS_KS) q[u] = plive ? __ldg(kp + (j0 + u) * rstep) : make_float2(0.0f, 0.0f);
             }
 #pragma unroll
             for (int u = 0; u < LB; ++u) {
                 A[threadIdx.x + (j0 + u) * NT] = r[u];
-                if (MODE == 2) KA[threadIdx.x + (j0 + u) * NT] = q[u];
+                if (MODE == 2 && MVR_TCOLS_KS) KA[threadIdx.x + (j0 + u) * NT] = q[u];
             }
         }
     }
@@ -190,8 +202,14 @@ __global__ void __launch_bounds__(16 * NP, NP == 16 ? 3 : 2)
             for (int t = 0; t < T; ++t) b[t] = A[(t + T * k1) * NP + c];
             if (MODE != 1) sdft<T, false>(b);
             if (MODE == 2) {
+                if (MVR_TCOLS_KS) {
 #pragma unroll
-                for (int k2 = 0; k2 < T; ++k2) b[k2] = cmul(b[k2], KA[(k2 + T * k1) * NP + c]);
+                    for (int k2 = 0; k2 < T; ++k2) b[k2] = cmul(b[k2], KA[(k2 + T * k1) * NP + c]);
+                } else {
+                    const float2 *kq = Kh + base + (long long)c * pstride + (long long)(T * k1) * estride;
+#pragma unroll
+                    for (int k2 = 0; k2 < T; ++k2) b[k2] = cmul(b[k2], __ldg(kq + (long long)k2 * estride));
+                }
             }
             if (MODE != 0) sdft<T, true>(b);
 #pragma unroll
@@ -228,7 +246,7 @@ __global__ void __launch_bounds__(16 * NP, NP == 16 ? 3 : 2)
 inline size_t tcols_smem(int V, int mode = 2, int np = kTColNP)
 {
     const size_t n = (size_t)V * kTColT;
-    return sizeof(float2) * (n * np + n + (mode == 2 ? n * np : 0));
+    return sizeof(float2) * (n * np + n + (mode == 2 && MVR_TCOLS_KS ? n * np : 0));
 }
 
 }  // namespace mvr
