@@ -68,7 +68,9 @@ __global__ void __launch_bounds__(256, MVR_PIPE_MINB)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
     float2 *stages = tw + n;
+    pdl_trigger();
     for (int i = threadIdx.x; i < n; i += 256) tw[i] = __ldg(&twg[i]);
+    pdl_wait();  // the spectra are the predecessor's output
     const int pc = threadIdx.x % NP;  // this thread's column in the copies and the stores
     const int prow = threadIdx.x / NP;
     // tile -> (block offset, base of column 0 at row 0, column stride, live columns)

@@ -22,6 +22,7 @@
 // CTA works on a tile with a single live column.
 #pragma once
 #include "cols_warp.cuh"
+#include "pdl.cuh"
 
 namespace mvr {
 
@@ -128,6 +129,7 @@ __global__ void __launch_bounds__(16 * NP, NP == 16 ? MVR_TCOLS_MINB : 2)
     float2 *A = reinterpret_cast<float2 *>(smem_raw);  // [n][NP]
     float2 *tw = A + n * NP;                            // [n]: exp(-2 pi i j / n)
     float2 *KA = tw + n;                                // MODE 2: [n][NP] tile of K^
+    pdl_trigger();
     for (int i = threadIdx.x; i < n; i += NT) tw[i] = __ldg(&twg[i]);
     // tile column p of row i at base + i * estride + p * pstride.  The grid covers the
     // other-axis indices olo + blockIdx.y < nother.  With gather, the last x tile of the grid
@@ -159,6 +161,7 @@ __global__ void __launch_bounds__(16 * NP, NP == 16 ? MVR_TCOLS_MINB : 2)
     const bool plive = pc < np;
     const long long coff = base + (long long)pc * pstride + (long long)(threadIdx.x / NP) * estride;
     const long long rstep = (long long)(NT / NP) * estride;
+    pdl_wait();  // the spectra are the predecessor's output
     {
         const float2 *sp = src + coff;
         const float2 *kp = Kh + coff;

@@ -614,9 +614,9 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
                         k_tcols_pipe<V_, 1><<<std::min(pg.ntiles, pipe_resident<V_, 1>()), kThreads, ps, stream_>>>(
                             src, dst, Kh, Hx, estride, ostride, Pc, tw, gather, ohi, rlo, rhi, olo, pg);
                     else
-                        k_tcols_pipe<V_, 2><<<std::min(pg.ntiles, pipe_resident<V_, 2>()), kThreads,
-                                              pipe_smem<V_, 2>(), stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc,
-                                                                             tw, gather, ohi, rlo, rhi, olo, pg);
+                        MVR_CUDA(launch_pdl(k_tcols_pipe<V_, 2>, std::min(pg.ntiles, pipe_resident<V_, 2>()), kThreads,
+                                            pipe_smem<V_, 2>(), stream_, src, dst, Kh, Hx, estride, ostride, Pc, tw,
+                                            gather, ohi, rlo, rhi, olo, pg));
                 });
                 MVR_LAUNCHED("k_tcols_pipe");
                 return prof_end();
@@ -625,14 +625,14 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
             const dim3 tgrid((unsigned)((hmain + kTColNP - 1) / kTColNP + gather), (unsigned)(ohi - olo), (unsigned)nb);
             TILE_COLS(tc, {
                 if (mode == 0)
-                    k_tcols<V_, 0><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw, gather,
-                                                                      ohi, rlo, rhi, olo);
+                    MVR_CUDA(launch_pdl(k_tcols<V_, 0>, tgrid, kThreads, ts, stream_, src, dst, Kh, Hx, estride, ostride, Pc, tw,
+                                       gather, ohi, rlo, rhi, olo));
                 else if (mode == 1)
-                    k_tcols<V_, 1><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw, gather,
-                                                                      ohi, rlo, rhi, olo);
+                    MVR_CUDA(launch_pdl(k_tcols<V_, 1>, tgrid, kThreads, ts, stream_, src, dst, Kh, Hx, estride, ostride, Pc, tw,
+                                       gather, ohi, rlo, rhi, olo));
                 else
-                    k_tcols<V_, 2><<<tgrid, kThreads, ts, stream_>>>(src, dst, Kh, Hx, estride, ostride, Pc, tw, gather,
-                                                                      ohi, rlo, rhi, olo);
+                    MVR_CUDA(launch_pdl(k_tcols<V_, 2>, tgrid, kThreads, ts, stream_, src, dst, Kh, Hx, estride, ostride, Pc, tw,
+                                       gather, ohi, rlo, rhi, olo));
             });
             MVR_LAUNCHED("k_tcols");
             return prof_end();

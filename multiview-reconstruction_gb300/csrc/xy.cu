@@ -82,8 +82,8 @@ cudaError_t fwd(int combo, const Src &src, float2 *S, const BlockMaps &bms, int 
 {
     set_limits();
     const dim3 grid((unsigned)Pz, (unsigned)nb);
-    XY_DISPATCH(combo, (k_xy_fwd<VX_, VY_, Src><<<grid, XYShape<VX_, VY_>::NT, xy_smem_bytes<VX_, VY_>(), s>>>(
-                           src, S, bms, Pc, twx, twy)));
+    XY_DISPATCH(combo, return launch_pdl(k_xy_fwd<VX_, VY_, Src>, grid, XYShape<VX_, VY_>::NT,
+                                         xy_smem_bytes<VX_, VY_>(), s, src, S, bms, Pc, twx, twy));
     return cudaGetLastError();
 }
 
@@ -112,8 +112,8 @@ cudaError_t xy_ratio(int combo, float2 *S, const float *img, const BlockMaps &bm
 {
     set_limits();
     const dim3 grid((unsigned)Pz, (unsigned)nb);
-    XY_DISPATCH(combo, (k_xy_ratio<VX_, VY_><<<grid, XYShape<VX_, VY_>::NT, xy_smem_bytes<VX_, VY_>(), s>>>(S, img, bms, Pc, twx,
-                                                                                                 twy)));
+    XY_DISPATCH(combo, return launch_pdl(k_xy_ratio<VX_, VY_>, grid, XYShape<VX_, VY_>::NT, xy_smem_bytes<VX_, VY_>(),
+                                         s, S, img, bms, Pc, twx, twy));
     return cudaGetLastError();
 }
 
@@ -129,9 +129,9 @@ cudaError_t xy_update(int combo, int epi, float2 *S, const UpdateArgs &ua, const
         if (planes < 1) return cudaSuccess;
     }
     const dim3 grid((unsigned)planes, (unsigned)nb);
-#define XY_UPD(E)                                                                                               \
-    XY_DISPATCH(combo, (k_xy_update<VX_, VY_, E><<<grid, XYShape<VX_, VY_>::NT, xy_smem_bytes<VX_, VY_>(), s>>>(S, ua, bms, \
-                                                                                                    Pc, twx, twy)))
+#define XY_UPD(E)                                                                                           \
+    XY_DISPATCH(combo, return launch_pdl(k_xy_update<VX_, VY_, E>, grid, XYShape<VX_, VY_>::NT,              \
+                                         xy_smem_bytes<VX_, VY_>(), s, S, ua, bms, Pc, twx, twy))
     switch (epi) {
     case EPI_SEQ: XY_UPD(EPI_SEQ); break;
     case EPI_MUL_FIRST: XY_UPD(EPI_MUL_FIRST); break;

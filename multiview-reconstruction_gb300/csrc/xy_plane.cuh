@@ -31,6 +31,7 @@
 #pragma once
 #include "rows_warp.cuh"
 #include "cols_tile.cuh"
+#include "pdl.cuh"
 
 namespace mvr {
 
@@ -374,6 +375,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
     constexpr int NT = SH::NT, RX = SH::RX;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     XYSmem<VX, VY> sm(smem_raw);
+    pdl_trigger();
     const BlockMap &bm = bms.m[blockIdx.y];
     const int z = blockIdx.x;
     float2 *Sp = S + (long long)blockIdx.y * Pc + (long long)z * SH::plane;
@@ -385,6 +387,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
     }
     if (MIR)
         for (int x = threadIdx.x; x < SH::Px; x += NT) sm.colx[x] = (int)mirror_x(bm, x);
+    pdl_wait();  // the source volume is the predecessor's output
     __syncthreads();
     // all loads of the thread's row items first, then their x phase 1
     float2 a[RX][VX];
@@ -431,6 +434,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
     constexpr int NT = SH::NT, RX = SH::RX;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     XYSmem<VX, VY> sm(smem_raw);
+    pdl_trigger();
     const BlockMap &bm = bms.m[blockIdx.y];
     const int z = blockIdx.x;
     float2 *Sp = S + (long long)blockIdx.y * Pc + (long long)z * SH::plane;
@@ -446,6 +450,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
         const long long gx = bm.off[0] + bx;
         sm.colx[x] = (bx >= 0 && bx < bm.b[0] && gx >= 0 && gx < bm.D[0]) ? (int)gx : -1;
     }
+    pdl_wait();
     xy_load_plane<VX, VY>(sm.A, Sp);
     __syncthreads();
     xy_y<VX, VY, true>(sm.A, sm.twy, sm.posy);
@@ -489,6 +494,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double red_s[32], red_m[32];
     XYSmem<VX, VY> sm(smem_raw);
+    pdl_trigger();
     const BlockMap &bm = bms.m[blockIdx.y];
     int z = blockIdx.x;
     if (ua.prune) {  // the grid covers the deepest write region of the batch
@@ -523,6 +529,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
             sm.colx2[x] = (in && gx >= 0 && gx < bm.D[0]) ? (int)gx : -1;
             sm.colx3[x] = (in && x >= bm.wlo[0] && x < bm.whi[0]) ? x : -1;
         }
+        pdl_wait();
         xy_load_plane<VX, VY>(sm.A, Sp);
         __syncthreads();
         xy_y<VX, VY, true>(sm.A, sm.twy, sm.posy);
@@ -579,6 +586,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
             }
         }
     } else {
+        pdl_wait();
         xy_load_plane<VX, VY>(sm.A, Sp);
         __syncthreads();
         xy_y<VX, VY, true>(sm.A, sm.twy, sm.posy);
