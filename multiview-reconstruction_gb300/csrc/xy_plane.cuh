@@ -280,12 +280,25 @@ __device__ __forceinline__ void xy_y(float2 *A, const float2 *twy, const int *po
             }
         }
     } else {
-        for (int q = threadIdx.x; q < Py; q += NT) {
-            const float2 a = A[q * S::SR], b = A[q * S::SR + m];
-            A[q * S::SR] = make_float2(a.x - b.y, a.y + b.x);
+        // phase 2 inverse; the items of column 0 first recombine Y0 + i Ym from columns 0 and m
+        constexpr int T = 16, items = m * VY;
+        for (int it = threadIdx.x; it < items; it += NT) {
+            const int k1 = it / m, p = it - k1 * m;
+            float2 *b0 = A + p + T * k1 * S::SR;
+            float2 b[T];
+#pragma unroll
+            for (int t = 0; t < T; ++t) b[t] = b0[t * S::SR];
+            if (p == 0) {
+#pragma unroll
+                for (int t = 0; t < T; ++t) {
+                    const float2 c = b0[t * S::SR + m];
+                    b[t] = make_float2(b[t].x - c.y, b[t].y + c.x);
+                }
+            }
+            sdft<T, true>(b);
+#pragma unroll
+            for (int t = 0; t < T; ++t) b0[t * S::SR] = b[t];
         }
-        __syncthreads();
-        tp_phase2<VY, m, 1, S::SR, true, NT>(A);
         __syncthreads();
         tp_phase1<VY, m, 1, S::SR, true, NT>(A, twy, 1);
     }
