@@ -3,6 +3,7 @@
 #include "xy_plane.cuh"
 
 #include <algorithm>
+#include <cstdlib>
 #include <mutex>
 
 namespace mvr {
@@ -65,6 +66,20 @@ void set_limits_one()
     cudaFuncSetAttribute(k_xy_update<VX, VY, EPI_NLL>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
 }
 
+// CTAs of the persistent plane kernels: one per SM (MVR_XY_PERSIST=0: one per plane).
+int persist_ctas()
+{
+    static int n = 0;
+    if (!n) {
+        const char *e = std::getenv("MVR_XY_PERSIST");
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        n = (e && e[0] == '0') ? (1 << 30) : std::max(1, sms);
+    }
+    return n;
+}
+
 void set_limits()
 {
     static std::once_flag once;
@@ -81,9 +96,10 @@ cudaError_t fwd(int combo, const Src &src, float2 *S, const BlockMaps &bms, int 
                 const float2 *twx, const float2 *twy, cudaStream_t s)
 {
     set_limits();
-    const dim3 grid((unsigned)Pz, (unsigned)nb);
+    const int nitems = Pz * nb;
+    const dim3 grid((unsigned)std::min(nitems, persist_ctas()));
     XY_DISPATCH(combo, return launch_pdl(k_xy_fwd<VX_, VY_, Src>, grid, XYShape<VX_, VY_>::NT,
-                                         xy_smem_bytes<VX_, VY_>(), s, src, S, bms, Pc, twx, twy));
+                                         xy_smem_bytes<VX_, VY_>(), s, src, S, bms, Pc, twx, twy, Pz, nitems));
     return cudaGetLastError();
 }
 
@@ -111,9 +127,10 @@ cudaError_t xy_ratio(int combo, float2 *S, const float *img, const BlockMaps &bm
                      const float2 *twx, const float2 *twy, cudaStream_t s)
 {
     set_limits();
-    const dim3 grid((unsigned)Pz, (unsigned)nb);
+    const int nitems = Pz * nb;
+    const dim3 grid((unsigned)std::min(nitems, persist_ctas()));
     XY_DISPATCH(combo, return launch_pdl(k_xy_ratio<VX_, VY_>, grid, XYShape<VX_, VY_>::NT, xy_smem_bytes<VX_, VY_>(),
-                                         s, S, img, bms, Pc, twx, twy));
+                                         s, S, img, bms, Pc, twx, twy, Pz, nitems));
     return cudaGetLastError();
 }
 

@@ -371,6 +371,19 @@ __device__ __forceinline__ void xy_store_plane(float2 *__restrict__ Sp, const fl
     for (int i = threadIdx.x; i < n4; i += blockDim.x) dst[i] = src[i];
 }
 
+// L2 prefetch of item `next`'s plane (persistent plane kernels): one 128-byte line per
+// thread and step, issued before the current plane is transformed.
+template <int VX, int VY>
+__device__ __forceinline__ void xy_prefetch_next(const float2 *S, long long Pc, int Pz, int next, int nitems)
+{
+    if (next >= nitems) return;
+    constexpr int bytes = XYShape<VX, VY>::plane * (int)sizeof(float2), NT = XYShape<VX, VY>::NT;
+    const int nb = next / Pz, nz = next - nb * Pz;
+    const char *p = reinterpret_cast<const char *>(S + (long long)nb * Pc + (long long)nz * XYShape<VX, VY>::plane);
+    for (int off = threadIdx.x * 128; off < bytes; off += NT * 128)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(p + off));
+}
+
 // ---- forward: source rows -> R2C x -> FFT y ---------------------------------------------
 template <typename Src>
 struct XYSrcTraits { static constexpr bool mirror = false; };
@@ -382,56 +395,60 @@ struct XYSrcTraits<SrcMirror<float>> { static constexpr bool mirror = true; };
 template <int VX, int VY, class Src>
 __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
     k_xy_fwd(Src src, float2 *__restrict__ S, const BlockMaps bms, long long Pc, const float2 *__restrict__ gtwx,
-             const float2 *__restrict__ gtwy)
+             const float2 *__restrict__ gtwy, int Pz, int nitems)
 {
     typedef XYShape<VX, VY> SH;
     constexpr int NT = SH::NT, RX = SH::RX;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     XYSmem<VX, VY> sm(smem_raw);
     pdl_trigger();
-    const BlockMap &bm = bms.m[blockIdx.y];
-    const int z = blockIdx.x;
-    float2 *Sp = S + (long long)blockIdx.y * Pc + (long long)z * SH::plane;
     sm.load_tables(gtwx, gtwy);
     constexpr bool MIR = XYSrcTraits<Src>::mirror;
-    for (int y = threadIdx.x; y < SH::Py; y += NT) {
-        const typename Src::Row r = src.row(bm, y, z);
-        sm.rowb[y] = r.base;
-    }
-    if (MIR)
-        for (int x = threadIdx.x; x < SH::Px; x += NT) sm.colx[x] = (int)mirror_x(bm, x);
     pdl_wait();  // the source volume is the predecessor's output
-    __syncthreads();
-    // all loads of the thread's row items first, then their x phase 1
-    float2 a[RX][VX];
+    // persistent: the CTA walks the (block, plane) items blockIdx.x, + gridDim.x, ...
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const int bi = item / Pz, z = item - bi * Pz;
+        const BlockMap &bm = bms.m[bi];
+        float2 *Sp = S + (long long)bi * Pc + (long long)z * SH::plane;
+        for (int y = threadIdx.x; y < SH::Py; y += NT) {
+            const typename Src::Row r = src.row(bm, y, z);
+            sm.rowb[y] = r.base;
+        }
+        if (MIR)
+            for (int x = threadIdx.x; x < SH::Px; x += NT) sm.colx[x] = (int)mirror_x(bm, x);
+        __syncthreads();
+        // all loads of the thread's row items first, then their x phase 1
+        float2 a[RX][VX];
 #pragma unroll
-    for (int r = 0; r < RX; ++r) {
-        const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;
+        for (int r = 0; r < RX; ++r) {
+            const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;
 #pragma unroll
-        for (int v = 0; v < VX; ++v) {
-            const int x = 2 * (t + 16 * v);
-            if constexpr (MIR) {
-                const float *pr = src.vol + sm.rowb[y];
-                const int2 cx = *reinterpret_cast<const int2 *>(sm.colx + x);  // x even: one 8-byte read
-                a[r][v] = make_float2(__ldg(pr + cx.x), __ldg(pr + cx.y));
-            } else {
-                typename Src::Row row;
-                row.base = sm.rowb[y];
-                a[r][v] = make_float2(src.template at<float>(row, bm, x), src.template at<float>(row, bm, x + 1));
+            for (int v = 0; v < VX; ++v) {
+                const int x = 2 * (t + 16 * v);
+                if constexpr (MIR) {
+                    const float *pr = src.vol + sm.rowb[y];
+                    const int2 cx = *reinterpret_cast<const int2 *>(sm.colx + x);  // x even: one 8-byte read
+                    a[r][v] = make_float2(__ldg(pr + cx.x), __ldg(pr + cx.y));
+                } else {
+                    typename Src::Row row;
+                    row.base = sm.rowb[y];
+                    a[r][v] = make_float2(src.template at<float>(row, bm, x), src.template at<float>(row, bm, x + 1));
+                }
             }
         }
-    }
 #pragma unroll
-    for (int r = 0; r < RX; ++r) {
-        const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;
-        xrow_p1<VX, false>(a[r], sm.twx, t);
+        for (int r = 0; r < RX; ++r) {
+            const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;
+            xrow_p1<VX, false>(a[r], sm.twx, t);
 #pragma unroll
-        for (int v = 0; v < VX; ++v) sm.A[y * SH::SR + t + 16 * v] = a[r][v];
+            for (int v = 0; v < VX; ++v) sm.A[y * SH::SR + t + 16 * v] = a[r][v];
+        }
+        __syncthreads();
+        xy_x_forward_p2<VX, VY>(sm.A, sm.twx, sm.posx);
+        xy_y<VX, VY, false>(sm.A, sm.twy, sm.posy);
+        xy_store_plane<VX, VY>(Sp, sm.A);
+        __syncthreads();  // the next item rewrites the plane and the row / column tables
     }
-    __syncthreads();
-    xy_x_forward_p2<VX, VY>(sm.A, sm.twx, sm.posx);
-    xy_y<VX, VY, false>(sm.A, sm.twy, sm.posy);
-    xy_store_plane<VX, VY>(Sp, sm.A);
 }
 
 // ---- C2R -> quotient -> R2C ----------------------------------------------------------
@@ -441,59 +458,65 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
 template <int VX, int VY>
 __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
     k_xy_ratio(float2 *__restrict__ S, const float *__restrict__ img, const BlockMaps bms, long long Pc,
-               const float2 *__restrict__ gtwx, const float2 *__restrict__ gtwy)
+               const float2 *__restrict__ gtwx, const float2 *__restrict__ gtwy, int Pz, int nitems)
 {
     typedef XYShape<VX, VY> SH;
     constexpr int NT = SH::NT, RX = SH::RX;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     XYSmem<VX, VY> sm(smem_raw);
     pdl_trigger();
-    const BlockMap &bm = bms.m[blockIdx.y];
-    const int z = blockIdx.x;
-    float2 *Sp = S + (long long)blockIdx.y * Pc + (long long)z * SH::plane;
     sm.load_tables(gtwx, gtwy);
-    const int ez = ext_e(z, bm.P[2], bm.L[2]);
-    for (int y = threadIdx.x; y < SH::Py; y += NT) {
-        const int ey = ext_e(y, bm.P[1], bm.L[1]);
-        const bool rin = ey >= 0 && ey < bm.b[1] && ez >= 0 && ez < bm.b[2];
-        sm.rowb[y] = rin ? zero_row(bm, ey, ez).base : -1;
-    }
-    for (int x = threadIdx.x; x < SH::Px; x += NT) {
-        const int bx = ext_e(x, bm.P[0], bm.L[0]);
-        const long long gx = bm.off[0] + bx;
-        sm.colx[x] = (bx >= 0 && bx < bm.b[0] && gx >= 0 && gx < bm.D[0]) ? (int)gx : -1;
-    }
     pdl_wait();
-    xy_load_plane<VX, VY>(sm.A, Sp);
-    __syncthreads();
-    xy_y<VX, VY, true>(sm.A, sm.twy, sm.posy);
-    xy_x_inverse_p2<VX, VY>(sm.A, sm.twx, sm.posx);
-#pragma unroll 1
-    for (int r = 0; r < RX; ++r) {
-        const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;
-        const long long rb = sm.rowb[y];
-        float im[VX][2];
-#pragma unroll
-        for (int v = 0; v < VX; ++v) {
-            const int2 cx = *reinterpret_cast<const int2 *>(sm.colx + 2 * (t + 16 * v));
-            im[v][0] = (rb >= 0 && cx.x >= 0) ? __ldg(img + rb + cx.x) : 0.0f;
-            im[v][1] = (rb >= 0 && cx.y >= 0) ? __ldg(img + rb + cx.y) : 0.0f;
+    // persistent: the CTA walks the (block, plane) items blockIdx.x, + gridDim.x, ...
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const int bi = item / Pz, z = item - bi * Pz;
+        const BlockMap &bm = bms.m[bi];
+        float2 *Sp = S + (long long)bi * Pc + (long long)z * SH::plane;
+        xy_prefetch_next<VX, VY>(S, Pc, Pz, item + gridDim.x, nitems);
+        const int ez = ext_e(z, bm.P[2], bm.L[2]);
+        for (int y = threadIdx.x; y < SH::Py; y += NT) {
+            const int ey = ext_e(y, bm.P[1], bm.L[1]);
+            const bool rin = ey >= 0 && ey < bm.b[1] && ez >= 0 && ez < bm.b[2];
+            sm.rowb[y] = rin ? zero_row(bm, ey, ez).base : -1;
         }
-        float2 a[VX];
-        float2 *row = sm.A + y * SH::SR + t;
+        for (int x = threadIdx.x; x < SH::Px; x += NT) {
+            const int bx = ext_e(x, bm.P[0], bm.L[0]);
+            const long long gx = bm.off[0] + bx;
+            sm.colx[x] = (bx >= 0 && bx < bm.b[0] && gx >= 0 && gx < bm.D[0]) ? (int)gx : -1;
+        }
+        xy_load_plane<VX, VY>(sm.A, Sp);
+        __syncthreads();
+        xy_y<VX, VY, true>(sm.A, sm.twy, sm.posy);
+        xy_x_inverse_p2<VX, VY>(sm.A, sm.twx, sm.posx);
+#pragma unroll 1
+        for (int r = 0; r < RX; ++r) {
+            const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;
+            const long long rb = sm.rowb[y];
+            float im[VX][2];
 #pragma unroll
-        for (int v = 0; v < VX; ++v) a[v] = row[16 * v];
-        xrow_p1<VX, true>(a, sm.twx, t);  // natural order: a[v] = conv1 at x = 2 (t + 16 v) + {0, 1}
+            for (int v = 0; v < VX; ++v) {
+                const int2 cx = *reinterpret_cast<const int2 *>(sm.colx + 2 * (t + 16 * v));
+                im[v][0] = (rb >= 0 && cx.x >= 0) ? __ldg(img + rb + cx.x) : 0.0f;
+                im[v][1] = (rb >= 0 && cx.y >= 0) ? __ldg(img + rb + cx.y) : 0.0f;
+            }
+            float2 a[VX];
+            float2 *row = sm.A + y * SH::SR + t;
 #pragma unroll
-        for (int v = 0; v < VX; ++v) a[v] = make_float2(quotient_fast(im[v][0], a[v].x), quotient_fast(im[v][1], a[v].y));
-        xrow_p1<VX, false>(a, sm.twx, t);
+            for (int v = 0; v < VX; ++v) a[v] = row[16 * v];
+            xrow_p1<VX, true>(a, sm.twx, t);  // natural order: a[v] = conv1 at x = 2 (t + 16 v) + {0, 1}
 #pragma unroll
-        for (int v = 0; v < VX; ++v) row[16 * v] = a[v];
+            for (int v = 0; v < VX; ++v)
+                a[v] = make_float2(quotient_fast(im[v][0], a[v].x), quotient_fast(im[v][1], a[v].y));
+            xrow_p1<VX, false>(a, sm.twx, t);
+#pragma unroll
+            for (int v = 0; v < VX; ++v) row[16 * v] = a[v];
+        }
+        __syncthreads();
+        xy_x_forward_p2<VX, VY>(sm.A, sm.twx, sm.posx);
+        xy_y<VX, VY, false>(sm.A, sm.twy, sm.posy);
+        xy_store_plane<VX, VY>(Sp, sm.A);
+        __syncthreads();  // the next item rewrites the plane and the row / column tables
     }
-    __syncthreads();
-    xy_x_forward_p2<VX, VY>(sm.A, sm.twx, sm.posx);
-    xy_y<VX, VY, false>(sm.A, sm.twy, sm.posy);
-    xy_store_plane<VX, VY>(Sp, sm.A);
 }
 
 // ---- C2R -> update epilogue --------------------------------------------------------------
