@@ -248,6 +248,9 @@ typedef struct mvr_fuse_view {
     int decon_blend;          /* the same for the deconvolution weight */
     float decon_border[3];
     float decon_range[3];
+    int intensity_adjust;     /* 1: every image value v becomes (float)(v m00 + m01) before the
+                                 interpolation (IntensityAdjuster, intensity[] = {m00, m01}) */
+    double intensity[2];
 } mvr_fuse_view;
 /* bb_min: world coordinate of the box's first voxel; bb_dims {x, y, z}; image_out and
  * weight_out: device float volumes of the box.  Synchronous on `stream`. */

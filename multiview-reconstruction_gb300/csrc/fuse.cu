@@ -36,6 +36,8 @@ struct FuseView {
     double inv[12];  // world -> view pixel, row-packed 3 x 4
     float fb[3], fr[3], db[3], dr[3];
     int fblend, dblend;
+    int adjust;        // intensity adjustment v -> v m00 + m01 (double, stored as float)
+    double m00, m01;
 };
 
 struct FuseViews {
@@ -67,14 +69,20 @@ __device__ __forceinline__ float blend_weight(const float *loc, const int *dims,
 }
 
 // Linear interpolation of a float volume at t (all eight neighbours exist: t is strictly
-// inside), the interpolator of the reference's views (NLinearInterpolator3D order).
-__device__ __forceinline__ float trilinear(const float *__restrict__ img, const int *dims, const double *t)
+// inside), the interpolator of the reference's views (NLinearInterpolator3D order); with
+// `adjust` every neighbour goes through the intensity adjustment first
+// (IntensityAdjuster.apply, fusion/intensityadjust/IntensityAdjuster.java: v m00 + m01 in
+// double, stored as float).
+__device__ __forceinline__ float trilinear(const FuseView &v, const double *t)
 {
     const double f[3] = {floor(t[0]), floor(t[1]), floor(t[2])};
     const double w[3] = {__dsub_rn(t[0], f[0]), __dsub_rn(t[1], f[1]), __dsub_rn(t[2], f[2])};
-    const long long sy = dims[0], sz = (long long)dims[0] * dims[1];
-    const float *p = img + (long long)f[2] * sz + (long long)f[1] * sy + (long long)f[0];
-    return nlinear3(w, [&](int dx, int dy, int dz) { return __ldg(p + dz * sz + dy * sy + dx); });
+    const long long sy = v.dims[0], sz = (long long)v.dims[0] * v.dims[1];
+    const float *p = v.img + (long long)f[2] * sz + (long long)f[1] * sy + (long long)f[0];
+    return nlinear3(w, [&](int dx, int dy, int dz) {
+        const float x = __ldg(p + dz * sz + dy * sy + dx);
+        return v.adjust ? __double2float_rn(__dadd_rn(__dmul_rn((double)x, v.m00), v.m01)) : x;
+    });
 }
 
 __global__ void k_fuse_group(FuseViews fv, long long bx, long long by, long long bz, int nx, int ny, int nz,
@@ -100,7 +108,7 @@ __global__ void k_fuse_group(FuseViews fv, long long bx, long long by, long long
             float val = 0.0f;  // outsideValueImg
             if (t[0] > 0.0 && t[1] > 0.0 && t[2] > 0.0 && t[0] < v.dims[0] - 1 && t[1] < v.dims[1] - 1 &&
                 t[2] < v.dims[2] - 1)
-                val = fmaxf(1.0f, trilinear(v.img, v.dims, t));  // minValueImg
+                val = fmaxf(1.0f, trilinear(v, t));  // minValueImg
             sumI += (double)val * (double)wf;
             sumW += (double)wf;
         }
@@ -148,6 +156,9 @@ extern "C" MVR_API int mvr_fuse_group(const mvr_fuse_view *views, int num_views,
         }
         v.fblend = s.fusion_blend;
         v.dblend = s.decon_blend;
+        v.adjust = s.intensity_adjust ? 1 : 0;
+        v.m00 = s.intensity[0];
+        v.m01 = s.intensity[1];
         v.img = s.img;
         if (!invert_affine(s.model, v.inv)) return fuse_fail(MVR_ERR_ARG, "mvr_fuse_group: a view model is singular");
     }

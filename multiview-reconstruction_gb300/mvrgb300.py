@@ -557,14 +557,16 @@ def device_info(device: int = 0) -> dict:
 class _FuseView(C.Structure):
     _fields_ = [("img", C.c_void_p), ("dims", C.c_int * 3), ("model", C.c_double * 12), ("fusion_blend", C.c_int),
                 ("fusion_border", C.c_float * 3), ("fusion_range", C.c_float * 3), ("decon_blend", C.c_int),
-                ("decon_border", C.c_float * 3), ("decon_range", C.c_float * 3)]
+                ("decon_border", C.c_float * 3), ("decon_range", C.c_float * 3), ("intensity_adjust", C.c_int),
+                ("intensity", C.c_double * 2)]
 
 
 def fuse_group(views, bb_min, bb_dims, image_out_ptr: int, weight_out_ptr: int, device: int = 0, stream: int = 0):
     """ProcessInputImages.fuseGroups for one group on the device.  views: dicts with
     'img_ptr' (device float volume), 'dims' (x, y, z), 'model' (3 x 4 view -> world) and
     optional 'fusion' / 'decon' blendings as (border xyz, range xyz).  Writes the fused image
-    and the summed deconvolution weight of the bounding box (device float volumes)."""
+    and the summed deconvolution weight of the bounding box (device float volumes).  An optional
+    'intensity' = (m00, m01) applies the view's intensity adjustment v m00 + m01."""
     L = load()
     arr = (_FuseView * len(views))()
     for k, v in enumerate(views):
@@ -579,6 +581,9 @@ def fuse_group(views, bb_min, bb_dims, image_out_ptr: int, weight_out_ptr: int, 
             if b is not None:
                 setattr(a, border, (C.c_float * 3)(*b[0]))
                 setattr(a, rng, (C.c_float * 3)(*b[1]))
+        if v.get("intensity") is not None:
+            a.intensity_adjust = 1
+            a.intensity = (C.c_double * 2)(*v["intensity"])
     rc = L.mvr_fuse_group(C.cast(arr, C.c_void_p), len(views), (C.c_longlong * 3)(*bb_min), (C.c_int * 3)(*bb_dims),
                           C.c_void_p(image_out_ptr), C.c_void_p(weight_out_ptr), device,
                           C.c_void_p(stream) if stream else None)

@@ -412,7 +412,8 @@ def fuse_group(views, bb_min, bb_dims):
     (TransformedInputRandomAccess.get, AbstractTransformedIntervalRandomAccess
     .intersectsLinearInterpolation), weighted by its blending and averaged (FusedRandomAccess
     .get); the deconvolution weight is the sum of the views' deconvolution blendings
-    (CombineWeightsSumRandomAccess.get).  Returns (image, weight) float32 [z][y][x]."""
+    (CombineWeightsSumRandomAccess.get).  An optional 'intensity' = (m00, m01) adjusts the view's
+    values first (IntensityAdjuster).  Returns (image, weight) float32 [z][y][x]."""
     nx, ny, nz = bb_dims
     z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
     s = np.stack([x + bb_min[0], y + bb_min[1], z + bb_min[2]], axis=-1).astype(np.float64)
@@ -422,6 +423,11 @@ def fuse_group(views, bb_min, bb_dims):
     sumD = np.zeros(s.shape[:-1])
     for v in views:
         img = np.asarray(v["img"], dtype=np.float32)
+        if v.get("intensity") is not None:
+            # IntensityAdjuster.apply (fusion/intensityadjust/IntensityAdjuster.java): v m00 + m01
+            # in double, stored as float, before the interpolation
+            m00, m01 = v["intensity"]
+            img = (img.astype(np.float64) * m00 + m01).astype(np.float32)
         dims = (img.shape[2], img.shape[1], img.shape[0])
         inv = _invert_affine(v["model"])
         t = apply_affine(inv, s)

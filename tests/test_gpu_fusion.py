@@ -30,6 +30,8 @@ def test_fuse_group_matches_oracle(blend):
         img = rng.uniform(0, 300, (20, 40, 48)).astype(np.float32)  # [z][y][x]
         m = model(ang, 1.5, (2.37 + k, -1.71, tz + 0.43))  # fractional: samples rarely land on a border
         v = {"img": img, "model": m}
+        if k == 1:
+            v["intensity"] = (1.37, -4.25)  # IntensityAdjuster of the second view
         if blend:
             v["fusion"] = ((2.0, 2.0, 1.0), (10.0, 10.0, 4.0))
             v["decon"] = ((1.0, 1.0, 0.5), (6.0, 6.0, 3.0))
@@ -42,7 +44,7 @@ def test_fuse_group_matches_oracle(blend):
     gv = []
     for v, d in zip(views, dev):
         g = {"img_ptr": d.data_ptr(), "dims": (v["img"].shape[2], v["img"].shape[1], v["img"].shape[0]),
-             "model": v["model"]}
+             "model": v["model"], "intensity": v.get("intensity")}
         if blend:
             g["fusion"], g["decon"] = v["fusion"], v["decon"]
         gv.append(g)

@@ -282,6 +282,10 @@ def test_fusion_known_answers():
     assert wts[0] == 0 and abs(wts[1] - 0.5) < 1e-6 and wts[2] == 1
     # two views with complementary blending average with their weights; the deconvolution
     # weight is the plain sum
+    # intensity adjustment v m00 + m01 (double, stored as float) before the interpolation
+    im, _ = O.fuse_group([{"img": img, "model": ident, "intensity": (2.5, 3.0)}], (0, 0, 0), (8, 7, 6))
+    adj = (img.astype(np.float64) * 2.5 + 3.0).astype(np.float32)
+    assert np.array_equal(im[1:-1, 1:-1, 1:-1], np.maximum(1, adj[1:-1, 1:-1, 1:-1]))
     im, w = O.fuse_group([{"img": img, "model": ident}, {"img": 3 * img, "model": ident}], (0, 0, 0), (8, 7, 6))
     assert np.allclose(im[1:-1, 1:-1, 1:-1], 0.5 * (np.maximum(1, img) + np.maximum(1, 3 * img))[1:-1, 1:-1, 1:-1],
                        rtol=1e-6)
