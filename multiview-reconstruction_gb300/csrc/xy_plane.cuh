@@ -3,7 +3,8 @@
 // held in shared memory.
 //
 // For FFT domains Px = 32 VX (real x rows of m = 16 VX packed complex values) and
-// Py = 16 VY, one CTA takes one z-plane of one block:
+// Py = 16 VY, a CTA works on one z-plane of one block at a time (k_xy_fwd and k_xy_ratio are
+// persistent: one CTA per SM walks the (block, plane) items; k_xy_update takes one plane):
 //   k_xy_fwd     rows from the source (psi under the mirror mapping, a zero-extended
 //                block, or a wrapped kernel) -> R2C along x -> FFT along y -> plane of S
 //   k_xy_ratio   plane of S -> inverse y -> C2R along x -> quotient img / conv1
