@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(256) k_rows_fwd(Src src, typename Cx<T>::t *__
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int r = warp; r < nr; r += nw) {
         const long long row = row0 + r;
-        const int y = (int)(row % bm.P[1]), z = (int)(row / bm.P[1]);
+        const int z = (int)((unsigned)row / (unsigned)bm.P[1]), y = (int)row - z * bm.P[1];  // rows < 2^31
         const typename Src::Row R = src.row(bm, y, z);
         for (int c0 = 0; c0 < m; c0 += 32 * kRowBatch) {
             T v0[kRowBatch], v1[kRowBatch];
@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(256) k_rows_ratio(typename Cx<T>::t *__restric
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int r = warp; r < nr; r += nw) {
         const long long row = row0 + r;
-        const int y = (int)(row % bm.P[1]), z = (int)(row / bm.P[1]);
+        const int z = (int)((unsigned)row / (unsigned)bm.P[1]), y = (int)row - z * bm.P[1];  // rows < 2^31
         const int ey = ext_e(y, bm.P[1], bm.L[1]), ez = ext_e(z, bm.P[2], bm.L[2]);
         const bool rin = ey >= 0 && ey < bm.b[1] && ez >= 0 && ez < bm.b[2];
         const ZeroRow zr = rin ? zero_row(bm, ey, ez) : ZeroRow{-1};
@@ -671,7 +671,7 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int r = warp; r < nr; r += nw) {
         const long long row = row0 + r;
-        const int y = (int)(row % bm.P[1]), z = (int)(row / bm.P[1]);
+        const int z = (int)((unsigned)row / (unsigned)bm.P[1]), y = (int)row - z * bm.P[1];  // rows < 2^31
         if (y >= bm.b[1] || z >= bm.b[2]) continue;  // extension rows carry no block voxels
         update_row<T, EPI>(Z + r * ps, m, bm, ua, y, z, lane, ksum, kcomp, kmax);
     }

@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(256) k_wrows_fwd(const float *__restrict__ psi
     row_x_init(rx, bm, 2 * m, true);
     const long long nrows = (long long)bm.P[1] * bm.P[2];
     for (long long row = (long long)blockIdx.x * 8 + wib; row < nrows; row += (long long)gridDim.x * 8) {
-        const int y = (int)(row % bm.P[1]), z = (int)(row / bm.P[1]);
+        const int z = (int)((unsigned)row / (unsigned)bm.P[1]), y = (int)row - z * bm.P[1];  // rows < 2^31
         const float *pr = psi + mirror_row(bm, y, z).base;
         float2 a[R];
 #pragma unroll
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(256) k_wrows_ratio(float2 *__restrict__ S, con
         float2 *Srow = Sb + row * (m + 1);
         float2 a[R];
         warp_c2r_pre<R>(Srow, a, t, lane);
-        const int y = (int)(row % bm.P[1]), z = (int)(row / bm.P[1]);
+        const int z = (int)((unsigned)row / (unsigned)bm.P[1]), y = (int)row - z * bm.P[1];  // rows < 2^31
         const int ey = ext_e(y, bm.P[1], bm.L[1]), ez = ext_e(z, bm.P[2], bm.L[2]);
         const bool rin = ey >= 0 && ey < bm.b[1] && ez >= 0 && ez < bm.b[2];
         const long long zb = rin ? zero_row(bm, ey, ez).base : -1;
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(256) k_wrows_update(float2 *__restrict__ S, Up
     const long long r0 = ua.prune ? (long long)bm.wlo[2] * bm.P[1] : 0;
     const long long nrows = ua.prune ? (long long)bm.whi[2] * bm.P[1] : (long long)bm.P[1] * bm.P[2];
     for (long long row = r0 + (long long)blockIdx.x * 8 + wib; row < nrows; row += (long long)gridDim.x * 8) {
-        const int y = (int)(row % bm.P[1]), z = (int)(row / bm.P[1]);
+        const int z = (int)((unsigned)row / (unsigned)bm.P[1]), y = (int)row - z * bm.P[1];  // rows < 2^31
         if (y >= bm.b[1] || z >= bm.b[2]) continue;  // extension rows carry no block voxels
         const bool wrow = y >= bm.wlo[1] && y < bm.whi[1] && z >= bm.wlo[2] && z < bm.whi[2];
         if (ua.prune && !wrow) continue;
