@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(256) k_wrows_ratio(float2 *__restrict__ S, con
 #pragma unroll
         for (int s = 0; s < R; ++s) {
             const float2 c = srow[wib][lane + 32 * s];  // conv1 at x = 2q, 2q+1
-            a[s] = make_float2(quotient(im[s][0], c.x), quotient(im[s][1], c.y));
+            a[s] = make_float2(quotient_fast(im[s][0], c.x), quotient_fast(im[s][1], c.y));
         }
         __syncwarp();
         warp_fft<R, false>(a, t, lane);
@@ -242,7 +242,12 @@ __global__ void __launch_bounds__(256) k_wrows_update(float2 *__restrict__ S, Up
     const float *psrc = reinterpret_cast<const float *>(ua.psi_src);
     float *pdst = reinterpret_cast<float *>(ua.psi_dst);
     const float *wgt = ua.weight[0];
-    const float minI = ua.minI, maxI = ua.maxI;
+    UpdConst uc;
+    uc.minI = ua.minI;
+    uc.maxI = ua.maxI;
+    uc.inv_maxI = 1.0f / ua.maxI;
+    uc.two_lambda = ua.two_lambda;
+    uc.tik = ua.tik != 0;
     float ksum = 0.0f, kcomp = 0.0f, kmax = -1.0f;
     // all rows, or (prune) the rows of the write region's planes
     const long long r0 = ua.prune ? (long long)bm.wlo[2] * bm.P[1] : 0;
@@ -278,7 +283,7 @@ __global__ void __launch_bounds__(256) k_wrows_update(float2 *__restrict__ S, Up
             for (int h = 0; h < 2; ++h) {
                 if (!((inb >> (2 * s + h)) & 1u)) continue;
                 const float last = lastv[s][h];
-                const float next = next_value(last, cv[h], wv[s][h], ua.two_lambda, ua.tik, minI, maxI);
+                const float next = next_value_fast(last, cv[h], wv[s][h], uc);
                 const float ch = next - last;  // signed change (DeconvolutionMethods.java:308)
                 const float ky = ch - kcomp;
                 const float kt = ksum + ky;
