@@ -59,3 +59,49 @@ def test_argument_errors_before_any_device_work(lib):
     with pytest.raises(M.MvrError) as e:
         M.BlockWorker((16, 16, 16), boundary=7)
     assert e.value.code == M.ERR_ARG
+
+
+def test_psf_transformed_dims_host_geometry(lib):
+    # transformPSF's output size is host arithmetic (no device work): it matches the oracle's
+    # restatement for rotations, scalings and translations
+    import math
+
+    import numpy as np
+
+    import oracle as O
+
+    def model(ay, az, scale, t):
+        a, b = math.radians(ay), math.radians(az)
+        ry = np.array([[math.cos(a), 0, math.sin(a)], [0, 1, 0], [-math.sin(a), 0, math.cos(a)]])
+        rz = np.array([[math.cos(b), -math.sin(b), 0], [math.sin(b), math.cos(b), 0], [0, 0, 1]])
+        return np.hstack([rz @ ry @ np.diag(scale), np.asarray(t, dtype=np.float64).reshape(3, 1)])
+
+    for dims in [(9, 5, 7), (31, 31, 61), (15, 11, 13)]:
+        for m in [model(0, 0, (1, 1, 1), (0, 0, 0)), model(0, 90, (1, 1, 1), (3, 4, 5)),
+                  model(35, 20, (1, 1, 2.5), (3.2, -1.1, 7.9)), model(-50, 0, (0.5, 0.5, 1.3), (0, 0, 0)),
+                  model(45, 45, (1.5, 1, 1), (0, 0, 0))]:
+            assert M.psf_transformed_dims(dims, m) == O.psf_transformed_geometry(dims, m)[0]
+    with pytest.raises(M.MvrError) as e:
+        M.psf_transformed_dims((5, 5, 5), np.full((3, 4), np.nan))
+    assert e.value.code == M.ERR_ARG
+
+
+def test_psf_and_fusion_argument_errors_before_any_device_work(lib):
+    import numpy as np
+
+    with pytest.raises(M.MvrError) as e:
+        M.psf_extract(0, (8, 8, 8), [(1, 1, 1)], (5, 5, 5), 0)  # NULL image and output
+    assert e.value.code == M.ERR_ARG
+    with pytest.raises(M.MvrError) as e:
+        M.psf_transform_normalized(0, (5, 5, 5), np.hstack([np.eye(3), np.zeros((3, 1))]), 0, (5, 5, 5))
+    assert e.value.code == M.ERR_ARG
+    with pytest.raises(M.MvrError) as e:
+        M.psf_average([], [], True, 0)
+    assert e.value.code == M.ERR_ARG
+    with pytest.raises(M.MvrError) as e:
+        M.psf_projection(0, (5, 5, 5), 3, True, 0)
+    assert e.value.code == M.ERR_ARG
+    with pytest.raises(M.MvrError) as e:
+        M.fuse_group([{"img_ptr": 0, "dims": (8, 8, 8), "model": np.hstack([np.eye(3), np.zeros((3, 1))])}],
+                     (0, 0, 0), (4, 4, 4), 1, 1)
+    assert e.value.code == M.ERR_ARG
