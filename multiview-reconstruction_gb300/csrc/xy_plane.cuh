@@ -473,7 +473,6 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
         const int bi = item / Pz, z = item - bi * Pz;
         const BlockMap &bm = bms.m[bi];
         float2 *Sp = S + (long long)bi * Pc + (long long)z * SH::plane;
-        xy_prefetch_next<VX, VY>(S, Pc, Pz, item + gridDim.x, nitems);
         const int ez = ext_e(z, bm.P[2], bm.L[2]);
         for (int y = threadIdx.x; y < SH::Py; y += NT) {
             const int ey = ext_e(y, bm.P[1], bm.L[1]);
@@ -512,6 +511,8 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
 #pragma unroll
             for (int v = 0; v < VX; ++v) row[16 * v] = a[v];
         }
+        // the next item's plane into L2 while this one is transformed forward
+        xy_prefetch_next<VX, VY>(S, Pc, Pz, item + gridDim.x, nitems);
         __syncthreads();
         xy_x_forward_p2<VX, VY>(sm.A, sm.twx, sm.posx);
         xy_y<VX, VY, false>(sm.A, sm.twy, sm.posy);
