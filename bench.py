@@ -219,7 +219,8 @@ def max_over_ranks(x, ws):
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    on_gpu = torch.cuda.is_available() and dist.get_backend() == "nccl"
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if on_gpu else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
