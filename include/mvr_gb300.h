@@ -176,7 +176,9 @@ MVR_API int mvr_decon_get_psi(mvr_decon *h, float *psi);
  * stream, then synchronised). */
 MVR_API int mvr_decon_get_psi_device(mvr_decon *h, float *psi_device);
 /* runIterations: `iterations` more iterations.  stats (or NULL) receives per iteration
- * and view-step {sumChange, maxChange} (Seq: num_views steps, Mul: 1 step). */
+ * and view-step {sumChange, maxChange} (Seq: num_views steps, Mul: 1 step).  With stats NULL
+ * the block voxels outside the regions written back to psi (which the reference computes
+ * and discards) are not computed; psi is bit-identical either way. */
 MVR_API int mvr_decon_run(mvr_decon *h, int iterations, double *stats);
 /* Prepared kernel1 / kernel2 of a view (DeconViewPSF.getKernel1/getKernel2). */
 MVR_API int mvr_decon_get_kernels(mvr_decon *h, int view, float *kernel1, float *kernel2);
