@@ -175,6 +175,15 @@ MVR_API int mvr_decon_get_psi(mvr_decon *h, float *psi);
 /* Copy of psi as float into a device buffer of the volume's size (queued on the handle's
  * stream, then synchronised). */
 MVR_API int mvr_decon_get_psi_device(mvr_decon *h, float *psi_device);
+/* The block grid of one view (host arithmetic, no device work): BlockGeneratorFixedSizePrecise
+ * .divideIntoBlocks (MV/cuda/BlockGeneratorFixedSizePrecise.java:59-131) for the doubled kernel
+ * 2 kernel_size - 1 (DeconView.java:155-157), in x-fastest block order, and BlockSorter's slab
+ * dimension for min_required blocks per slab (MV/cuda/BlockSorter.java:55-143).  blocks receives
+ * up to `capacity` records of 12 values {offset[3], effective offset[3], effective size[3],
+ * effective offset inside the block[3]} ({x, y, z} each).  Returns the number of blocks, or
+ * -MVR_ERR_ARG (also when the block is smaller than the doubled kernel). */
+MVR_API int mvr_block_grid(const long long dims[3], const int kernel_size[3], const int block_size[3],
+                           int min_required, long long *blocks, int capacity, int *sort_dim);
 /* runIterations: `iterations` more iterations.  stats (or NULL) receives per iteration
  * and view-step {sumChange, maxChange} (Seq: num_views steps, Mul: 1 step).  With stats NULL
  * the block voxels outside the regions written back to psi (which the reference computes

@@ -330,7 +330,7 @@ struct BlockDesc {
 // doubled kernel kk = 2k-1 (DeconView 155-157).  Returns false when the block is
 // smaller than the doubled kernel.
 static bool divide_blocks(const long long D[3], const int kk[3], const int b[3], std::vector<BlockDesc> &out,
-                          int &sort_dim)
+                          int &sort_dim, int min_required = 1)
 {
     long long eff[3], nb[3];
     for (int d = 0; d < 3; ++d) {
@@ -349,7 +349,7 @@ static bool divide_blocks(const long long D[3], const int kk[3], const int b[3],
     std::sort(srt, srt + 3);
     sort_dim = 2;
     for (int i = 0; i < 3; ++i) {
-        if (srt[i] >= 1 || i == 2) {
+        if (srt[i] >= min_required || i == 2) {
             for (int d = 0; d < 3; ++d)
                 if (sz[d] == srt[i]) sort_dim = d;  // last d with this product
             break;
@@ -1501,4 +1501,32 @@ extern "C" int mvr_decon_init_psi(mvr_decon *h, int method, double sigma, double
 extern "C" int mvr_decon_likelihood(mvr_decon *h, double *total, double *per_view)
 {
     return h ? h->impl->likelihood(total, per_view) : MVR_ERR_ARG;
+}
+
+// BlockGeneratorFixedSizePrecise.divideIntoBlocks (MV/cuda/BlockGeneratorFixedSizePrecise.java:
+// 59-131) with the doubled kernel 2k-1 of DeconView (MV/deconvolution/DeconView.java:155-157)
+// and BlockSorter's slab dimension (MV/cuda/BlockSorter.java:55-143): host arithmetic only.
+extern "C" MVR_API int mvr_block_grid(const long long dims[3], const int kernel_size[3], const int block_size[3],
+                                      int min_required, long long *blocks, int capacity, int *sort_dim)
+{
+    if (!dims || !kernel_size || !block_size || capacity < 0 || (capacity > 0 && !blocks)) return -MVR_ERR_ARG;
+    long long D[3];
+    int kk[3];
+    for (int d = 0; d < 3; ++d) {
+        if (dims[d] < 1 || kernel_size[d] < 1 || block_size[d] < 1) return -MVR_ERR_ARG;
+        D[d] = dims[d];
+        kk[d] = 2 * kernel_size[d] - 1;
+    }
+    std::vector<mvr::BlockDesc> all;
+    int sd = 2;
+    if (!mvr::divide_blocks(D, kk, block_size, all, sd, min_required < 1 ? 1 : min_required)) return -MVR_ERR_ARG;
+    if (sort_dim) *sort_dim = sd;
+    for (size_t i = 0; i < all.size() && (long long)i < capacity; ++i)
+        for (int d = 0; d < 3; ++d) {
+            blocks[12 * i + d] = all[i].off[d];
+            blocks[12 * i + 3 + d] = all[i].eoff[d];
+            blocks[12 * i + 6 + d] = all[i].esize[d];
+            blocks[12 * i + 9 + d] = all[i].eloc[d];
+        }
+    return (int)all.size();
 }

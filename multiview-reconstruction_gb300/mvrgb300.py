@@ -48,7 +48,7 @@ EXPORTS = [
     "mvr_decon_set_graphs", "mvr_decon_graphs_captured", "mvr_decon_init_psi", "mvr_fuse_group",
     "mvr_fuse_last_error", "mvr_psf_extract", "mvr_psf_transformed_dims", "mvr_psf_transform_normalized",
     "mvr_psf_average", "mvr_psf_make_same_size", "mvr_psf_projection", "mvr_psf_remove_min_projections",
-    "mvr_psf_last_error",
+    "mvr_psf_last_error", "mvr_block_grid",
     "mvr_unet_create", "mvr_unet_destroy", "mvr_unet_last_error", "mvr_unet_num_params", "mvr_unet_get_params",
     "mvr_unet_set_params", "mvr_unet_get_grads", "mvr_unet_set_input", "mvr_unet_forward", "mvr_unet_train_step",
     "mvr_unet_propose", "mvr_conv3d_tc", "mvr_conv3d_tc_wgrad", "mvr_conv3d_tc_last_error",
@@ -157,6 +157,7 @@ def load() -> C.CDLL:
     L.mvr_psf_projection.argtypes = [P, P, C.c_int, C.c_int, P, P, C.c_int, P]
     L.mvr_psf_remove_min_projections.argtypes = [P, P, C.c_int, P]
     L.mvr_psf_last_error.restype = C.c_char_p
+    L.mvr_block_grid.argtypes = [P, P, P, C.c_int, P, C.c_int, P]
     L.mvr_decon_graphs_captured.argtypes = [P]
     L.mvr_decon_likelihood.argtypes = [P, P, P]
     L.mvr_unet_create.argtypes = [C.c_int, P, C.c_uint, C.c_int, C.POINTER(P)]
@@ -703,4 +704,23 @@ def load_group_transform_psfs(groups, same_size_for_all: bool = True, device: in
         out = res
     torch.cuda.synchronize(device)
     return [a.cpu().numpy() for a in out]
+
+
+def block_grid(dims, kernel_size, block_size, min_required: int = 1):
+    """BlockGeneratorFixedSizePrecise.divideIntoBlocks + BlockSorter's slab dimension (host):
+    returns (blocks as dicts with offset / eff_offset / eff_size / eff_local, each (x, y, z),
+    slab dimension)."""
+    L = load()
+    d = (C.c_longlong * 3)(*dims)
+    k = (C.c_int * 3)(*kernel_size)
+    b = (C.c_int * 3)(*block_size)
+    n = L.mvr_block_grid(d, k, b, min_required, None, 0, None)
+    if n < 0:
+        raise MvrError(-n, "mvr_block_grid: bad sizes or a block smaller than the doubled kernel")
+    out = np.zeros((max(n, 1), 12), dtype=np.int64)
+    sd = C.c_int(-1)
+    L.mvr_block_grid(d, k, b, min_required, _p(out), n, C.byref(sd))
+    return [dict(offset=tuple(int(v) for v in r[0:3]), eff_offset=tuple(int(v) for v in r[3:6]),
+                 eff_size=tuple(int(v) for v in r[6:9]), eff_local=tuple(int(v) for v in r[9:12]))
+            for r in out[:n]], sd.value
 

@@ -105,3 +105,27 @@ def test_psf_and_fusion_argument_errors_before_any_device_work(lib):
         M.fuse_group([{"img_ptr": 0, "dims": (8, 8, 8), "model": np.hstack([np.eye(3), np.zeros((3, 1))])}],
                      (0, 0, 0), (4, 4, 4), 1, 1)
     assert e.value.code == M.ERR_ARG
+
+
+@pytest.mark.parametrize("dims,k,b", [((256, 256, 256), (31, 31, 61), (192, 192, 192)),
+                                      ((512, 512, 256), (21, 21, 41), (192, 192, 256)),
+                                      ((200, 180, 150), (9, 9, 15), (128, 128, 64)),
+                                      ((37, 41, 29), (5, 7, 3), (20, 24, 16)),
+                                      ((1024, 1024, 512), (41, 41, 81), (256, 256, 256))])
+def test_block_grid_matches_oracle(lib, dims, k, b):
+    # the host block grid of the whole-volume driver (BlockGeneratorFixedSizePrecise with the
+    # doubled kernel, BlockSorter's slab dimension) against the oracle's C restatement
+    import numpy as np
+
+    import oracle as O
+
+    kk = tuple(2 * x - 1 for x in k)
+    ref = O.divide_into_blocks(dims, kk, b)
+    for mr in (1, 2, 4, 1000):
+        got, sd = M.block_grid(dims, k, b, mr)
+        assert [tuple(map(int, g[key])) for g in got for key in ("offset", "eff_offset", "eff_size", "eff_local")] == \
+               [tuple(map(int, r[key])) for r in ref for key in ("offset", "eff_offset", "eff_size", "eff_local")]
+        nb = [int(np.ceil(dims[d] / (b[d] - kk[d] + 1))) for d in range(3)]
+        assert sd == O.sort_dim(nb, mr)
+    with pytest.raises(M.MvrError):
+        M.block_grid(dims, (b[0], 3, 3), b)  # block smaller than the doubled kernel
