@@ -571,7 +571,8 @@ def psf_projection(psf, dim=-1, use_max=True):
     for k in range(d[dim]):
         v = np.take(a, k, axis=ax)
         ext = np.where(v > ext, v, ext) if use_max else np.where(v < ext, v, ext)
-    return ext.astype(np.float32), dim
+    with np.errstate(over="ignore"):  # an all-NaN line keeps -+DBL_MAX, which rounds to -+inf
+        return ext.astype(np.float32), dim
 
 
 def psf_remove_min_projections(psf):

@@ -360,3 +360,40 @@ def test_psf_combination_known_answers():
     # removing the min projections of a separable ramp leaves zeros
     r = (np.arange(4)[None, None, :] + 10 * np.arange(3)[None, :, None] + 100 * np.arange(5)[:, None, None])
     assert not O.psf_remove_min_projections(r.astype(np.float32)).any()
+
+
+def test_nlinear_against_direct_trilinear():
+    # the Gray-code float accumulation of the corners agrees with the exact trilinear form to
+    # float rounding, and reproduces the corner values at integer positions exactly
+    rng = np.random.default_rng(2)
+    img = rng.uniform(0, 100, (6, 7, 8)).astype(np.float32)
+    t = rng.uniform(0, 1, (200, 3)) * np.array([6.99, 5.99, 4.99])
+
+    def get(ix, iy, iz):
+        return img[iz, iy, ix]
+
+    got = O.nlinear(get, t).astype(np.float64)
+    f = np.floor(t).astype(int)
+    w = t - f
+    ref = np.zeros(len(t))
+    for dz in (0, 1):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                c = ((w[:, 0] if dx else 1 - w[:, 0]) * (w[:, 1] if dy else 1 - w[:, 1]) *
+                     (w[:, 2] if dz else 1 - w[:, 2]))
+                ref += c * img[f[:, 2] + dz, f[:, 1] + dy, f[:, 0] + dx]
+    assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max()
+    ti = np.array([[3, 2, 1], [0, 0, 0], [6, 5, 4]], dtype=np.float64)
+    assert np.array_equal(O.nlinear(get, ti), img[[1, 0, 4], [2, 0, 5], [3, 0, 6]])
+
+
+def test_psf_projection_and_average_edge_cases():
+    # projections skip NaN (the comparison fails) and an all-NaN line keeps the start value;
+    # the smallest-size average of equal sizes is the plain mean
+    a = np.ones((3, 4, 5), np.float32)
+    a[1, 2, 3] = np.nan
+    a[:, 0, 0] = np.nan
+    pr, d = O.psf_projection(a, 2, True)
+    assert d == 2 and pr[2, 3] == 1 and pr[0, 0] == np.float32(-np.inf)
+    b = np.full((3, 4, 5), 3, np.float32)
+    assert np.array_equal(O.psf_average([np.ones_like(b), b], max_size=False), np.full_like(b, 2))
