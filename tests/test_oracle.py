@@ -397,3 +397,45 @@ def test_psf_projection_and_average_edge_cases():
     assert d == 2 and pr[2, 3] == 1 and pr[0, 0] == np.float32(-np.inf)
     b = np.full((3, 4, 5), 3, np.float32)
     assert np.array_equal(O.psf_average([np.ones_like(b), b], max_size=False), np.full_like(b, 2))
+
+
+def test_psf_extract_against_scalar_loops():
+    # the vectorised restatement of extractPSFLocal against its loops written out, element by
+    # element, on a tiny periodic image
+    import math
+
+    rng = np.random.default_rng(4)
+    img = rng.uniform(0, 10, (4, 5, 6)).astype(np.float32)  # [z][y][x]
+    D = (6, 5, 4)
+    size = (3, 5, 3)
+    locs = [(0.25, 4.5, 3.75), (5.9, 0.1, 1.5)]
+    ref = np.zeros((size[2], size[1], size[0]), np.float32)
+    order = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 1, 1), (1, 1, 1), (1, 0, 1), (0, 0, 1)]
+    for l in locs:
+        for z in range(size[2]):
+            for y in range(size[1]):
+                for x in range(size[0]):
+                    t = [float(x - size[0] // 2) + l[0], float(y - size[1] // 2) + l[1], float(z - size[2] // 2) + l[2]]
+                    f = [math.floor(v) for v in t]
+                    w = [t[d] - f[d] for d in range(3)]
+                    acc = None
+                    for dx, dy, dz in order:
+                        wt = ((w[0] if dx else 1 - w[0]) * (w[1] if dy else 1 - w[1])) * (w[2] if dz else 1 - w[2])
+                        v = float(img[(f[2] + dz) % D[2], (f[1] + dy) % D[1], (f[0] + dx) % D[0]])
+                        term = np.float32(v * wt)
+                        acc = term if acc is None else np.float32(acc + term)
+                    ref[z, y, x] = np.float32(float(ref[z, y, x]) + float(acc))
+    assert np.array_equal(O.psf_extract(img, locs, size), ref)
+
+
+def test_load_group_transform_psfs_same_size():
+    rng = np.random.default_rng(6)
+    p = rng.gamma(2.0, 1.0, (9, 7, 7)).astype(np.float32)
+    ident = np.hstack([np.eye(3), np.zeros((3, 1))])
+    rot = np.array([[0, 0, 1, 0], [0, 1, 0, 0], [-1, 0, 0, 0]], dtype=np.float64)  # 90 degrees about y
+    out = O.load_group_transform_psfs([[(p, ident)], [(p, rot)]], same_size_for_all=True)
+    assert out[0].shape == out[1].shape == (9, 7, 9)
+    # the identity group is the normalised PSF centred in the larger box, extended with its minimum (0)
+    assert np.array_equal(out[0][:, :, 1:8], O.psf_normalize(p)) and not out[0][:, :, 0].any()
+    sep = O.load_group_transform_psfs([[(p, ident)], [(p, rot)]], same_size_for_all=False)
+    assert sep[0].shape == (9, 7, 7) and sep[1].shape == (7, 7, 9)
