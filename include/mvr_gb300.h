@@ -359,8 +359,11 @@ MVR_API const char *mvr_conv3d_tc_last_error(void);
  * Limits: the FFT domain (img + kernel - 1 per axis, rounded up to an even size with
  * prime factors <= 13) must be <= 1024 per axis and (x/2 + 1) * y * z <= 1048576;
  * larger sizes return MVR_ERR_UNSUPPORTED with the reason in err.
- * The first call on a device resolves the array's device address (and loads the
- * module); make that first call before any stream capture.  All calls share the one
+ * Every call resolves the array's device address in the calling thread's current
+ * context (cudaGetSymbolAddress) and computes its twiddle tables on the device, so
+ * nothing is cached across contexts or device resets and nothing is staged in host
+ * memory.  The first call on a device also loads the library's module there; make
+ * that first call before any stream capture.  All calls share the one
  * array and it keeps the last call's contents (every value is written before it is
  * read, nothing needs clearing); calls whose work overlaps on the GPU -- from
  * different streams or threads -- race on it.  It calls no cudaMalloc, cudaFree or

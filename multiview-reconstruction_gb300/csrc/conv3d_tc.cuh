@@ -84,8 +84,12 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(const __nv_bfloat16 *__restri
     uint32_t uses[2] = {0, 0};
     for (int t = 0; t < 27; ++t) {
         const int buf = t & 1;
-        if (t >= 2) {  // the MMAs that last read this buffer must be done
-            ok = ok && tc::mbar_wait(&mbar[buf], (uses[buf] - 1) & 1, kTcWaitIter);
+        if (t >= 2) {  // the MMAs that last read this buffer must be done; on a timeout
+                       // every thread stops before it writes the buffer again
+            if (!__syncthreads_and(tc::mbar_wait(&mbar[buf], (uses[buf] - 1) & 1, kTcWaitIter))) {
+                ok = false;
+                break;
+            }
         }
         // A: this thread's row, C channels of the neighbour at tap t
         const long long src = rv ? neighbour(g, x, y, z, b, t, sign) : -1;
@@ -119,7 +123,7 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(const __nv_bfloat16 *__restri
     for (int bb = 0; bb < 2; ++bb)
         if (uses[bb]) ok = tc::mbar_wait(&mbar[bb], (uses[bb] - 1) & 1, kTcWaitIter) && ok;
     tc::fence_after_sync();
-    __syncthreads();
+    ok = __syncthreads_and(ok) != 0;  // one outcome for the whole CTA (the TMEM loads are warp-wide)
     if (!ok) {
         if (tid == 0) atomicExch(err, 1);
     } else {
@@ -238,8 +242,12 @@ __global__ void __launch_bounds__(128) k_conv3d_brick(const __nv_bfloat16 *__res
     uint32_t uses[2] = {0, 0};
     for (int t = 0; t < 27; ++t) {
         const int buf = t & 1;
-        if (t >= 2) {  // the MMAs that last read this buffer must be done
-            ok = ok && tc::mbar_wait(&mbar[buf], (uses[buf] - 1) & 1, kTcWaitIter);
+        if (t >= 2) {  // the MMAs that last read this buffer must be done; on a timeout
+                       // every thread stops before it writes the buffer again
+            if (!__syncthreads_and(tc::mbar_wait(&mbar[buf], (uses[buf] - 1) & 1, kTcWaitIter))) {
+                ok = false;
+                break;
+            }
         }
         // A: this thread's row from the halo at tap t
         const int dz = (t / 9 - 1) * sign, dy = ((t / 3) % 3 - 1) * sign, dx = (t % 3 - 1) * sign;
@@ -271,7 +279,7 @@ __global__ void __launch_bounds__(128) k_conv3d_brick(const __nv_bfloat16 *__res
     for (int bb = 0; bb < 2; ++bb)
         if (uses[bb]) ok = tc::mbar_wait(&mbar[bb], (uses[bb] - 1) & 1, kTcWaitIter) && ok;
     tc::fence_after_sync();
-    __syncthreads();
+    ok = __syncthreads_and(ok) != 0;  // one outcome for the whole CTA (the TMEM loads are warp-wide)
     if (!ok) {
         if (tid == 0) atomicExch(err, 1);
     } else {
@@ -433,7 +441,10 @@ __global__ void __launch_bounds__(128) k_conv3d_shift(const __nv_bfloat16 *__res
         ++uses[buf];
         if (c + 1 < NCH) {
             const int nb = (c + 1) & 1;
-            if (c + 1 >= 2) ok = ok && tc::mbar_wait(&mbar[nb], (uses[nb] - 1) & 1, kTcWaitIter);
+            if (c + 1 >= 2 && !__syncthreads_and(tc::mbar_wait(&mbar[nb], (uses[nb] - 1) & 1, kTcWaitIter))) {
+                ok = false;  // every thread stops before it writes the buffer again
+                break;
+            }
             load_b(c + 1, nb);
             tc::fence_proxy_async();
             tc::fence_before_sync();
@@ -444,7 +455,7 @@ __global__ void __launch_bounds__(128) k_conv3d_shift(const __nv_bfloat16 *__res
     for (int bb = 0; bb < 2; ++bb)
         if (uses[bb]) ok = tc::mbar_wait(&mbar[bb], (uses[bb] - 1) & 1, kTcWaitIter) && ok;
     tc::fence_after_sync();
-    __syncthreads();
+    ok = __syncthreads_and(ok) != 0;  // one outcome for the whole CTA (the TMEM loads are warp-wide)
     const int lx = tid & 7, ly = tid >> 3;
     const int x = x0 + lx, y = y0 + ly;
     const bool rv = x < g.W && y < g.H;
@@ -517,7 +528,10 @@ __global__ void __launch_bounds__(128) k_wgrad_tc(const __nv_bfloat16 *__restric
     int stage = 0;
     for (long long k0 = n0; k0 < n1; k0 += KT, ++stage) {
         const int buf = stage & 1;
-        if (stage >= 2) ok = ok && tc::mbar_wait(&mbar[buf], (uses[buf] - 1) & 1, kTcWaitIter);
+        if (stage >= 2 && !__syncthreads_and(tc::mbar_wait(&mbar[buf], (uses[buf] - 1) & 1, kTcWaitIter))) {
+            ok = false;  // every thread stops before it writes the buffer again
+            break;
+        }
         // A: 16 row groups x KT voxels; a row group is 8 channels of one tap
         for (int s = tid; s < 16 * KT; s += 128) {
             const int rg = s / KT, k = s % KT;
@@ -564,7 +578,7 @@ __global__ void __launch_bounds__(128) k_wgrad_tc(const __nv_bfloat16 *__restric
     for (int bb = 0; bb < 2; ++bb)
         if (uses[bb]) ok = tc::mbar_wait(&mbar[bb], (uses[bb] - 1) & 1, kTcWaitIter) && ok;
     tc::fence_after_sync();
-    __syncthreads();
+    ok = __syncthreads_and(ok) != 0;  // one outcome for the whole CTA (the TMEM loads are warp-wide)
     if (!ok) {
         if (tid == 0) atomicExch(err, 1);
     } else if (stage > 0) {

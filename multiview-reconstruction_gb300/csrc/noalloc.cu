@@ -3,7 +3,6 @@
 // cannot allocate device memory.  See include/mvr_gb300.h for the contract.
 #include <cuda_runtime.h>
 
-#include <cmath>
 #include <cstdio>
 #include <mutex>
 
@@ -23,39 +22,51 @@ constexpr long long kScratchLen = 2 * kMaxPc + 3LL * kMaxAxis;
 // The scratch itself: 16 MiB + 24 KiB, resident on every device that loads the library.
 static __device__ __align__(256) float2 g_static_scratch[kScratchLen];
 
-constexpr int kMaxDevices = 64;
-struct DeviceSlot {
-    bool ready = false;
-    float2 *scratch = nullptr;  // device address of g_static_scratch on that device
-};
-DeviceSlot g_slots[kMaxDevices];
 std::mutex g_mutex;
-float2 g_host_tw[3][kMaxAxis];  // staging of the twiddle tables (guarded by g_mutex)
 
 void put_error(char *err, int len, const char *msg)
 {
     if (err && len > 0) std::snprintf(err, (size_t)len, "%s", msg);
 }
 
-int setup_device(int dev, char *err, int err_len)
+// Twiddle tables exp(-2 pi i k / n) of the three axes, written straight into the scratch
+// array: nothing is staged in host memory, so a call queues device work only.
+__global__ void k_static_twiddles(float2 *tw, int n0, int n1, int n2)
 {
-    DeviceSlot &s = g_slots[dev];
-    if (s.ready) return MVR_OK;
+    const int axis = blockIdx.y;
+    const int n = axis == 0 ? n0 : (axis == 1 ? n1 : n2);
+    float2 *t = tw + (size_t)axis * kMaxAxis;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        double s, c;
+        sincospi(-2.0 * (double)k / (double)n, &s, &c);
+        t[k] = make_float2((float)c, (float)s);
+    }
+}
+
+// Resolves the scratch array's device address in the current context and raises the
+// dynamic shared-memory limit of the kernels this entry point launches.  Done on every
+// call (both are cheap and allocate nothing), so a new context or a reset device never
+// sees an address or a limit left over from an earlier one.
+int setup_device(float2 **scratch, char *err, int err_len)
+{
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    const int m = 227 * 1024;
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_rows_fwd<float, SrcKernel, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_rows_fwd<float, SrcZero<float>, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 m);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cols<float, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cols<float, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_cols<float, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_rows_update<float, EPI_STORE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     if (e != cudaSuccess) {
         put_error(err, err_len, cudaGetErrorString(e));
         return MVR_ERR_CUDA;
     }
-    const int m = 227 * 1024;
-    cudaFuncSetAttribute(k_rows_fwd<float, SrcKernel, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    cudaFuncSetAttribute(k_rows_fwd<float, SrcZero<float>, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    cudaFuncSetAttribute(k_cols<float, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    cudaFuncSetAttribute(k_cols<float, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    cudaFuncSetAttribute(k_cols<float, 2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    cudaFuncSetAttribute(k_rows_update<float, EPI_STORE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
-    s.scratch = static_cast<float2 *>(p);
-    s.ready = true;
+    *scratch = static_cast<float2 *>(p);
     return MVR_OK;
 }
 
@@ -96,31 +107,16 @@ extern "C" int mvr_convolve_static(const float *img, const int img_size[3], cons
         put_error(err, err_len, msg);
         return MVR_ERR_UNSUPPORTED;
     }
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
-        put_error(err, err_len, e != cudaSuccess ? cudaGetErrorString(e) : "device ordinal out of range");
-        return MVR_ERR_CUDA;
-    }
     std::lock_guard<std::mutex> lock(g_mutex);
-    int rc = setup_device(dev, err, err_len);
+    float2 *scr = nullptr;
+    int rc = setup_device(&scr, err, err_len);
     if (rc != MVR_OK) return rc;
-    float2 *scr = g_slots[dev].scratch;
+    cudaError_t e;
     float2 *Sk = scr;           // kernel spectrum
     float2 *S = scr + kMaxPc;   // image spectrum
     float2 *tw[3] = {scr + 2 * kMaxPc, scr + 2 * kMaxPc + kMaxAxis, scr + 2 * kMaxPc + 2 * kMaxAxis};
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    for (int d = 0; d < 3; ++d) {
-        for (int k = 0; k < P[d]; ++k) {
-            const double a = -2.0 * M_PI * (double)k / (double)P[d];
-            g_host_tw[d][k] = make_float2((float)std::cos(a), (float)std::sin(a));
-        }
-        e = cudaMemcpyAsync(tw[d], g_host_tw[d], sizeof(float2) * (size_t)P[d], cudaMemcpyHostToDevice, s);
-        if (e != cudaSuccess) {
-            put_error(err, err_len, cudaGetErrorString(e));
-            return MVR_ERR_CUDA;
-        }
-    }
+    k_static_twiddles<<<dim3(4, 3), 256, 0, s>>>(tw[0], P[0], P[1], P[2]);
     const FftDesc dx = make_desc(P[0] / 2), dy = make_desc(P[1]), dz = make_desc(P[2]);
     const int m = P[0] / 2;
     int RP = 16;
