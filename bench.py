@@ -10,11 +10,15 @@ Synthetic seeded data stands in for the reference's microscopy datasets.
 A step is one full iteration (all 4 views, all blocks) over the whole volume.
 Metric: voxel-iterations/s = 256^3 * steps / seconds.
 
-  value  device-resident inputs, CUDA events on the library's stream around K steps
-  e2e    the public C ABI with pinned host buffers: every step uploads the 4 images,
-         4 raw weights and psi, runs one iteration and reads psi back
-  --impl reference  the CPU restatement of the reference block iteration (oracle/,
-         all host threads) on a bounded sample of the same workload
+  value       device-resident inputs, CUDA events on the library's stream around K steps
+  e2e         the public C ABI with pinned host buffers: every step uploads the 4 images,
+              4 raw weights and psi, runs one iteration and reads psi back
+  e2e_block   the per-block plugin call (mvr_block_run_seq, ComputeBlockSeqThread.
+              runIteration) with host buffers, 64 calls per iteration from 2 worker threads
+  err_vs_fp64 relative L2 of the FP32 iterations against the FP64 run of the same ones
+  --impl reference  the float32 CPU restatement of the reference block iteration with its
+              padded real-to-complex FFT convolution (oracle/cpu_reference.py, all host
+              threads) on a bounded sample of the same workload
 """
 from __future__ import annotations
 
@@ -41,9 +45,11 @@ UNIT = "voxel-iterations/s"
 class Workload:
     """A named deconvolution workload: volume, views, compute block, PSF sizes per view."""
 
-    def __init__(self, name, dims, views, block, psfs, lam, make, desc):
+    def __init__(self, name, dims, views, block, psfs, lam, make, desc, psf_type=1, weight_norm=1, fp64_iters=None):
         self.name, self.dims, self.views, self.block, self.psfs, self.lam = name, dims, views, block, psfs, lam
         self.make, self.desc = make, desc
+        self.psf_type, self.weight_norm = psf_type, weight_norm  # MVR_PSF_*, MVR_WEIGHTS_*
+        self.fp64_iters = fp64_iters  # iterations of the FP64 comparison (None: warm-up + timed)
         self.nvox = dims[0] * dims[1] * dims[2]
         self.metric = f"voxel-iterations/s ({views} views)"
 
@@ -56,12 +62,21 @@ class Workload:
     def view_blocks_per_iter(self):
         return sum(len(self.blocks(v)) for v in range(self.views))
 
+    def input_bytes(self):
+        return (2 * self.views + 1) * self.nvox * 4
+
+    def flush_l2(self):
+        """Inputs below twice the 129 MB L2: the bench flushes L2 before every timed step."""
+        return self.input_bytes() < 2 * 129e6
+
     def config(self, boundary):
+        mib = self.input_bytes() / 2**20
+        l2 = (f"L2 flushed before every timed step (a 512 MiB write outside the step's events; inputs "
+              f"{mib:.0f} MiB)" if self.flush_l2() else
+              f"inputs larger than L2 ({self.views} images + {self.views} weights + psi = {mib:.0f} MiB)")
         return {"workload": self.desc, "views": self.views, "dims": list(self.dims), "block": list(self.block),
                 "psf": [list(p) for p in self.psfs] if len(set(self.psfs)) > 1 else list(self.psfs[0]),
-                "lambda": self.lam, "iterations_per_step": 1, "boundary": boundary,
-                "l2": f"inputs larger than L2 ({self.views} images + {self.views} weights + psi = "
-                      f"{(2 * self.views + 1) * self.nvox * 4 / 2**20:.0f} MiB)",
+                "lambda": self.lam, "iterations_per_step": 1, "boundary": boundary, "l2": l2,
                 "data": "seeded synthetic beads + ellipsoid, Poisson, background 10"}
 
 
@@ -85,6 +100,12 @@ def _make_large():
     return synthetic.config_large(torch.cuda.current_device() if torch.cuda.is_available() else "cpu")
 
 
+def _make_small():
+    import synthetic
+
+    return synthetic.config_small()
+
+
 def _psf_sizes_6():
     import synthetic
 
@@ -92,16 +113,21 @@ def _psf_sizes_6():
 
 
 WORKLOADS = {
+    "2view128": lambda: Workload("2view128", (128, 128, 64), 2, (192, 192, 128), [(15, 15, 31)] * 2, 0.0, _make_small,
+                                 "2 views 128x128x64 float32, PSF 15x15x31 at 0/90 degrees, efficient-Bayesian, "
+                                 "all-one weights, one block (192x192x128 compute block), lambda 0, Seq",
+                                 psf_type=2, weight_norm=0),
     "4view256": lambda: Workload("4view256", (256, 256, 256), 4, (192, 192, 192), [(31, 31, 61)] * 4, 0.006, _make256,
                                  "4 views 256^3 float32, PSF 31x31x61 Optimization-I, blocks 192^3, Seq (OSEM-like)"),
     "6view512": lambda: Workload("6view512", (512, 512, 256), 6, (192, 192, 256), _psf_sizes_6(), 0.006, _make512,
                                  "6 views 512x512x256 float32, PSFs 21x21x41 ... 41x41x81 per view, "
                                  "Optimization-I, compute blocks 192x192x256 (effective 112-152 x 112-152 x 96-176, "
-                                 "uneven edge blocks), Seq"),
+                                 "uneven edge blocks), Seq", fp64_iters=5),
     "8view1024": lambda: Workload("8view1024", (1024, 1024, 512), 8, (256, 256, 256), [(41, 41, 81)] * 8, 0.006,
                                   _make_large,
                                   "8 views 1024x1024x512 (uint16 recorded, converted to float32), 20000 nuclei-like "
-                                  "blobs, PSF 41x41x81 at 45 degree steps, compute blocks 256^3 (216 per view), Seq"),
+                                  "blobs, PSF 41x41x81 at 45 degree steps, compute blocks 256^3 (216 per view), Seq",
+                                  fp64_iters=2),
 }
 W = None  # the workload of this run (set in main)
 
@@ -225,59 +251,59 @@ def max_over_ranks(x, ws):
     return float(t.item())
 
 
-def cpu_block_sample(ds, k1s, k2s, mx, n_blocks):
-    """Times the oracle (reference-faithful CPU block iteration) on n_blocks view-blocks
-    of the workload; returns (seconds per view-block, threads)."""
+def prepare_reference_inputs(ds):
+    """Set-up of the CPU sample, outside any timed region: the kernels (DeconViewPSF.init,
+    the C oracle), the normalised weights per block and the per-view maxima / psi0
+    (PsiInitAvgPrecise).  Host volumes are normalised whole; device volumes (the large
+    workload) per sampled block (the rule is per voxel).  Returns (k1s, k2s, weight_block,
+    image_block, mx, psi0) with the block functions of cpu_reference.BlockSampler."""
+    import cpu_reference as R
     import oracle
 
-    D = W.dims
-    B = W.block
-    times = []
-    for i in range(n_blocks):
-        v = i % W.views
-        blocks = W.blocks(v)
-        bl = blocks[(5 + i) % len(blocks)]
-        off = bl["offset"]
-        idx = [np.arange(off[d], off[d] + B[d]) for d in range(3)]
-        psi = np.full((B[2], B[1], B[0]), 50.0, np.float32)
-        img = np.zeros_like(psi)
-        w = np.zeros_like(psi)
+    k1s, k2s = oracle.psf_init(ds.psfs, W.psf_type, 0)
+    on_dev = not isinstance(ds.images[0], np.ndarray)
+    if not on_dev:
+        if W.weight_norm == 0:
+            ws = [np.ascontiguousarray(w, dtype=np.float32) for w in ds.weights]
+        else:
+            ws = oracle.normalize_weights(ds.weights, smooth=W.weight_norm == 2)
+        psi0, mx, _ = oracle.psi_init_avg(ds.images)
+        return (k1s, k2s, (lambda v, off, b: R.extract(ws[v], off, b, "zero")),
+                (lambda v, off, b: R.extract(ds.images[v], off, b, "zero")), mx, psi0)
+
+    def box(vol, off, b):
+        D = (vol.shape[2], vol.shape[1], vol.shape[0])
+        idx = [np.arange(off[d], off[d] + b[d]) for d in range(3)]
         ok = [(idx[d] >= 0) & (idx[d] < D[d]) for d in range(3)]
+        out = np.zeros((b[2], b[1], b[0]), dtype=np.float32)
         sub = np.ix_(idx[2][ok[2]], idx[1][ok[1]], idx[0][ok[0]])
         dst = np.ix_(np.nonzero(ok[2])[0], np.nonzero(ok[1])[0], np.nonzero(ok[0])[0])
-        img[dst] = _region(ds.images[v], sub)
-        if isinstance(ds.weights[v], np.ndarray):
-            w[dst] = ds.weights[v][sub]
-        else:  # raw device weights: normalise this region with the hard rule
-            raw = [_region(ds.weights[u], sub) for u in range(W.views)]
-            w[dst] = oracle.normalize_weights(raw)[v]
-        t0 = time.perf_counter()
-        oracle.block_seq(psi, img, w, k1s[v], k2s[v], W.lam, 1e-4, float(mx[v]))
-        times.append(time.perf_counter() - t0)
-    return float(np.mean(times)), oracle.num_threads()
+        out[dst] = _region(vol, sub)
+        return out
+
+    def weight_block(v, off, b):
+        return oracle.normalize_weights([box(ds.weights[u], off, b) for u in range(W.views)])[v]
+
+    return k1s, k2s, weight_block, (lambda v, off, b: box(ds.images[v], off, b)), None, None
 
 
-def cpu_sample_text(n):
-    dom = "x".join(str(W.block[d] + W.psfs[0][d] - 1) for d in range(3))
-    return (f"{n} view-block(s) of {W.block[0]}x{W.block[1]}x{W.block[2]} (reference boundary, FFT domain about "
-            f"{dom}), extrapolated to the {W.view_blocks_per_iter()} view-blocks of one iteration")
+def cpu_sampler(ds, psi, mx, prep):
+    import cpu_reference as R
+
+    k1s, k2s, weight_block, image_block, _, _ = prep
+    grids = [W.blocks(v) for v in range(W.views)]
+    return R.BlockSampler(psi, None, None, k1s, k2s, grids, W.block, W.lam, mx, image_block=image_block,
+                          weight_block=weight_block)
 
 
-def prepare_reference_inputs(ds, mx=None):
-    """Kernels, normalised weights and per-view maxima for the CPU sample.  For device
-    volumes (the large workload) the weights are normalised per sampled block (the hard
-    rule is per voxel) and the maxima come from the GPU run (mx)."""
-    import oracle
-
-    k1s, k2s = oracle.psf_init(ds.psfs, oracle.PSF_OPTIMIZATION_I, 0)
-    if mx is None:
-        ws = oracle.normalize_weights(ds.weights)
-        _, mx, _ = oracle.psi_init_avg(ds.images)
-        ds.weights = ws
-    return k1s, k2s, mx
+def cpu_sample_text(steps, sampler):
+    P = sampler._convolvers(0)[0].P
+    return (f"{steps} step(s) of one {W.block[0]}x{W.block[1]}x{W.block[2]} block per view (views in order, effective "
+            f"regions pasted back into psi), float32 real-to-complex FFTs at the padded size {P[0]}x{P[1]}x{P[2]} "
+            f"(util/FFTConvolution), {sampler.workers} host threads; value = voxel-iterations advanced / seconds")
 
 
-def _region(vol, sub, normalise_with=None):
+def _region(vol, sub):
     """vol[sub] as a host array (vol a host array or a device tensor)."""
     if isinstance(vol, np.ndarray):
         return vol[sub]
@@ -287,35 +313,69 @@ def _region(vol, sub, normalise_with=None):
     return vol.index_select(0, idx[0]).index_select(1, idx[1]).index_select(2, idx[2]).cpu().numpy()
 
 
+def time_cpu_sampler(sampler, warmup, steps):
+    sampler.prepare()
+    for _ in range(warmup):
+        sampler.step()
+    t0 = time.perf_counter()
+    adv = 0.0
+    for _ in range(steps):
+        adv += sampler.step()
+    wall = time.perf_counter() - t0
+    return adv / wall, wall
+
+
 def run_reference(args, ws, rank):
+    """The reference's CPU block iteration restated in float32 with its padded R2C FFT
+    convolution, on all host threads, one block per view per step on real psi."""
     if rank != 0:
         return
     import oracle
 
     oracle.build()
     ds = make_data()
-    k1s, k2s, mx = prepare_reference_inputs(ds)
-    threads = oracle.num_threads()
-    for _ in range(args.warmup):
-        cpu_block_sample(ds, k1s, k2s, mx, 1)
-    t0 = time.perf_counter()
-    per_vb = []
-    for _ in range(args.steps):
-        t, _ = cpu_block_sample(ds, k1s, k2s, mx, 1)
-        per_vb.append(t)
-    wall = time.perf_counter() - t0
-    t_vb = float(np.mean(per_vb))
-    nvb = W.view_blocks_per_iter()
-    value = W.nvox / (t_vb * nvb)
-    sample = cpu_sample_text(1) + " (one view-block per step)"
+    prep = prepare_reference_inputs(ds)
+    psi0, mx = prep[5], prep[4]
+    if psi0 is None:  # device-synthesised volumes: psi0 and the maxima on the host
+        import torch
+
+        mx = np.array([float(torch.max(im)) for im in ds.images], dtype=np.float32)
+        avg = float(np.mean([float(im[im > 0].mean()) for im in ds.images]))
+        psi0 = np.full((W.dims[2], W.dims[1], W.dims[0]), avg, np.float32)
+    smp = cpu_sampler(ds, psi0, mx, prep)
+    try:
+        value, wall = time_cpu_sampler(smp, args.warmup, args.steps)
+        sample = cpu_sample_text(args.steps, smp)
+        threads = smp.workers
+    finally:
+        smp.close()
     line = {"impl": "reference", "metric": W.metric, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_vb * nvb,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": W.config("reference (mirror-single / value-1 extension)"),
+            "data": "synthetic", "config": W.config("reference (mirror-single / value-1 extension, padded FFT)"),
             "wall_s": wall,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def fp64_error(M, views, n_iter, dev, boundary, d_img, d_w, ds):
+    """Relative L2 of n_iter FP32 iterations against n_iter FP64 iterations of the same
+    run from the same psi0 (PsiInitAvgPrecise); both through the whole-volume C ABI."""
+    out = {}
+    for prec in (M.PRECISION_FP32, M.PRECISION_FP64):
+        with M.Deconvolution(W.dims, W.views, W.block, mul=False, psf_type=W.psf_type, psf_norm_threads=0, lam=W.lam,
+                             boundary=boundary, precision=prec, weight_norm=W.weight_norm, device=dev) as d:
+            for v in range(views):
+                d.set_view_device(v, d_img[v].data_ptr(), d_w[v].data_ptr(), ds.psfs[v])
+            d.prepare()
+            d.run_iterations(n_iter)
+            out[prec] = d.get_psi()
+    a = out[M.PRECISION_FP32].astype(np.float64)
+    b = out[M.PRECISION_FP64].astype(np.float64)
+    return {"value": float(np.linalg.norm(a - b) / np.linalg.norm(b)), "iterations": n_iter,
+            "what": "relative L2 of psi after the FP32 iterations against the FP64 run of the same iterations "
+                    "(same psi0, same kernels, every stage in double)"}
 
 
 def run_gb300(args, ws, rank, local):
@@ -338,8 +398,8 @@ def run_gb300(args, ws, rank, local):
     on_dev = torch.is_tensor(ds.images[0])  # synthesised on the device (large workload)
     d_img = ds.images if on_dev else [torch.from_numpy(a).to(f"cuda:{dev}") for a in ds.images]
     d_w = ds.weights if on_dev else [torch.from_numpy(a).to(f"cuda:{dev}") for a in ds.weights]
-    dec = M.Deconvolution(W.dims, W.views, W.block, mul=False, psf_type=M.PSF_OPTIMIZATION_I, psf_norm_threads=0,
-                          lam=W.lam, boundary=boundary, precision=M.PRECISION_FP32, weight_norm=M.WEIGHTS_HARD,
+    dec = M.Deconvolution(W.dims, W.views, W.block, mul=False, psf_type=W.psf_type, psf_norm_threads=0,
+                          lam=W.lam, boundary=boundary, precision=M.PRECISION_FP32, weight_norm=W.weight_norm,
                           batch_blocks=args.batch, device=dev)
     for v in range(W.views):
         dec.set_view_device(v, d_img[v].data_ptr(), d_w[v].data_ptr(), ds.psfs[v])
@@ -357,15 +417,29 @@ def run_gb300(args, ws, rank, local):
     barrier(ws)
     torch.cuda.synchronize()
     launches0 = dec.launch_count()
+    flush = W.flush_l2()
     with ClockSampler(dev) as clk:
-        e0.record(stream)
-        for _ in range(args.steps):
-            dec.run_iterations(1)
-        e1.record(stream)
+        if flush:
+            # inputs smaller than L2: a 512 MiB write flushes it before every step, outside
+            # the per-step event pair
+            junk = torch.empty(128 << 20, dtype=torch.float32, device=f"cuda:{dev}")
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(args.steps)]
+            with torch.cuda.stream(stream):
+                for a, b in ev:
+                    junk.fill_(1.0)
+                    a.record(stream)
+                    dec.run_iterations(1)
+                    b.record(stream)
+        else:
+            e0.record(stream)
+            for _ in range(args.steps):
+                dec.run_iterations(1)
+            e1.record(stream)
         torch.cuda.synchronize()
         dec.synchronize()
     launches = dec.launch_count() - launches0
-    ms = e0.elapsed_time(e1)
+    ms = sum(a.elapsed_time(b) for a, b in ev) if flush else e0.elapsed_time(e1)
     barrier(ws)
     ms = max_over_ranks(ms, ws)
     clocks = clk.summary()
@@ -417,18 +491,28 @@ def run_gb300(args, ws, rank, local):
     # ---- e2e: public C ABI with pinned host buffers, copies inside the timed region ----
     if args.no_e2e or on_dev:
         e2e = None  # the large workload keeps its volumes on the device only
+        e2e_block = None
     else:
         e2e = run_e2e(args, ws, dev, ds, dec, shape, boundary)
+        e2e_block = run_e2e_block(args, ws, dev, ds, dec, dec_max)
+    psi_now = dec.get_psi()
+    dec.close()
+    # ---- every result's error against an FP64 run of the same iterations ----
+    n64 = W.fp64_iters if W.fp64_iters is not None else args.warmup + args.steps
+    err64 = fp64_error(M, W.views, n64, dev, boundary, d_img, d_w, ds) if not args.no_fp64 else None
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         import oracle
 
         oracle.build()
-        k1s, k2s, mx = prepare_reference_inputs(ds, dec_max if on_dev else None)
-        t_vb, threads = cpu_block_sample(ds, k1s, k2s, mx, args.cpu_blocks)
-        cpu = {"value": W.nvox / (t_vb * W.view_blocks_per_iter()), "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": cpu_sample_text(args.cpu_blocks)}
-    dec.close()
+        prep = prepare_reference_inputs(ds)
+        smp = cpu_sampler(ds, psi_now, dec_max, prep)  # the GPU run's psi: real data, not a constant
+        try:
+            cval, _ = time_cpu_sampler(smp, 0, args.cpu_steps)
+            cpu = {"value": cval, "unit": UNIT, "cores": smp.workers, "kind": "port",
+                   "sample": cpu_sample_text(args.cpu_steps, smp)}
+        finally:
+            smp.close()
     learned_res = None
     if args.learned and rank == 0:
         import learned
@@ -448,6 +532,10 @@ def run_gb300(args, ws, rank, local):
                                             "voxels outside the write regions, which the reference discards)"}}
         if learned_res is not None:
             line["learned"] = learned_res
+        if e2e_block is not None:
+            line["e2e_block"] = e2e_block
+        if err64 is not None:
+            line["err_vs_fp64"] = err64
         print(json.dumps(line), flush=True)
 
 
@@ -462,9 +550,9 @@ def run_e2e(args, ws, dev, ds, dec, shape, boundary):
     h_w = [torch.from_numpy(a).pin_memory() for a in ds.weights]
     h_psi = torch.empty(shape, dtype=torch.float32).pin_memory()
     h_psi.copy_(torch.from_numpy(dec.get_psi()))
-    e2e_dec = M.Deconvolution(W.dims, W.views, W.block, mul=False, psf_type=M.PSF_OPTIMIZATION_I,
-                              psf_norm_threads=0, lam=W.lam, boundary=boundary, precision=M.PRECISION_FP32, weight_norm=M.WEIGHTS_HARD,
-                              device=dev)
+    e2e_dec = M.Deconvolution(W.dims, W.views, W.block, mul=False, psf_type=W.psf_type,
+                              psf_norm_threads=0, lam=W.lam, boundary=boundary, precision=M.PRECISION_FP32,
+                              weight_norm=W.weight_norm, device=dev)
     for v in range(W.views):
         e2e_dec.set_view(v, h_img[v].numpy(), h_w[v].numpy(), ds.psfs[v])
     e2e_dec.prepare()
@@ -491,6 +579,70 @@ def run_e2e(args, ws, dev, ds, dec, shape, boundary):
     e2e_dec.close()
     return {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "steps": e2e_steps}
+
+
+def run_e2e_block(args, ws, dev, ds, dec, dec_max, workers=2, iters=2):
+    """The drop-in per-block path: mvr_block_run_seq (ComputeBlockSeqThread.runIteration,
+    ComputeBlockSeqThread.java:54-61) with host buffers, one call per view-block as the
+    reference's driver issues them (MultiViewDeconvolutionSeq.java:91-150), from `workers`
+    host threads with one block worker each (numParallelBlocks = 2, so one worker's copies
+    overlap the other's kernels).  A call uploads the psi, image and weight block, runs
+    the iteration and returns the psi block and its statistics.  Timed: the calls of each
+    view-step; the driver's own block copies out of and into the volumes
+    (Block.copyBlock / pasteBlock, Java-side) run between them untimed."""
+    import concurrent.futures as cf
+
+    import cpu_reference as R
+    import mvrgb300 as M
+
+    psi = dec.get_psi()
+    wts = [dec.weights(v) for v in range(W.views)]
+    boundary = M.BOUNDARY_CIRCULAR
+    wk = [M.BlockWorker(W.block, 1e-4, W.lam, W.views, boundary, dev) for _ in range(workers)]
+    try:
+        for w in wk:
+            for v in range(W.views):
+                k1, k2 = dec.kernels(v, ds.psfs[v].shape)
+                w.set_kernels(v, k1, k2)
+        grids = [W.blocks(v) for v in range(W.views)]
+        inputs = [[(R.extract(ds.images[v], bl["offset"], W.block, "zero"),
+                    R.extract(wts[v], bl["offset"], W.block, "zero")) for bl in grids[v]] for v in range(W.views)]
+        pool = cf.ThreadPoolExecutor(max_workers=workers)
+        calls = 0
+        call_s = []
+        for it in range(1 + iters):
+            t_it = 0.0
+            for v in range(W.views):
+                pb = [R.extract(psi, bl["offset"], W.block, "mirror") for bl in grids[v]]
+                jobs = list(range(len(pb)))
+
+                def run(j, v=v, pb=pb):
+                    w = wk[j % workers]
+                    im, wt = inputs[v][j]
+                    w.run_iteration(v, pb[j], im, wt, float(dec_max[v]))
+
+                t0 = time.perf_counter()
+                # worker j % workers takes block j: each worker's calls stay in order
+                list(pool.map(lambda r: [run(j) for j in jobs[r::workers]], range(workers)))
+                t_it += time.perf_counter() - t0
+                for j, bl in enumerate(grids[v]):
+                    R.paste(psi, pb[j], bl["eff_offset"], bl["eff_size"], bl["eff_local"])
+                if it:
+                    calls += len(pb)
+            if it:
+                call_s.append(t_it)
+        pool.shutdown()
+    finally:
+        for w in wk:
+            w.close()
+    t = float(np.mean(call_s))
+    nb = 4 * W.block[0] * W.block[1] * W.block[2]
+    return {"value": ws * W.nvox / t, "unit": UNIT, "h2d_bytes_per_step": 3 * nb * calls // iters,
+            "d2h_bytes_per_step": nb * calls // iters, "calls_per_step": calls // iters, "steps": iters,
+            "workers": workers, "boundary": "circular (the pasted effective regions are the reference boundary's; "
+                                            "the per-block statistics differ)",
+            "note": "timed: the mvr_block_run_seq calls of each view-step with pageable host buffers; the driver's "
+                    "block copies out of / into the volumes run untimed between view-steps"}
 
 
 def run_psf(args):
@@ -564,7 +716,9 @@ def main():
     ap.add_argument("--boundary", choices=["circular", "reference"], default="circular")
     ap.add_argument("--batch", type=int, default=0,
                     help="blocks per batched launch (1..16); 0 = autotuned")
-    ap.add_argument("--cpu-blocks", type=int, default=2)
+    ap.add_argument("--cpu-steps", type=int, default=2,
+                    help="steps of the CPU baseline sample (one block per view each)")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--learned", action="store_true",

@@ -296,10 +296,14 @@ __global__ void k_convert(const A *__restrict__ in, B *__restrict__ out, long lo
         out[i] = (B)in[i];
 }
 
-// any non-zero weight inside the block's box (zero outside the volume)
-__global__ void k_block_content(const float *__restrict__ w, long long D0, long long D1, long long D2, long long ox,
-                                long long oy, long long oz, int bx, int by, int bz, int *flag)
+// DeconView.filterBlocksForContent (DeconView.java:204-274): flags[b] = 1 when block b's
+// box (offsets offs[3 b .. 3 b + 2], size bx x by x bz, zero outside the volume) holds a
+// non-zero weight.  One launch covers every block of a step (blockIdx.y = block).
+__global__ void k_block_content(const float *__restrict__ w, long long D0, long long D1, long long D2,
+                                const long long *__restrict__ offs, int bx, int by, int bz, int *flags)
 {
+    const int blk = blockIdx.y;
+    const long long ox = offs[3 * blk], oy = offs[3 * blk + 1], oz = offs[3 * blk + 2];
     const long long n = (long long)bx * by * bz;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const long long x = ox + i % bx;
@@ -307,7 +311,7 @@ __global__ void k_block_content(const float *__restrict__ w, long long D0, long 
         const long long y = oy + t % by, z = oz + t / by;
         if (x < 0 || y < 0 || z < 0 || x >= D0 || y >= D1 || z >= D2) continue;
         if (w[(z * D1 + y) * D0 + x] != 0.0f) {
-            *flag = 1;
+            flags[blk] = 1;
             return;
         }
     }
@@ -539,7 +543,6 @@ private:
     std::vector<float> max_;
     double *d_scratch_ = nullptr;  // reductions
     int *d_perm_ = nullptr;
-    int *d_flag_ = nullptr;
     double *d_stats_ = nullptr;
     long long stats_cap_ = 0;
     bool prepared_ = false;
@@ -569,7 +572,6 @@ Decon<T>::~Decon()
     cudaFree(stage_);
     cudaFree(d_scratch_);
     cudaFree(d_perm_);
-    cudaFree(d_flag_);
     cudaFree(d_stats_);
     drop_graphs();
 }
@@ -598,7 +600,6 @@ int Decon<T>::init()
     D_CUDA(cudaMalloc(&psi_, sizeof(T) * (size_t)n_));
     D_CUDA(cudaMalloc(&stage_, sizeof(T) * (size_t)n_));
     D_CUDA(cudaMalloc(&d_scratch_, sizeof(double) * 2 * 4096 + sizeof(long long) * 4096 + sizeof(float) * 4096 * kMaxViews));
-    D_CUDA(cudaMalloc(&d_flag_, sizeof(int)));
     return MVR_OK;
 }
 
@@ -832,19 +833,40 @@ int Decon<T>::prepare()
         if (!divide_blocks(D, kk, p_.block_size, all, sort_dim_[st]))
             return fail(MVR_ERR_ARG, "block size smaller than the doubled kernel (2k-1)");
         const float *wcheck = views_[st].w;  // Mul: view 0's grid and weight
-        for (auto &bd : all) {
-            int keep = 1;
-            if (p_.filter_blocks) {
-                D_CUDA(cudaMemsetAsync(d_flag_, 0, sizeof(int), s));
-                const long long bn = (long long)p_.block_size[0] * p_.block_size[1] * p_.block_size[2];
-                k_block_content<<<grid_for(bn), 256, 0, s>>>(wcheck, D[0], D[1], D[2], bd.off[0], bd.off[1], bd.off[2],
-                                                            p_.block_size[0], p_.block_size[1], p_.block_size[2], d_flag_);
-                D_CUDA(cudaGetLastError());
-                D_CUDA(cudaMemcpyAsync(&keep, d_flag_, sizeof(int), cudaMemcpyDeviceToHost, s));
-                D_CUDA(cudaStreamSynchronize(s));
+        std::vector<int> keep(all.size(), 1);
+        if (p_.filter_blocks && !all.empty()) {
+            // one launch over all blocks of the step, one copy of the flags back
+            const int nb = (int)all.size();
+            std::vector<long long> offs(3 * (size_t)nb);
+            for (int b = 0; b < nb; ++b)
+                for (int d = 0; d < 3; ++d) offs[3 * (size_t)b + d] = all[b].off[d];
+            long long *d_offs = nullptr;
+            int *d_flags = nullptr;
+            D_CUDA(cudaMalloc(&d_offs, sizeof(long long) * offs.size()));
+            const cudaError_t ea = cudaMalloc(&d_flags, sizeof(int) * (size_t)nb);
+            if (ea != cudaSuccess) {
+                cudaFree(d_offs);
+                D_CUDA(ea);
             }
-            if (keep) blocks_[st].push_back(bd);
+            cudaError_t e = cudaMemcpyAsync(d_offs, offs.data(), sizeof(long long) * offs.size(),
+                                            cudaMemcpyHostToDevice, s);
+            if (e == cudaSuccess) e = cudaMemsetAsync(d_flags, 0, sizeof(int) * (size_t)nb, s);
+            if (e == cudaSuccess) {
+                const long long bn = (long long)p_.block_size[0] * p_.block_size[1] * p_.block_size[2];
+                const int gx = (int)std::max<long long>(1, std::min<long long>((bn + 255) / 256, 64));
+                k_block_content<<<dim3(gx, nb), 256, 0, s>>>(wcheck, D[0], D[1], D[2], d_offs, p_.block_size[0],
+                                                            p_.block_size[1], p_.block_size[2], d_flags);
+                e = cudaGetLastError();
+            }
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(keep.data(), d_flags, sizeof(int) * (size_t)nb, cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            cudaFree(d_offs);
+            cudaFree(d_flags);
+            D_CUDA(e);
         }
+        for (size_t b = 0; b < all.size(); ++b)
+            if (keep[b]) blocks_[st].push_back(all[b]);
         // every block of a batch reads psi before the step when the slab's effective
         // size >= k-1 (deferred write-back, MultiViewDeconvolutionSeq 79-162)
         const int sd = sort_dim_[st];

@@ -468,6 +468,45 @@ __global__ void __launch_bounds__(256) k_rows_ratio(typename Cx<T>::t *__restric
     r2c_post_store(Z2, ps, S, row0, nr, m, tw);
 }
 
+// ---- the running product of the Mul update ---------------------------------------------
+// computeNextValueMul (DeconvolutionMethods.java:370-387) multiplies the views' conv2
+// values in double and takes pow(prod, 1 / V).  A float product of 4-16 factors can leave
+// the float range where the double one does not (a tiny blurred value makes one factor
+// huge), so the float path keeps the product as a float mantissa in [0.5, 1) and a
+// power-of-two exponent (stored as a float pair, 8 bytes per voxel; every factor is split
+// with frexpf first, so no partial product under- or overflows).  Zero, signed, Inf and NaN
+// factors propagate as in the double product.
+__device__ __forceinline__ float2 mulprod_first(float c)
+{
+    int e;
+    const float m = frexpf(c, &e);
+    return make_float2(m, (float)e);
+}
+__device__ __forceinline__ float2 mulprod_acc(float2 p, float c)
+{
+    int ec, e2;
+    const float mc = frexpf(c, &ec);
+    const float m = frexpf(__fmul_rn(p.x, mc), &e2);
+    return make_float2(m, p.y + (float)(ec + e2));
+}
+// pow(prod, 1 / V) rounded to float: 2^(e / V) split into an integer power q and a
+// remainder r < V, so the float power function only sees m 2^r in [0.5, 2^(V-1)).
+// Math.pow of a negative base with the non-integer exponent 1 / V (V >= 2) is NaN.
+__device__ __forceinline__ float mulprod_root(float2 p, int V)
+{
+    const float m = p.x;
+    const int e = (int)p.y;
+    if (V == 1) return ldexpf(m, e);
+    if (m == 0.0f) return 0.0f;
+    if (!(m > 0.0f)) return __int_as_float(0x7fc00000);  // negative or NaN
+    if (isinf(m)) return m;
+    const int q = e >= 0 ? e / V : -((V - 1 - e) / V);
+    const int r = e - q * V;
+    const float x = ldexpf(m, r);
+    const float y = V == 2 ? __fsqrt_rn(x) : powf(x, 1.0f / (float)V);
+    return ldexpf(y, q);
+}
+
 // ---- C2R -> update -------------------------------------------------------------------
 enum { EPI_SEQ = 0, EPI_MUL_FIRST = 1, EPI_MUL_ACC = 2, EPI_MUL_FINAL = 3, EPI_STORE = 4, EPI_NLL = 5 };
 
@@ -476,7 +515,8 @@ struct UpdateArgs {
     void *psi_dst;        // T output volume (write region only)
     const float *weight[kMaxViews];
     int nviews;
-    void *prod;           // Mul: running product over views (T), block layout [bz][by][bx]
+    void *prod;           // Mul: running product over views, block layout [bz][by][bx], 8 bytes a
+                          // voxel (double for the FP64 path, mulprod_* float pairs for FP32)
     float *store;         // EPI_STORE: conv result, block layout
     const float *img;     // EPI_NLL: the view's image (zero outside the volume)
     double lambda;
@@ -536,7 +576,12 @@ __device__ __forceinline__ void update_row(const typename Cx<T>::t *zz, int m, c
                     ua.store[brow + x] = (float)integral;
                     continue;
                 }
-                if (EPI == EPI_MUL_FIRST) { reinterpret_cast<T *>(ua.prod)[brow + x] = integral; continue; }
+                if (EPI == EPI_MUL_FIRST) {
+                    if constexpr (sizeof(T) == sizeof(float))
+                        reinterpret_cast<float2 *>(ua.prod)[brow + x] = mulprod_first((float)integral);
+                    else reinterpret_cast<T *>(ua.prod)[brow + x] = integral;
+                    continue;
+                }
                 if (EPI == EPI_NLL) {
                     // Poisson negative log-likelihood w * (conv1 - img ln conv1) over img > 0,
                     // each volume voxel once (write region of its block)
@@ -552,7 +597,15 @@ __device__ __forceinline__ void update_row(const typename Cx<T>::t *zz, int m, c
                     ksum = kt;
                     continue;
                 }
-                if (EPI == EPI_MUL_ACC) { reinterpret_cast<T *>(ua.prod)[brow + x] *= integral; continue; }
+                if (EPI == EPI_MUL_ACC) {
+                    if constexpr (sizeof(T) == sizeof(float)) {
+                        float2 *pp = reinterpret_cast<float2 *>(ua.prod) + brow + x;
+                        *pp = mulprod_acc(*pp, (float)integral);
+                    } else {
+                        reinterpret_cast<T *>(ua.prod)[brow + x] *= integral;
+                    }
+                    continue;
+                }
                 const T last = lastv[u][h];
                 T next;
                 if (EPI == EPI_SEQ) {
@@ -562,17 +615,20 @@ __device__ __forceinline__ void update_row(const typename Cx<T>::t *zz, int m, c
                     else
                         next = next_value(last, integral, (T)wv[u][h], ua.lambda, (T)ua.minI, (T)ua.maxI);
                 } else {  // EPI_MUL_FINAL: DeconvolutionMethods.computeNextValueMul 370-419
-                    // the product and the weight sum in T (the reference uses double; on this
-                    // GPU the double rate is a small fraction of the float rate, and the float
-                    // product of V factors near 1 stays within a few ulp)
-                    const T prod = (ua.nviews == 1 ? (T)1 : reinterpret_cast<const T *>(ua.prod)[brow + x]) * integral;
+                    // the weight sum in T (the reference uses double; the float sum of V
+                    // weights in [0, 1] stays within an ulp), the product as above
                     T sumW = 0;
                     for (int v = 0; v < ua.nviews; ++v) sumW += (T)zero_at(ua.weight[v], bm, zr, x);
                     T root;
-                    if (sizeof(T) == sizeof(double)) root = (T)pow((double)prod, 1.0 / ua.nviews);
-                    else if (ua.nviews == 1) root = prod;
-                    else if (ua.nviews == 2) root = (T)__fsqrt_rn((float)prod);
-                    else root = (T)powf((float)prod, 1.0f / (float)ua.nviews);
+                    if constexpr (sizeof(T) == sizeof(double)) {
+                        const T prod = (ua.nviews == 1 ? (T)1 : reinterpret_cast<const T *>(ua.prod)[brow + x]) * integral;
+                        root = (T)pow((double)prod, 1.0 / ua.nviews);
+                    } else {
+                        const float2 p = ua.nviews == 1 ? mulprod_first((float)integral)
+                                                        : mulprod_acc(reinterpret_cast<const float2 *>(ua.prod)[brow + x],
+                                                                      (float)integral);
+                        root = (T)mulprod_root(p, ua.nviews);
+                    }
                     sumW = sumW < (T)1 ? sumW : (T)1;
                     if constexpr (sizeof(T) == sizeof(float))
                         next = next_value((float)last, (float)root, (float)sumW, ua.two_lambda, ua.tik, ua.minI, ua.maxI);
@@ -649,7 +705,7 @@ __global__ void __launch_bounds__(256) k_rows_update(typename Cx<T>::t *__restri
     const BlockMap &bm = bms.m[blockIdx.y];
     S += (long long)blockIdx.y * Pc;
     const long long bvox = (long long)bm.b[0] * bm.b[1] * bm.b[2];
-    if (ua.prod) ua.prod = reinterpret_cast<T *>(ua.prod) + (long long)blockIdx.y * bvox;
+    if (ua.prod) ua.prod = reinterpret_cast<double *>(ua.prod) + (long long)blockIdx.y * bvox;  // 8 bytes a voxel
     if (ua.store) ua.store += (long long)blockIdx.y * bvox;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double red_s[32], red_m[32];

@@ -541,7 +541,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
     }
     float2 *Sp = S + (long long)blockIdx.y * Pc + (long long)z * SH::plane;
     const long long bvox = (long long)bm.b[0] * bm.b[1] * bm.b[2];
-    if (ua.prod) ua.prod = reinterpret_cast<float *>(ua.prod) + (long long)blockIdx.y * bvox;
+    if (ua.prod) ua.prod = reinterpret_cast<float2 *>(ua.prod) + (long long)blockIdx.y * bvox;  // mulprod_* pairs
     if (ua.store) ua.store += (long long)blockIdx.y * bvox;
     sm.load_tables(gtwx, gtwy);
     float ksum = 0.0f, kcomp = 0.0f, kmax = -1.0f;

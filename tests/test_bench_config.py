@@ -26,4 +26,22 @@ def test_workload_config_fields():
         w = make()
         c = w.config("circular")
         assert c["views"] == w.views and c["dims"] == list(w.dims) and c["block"] == list(w.block)
-        assert "inputs larger than L2" in c["l2"]
+        assert ("inputs larger than L2" in c["l2"]) != w.flush_l2()
+    assert bench.WORKLOADS["2view128"]().flush_l2() and not bench.WORKLOADS["4view256"]().flush_l2()
+
+
+def test_reference_arm_line_on_the_two_view_workload():
+    # the CPU arm end to end (float32 padded R2C restatement, one block per view per step)
+    import json
+    import subprocess
+
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload",
+                        "2view128", "--steps", "1", "--warmup", "0"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "voxel-iterations/s" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    # one step advances the whole 128x128x64 volume by one iteration (one block)
+    assert abs(line["value"] * line["ms_per_step"] / 1e3 - 128 * 128 * 64) < 1.0
