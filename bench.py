@@ -46,6 +46,10 @@ class Workload:
     """A named deconvolution workload: volume, views, compute block, PSF sizes per view."""
 
     def __init__(self, name, dims, views, block, psfs, lam, make, desc, psf_type=1, weight_norm=1, fp64_iters=None):
+        # block: one compute block (x, y, z) for every view, or a list with one per view
+        per_view = isinstance(block[0], (tuple, list))
+        self.vblocks = [tuple(b) for b in block] if per_view else [tuple(block)] * views
+        block = self.vblocks[0]
         self.name, self.dims, self.views, self.block, self.psfs, self.lam = name, dims, views, block, psfs, lam
         self.make, self.desc = make, desc
         self.psf_type, self.weight_norm = psf_type, weight_norm  # MVR_PSF_*, MVR_WEIGHTS_*
@@ -57,7 +61,16 @@ class Workload:
         import oracle
 
         kk = tuple(2 * k - 1 for k in self.psfs[v])
-        return oracle.divide_into_blocks(self.dims, kk, self.block)
+        return oracle.divide_into_blocks(self.dims, kk, self.vblocks[v])
+
+    def per_view_blocks(self):
+        return len(set(self.vblocks)) > 1
+
+    def setup_blocks(self, d):
+        """Per-view compute blocks on a Deconvolution handle (before prepare)."""
+        if self.per_view_blocks():
+            for v in range(self.views):
+                d.set_view_block_size(v, self.vblocks[v])
 
     def view_blocks_per_iter(self):
         return sum(len(self.blocks(v)) for v in range(self.views))
@@ -74,7 +87,8 @@ class Workload:
         l2 = (f"L2 flushed before every timed step (a 512 MiB write outside the step's events; inputs "
               f"{mib:.0f} MiB)" if self.flush_l2() else
               f"inputs larger than L2 ({self.views} images + {self.views} weights + psi = {mib:.0f} MiB)")
-        return {"workload": self.desc, "views": self.views, "dims": list(self.dims), "block": list(self.block),
+        blk = [list(b) for b in self.vblocks] if self.per_view_blocks() else list(self.block)
+        return {"workload": self.desc, "views": self.views, "dims": list(self.dims), "block": blk,
                 "psf": [list(p) for p in self.psfs] if len(set(self.psfs)) > 1 else list(self.psfs[0]),
                 "lambda": self.lam, "iterations_per_step": 1, "boundary": boundary, "l2": l2,
                 "data": "seeded synthetic beads + ellipsoid, Poisson, background 10"}
@@ -112,6 +126,24 @@ def _psf_sizes_6():
     return [tuple(p) for p in synthetic.PSF_SIZES_6]
 
 
+def friendly(n, even=False):
+    """Smallest size >= n with prime factors <= 13 (even when asked): a circular FFT
+    domain the library accepts."""
+    while True:
+        k = n
+        for r in (2, 3, 5, 7, 11, 13):
+            while k % r == 0:
+                k //= r
+        if k == 1 and (not even or n % 2 == 0):
+            return n
+        n += 1
+
+
+def _blocks_6():
+    """128^3 effective blocks: compute block 128 + 2 (k - 1) per axis and view."""
+    return [tuple(friendly(128 + 2 * (p[d] - 1), even=d == 0) for d in range(3)) for p in _psf_sizes_6()]
+
+
 WORKLOADS = {
     "2view128": lambda: Workload("2view128", (128, 128, 64), 2, (192, 192, 128), [(15, 15, 31)] * 2, 0.0, _make_small,
                                  "2 views 128x128x64 float32, PSF 15x15x31 at 0/90 degrees, efficient-Bayesian, "
@@ -119,7 +151,13 @@ WORKLOADS = {
                                  psf_type=2, weight_norm=0),
     "4view256": lambda: Workload("4view256", (256, 256, 256), 4, (192, 192, 192), [(31, 31, 61)] * 4, 0.006, _make256,
                                  "4 views 256^3 float32, PSF 31x31x61 Optimization-I, blocks 192^3, Seq (OSEM-like)"),
-    "6view512": lambda: Workload("6view512", (512, 512, 256), 6, (192, 192, 256), _psf_sizes_6(), 0.006, _make512,
+    "6view512": lambda: Workload("6view512", (512, 512, 256), 6, _blocks_6(), _psf_sizes_6(), 0.006, _make512,
+                                 "6 views 512x512x256 float32, PSFs 21x21x41 ... 41x41x81 per view, "
+                                 "Optimization-I, 128^3 effective blocks plus each view's overlap: compute blocks "
+                                 "128 + 2 (k - 1) per axis (rounded up to an FFT-friendly size where needed), "
+                                 "32 blocks per view including uneven edge blocks, Seq", fp64_iters=5),
+    "6view512fixed": lambda: Workload("6view512fixed", (512, 512, 256), 6, (192, 192, 256), _psf_sizes_6(), 0.006,
+                                      _make512,
                                  "6 views 512x512x256 float32, PSFs 21x21x41 ... 41x41x81 per view, "
                                  "Optimization-I, compute blocks 192x192x256 (effective 112-152 x 112-152 x 96-176, "
                                  "uneven edge blocks), Seq", fp64_iters=5),
@@ -292,7 +330,7 @@ def cpu_sampler(ds, psi, mx, prep):
 
     k1s, k2s, weight_block, image_block, _, _ = prep
     grids = [W.blocks(v) for v in range(W.views)]
-    return R.BlockSampler(psi, None, None, k1s, k2s, grids, W.block, W.lam, mx, image_block=image_block,
+    return R.BlockSampler(psi, None, None, k1s, k2s, grids, W.vblocks, W.lam, mx, image_block=image_block,
                           weight_block=weight_block)
 
 
@@ -366,6 +404,7 @@ def fp64_error(M, views, n_iter, dev, boundary, d_img, d_w, ds):
     for prec in (M.PRECISION_FP32, M.PRECISION_FP64):
         with M.Deconvolution(W.dims, W.views, W.block, mul=False, psf_type=W.psf_type, psf_norm_threads=0, lam=W.lam,
                              boundary=boundary, precision=prec, weight_norm=W.weight_norm, device=dev) as d:
+            W.setup_blocks(d)
             for v in range(views):
                 d.set_view_device(v, d_img[v].data_ptr(), d_w[v].data_ptr(), ds.psfs[v])
             d.prepare()
@@ -401,6 +440,7 @@ def run_gb300(args, ws, rank, local):
     dec = M.Deconvolution(W.dims, W.views, W.block, mul=False, psf_type=W.psf_type, psf_norm_threads=0,
                           lam=W.lam, boundary=boundary, precision=M.PRECISION_FP32, weight_norm=W.weight_norm,
                           batch_blocks=args.batch, device=dev)
+    W.setup_blocks(dec)
     for v in range(W.views):
         dec.set_view_device(v, d_img[v].data_ptr(), d_w[v].data_ptr(), ds.psfs[v])
     dec.prepare()
@@ -481,9 +521,12 @@ def run_gb300(args, ws, rank, local):
                 "path_achieved": path_bytes / (total_ms / 1e3) / 1e9, "kernels": kernels}
     # the whole path against the algorithmic byte model of one view-block, 28 N + 48 Pc
     # (N block voxels, Pc = (bx / 2 + 1) by bz spectrum values), over the timed steps
-    bn = W.block[0] * W.block[1] * W.block[2]
-    bpc = (W.block[0] // 2 + 1) * W.block[1] * W.block[2]
-    b_it = W.view_blocks_per_iter() * (28.0 * bn + 48.0 * bpc)
+    b_it = 0.0
+    for v in range(W.views):
+        b = W.vblocks[v]
+        bn = b[0] * b[1] * b[2]
+        bpc = (b[0] // 2 + 1) * b[1] * b[2]
+        b_it += len(W.blocks(v)) * (28.0 * bn + 48.0 * bpc)
     roofline["model_bytes_per_iteration"] = b_it
     roofline["model_achieved"] = b_it * args.steps / (ms / 1e3) / 1e9
     roofline["model_frac"] = roofline["model_achieved"] / peak
@@ -494,7 +537,8 @@ def run_gb300(args, ws, rank, local):
         e2e_block = None
     else:
         e2e = run_e2e(args, ws, dev, ds, dec, shape, boundary)
-        e2e_block = run_e2e_block(args, ws, dev, ds, dec, dec_max)
+        # one block worker size: the per-block path of one-block-size workloads
+        e2e_block = None if W.per_view_blocks() else run_e2e_block(args, ws, dev, ds, dec, dec_max)
     psi_now = dec.get_psi()
     dec.close()
     # ---- every result's error against an FP64 run of the same iterations ----
@@ -553,6 +597,7 @@ def run_e2e(args, ws, dev, ds, dec, shape, boundary):
     e2e_dec = M.Deconvolution(W.dims, W.views, W.block, mul=False, psf_type=W.psf_type,
                               psf_norm_threads=0, lam=W.lam, boundary=boundary, precision=M.PRECISION_FP32,
                               weight_norm=W.weight_norm, device=dev)
+    W.setup_blocks(e2e_dec)
     for v in range(W.views):
         e2e_dec.set_view(v, h_img[v].numpy(), h_w[v].numpy(), ds.psfs[v])
     e2e_dec.prepare()

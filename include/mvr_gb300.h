@@ -164,6 +164,12 @@ MVR_API int mvr_decon_set_view(mvr_decon *h, int view, const float *img, const f
  * outlive the handle). */
 MVR_API int mvr_decon_set_view_device(mvr_decon *h, int view, const float *img, const float *weight,
                                       const float *psf, const int psf_size[3]);
+/* The compute block size of one view ({x, y, z}; NULL restores the handle's block_size),
+ * before mvr_decon_prepare.  DeconView takes its block size per view
+ * (MV/deconvolution/DeconView.java:118-184): with per-view PSF sizes, a block of
+ * E + 2 (k_v - 1) per axis gives every view effective blocks of E (the doubled kernel
+ * 2 k_v - 1).  Multiplicative mode needs one grid: equal block sizes. */
+MVR_API int mvr_decon_set_view_block_size(mvr_decon *h, int view, const int block_size[3]);
 /* Replaces a view's image and raw weight (host) without redoing the PSF preparation. */
 MVR_API int mvr_decon_update_images(mvr_decon *h, int view, const float *img, const float *weight);
 /* DeconViews + DeconViewPSF.init, weight normalisation, block grids, PsiInitAvgPrecise. */

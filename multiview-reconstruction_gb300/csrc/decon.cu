@@ -407,6 +407,7 @@ public:
     virtual ~DeconBase() = default;
     virtual int set_images(int v, const float *img, const float *w, bool on_device) = 0;
     virtual int set_psf(int v, const float *psf, const int dims[3]) = 0;
+    virtual int set_view_block(int v, const int block[3]) = 0;
     virtual int prepare() = 0;
     virtual int set_psi(const float *psi, bool on_device) = 0;
     virtual int get_psi(float *psi) = 0;
@@ -438,6 +439,7 @@ public:
     int init();
     int set_images(int v, const float *img, const float *w, bool on_device) override;
     int set_psf(int v, const float *psf, const int dims[3]) override;
+    int set_view_block(int v, const int block[3]) override;
     int prepare() override;
     int set_psi(const float *psi, bool on_device) override;
     int get_psi(float *psi) override;
@@ -463,8 +465,10 @@ private:
         bool own_img = false, own_w = false;
         std::vector<float> psf;
         int kd[3] = {0, 0, 0};
+        int block[3] = {0, 0, 0};            // compute block size of this view (0: the handle's)
         float *k1 = nullptr, *k2 = nullptr;  // device, prepared kernels
         Plan<T> plan;
+        const int *bsize(const int *dflt) const { return block[0] > 0 ? block : dflt; }
     };
     int fail(int c, const std::string &m)
     {
@@ -655,6 +659,21 @@ int Decon<T>::set_psf(int v, const float *psf, const int dims[3])
 }
 
 template <typename T>
+int Decon<T>::set_view_block(int v, const int block[3])
+{
+    if (v < 0 || v >= p_.num_views) return fail(MVR_ERR_ARG, "view out of range");
+    if (!block) {
+        std::memset(views_[v].block, 0, sizeof(views_[v].block));
+    } else {
+        for (int d = 0; d < 3; ++d)
+            if (block[d] < 1) return fail(MVR_ERR_ARG, "block sizes must be >= 1");
+        std::memcpy(views_[v].block, block, sizeof(views_[v].block));
+    }
+    prepared_ = false;
+    return MVR_OK;
+}
+
+template <typename T>
 int Decon<T>::norm_to_sum1(float *k, long long n)
 {
     const long long first = p_.psf_norm_threads > 0 ? first_portion(n, p_.psf_norm_threads) : 0;
@@ -803,6 +822,9 @@ int Decon<T>::prepare()
             if (std::memcmp(views_[v].kd, views_[0].kd, sizeof(views_[0].kd)) != 0)
                 return fail(MVR_ERR_ARG, "multiplicative mode needs one block grid: equal PSF sizes "
                                          "(MultiViewDeconvolutionMul.testBlockIntegrity)");
+        for (int v = 1; v < nv; ++v)
+            if (std::memcmp(views_[v].bsize(p_.block_size), views_[0].bsize(p_.block_size), 3 * sizeof(int)) != 0)
+                return fail(MVR_ERR_ARG, "multiplicative mode needs one block grid: equal block sizes");
     }
     // weights
     if (p_.weight_norm != MVR_WEIGHTS_AS_GIVEN) {
@@ -818,7 +840,8 @@ int Decon<T>::prepare()
     }
     // PSFs and their spectra for this block size
     D_TRY(psf_init());
-    for (auto &vw : views_) D_TRY(eng(engine_.make_plan(vw.plan, p_.block_size, vw.k1, vw.kd, vw.k2, vw.kd, true)));
+    for (auto &vw : views_)
+        D_TRY(eng(engine_.make_plan(vw.plan, vw.bsize(p_.block_size), vw.k1, vw.kd, vw.k2, vw.kd, true)));
     // block grids per step
     const long long D[3] = {p_.dims[0], p_.dims[1], p_.dims[2]};
     const int steps = num_steps();
@@ -830,7 +853,8 @@ int Decon<T>::prepare()
         int kk[3];
         for (int d = 0; d < 3; ++d) kk[d] = 2 * vw.kd[d] - 1;
         std::vector<BlockDesc> all;
-        if (!divide_blocks(D, kk, p_.block_size, all, sort_dim_[st]))
+        const int *bs = vw.bsize(p_.block_size);
+        if (!divide_blocks(D, kk, bs, all, sort_dim_[st]))
             return fail(MVR_ERR_ARG, "block size smaller than the doubled kernel (2k-1)");
         const float *wcheck = views_[st].w;  // Mul: view 0's grid and weight
         std::vector<int> keep(all.size(), 1);
@@ -852,10 +876,10 @@ int Decon<T>::prepare()
                                             cudaMemcpyHostToDevice, s);
             if (e == cudaSuccess) e = cudaMemsetAsync(d_flags, 0, sizeof(int) * (size_t)nb, s);
             if (e == cudaSuccess) {
-                const long long bn = (long long)p_.block_size[0] * p_.block_size[1] * p_.block_size[2];
+                const long long bn = (long long)bs[0] * bs[1] * bs[2];
                 const int gx = (int)std::max<long long>(1, std::min<long long>((bn + 255) / 256, 64));
-                k_block_content<<<dim3(gx, nb), 256, 0, s>>>(wcheck, D[0], D[1], D[2], d_offs, p_.block_size[0],
-                                                            p_.block_size[1], p_.block_size[2], d_flags);
+                k_block_content<<<dim3(gx, nb), 256, 0, s>>>(wcheck, D[0], D[1], D[2], d_offs, bs[0], bs[1], bs[2],
+                                                            d_flags);
                 e = cudaGetLastError();
             }
             if (e == cudaSuccess)
@@ -870,7 +894,7 @@ int Decon<T>::prepare()
         // every block of a batch reads psi before the step when the slab's effective
         // size >= k-1 (deferred write-back, MultiViewDeconvolutionSeq 79-162)
         const int sd = sort_dim_[st];
-        const long long eff = p_.block_size[sd] - kk[sd] + 1;
+        const long long eff = bs[sd] - kk[sd] + 1;
         jacobi_[st] = (eff >= vw.kd[sd] - 1 && blocks_[st].size() == all.size()) ? 1 : 0;
     }
     // psi init: PsiInitAvgPrecise (average over views with data) and max per view
@@ -1457,6 +1481,11 @@ extern "C" int mvr_decon_set_view_device(mvr_decon *h, int view, const float *im
     if (!h) return MVR_ERR_ARG;
     int rc = h->impl->set_images(view, img, weight, true);
     return rc != MVR_OK ? rc : h->impl->set_psf(view, psf, psf_size);
+}
+
+extern "C" int mvr_decon_set_view_block_size(mvr_decon *h, int view, const int block_size[3])
+{
+    return h ? h->impl->set_view_block(view, block_size) : MVR_ERR_ARG;
 }
 
 extern "C" int mvr_decon_update_images(mvr_decon *h, int view, const float *img, const float *weight)

@@ -232,7 +232,10 @@ class BlockSampler:
         self.k1s, self.k2s = k1s, k2s
         self.grids = grids  # per view: list of dicts (offset, eff_offset, eff_size, eff_local)
         self.views = len(grids)
-        self.b = tuple(block_xyz)
+        # one block size (x, y, z) for every view, or a list with one per view
+        per_view = isinstance(block_xyz[0], (tuple, list))
+        self.bs = [tuple(b) for b in block_xyz] if per_view else [tuple(block_xyz)] * self.views
+        self.b = self.bs[0]
         self.lam, self.mx, self.min_value = lam, list(max_intensities), min_value
         self.image_block = image_block or (lambda v, off, b: extract(images[v], off, b, "zero"))
         self.weight_block = weight_block or (lambda v, off, b: extract(weights[v], off, b, "zero"))
@@ -246,8 +249,8 @@ class BlockSampler:
 
     def _convolvers(self, v):
         if v not in self.conv:
-            self.conv[v] = (PaddedConvolver(self.b, self.k1s[v], self.workers),
-                            PaddedConvolver(self.b, self.k2s[v], self.workers))
+            self.conv[v] = (PaddedConvolver(self.bs[v], self.k1s[v], self.workers),
+                            PaddedConvolver(self.bs[v], self.k2s[v], self.workers))
         return self.conv[v]
 
     def prepare(self):
@@ -262,9 +265,10 @@ class BlockSampler:
             grid = self.grids[v]
             bl = grid[self.step_index % len(grid)]
             c1, c2 = self._convolvers(v)
-            p = extract(self.psi, bl["offset"], self.b, "mirror")
-            img = self.image_block(v, bl["offset"], self.b)
-            w = self.weight_block(v, bl["offset"], self.b)
+            b = self.bs[v]
+            p = extract(self.psi, bl["offset"], b, "mirror")
+            img = self.image_block(v, bl["offset"], b)
+            w = self.weight_block(v, bl["offset"], b)
             block_seq(p, img, w, c1, c2, self.lam, self.min_value, self.mx[v], self.pool, self.workers)
             paste(self.psi, p, bl["eff_offset"], bl["eff_size"], bl["eff_local"])
             es = bl["eff_size"]

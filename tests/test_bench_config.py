@@ -14,9 +14,16 @@ def test_workload_block_grids():
     w = bench.WORKLOADS["4view256"]()
     assert [len(w.blocks(v)) for v in range(4)] == [16] * 4  # 2 x 2 x 4 blocks of 192^3
     assert w.view_blocks_per_iter() == 64 and w.metric == "voxel-iterations/s (4 views)"
-    w = bench.WORKLOADS["6view512"]()
+    w = bench.WORKLOADS["6view512fixed"]()
     # effective sizes 192 - 2(k-1): 152 ... 112 in x/y, 256 - 2(k-1): 176 ... 96 in z
     assert [len(w.blocks(v)) for v in range(6)] == [32, 32, 32, 32, 75, 75]
+    # 128^3 effective blocks plus each view's overlap: 4 x 4 x 2 blocks in every view
+    w = bench.WORKLOADS["6view512"]()
+    assert w.per_view_blocks() and [len(w.blocks(v)) for v in range(6)] == [32] * 6
+    for v, k in enumerate(w.psfs):
+        b = w.vblocks[v]
+        assert all(b[d] >= 128 + 2 * (k[d] - 1) for d in range(3))
+        assert all(w.blocks(v)[0]["eff_size"][d] >= 128 for d in range(3))  # the last block may be clipped
     w = bench.WORKLOADS["8view1024"]()
     assert [len(w.blocks(v)) for v in range(8)] == [216] * 8
 
@@ -25,7 +32,8 @@ def test_workload_config_fields():
     for name, make in bench.WORKLOADS.items():
         w = make()
         c = w.config("circular")
-        assert c["views"] == w.views and c["dims"] == list(w.dims) and c["block"] == list(w.block)
+        blk = [list(b) for b in w.vblocks] if w.per_view_blocks() else list(w.block)
+        assert c["views"] == w.views and c["dims"] == list(w.dims) and c["block"] == blk
         assert ("inputs larger than L2" in c["l2"]) != w.flush_l2()
     assert bench.WORKLOADS["2view128"]().flush_l2() and not bench.WORKLOADS["4view256"]().flush_l2()
 

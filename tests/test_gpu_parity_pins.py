@@ -278,3 +278,30 @@ def test_weight_empty_block_is_dropped_and_batch_order_runs():
         d.prepare()
         d.run_iterations(2)
         assert rel(d.get_psi(), unfiltered) <= 1e-4
+
+
+# ---- per-view compute blocks (DeconView takes its block size per view) -------------------
+
+def test_per_view_block_sizes_against_one_block_oracle():
+    # effective blocks of 16 voxels plus each view's overlap; with every effective region at
+    # least k - 1 along the slab axis the blocked result equals the one-block result
+    rng = np.random.default_rng(12)
+    dims = (48, 40, 36)
+    shape = dims[::-1]
+    ks = [(5, 5, 7), (7, 7, 9), (9, 9, 11)]
+    psfs = [synthetic.make_psf(k, 1.0, 1.5, a) for k, a in zip(ks, (0.0, 60.0, 120.0))]
+    imgs = [rng.uniform(5, 100, shape).astype(np.float32) for _ in range(3)]
+    ws = [rng.uniform(0.2, 1, shape).astype(np.float32) for _ in range(3)]
+    k1s, k2s = O.psf_init(psfs, O.PSF_OPTIMIZATION_I, 0)
+    psi0, mx, _ = O.psi_init_avg(imgs)
+    one = (64, 56, 56)  # one block for every view
+    ref, _ = O.decon_run(psi0, imgs, ws, k1s, k2s, one, 2, lam=0.006, max_intensities=mx)
+    with M.Deconvolution(dims, 3, one, psf_type=M.PSF_OPTIMIZATION_I, psf_norm_threads=0, lam=0.006,
+                         weight_norm=M.WEIGHTS_AS_GIVEN, boundary=M.BOUNDARY_REFERENCE) as d:
+        for v in range(3):
+            d.set_view(v, imgs[v], ws[v], psfs[v])
+            d.set_view_block_size(v, tuple(16 + 2 * (ks[v][i] - 1) for i in range(3)))
+        d.prepare()
+        d.run_iterations(2)
+        psi = d.get_psi()
+    assert rel(psi, ref) <= 1e-4
