@@ -444,6 +444,8 @@ def run_gb300(args, ws, rank, local):
     for v in range(W.views):
         dec.set_view_device(v, d_img[v].data_ptr(), d_w[v].data_ptr(), ds.psfs[v])
     dec.prepare()
+    autotune = {"schedules": [M.schedule_name(dec.schedule(v)) for v in range(W.views)],
+                "trials": [dict(t, ms=round(t["ms"], 4)) for t in dec.tuning()]}
     dec_max = dec.max_intensities()
     stream = torch.cuda.ExternalStream(dec.stream_ptr(), device=f"cuda:{dev}")
     batch = dec.batch()
@@ -567,7 +569,7 @@ def run_gb300(args, ws, rank, local):
         line = {"metric": W.metric, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": dict(W.config(args.boundary), batch_blocks=batch), "clocks": clocks,
+                "config": dict(W.config(args.boundary), batch_blocks=batch), "clocks": clocks, "autotune": autotune,
                 "gpu_launches": launches, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                 "with_statistics": {"ms_per_step": stats_ms, "value": ws * W.nvox / (stats_ms / 1e3),
                                     "steps": stat_steps,

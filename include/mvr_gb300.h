@@ -227,6 +227,26 @@ MVR_API int mvr_decon_batch(const mvr_decon *h);
 MVR_API int mvr_decon_set_graphs(mvr_decon *h, int on);
 /* Number of captured iteration graphs held by the handle. */
 MVR_API int mvr_decon_graphs_captured(const mvr_decon *h);
+/* FFT schedules.  mvr_decon_prepare times, per view-step, every schedule the step's FFT
+ * domain admits and keeps the fastest (then the blocks per launch, unless batch_blocks fixes
+ * it); the batched, autotuned form of the iteration loop (no reference counterpart: the
+ * reference's FFT has one fixed schedule).  Codes: MVR_SCHED_ROWS (row and column kernels),
+ * MVR_SCHED_PLANE (x and y fused per z-plane, one CTA per plane), MVR_SCHED_PLANE_PERSIST
+ * (the same with one CTA per SM walking the planes), plus MVR_SCHED_ZPIPE when the Z pass
+ * runs the persistent double-buffered column kernel.  Every schedule computes the same
+ * iteration (results agree to float rounding).
+ * mvr_decon_set_schedule (before prepare): force `code` for every view, -1 = autotune.
+ * mvr_decon_schedule: the code in use for a view (negative on error).
+ * mvr_decon_tuning: the autotuner's trials, up to `capacity` of them into the arrays (any may
+ * be NULL): view-step (-1 for a batch trial), code (-1 for a batch trial), blocks per launch,
+ * ms per view-step; returns the number of trials. */
+#define MVR_SCHED_ROWS 0
+#define MVR_SCHED_PLANE 1
+#define MVR_SCHED_PLANE_PERSIST 2
+#define MVR_SCHED_ZPIPE 4
+MVR_API int mvr_decon_set_schedule(mvr_decon *h, int code);
+MVR_API int mvr_decon_schedule(const mvr_decon *h, int view);
+MVR_API int mvr_decon_tuning(const mvr_decon *h, int capacity, int *step, int *code, int *batch, float *ms);
 
 /* PsiInit (MV/deconvolution/init/): re-initialise psi and the per-view maxima on the
  * device after mvr_decon_prepare (which runs MVR_PSI_INIT_AVG_PRECISE).

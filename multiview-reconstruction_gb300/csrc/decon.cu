@@ -429,6 +429,9 @@ public:
     virtual int set_graphs(bool on) = 0;
     virtual int psi_init(int method, double sigma, double *avg) = 0;
     virtual int graphs_captured() const = 0;
+    virtual int set_schedule(int code) = 0;
+    virtual int schedule(int view) const = 0;
+    virtual int tuning(int capacity, int *step, int *code, int *batch, float *ms) const = 0;
 };
 
 template <typename T>
@@ -528,12 +531,22 @@ public:
         return MVR_OK;
     }
     int graphs_captured() const override { return (int)graphs_.size(); }
+    int set_schedule(int code) override;
+    int schedule(int view) const override;
+    int tuning(int capacity, int *step, int *code, int *batch, float *ms) const override;
     int psi_init(int method, double sigma, double *avg) override;
 
 private:
     int normalize_weights();
     int batch_ = 1;
-    std::vector<std::pair<int, float>> tune_;  // (blocks per launch, ms per view-step)
+    struct Trial {
+        int step;   // view-step of a schedule trial, -1 for a batch trial
+        int code;   // FFT schedule (SCHED_*), -1 for a batch trial
+        int batch;  // blocks per launch
+        float ms;   // one view-step
+    };
+    std::vector<Trial> tune_;
+    int force_sched_ = -1;  // FFT schedule forced for every view, -1: autotuned
     bool weights_dirty_ = false;
 
     mvr_decon_params p_;
@@ -1280,43 +1293,127 @@ int Decon<T>::run_iteration(double *stats_base, size_t stats_stride)
     return MVR_OK;
 }
 
-// Batch size per launch: the fastest of 1, 2, 4, 8, 16 blocks on one view-step
-// (CUDA events on the engine stream), unless fixed by the parameters.
+// The autotuner, at prepare: per view-step, the FFT schedule (row / column kernels, plane
+// kernels with one CTA per plane or persistent, and the Z pass with the one-tile-per-CTA or the
+// persistent double-buffered column kernel) that runs the step fastest at the largest batch;
+// then the blocks per launch (1, 2, 4, 8, 16) with those schedules.  Every candidate runs the
+// step twice (warm, then timed with CUDA events on the engine stream) as a trial that reads
+// psi and writes only the staging volume.  A forced schedule (mvr_decon_set_schedule) or one
+// of the environment switches MVR_PLANE_KERNELS / MVR_XY_PERSIST / MVR_COLS_PIPE skips the
+// schedule search; a fixed batch_blocks skips the batch search.
+namespace {
+bool sched_env_forced()
+{
+    for (const char *v : {"MVR_PLANE_KERNELS", "MVR_XY_PERSIST", "MVR_COLS_PIPE"})
+        if (std::getenv(v)) return true;
+    return false;
+}
+}  // namespace
+
 template <typename T>
 int Decon<T>::autotune()
 {
     size_t maxb = 1;
     for (auto &b : blocks_) maxb = std::max(maxb, b.size());
     const int cap = (int)std::min<size_t>(maxb, kMaxBatch);
-    if (p_.batch_blocks > 0) {
-        batch_ = std::min(p_.batch_blocks, kMaxBatch);
-        return MVR_OK;
-    }
-    batch_ = 1;
-    if (cap <= 1 || !jacobi_[0]) return MVR_OK;
     cudaStream_t s = engine_.stream();
     cudaEvent_t a, b;
     D_CUDA(cudaEventCreate(&a));
-    D_CUDA(cudaEventCreate(&b));
-    float best = 1e30f;
+    const cudaError_t eb = cudaEventCreate(&b);
+    if (eb != cudaSuccess) {
+        cudaEventDestroy(a);
+        D_CUDA(eb);
+    }
     tune_.clear();
-    for (int cand = 1; cand <= cap; cand *= 2) {
-        D_TRY(run_step(0, nullptr, true, cand));  // warm (allocates the batch's scratch)
+    auto time_step = [&](int st, int batch, float &ms) -> int {
+        D_TRY(run_step(st, nullptr, true, batch));  // warm (allocates the batch's scratch)
         D_CUDA(cudaEventRecord(a, s));
-        D_TRY(run_step(0, nullptr, true, cand));
+        D_TRY(run_step(st, nullptr, true, batch));
         D_CUDA(cudaEventRecord(b, s));
         D_CUDA(cudaEventSynchronize(b));
-        float ms = 0.0f;
         D_CUDA(cudaEventElapsedTime(&ms, a, b));
-        tune_.push_back({cand, ms});
-        if (ms < best) {
-            best = ms;
-            batch_ = cand;
+        return MVR_OK;
+    };
+    auto body = [&]() -> int {
+        const int bt = p_.batch_blocks > 0 ? std::min(p_.batch_blocks, kMaxBatch) : cap;
+        const bool env = sched_env_forced();
+        for (int st = 0; st < num_steps(); ++st) {
+            std::vector<View *> vs;
+            if (p_.mul)
+                for (auto &vw : views_) vs.push_back(&vw);
+            else vs.push_back(&views_[st]);
+            if (force_sched_ >= 0) {
+                for (View *vw : vs) D_TRY(eng(engine_.set_schedule(vw->plan, force_sched_)));
+                continue;
+            }
+            const std::vector<int> cands = engine_.schedule_candidates(vs[0]->plan);
+            if (env || cands.size() <= 1 || blocks_[st].empty()) continue;
+            float best = 1e30f;
+            int bestc = engine_.schedule(vs[0]->plan);
+            for (int c : cands) {
+                for (View *vw : vs) D_TRY(eng(engine_.set_schedule(vw->plan, c)));
+                float ms = 0.0f;
+                D_TRY(time_step(st, bt, ms));
+                tune_.push_back({st, c, bt, ms});
+                if (ms < best) {
+                    best = ms;
+                    bestc = c;
+                }
+            }
+            for (View *vw : vs) D_TRY(eng(engine_.set_schedule(vw->plan, bestc)));
         }
-    }
+        if (p_.batch_blocks > 0) {
+            batch_ = std::min(p_.batch_blocks, kMaxBatch);
+            return MVR_OK;
+        }
+        batch_ = 1;
+        if (cap <= 1 || !jacobi_[0]) return MVR_OK;
+        float best = 1e30f;
+        for (int cand = 1; cand <= cap; cand *= 2) {
+            float ms = 0.0f;
+            D_TRY(time_step(0, cand, ms));
+            tune_.push_back({-1, -1, cand, ms});
+            if (ms < best) {
+                best = ms;
+                batch_ = cand;
+            }
+        }
+        return MVR_OK;
+    };
+    const int rc = body();
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    return rc;
+}
+
+template <typename T>
+int Decon<T>::set_schedule(int code)
+{
+    if (code < -1 || code > (SCHED_PLANE_PERSIST | SCHED_ZPIPE) || (code >= 0 && (code & 3) == 3))
+        return fail(MVR_ERR_ARG, "unknown FFT schedule code");
+    force_sched_ = code;
+    prepared_ = false;
     return MVR_OK;
+}
+
+template <typename T>
+int Decon<T>::schedule(int view) const
+{
+    if (view < 0 || view >= p_.num_views) return -MVR_ERR_ARG;
+    return engine_.schedule(views_[view].plan);
+}
+
+template <typename T>
+int Decon<T>::tuning(int capacity, int *step, int *code, int *batch, float *ms) const
+{
+    const int n = (int)tune_.size();
+    for (int i = 0; i < n && i < capacity; ++i) {
+        if (step) step[i] = tune_[i].step;
+        if (code) code[i] = tune_[i].code;
+        if (batch) batch[i] = tune_[i].batch;
+        if (ms) ms[i] = tune_[i].ms;
+    }
+    return n;
 }
 
 template <typename T>
@@ -1481,6 +1578,22 @@ extern "C" int mvr_decon_set_view_device(mvr_decon *h, int view, const float *im
     if (!h) return MVR_ERR_ARG;
     int rc = h->impl->set_images(view, img, weight, true);
     return rc != MVR_OK ? rc : h->impl->set_psf(view, psf, psf_size);
+}
+
+extern "C" int mvr_decon_set_schedule(mvr_decon *h, int code)
+{
+    return h ? h->impl->set_schedule(code) : MVR_ERR_ARG;
+}
+
+extern "C" int mvr_decon_schedule(const mvr_decon *h, int view)
+{
+    return h ? h->impl->schedule(view) : -MVR_ERR_ARG;
+}
+
+extern "C" int mvr_decon_tuning(const mvr_decon *h, int capacity, int *step, int *code, int *batch, float *ms)
+{
+    if (!h || capacity < 0) return -MVR_ERR_ARG;
+    return h->impl->tuning(capacity, step, code, batch, ms);
 }
 
 extern "C" int mvr_decon_set_view_block_size(mvr_decon *h, int view, const int block_size[3])

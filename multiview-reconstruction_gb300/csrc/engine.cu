@@ -436,6 +436,45 @@ void Engine<T>::free_plan(Plan<T> &pl)
 }
 
 template <typename T>
+std::vector<int> Engine<T>::schedule_candidates(const Plan<T> &pl) const
+{
+    std::vector<int> paths = {SCHED_ROWS};
+    if (pl.xy_cap) {
+        paths.push_back(SCHED_PLANE);
+        paths.push_back(SCHED_PLANE_PERSIST);
+    }
+    std::vector<int> out;
+    for (int p : paths) {
+        out.push_back(p);
+        if (sizeof(T) == sizeof(float) && pl.tcz) out.push_back(p | SCHED_ZPIPE);
+    }
+    return out;
+}
+
+template <typename T>
+int Engine<T>::schedule(const Plan<T> &pl) const
+{
+    const int path = pl.xy ? (pl.persist ? SCHED_PLANE_PERSIST : SCHED_PLANE) : SCHED_ROWS;
+    const bool zp = pl.zpipe >= 0 ? pl.zpipe == 1 : (cols_pipe_enabled() && pl.tcz == 16);
+    return path | (zp && sizeof(T) == sizeof(float) && pl.tcz ? SCHED_ZPIPE : 0);
+}
+
+template <typename T>
+int Engine<T>::set_schedule(Plan<T> &pl, int code)
+{
+    const int path = code & 3;
+    if (path > SCHED_PLANE_PERSIST || code < 0 || code > (SCHED_PLANE_PERSIST | SCHED_ZPIPE))
+        return fail(ERR_ARG, "unknown FFT schedule");
+    if (path != SCHED_ROWS && !pl.xy_cap) return fail(ERR_UNSUPPORTED, "no plane kernels for this FFT domain");
+    if ((code & SCHED_ZPIPE) && !(sizeof(T) == sizeof(float) && pl.tcz))
+        return fail(ERR_UNSUPPORTED, "no tile column kernels for this Z length");
+    pl.xy = path == SCHED_ROWS ? 0 : pl.xy_cap;
+    pl.persist = path == SCHED_PLANE_PERSIST ? 1 : 0;
+    pl.zpipe = (code & SCHED_ZPIPE) ? 1 : 0;
+    return OK;
+}
+
+template <typename T>
 int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int kd1[3], const float *k2,
                          const int kd2[3], bool k_on_device)
 {
@@ -492,7 +531,10 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
         // plane kernels: FP32, z along the tile column kernels; MVR_PLANE_KERNELS=0 turns them off
         const char *env = std::getenv("MVR_PLANE_KERNELS");
         const bool allow = !(env && env[0] == '0');
-        pl.xy = (allow && sizeof(T) == sizeof(float) && pl.tcz) ? xy_combo(pl.P) : 0;
+        pl.xy_cap = (sizeof(T) == sizeof(float) && pl.tcz) ? xy_combo(pl.P) : 0;
+        pl.xy = allow ? pl.xy_cap : 0;
+        pl.persist = 1;
+        pl.zpipe = -1;
     }
     pl.wcy = pl.tcy ? 0 : warp_col_radix<T>(pl.P[1]);
     pl.wcz = pl.tcz ? 0 : warp_col_radix<T>(pl.P[2]);
@@ -537,7 +579,7 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
         if constexpr (sizeof(T) == sizeof(float)) {
             if (pl.xy) {
                 ++launches_;
-                MVR_CUDA(xy_fwd_kernel(pl.xy, src, S0_, bms, 1, pl.P[2], pl.Pc, pl.twx, pl.twy, stream_));
+                MVR_CUDA(xy_fwd_kernel(pl.xy, src, S0_, bms, 1, pl.P[2], pl.Pc, pl.twx, pl.twy, stream_, pl.persist != 0));
                 MVR_TRY(launch_cols(pl, 2, 0, S0_, which == 0 ? pl.k1h : pl.k2h, nullptr, 1));
                 continue;
             }
@@ -598,7 +640,9 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
             // other-axis indices (an extra x tile of the same grid)
             const int gather = (Hx > 1 && Hx % kTColNP == 1) ? 1 : 0;
             const int hmain = gather ? Hx - 1 : Hx;
-            if (cols_pipe_enabled() && tc == 16 && mode == 2) {
+            const bool pipe = pl.zpipe >= 0 ? (pl.zpipe == 1 && axis == 2 && mode == 2)
+                                            : (cols_pipe_enabled() && tc == 16 && mode == 2);
+            if (pipe) {
                 PipeGeom pg;
                 pg.hmain = (hmain + kTColNP - 1) / kTColNP;
                 pg.ny = ohi - olo;
@@ -794,7 +838,7 @@ int Engine<T>::launch_xy_fwd(const Plan<T> &pl, const BlockMaps &bms, int nb, co
     if constexpr (sizeof(T) == sizeof(float)) {
         const double nv = (double)pl.b[0] * pl.b[1] * pl.b[2];
         MVR_TRY(prof_begin(KK_XY_FWD, nb * (sizeof(T) * nv + sizeof(V) * (double)pl.Pc)));
-        MVR_CUDA(xy_fwd_mirror(pl.xy, src, S, bms, nb, pl.P[2], pl.Pc, pl.twx, pl.twy, stream_));
+        MVR_CUDA(xy_fwd_mirror(pl.xy, src, S, bms, nb, pl.P[2], pl.Pc, pl.twx, pl.twy, stream_, pl.persist != 0));
         return prof_end();
     }
     return fail(ERR_STATE, "plane kernels are FP32 only");
@@ -806,7 +850,7 @@ int Engine<T>::launch_xy_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, 
     if constexpr (sizeof(T) == sizeof(float)) {
         const double nv = (double)pl.b[0] * pl.b[1] * pl.b[2];
         MVR_TRY(prof_begin(KK_XY_RATIO, nb * (2.0 * sizeof(V) * (double)pl.Pc + 4.0 * nv)));
-        MVR_CUDA(xy_ratio(pl.xy, S, img, bms, nb, pl.P[2], pl.Pc, pl.twx, pl.twy, stream_));
+        MVR_CUDA(xy_ratio(pl.xy, S, img, bms, nb, pl.P[2], pl.Pc, pl.twx, pl.twy, stream_, pl.persist != 0));
         return prof_end();
     }
     return fail(ERR_STATE, "plane kernels are FP32 only");

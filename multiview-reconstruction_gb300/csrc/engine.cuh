@@ -61,7 +61,18 @@ struct Plan {
     int tcy = 0, tcz = 0;  // FP32 columns of 16 tc (tc = 4, 6, 8, 12, 16) take the two-phase tile kernels (preferred)
     int xy = 0;            // plane kernels (x and y fused per z-plane): shape code, 0 = row / column kernels
     size_t smem_row = 0, smem_coly = 0, smem_colz = 0;
+    // FFT schedule (chosen by the autotuner of the whole-volume driver, or forced):
+    int xy_cap = 0;        // the plane-kernel shape this domain allows (0: none)
+    int persist = 1;       // plane kernels: forward / quotient passes as one CTA per SM walking the planes
+                           // (1) or one CTA per plane (0)
+    int zpipe = -1;        // Z pass of the tile column kernels: persistent double-buffered (1), one tile per
+                           // CTA (0), or -1: the built-in choice (persistent for 256-long columns only)
 };
+
+// FFT schedule codes (Engine::schedule_candidates / set_schedule):
+//   path: 0 row / column kernels, 1 plane kernels one CTA per plane, 2 plane kernels persistent;
+//   + 4 when the Z pass of the convolutions uses the persistent double-buffered column kernel.
+enum { SCHED_ROWS = 0, SCHED_PLANE = 1, SCHED_PLANE_PERSIST = 2, SCHED_ZPIPE = 4 };
 
 // Where the block's output goes (volume driver) or the block itself (block API).
 struct BlockPlace {
@@ -90,6 +101,10 @@ public:
     int make_plan(Plan<T> &pl, const int b[3], const float *k1, const int kd1[3], const float *k2,
                   const int kd2[3], bool k_on_device = false);
     void free_plan(Plan<T> &pl);
+    // The FFT schedules a plan admits (codes SCHED_*), and the one in use.
+    std::vector<int> schedule_candidates(const Plan<T> &pl) const;
+    int schedule(const Plan<T> &pl) const;
+    int set_schedule(Plan<T> &pl, int code);
 
     // One sequential iteration (ComputeBlockSeqThread.runIteration) of view plan pl on
     // nb (1..16) blocks in one batched launch per pass; all blocks read the same psi

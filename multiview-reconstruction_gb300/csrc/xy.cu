@@ -93,11 +93,11 @@ void set_limits()
 
 template <class Src>
 cudaError_t fwd(int combo, const Src &src, float2 *S, const BlockMaps &bms, int nb, int Pz, long long Pc,
-                const float2 *twx, const float2 *twy, cudaStream_t s)
+                const float2 *twx, const float2 *twy, cudaStream_t s, bool persist)
 {
     set_limits();
     const int nitems = Pz * nb;
-    const dim3 grid((unsigned)std::min(nitems, persist_ctas()));
+    const dim3 grid((unsigned)(persist ? std::min(nitems, persist_ctas()) : nitems));
     XY_DISPATCH(combo, return launch_pdl(k_xy_fwd<VX_, VY_, Src>, grid, XYShape<VX_, VY_>::NT,
                                          xy_smem_bytes<VX_, VY_>(), s, src, S, bms, Pc, twx, twy, Pz, nitems));
     return cudaGetLastError();
@@ -106,29 +106,29 @@ cudaError_t fwd(int combo, const Src &src, float2 *S, const BlockMaps &bms, int 
 }  // namespace
 
 cudaError_t xy_fwd_mirror(int combo, const float *psi, float2 *S, const BlockMaps &bms, int nb, int Pz, long long Pc,
-                          const float2 *twx, const float2 *twy, cudaStream_t s)
+                          const float2 *twx, const float2 *twy, cudaStream_t s, bool persist)
 {
-    return fwd(combo, SrcMirror<float>{psi}, S, bms, nb, Pz, Pc, twx, twy, s);
+    return fwd(combo, SrcMirror<float>{psi}, S, bms, nb, Pz, Pc, twx, twy, s, persist);
 }
 
 cudaError_t xy_fwd_zero(int combo, const float *blk, float2 *S, const BlockMaps &bms, int nb, int Pz, long long Pc,
-                        const float2 *twx, const float2 *twy, cudaStream_t s)
+                        const float2 *twx, const float2 *twy, cudaStream_t s, bool persist)
 {
-    return fwd(combo, SrcZero<float>{blk}, S, bms, nb, Pz, Pc, twx, twy, s);
+    return fwd(combo, SrcZero<float>{blk}, S, bms, nb, Pz, Pc, twx, twy, s, persist);
 }
 
 cudaError_t xy_fwd_kernel(int combo, const SrcKernel &src, float2 *S, const BlockMaps &bms, int nb, int Pz,
-                          long long Pc, const float2 *twx, const float2 *twy, cudaStream_t s)
+                          long long Pc, const float2 *twx, const float2 *twy, cudaStream_t s, bool persist)
 {
-    return fwd(combo, src, S, bms, nb, Pz, Pc, twx, twy, s);
+    return fwd(combo, src, S, bms, nb, Pz, Pc, twx, twy, s, persist);
 }
 
 cudaError_t xy_ratio(int combo, float2 *S, const float *img, const BlockMaps &bms, int nb, int Pz, long long Pc,
-                     const float2 *twx, const float2 *twy, cudaStream_t s)
+                     const float2 *twx, const float2 *twy, cudaStream_t s, bool persist)
 {
     set_limits();
     const int nitems = Pz * nb;
-    const dim3 grid((unsigned)std::min(nitems, persist_ctas()));
+    const dim3 grid((unsigned)(persist ? std::min(nitems, persist_ctas()) : nitems));
     XY_DISPATCH(combo, return launch_pdl(k_xy_ratio<VX_, VY_>, grid, XYShape<VX_, VY_>::NT, xy_smem_bytes<VX_, VY_>(),
                                          s, S, img, bms, Pc, twx, twy, Pz, nitems));
     return cudaGetLastError();

@@ -11,15 +11,17 @@ namespace mvr {
 int xy_combo(const int P[3]);
 size_t xy_smem(int combo);
 
-// One CTA per z-plane (grid Pz x nb); every call returns the launch status.
+// The forward and quotient passes walk the (block, plane) items with one CTA per SM
+// (persist, unless MVR_XY_PERSIST=0) or take one CTA per plane; the update pass takes one
+// CTA per plane (grid Pz x nb).  Every call returns the launch status.
 cudaError_t xy_fwd_mirror(int combo, const float *psi, float2 *S, const BlockMaps &bms, int nb, int Pz, long long Pc,
-                          const float2 *twx, const float2 *twy, cudaStream_t s);
+                          const float2 *twx, const float2 *twy, cudaStream_t s, bool persist = true);
 cudaError_t xy_fwd_zero(int combo, const float *blk, float2 *S, const BlockMaps &bms, int nb, int Pz, long long Pc,
-                        const float2 *twx, const float2 *twy, cudaStream_t s);
+                        const float2 *twx, const float2 *twy, cudaStream_t s, bool persist = true);
 cudaError_t xy_fwd_kernel(int combo, const SrcKernel &src, float2 *S, const BlockMaps &bms, int nb, int Pz,
-                          long long Pc, const float2 *twx, const float2 *twy, cudaStream_t s);
+                          long long Pc, const float2 *twx, const float2 *twy, cudaStream_t s, bool persist = true);
 cudaError_t xy_ratio(int combo, float2 *S, const float *img, const BlockMaps &bms, int nb, int Pz, long long Pc,
-                     const float2 *twx, const float2 *twy, cudaStream_t s);
+                     const float2 *twx, const float2 *twy, cudaStream_t s, bool persist = true);
 cudaError_t xy_update(int combo, int epi, float2 *S, const UpdateArgs &ua, const BlockMaps &bms, int nb, int Pz,
                       long long Pc, const float2 *twx, const float2 *twy, cudaStream_t s);
 

@@ -45,7 +45,8 @@ EXPORTS = [
     "mvr_decon_get_max", "mvr_decon_get_weights", "mvr_decon_psi_device", "mvr_decon_synchronize",
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
     "mvr_kernel_name", "mvr_convolve_static", "mvr_decon_batch", "mvr_decon_likelihood",
-    "mvr_decon_set_graphs", "mvr_decon_graphs_captured", "mvr_decon_init_psi", "mvr_fuse_group",
+    "mvr_decon_set_graphs", "mvr_decon_graphs_captured", "mvr_decon_set_schedule", "mvr_decon_schedule",
+    "mvr_decon_tuning", "mvr_decon_init_psi", "mvr_fuse_group",
     "mvr_fuse_last_error", "mvr_psf_extract", "mvr_psf_transformed_dims", "mvr_psf_transform_normalized",
     "mvr_psf_average", "mvr_psf_make_same_size", "mvr_psf_projection", "mvr_psf_remove_min_projections",
     "mvr_psf_last_error", "mvr_block_grid",
@@ -56,6 +57,17 @@ EXPORTS = [
     "getMemDeviceCUDA", "getFreeMemDeviceCUDA", "getCUDAcomputeCapabilityMajorVersion",
     "getCUDAcomputeCapabilityMinorVersion", "mvr_free",
 ]
+
+
+SCHED_ROWS, SCHED_PLANE, SCHED_PLANE_PERSIST, SCHED_ZPIPE = 0, 1, 2, 4
+
+
+def schedule_name(code: int) -> str:
+    if code < 0:
+        return "batch trial"
+    path = {SCHED_ROWS: "row/column kernels", SCHED_PLANE: "plane kernels, one CTA per plane",
+            SCHED_PLANE_PERSIST: "plane kernels, persistent"}.get(code & 3, "?")
+    return path + (" + persistent Z pass" if code & SCHED_ZPIPE else "")
 
 
 class MvrError(RuntimeError):
@@ -124,6 +136,9 @@ def load() -> C.CDLL:
     L.mvr_decon_set_view_device.argtypes = [P, C.c_int, P, P, P, P]
     L.mvr_decon_update_images.argtypes = [P, C.c_int, P, P]
     L.mvr_decon_set_view_block_size.argtypes = [P, C.c_int, P]
+    L.mvr_decon_set_schedule.argtypes = [P, C.c_int]
+    L.mvr_decon_schedule.argtypes = [P, C.c_int]
+    L.mvr_decon_tuning.argtypes = [P, C.c_int, P, P, P, P]
     L.mvr_decon_prepare.argtypes = [P]
     L.mvr_decon_set_psi.argtypes = [P, P]
     L.mvr_decon_set_psi_device.argtypes = [P, P]
@@ -339,6 +354,26 @@ class Deconvolution:
         k = _f32(psf)
         self._check(self._lib.mvr_decon_set_view_device(self._h, view, C.c_void_p(img_ptr), C.c_void_p(weight_ptr),
                                                         _p(k), _size_xyz(k)))
+
+    def set_schedule(self, code: int):
+        """Forces an FFT schedule (SCHED_* code) for every view, -1 = autotuned; before prepare()."""
+        self._check(self._lib.mvr_decon_set_schedule(self._h, int(code)))
+
+    def schedule(self, view: int = 0) -> int:
+        c = self._lib.mvr_decon_schedule(self._h, view)
+        if c < 0:
+            raise MvrError(-c, "schedule: view out of range")
+        return c
+
+    def tuning(self):
+        """The autotuner's trials: dicts {step, code, schedule, batch, ms} (step and code -1
+        for a blocks-per-launch trial)."""
+        n = self._lib.mvr_decon_tuning(self._h, 0, None, None, None, None)
+        st, cd, bt = (np.zeros(max(n, 1), np.int32) for _ in range(3))
+        ms = np.zeros(max(n, 1), np.float32)
+        self._lib.mvr_decon_tuning(self._h, n, _p(st), _p(cd), _p(bt), _p(ms))
+        return [{"step": int(st[i]), "code": int(cd[i]), "schedule": schedule_name(int(cd[i])),
+                 "batch": int(bt[i]), "ms": float(ms[i])} for i in range(n)]
 
     def set_view_block_size(self, view, block_size):
         """Compute block size (x, y, z) of one view (None: the handle's), before prepare()."""
