@@ -657,6 +657,7 @@ def run_e2e_block(args, ws, dev, ds, dec, dec_max, workers=2, iters=2):
         pool = cf.ThreadPoolExecutor(max_workers=workers)
         calls = 0
         call_s = []
+        per_call = []
         for it in range(1 + iters):
             t_it = 0.0
             for v in range(W.views):
@@ -666,7 +667,9 @@ def run_e2e_block(args, ws, dev, ds, dec, dec_max, workers=2, iters=2):
                 def run(j, v=v, pb=pb):
                     w = wk[j % workers]
                     im, wt = inputs[v][j]
+                    c0 = time.perf_counter()
                     w.run_iteration(v, pb[j], im, wt, float(dec_max[v]))
+                    per_call.append(time.perf_counter() - c0)
 
                 t0 = time.perf_counter()
                 # worker j % workers takes block j: each worker's calls stay in order
@@ -678,6 +681,8 @@ def run_e2e_block(args, ws, dev, ds, dec, dec_max, workers=2, iters=2):
                     calls += len(pb)
             if it:
                 call_s.append(t_it)
+            else:
+                per_call.clear()
         pool.shutdown()
     finally:
         for w in wk:
@@ -686,7 +691,8 @@ def run_e2e_block(args, ws, dev, ds, dec, dec_max, workers=2, iters=2):
     nb = 4 * W.block[0] * W.block[1] * W.block[2]
     return {"value": ws * W.nvox / t, "unit": UNIT, "h2d_bytes_per_step": 3 * nb * calls // iters,
             "d2h_bytes_per_step": nb * calls // iters, "calls_per_step": calls // iters, "steps": iters,
-            "workers": workers, "boundary": "circular (the pasted effective regions are the reference boundary's; "
+            "workers": workers, "ms_per_call": 1e3 * float(np.mean(per_call)) if per_call else None,
+            "boundary": "circular (the pasted effective regions are the reference boundary's; "
                                             "the per-block statistics differ)",
             "note": "timed: the mvr_block_run_seq calls of each view-step with pageable host buffers; the driver's "
                     "block copies out of / into the volumes run untimed between view-steps"}

@@ -468,9 +468,13 @@ int Engine<T>::set_schedule(Plan<T> &pl, int code)
     if (path != SCHED_ROWS && !pl.xy_cap) return fail(ERR_UNSUPPORTED, "no plane kernels for this FFT domain");
     if ((code & SCHED_ZPIPE) && !(sizeof(T) == sizeof(float) && pl.tcz))
         return fail(ERR_UNSUPPORTED, "no tile column kernels for this Z length");
-    pl.xy = path == SCHED_ROWS ? 0 : pl.xy_cap;
+    const int xy = path == SCHED_ROWS ? 0 : pl.xy_cap;
+    if ((xy != 0) != (pl.kspec_xy != 0) && !pl.ksrc1)
+        return fail(ERR_STATE, "the plan's kernels are not on the device: its path cannot change");
+    pl.xy = xy;
     pl.persist = path == SCHED_PLANE_PERSIST ? 1 : 0;
     pl.zpipe = (code & SCHED_ZPIPE) ? 1 : 0;
+    if ((pl.xy != 0) != (pl.kspec_xy != 0)) return kernel_spectra(pl, pl.ksrc1, pl.ksrc2, true);  // other layout
     return OK;
 }
 
@@ -551,6 +555,19 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
     // kernel spectra, scaled by 1 / (Px Py Pz) so that the inverse needs no scaling
     MVR_CUDA(cudaMalloc(&pl.k1h, sizeof(V) * (size_t)pl.Pc));
     if (k2) MVR_CUDA(cudaMalloc(&pl.k2h, sizeof(V) * (size_t)pl.Pc));
+    pl.ksrc1 = k_on_device ? k1 : nullptr;
+    pl.ksrc2 = k_on_device ? k2 : nullptr;
+    return kernel_spectra(pl, k1, k2, k_on_device);
+}
+
+// The kernel spectra K1^, K2^ of a plan, computed by the forward kernels of the plan's path
+// (the plane kernels leave x and y in tile order, the row / column kernels in natural order;
+// every product is taken position by position, so K^ must come from the same path).
+template <typename T>
+int Engine<T>::kernel_spectra(Plan<T> &pl, const float *k1, const float *k2, bool k_on_device)
+{
+    const int *kd1 = pl.kd;
+    const long long nrows = (long long)pl.P[1] * pl.P[2];
     const long long kn = (long long)kd1[0] * kd1[1] * kd1[2];
     if (!k_on_device && kn > kcap_) {
         cudaFree(kbuf_);
@@ -568,6 +585,7 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
     }
     bm.fast_x = block_fast_x(bm);
     const double scale = 1.0 / ((double)pl.P[0] * pl.P[1] * pl.P[2]);
+    pl.kspec_xy = pl.xy;
     for (int which = 0; which < (k2 ? 2 : 1); ++which) {
         const float *kh = which == 0 ? k1 : k2;
         const float *kdev = kh;

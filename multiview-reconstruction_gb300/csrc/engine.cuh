@@ -67,6 +67,8 @@ struct Plan {
                            // (1) or one CTA per plane (0)
     int zpipe = -1;        // Z pass of the tile column kernels: persistent double-buffered (1), one tile per
                            // CTA (0), or -1: the built-in choice (persistent for 256-long columns only)
+    int kspec_xy = 0;      // the path (plane shape or 0) K1^ / K2^ were computed with
+    const float *ksrc1 = nullptr, *ksrc2 = nullptr;  // device kernels (whole-volume driver), for recomputing K^
 };
 
 // FFT schedule codes (Engine::schedule_candidates / set_schedule):
@@ -102,6 +104,7 @@ public:
                   const int kd2[3], bool k_on_device = false);
     void free_plan(Plan<T> &pl);
     // The FFT schedules a plan admits (codes SCHED_*), and the one in use.
+    int kernel_spectra(Plan<T> &pl, const float *k1, const float *k2, bool k_on_device);
     std::vector<int> schedule_candidates(const Plan<T> &pl) const;
     int schedule(const Plan<T> &pl) const;
     int set_schedule(Plan<T> &pl, int code);
