@@ -586,8 +586,8 @@ def run_gb300(args, ws, rank, local):
 
 
 def run_e2e(args, ws, dev, ds, dec, shape, boundary):
-    """The public C ABI with pinned host buffers: every step uploads the 4 images, the 4
-    raw weights and psi, runs one iteration and reads psi back."""
+    """The public C ABI with pinned host buffers: every step uploads the images, the raw
+    weights and psi, runs one iteration and reads psi back (mvr_decon_run_host)."""
     import torch
 
     import mvrgb300 as M
@@ -605,20 +605,16 @@ def run_e2e(args, ws, dev, ds, dec, shape, boundary):
     e2e_dec.prepare()
     out = h_psi.numpy()
     e2e_steps = max(1, min(args.steps, 10))
+    imgs = [a.numpy() for a in h_img]
+    wts = [a.numpy() for a in h_w]
     for _ in range(min(2, args.warmup)):
-        for v in range(W.views):
-            e2e_dec.update_images(v, h_img[v].numpy(), h_w[v].numpy())
-        e2e_dec.set_psi(out)
-        e2e_dec.run_iterations(1)
-        e2e_dec.get_psi(out)
+        e2e_dec.run_host(1, imgs, wts, out)
     barrier(ws)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        for v in range(W.views):
-            e2e_dec.update_images(v, h_img[v].numpy(), h_w[v].numpy())
-        e2e_dec.set_psi(out)
-        e2e_dec.run_iterations(1)
-        e2e_dec.get_psi(out)
+        # mvr_decon_run_host: uploads (weights and psi, then the images overlapping the first
+        # view-steps), one iteration, psi back
+        e2e_dec.run_host(1, imgs, wts, out)
     e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
     e2e_value = ws * W.nvox * e2e_steps / e2e_s
     h2d = W.views * 2 * W.nvox * 4 + W.nvox * 4

@@ -195,6 +195,15 @@ MVR_API int mvr_block_grid(const long long dims[3], const int kernel_size[3], co
  * the block voxels outside the regions written back to psi (which the reference computes
  * and discards) are not computed; psi is bit-identical either way. */
 MVR_API int mvr_decon_run(mvr_decon *h, int iterations, double *stats);
+/* runIterations with the inputs on the host (no reference counterpart as one call: the
+ * reference driver holds images, weights and psi in host memory and copies blocks per call):
+ * uploads every view's image and raw weight and psi (host arrays of the volume's size, views
+ * set with mvr_decon_set_view), normalises the weights, runs `iterations` iterations and
+ * writes psi back.  The uploads run on a copy stream, weights and psi first, then the images
+ * in view order, and view-step v of the first iteration waits only for image v, so the image
+ * uploads overlap the computation; page-locked host buffers keep the copies asynchronous. */
+MVR_API int mvr_decon_run_host(mvr_decon *h, int iterations, const float *const *imgs, const float *const *weights,
+                               float *psi);
 /* Prepared kernel1 / kernel2 of a view (DeconViewPSF.getKernel1/getKernel2). */
 MVR_API int mvr_decon_get_kernels(mvr_decon *h, int view, float *kernel1, float *kernel2);
 /* Maximum intensity per view (PsiInit.getMax). */
@@ -232,7 +241,9 @@ MVR_API int mvr_decon_graphs_captured(const mvr_decon *h);
  * it); the batched, autotuned form of the iteration loop (no reference counterpart: the
  * reference's FFT has one fixed schedule).  Codes: MVR_SCHED_ROWS (row and column kernels),
  * MVR_SCHED_PLANE (x and y fused per z-plane, one CTA per plane), MVR_SCHED_PLANE_PERSIST
- * (the same with one CTA per SM walking the planes), plus MVR_SCHED_ZPIPE when the Z pass
+ * (the same with one CTA per SM walking the planes), MVR_SCHED_PAIR (a cluster of two CTAs per
+ * plane, each holding half of its rows, exchanging the radix-2 stage of the y transform through
+ * distributed shared memory: planes of 192 x 192 and 256 x 256), plus MVR_SCHED_ZPIPE when the Z pass
  * runs the persistent double-buffered column kernel.  Every schedule computes the same
  * iteration (results agree to float rounding).
  * mvr_decon_set_schedule (before prepare): force `code` for every view, -1 = autotune.
@@ -243,6 +254,7 @@ MVR_API int mvr_decon_graphs_captured(const mvr_decon *h);
 #define MVR_SCHED_ROWS 0
 #define MVR_SCHED_PLANE 1
 #define MVR_SCHED_PLANE_PERSIST 2
+#define MVR_SCHED_PAIR 3
 #define MVR_SCHED_ZPIPE 4
 MVR_API int mvr_decon_set_schedule(mvr_decon *h, int code);
 MVR_API int mvr_decon_schedule(const mvr_decon *h, int view);

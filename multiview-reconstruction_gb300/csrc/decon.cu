@@ -413,6 +413,7 @@ public:
     virtual int get_psi(float *psi) = 0;
     virtual int get_psi_device(float *psi) = 0;
     virtual int run(int iterations, double *stats) = 0;
+    virtual int run_host(int iterations, const float *const *imgs, const float *const *ws, float *psi) = 0;
     virtual int get_kernels(int v, float *k1, float *k2) = 0;
     virtual int get_max(float *mx) = 0;
     virtual int get_weights(int v, float *w) = 0;
@@ -448,6 +449,7 @@ public:
     int get_psi(float *psi) override;
     int get_psi_device(float *psi) override;
     int run(int iterations, double *stats) override;
+    int run_host(int iterations, const float *const *imgs, const float *const *ws, float *psi) override;
     int get_kernels(int v, float *k1, float *k2) override;
     int get_max(float *mx) override;
     int get_weights(int v, float *w) override;
@@ -562,6 +564,9 @@ private:
     int *d_perm_ = nullptr;
     double *d_stats_ = nullptr;
     long long stats_cap_ = 0;
+    cudaStream_t copy_ = nullptr;              // uploads of mvr_decon_run_host
+    cudaEvent_t ev_w_ = nullptr;               // weights and psi uploaded
+    std::vector<cudaEvent_t> ev_img_;          // image of view v uploaded
     bool prepared_ = false;
     std::string err_;
 };
@@ -590,6 +595,9 @@ Decon<T>::~Decon()
     cudaFree(d_scratch_);
     cudaFree(d_perm_);
     cudaFree(d_stats_);
+    for (cudaEvent_t e : ev_img_) cudaEventDestroy(e);
+    if (ev_w_) cudaEventDestroy(ev_w_);
+    if (copy_) cudaStreamDestroy(copy_);
     drop_graphs();
 }
 
@@ -1389,7 +1397,7 @@ int Decon<T>::autotune()
 template <typename T>
 int Decon<T>::set_schedule(int code)
 {
-    if (code < -1 || code > (SCHED_PLANE_PERSIST | SCHED_ZPIPE) || (code >= 0 && (code & 3) == 3))
+    if (code < -1 || code > (SCHED_PAIR | SCHED_ZPIPE))
         return fail(MVR_ERR_ARG, "unknown FFT schedule code");
     force_sched_ = code;
     prepared_ = false;
@@ -1414,6 +1422,69 @@ int Decon<T>::tuning(int capacity, int *step, int *code, int *batch, float *ms) 
         if (ms) ms[i] = tune_[i].ms;
     }
     return n;
+}
+
+// runIterations with host-resident inputs (MultiViewDeconvolution.runIterations on images,
+// raw weights and psi held by the caller): the uploads go out on a copy stream in the order
+// weights, psi, image 0, 1, ...; the weight normalisation waits for the weights and psi, and
+// view-step v of the first iteration for image v, so the image uploads overlap the first
+// view-steps.  psi comes back at the end.  With page-locked host buffers the copies run
+// asynchronously to the host; pageable buffers work but may serialise them.
+template <typename T>
+int Decon<T>::run_host(int iterations, const float *const *imgs, const float *const *ws, float *psi)
+{
+    if (!prepared_) return fail(MVR_ERR_STATE, "mvr_decon_prepare was not called");
+    if (!imgs || !ws || !psi || iterations < 1) return fail(MVR_ERR_ARG, "inputs must not be NULL, iterations >= 1");
+    const int nv = p_.num_views;
+    for (int v = 0; v < nv; ++v) {
+        if (!imgs[v] || !ws[v]) return fail(MVR_ERR_ARG, "image and weight pointers must not be NULL");
+        if (!views_[v].own_img || !views_[v].own_w)
+            return fail(MVR_ERR_STATE, "mvr_decon_run_host needs views set with mvr_decon_set_view (host arrays)");
+    }
+    D_CUDA(cudaSetDevice(p_.device));
+    cudaStream_t s = engine_.stream();
+    if (!copy_) D_CUDA(cudaStreamCreateWithFlags(&copy_, cudaStreamNonBlocking));
+    if (!ev_w_) D_CUDA(cudaEventCreateWithFlags(&ev_w_, cudaEventDisableTiming));
+    while ((int)ev_img_.size() < nv) {
+        cudaEvent_t e = nullptr;
+        D_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        ev_img_.push_back(e);
+    }
+    const size_t bytes = sizeof(float) * (size_t)n_;
+    // the copy stream starts after the work already queued on the compute stream (earlier
+    // iterations still read the buffers it overwrites)
+    D_CUDA(cudaEventRecord(ev_w_, s));
+    D_CUDA(cudaStreamWaitEvent(copy_, ev_w_, 0));
+    for (int v = 0; v < nv; ++v) D_CUDA(cudaMemcpyAsync(views_[v].w_raw, ws[v], bytes, cudaMemcpyHostToDevice, copy_));
+    float *psi_up = sizeof(T) == sizeof(float) ? reinterpret_cast<float *>(psi_) : reinterpret_cast<float *>(stage_);
+    D_CUDA(cudaMemcpyAsync(psi_up, psi, bytes, cudaMemcpyHostToDevice, copy_));
+    D_CUDA(cudaEventRecord(ev_w_, copy_));
+    for (int v = 0; v < nv; ++v) {
+        D_CUDA(cudaMemcpyAsync(views_[v].img, imgs[v], bytes, cudaMemcpyHostToDevice, copy_));
+        D_CUDA(cudaEventRecord(ev_img_[v], copy_));
+    }
+    D_CUDA(cudaStreamWaitEvent(s, ev_w_, 0));
+    if (sizeof(T) != sizeof(float)) {
+        // FP64 run: the uploaded float psi (in the staging volume) converted into psi
+        float *hold = nullptr;
+        D_CUDA(cudaMalloc(&hold, bytes));
+        D_CUDA(cudaMemcpyAsync(hold, psi_up, bytes, cudaMemcpyDeviceToDevice, s));
+        k_convert<float, T><<<grid_for(n_), 256, 0, s>>>(hold, psi_, n_);
+        D_CUDA(cudaGetLastError());
+        D_CUDA(cudaStreamSynchronize(s));
+        cudaFree(hold);
+    }
+    if (p_.weight_norm != MVR_WEIGHTS_AS_GIVEN) D_TRY(normalize_weights());
+    // the first iteration eagerly, each view-step after its image
+    const int steps = num_steps();
+    for (int st = 0; st < steps; ++st) {
+        if (p_.mul)
+            for (int v = 0; v < nv; ++v) D_CUDA(cudaStreamWaitEvent(s, ev_img_[v], 0));
+        else D_CUDA(cudaStreamWaitEvent(s, ev_img_[st], 0));
+        D_TRY(run_step(st, nullptr, false, batch_));
+    }
+    for (int it = 1; it < iterations; ++it) D_TRY(run_iteration(nullptr, 0));
+    return get_psi(psi);
 }
 
 template <typename T>
@@ -1578,6 +1649,12 @@ extern "C" int mvr_decon_set_view_device(mvr_decon *h, int view, const float *im
     if (!h) return MVR_ERR_ARG;
     int rc = h->impl->set_images(view, img, weight, true);
     return rc != MVR_OK ? rc : h->impl->set_psf(view, psf, psf_size);
+}
+
+extern "C" int mvr_decon_run_host(mvr_decon *h, int iterations, const float *const *imgs, const float *const *weights,
+                                  float *psi)
+{
+    return h ? h->impl->run_host(iterations, imgs, weights, psi) : MVR_ERR_ARG;
 }
 
 extern "C" int mvr_decon_set_schedule(mvr_decon *h, int code)

@@ -443,6 +443,7 @@ std::vector<int> Engine<T>::schedule_candidates(const Plan<T> &pl) const
         paths.push_back(SCHED_PLANE);
         paths.push_back(SCHED_PLANE_PERSIST);
     }
+    if (pl.pair_cap) paths.push_back(SCHED_PAIR);
     std::vector<int> out;
     for (int p : paths) {
         out.push_back(p);
@@ -454,7 +455,7 @@ std::vector<int> Engine<T>::schedule_candidates(const Plan<T> &pl) const
 template <typename T>
 int Engine<T>::schedule(const Plan<T> &pl) const
 {
-    const int path = pl.xy ? (pl.persist ? SCHED_PLANE_PERSIST : SCHED_PLANE) : SCHED_ROWS;
+    const int path = pl.xy >= 10000 ? SCHED_PAIR : (pl.xy ? (pl.persist ? SCHED_PLANE_PERSIST : SCHED_PLANE) : SCHED_ROWS);
     const bool zp = pl.zpipe >= 0 ? pl.zpipe == 1 : (cols_pipe_enabled() && pl.tcz == 16);
     return path | (zp && sizeof(T) == sizeof(float) && pl.tcz ? SCHED_ZPIPE : 0);
 }
@@ -463,18 +464,19 @@ template <typename T>
 int Engine<T>::set_schedule(Plan<T> &pl, int code)
 {
     const int path = code & 3;
-    if (path > SCHED_PLANE_PERSIST || code < 0 || code > (SCHED_PLANE_PERSIST | SCHED_ZPIPE))
-        return fail(ERR_ARG, "unknown FFT schedule");
-    if (path != SCHED_ROWS && !pl.xy_cap) return fail(ERR_UNSUPPORTED, "no plane kernels for this FFT domain");
+    if (code < 0 || code > (SCHED_PAIR | SCHED_ZPIPE)) return fail(ERR_ARG, "unknown FFT schedule");
+    if ((path == SCHED_PLANE || path == SCHED_PLANE_PERSIST) && !pl.xy_cap)
+        return fail(ERR_UNSUPPORTED, "no plane kernels for this FFT domain");
+    if (path == SCHED_PAIR && !pl.pair_cap) return fail(ERR_UNSUPPORTED, "no pair kernels for this FFT domain");
     if ((code & SCHED_ZPIPE) && !(sizeof(T) == sizeof(float) && pl.tcz))
         return fail(ERR_UNSUPPORTED, "no tile column kernels for this Z length");
-    const int xy = path == SCHED_ROWS ? 0 : pl.xy_cap;
-    if ((xy != 0) != (pl.kspec_xy != 0) && !pl.ksrc1)
+    const int xy = path == SCHED_ROWS ? 0 : (path == SCHED_PAIR ? pl.pair_cap : pl.xy_cap);
+    if (xy != pl.kspec_xy && !pl.ksrc1)
         return fail(ERR_STATE, "the plan's kernels are not on the device: its path cannot change");
     pl.xy = xy;
-    pl.persist = path == SCHED_PLANE_PERSIST ? 1 : 0;
+    pl.persist = path == SCHED_PLANE_PERSIST || path == SCHED_PAIR ? 1 : 0;
     pl.zpipe = (code & SCHED_ZPIPE) ? 1 : 0;
-    if ((pl.xy != 0) != (pl.kspec_xy != 0)) return kernel_spectra(pl, pl.ksrc1, pl.ksrc2, true);  // other layout
+    if (pl.xy != pl.kspec_xy) return kernel_spectra(pl, pl.ksrc1, pl.ksrc2, true);  // another spectrum layout
     return OK;
 }
 
@@ -536,7 +538,11 @@ int Engine<T>::make_plan(Plan<T> &pl, const int b[3], const float *k1, const int
         const char *env = std::getenv("MVR_PLANE_KERNELS");
         const bool allow = !(env && env[0] == '0');
         pl.xy_cap = (sizeof(T) == sizeof(float) && pl.tcz) ? xy_combo(pl.P) : 0;
+        pl.pair_cap = (sizeof(T) == sizeof(float) && pl.tcz) ? xy_pair_combo(pl.P) : 0;
         pl.xy = allow ? pl.xy_cap : 0;
+        // the pair kernels for the domains without single-CTA plane kernels (MVR_PAIR_KERNELS=1)
+        const char *pe = std::getenv("MVR_PAIR_KERNELS");
+        if (allow && !pl.xy && pl.pair_cap && pe && pe[0] == '1') pl.xy = pl.pair_cap;
         pl.persist = 1;
         pl.zpipe = -1;
     }
@@ -884,7 +890,7 @@ int Engine<T>::launch_xy_update(const Plan<T> &pl, const BlockMaps &bms, int nb,
         MVR_TRY(prof_end());
         if (stats_dev && (epi == EPI_SEQ || epi == EPI_MUL_FINAL || epi == EPI_NLL)) {
             MVR_TRY(prof_begin(KK_REDUCE, 16.0 * pl.P[2] * nb));
-            k_reduce_stats<double><<<nb, 1024, 0, stream_>>>(partials_, pl.P[2], stats_dev);
+            k_reduce_stats<double><<<nb, 1024, 0, stream_>>>(partials_, xy_partial_slots(pl.xy, pl.P[2]), stats_dev);
             MVR_LAUNCHED("k_reduce_stats");
             MVR_TRY(prof_end());
         }

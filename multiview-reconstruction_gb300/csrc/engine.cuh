@@ -63,6 +63,7 @@ struct Plan {
     size_t smem_row = 0, smem_coly = 0, smem_colz = 0;
     // FFT schedule (chosen by the autotuner of the whole-volume driver, or forced):
     int xy_cap = 0;        // the plane-kernel shape this domain allows (0: none)
+    int pair_cap = 0;      // the pair-kernel shape (two CTAs per plane) this domain allows (0: none)
     int persist = 1;       // plane kernels: forward / quotient passes as one CTA per SM walking the planes
                            // (1) or one CTA per plane (0)
     int zpipe = -1;        // Z pass of the tile column kernels: persistent double-buffered (1), one tile per
@@ -74,7 +75,8 @@ struct Plan {
 // FFT schedule codes (Engine::schedule_candidates / set_schedule):
 //   path: 0 row / column kernels, 1 plane kernels one CTA per plane, 2 plane kernels persistent;
 //   + 4 when the Z pass of the convolutions uses the persistent double-buffered column kernel.
-enum { SCHED_ROWS = 0, SCHED_PLANE = 1, SCHED_PLANE_PERSIST = 2, SCHED_ZPIPE = 4 };
+//   path 3: the pair kernels (a cluster of two CTAs per plane, persistent).
+enum { SCHED_ROWS = 0, SCHED_PLANE = 1, SCHED_PLANE_PERSIST = 2, SCHED_PAIR = 3, SCHED_ZPIPE = 4 };
 
 // Where the block's output goes (volume driver) or the block itself (block API).
 struct BlockPlace {

@@ -9,6 +9,11 @@ namespace mvr {
 
 // The plane-kernel shape for an FP32 FFT domain P (x, y), or 0 when none exists.
 int xy_combo(const int P[3]);
+// The pair-kernel shape (two CTAs per plane, a thread-block cluster) for P, or 0.  Shape codes
+// >= 10000 select the pair kernels in every launcher below.
+int xy_pair_combo(const int P[3]);
+// Statistics partials per block written by an update launch over `planes` planes.
+int xy_partial_slots(int combo, int planes);
 size_t xy_smem(int combo);
 
 // The forward and quotient passes walk the (block, plane) items with one CTA per SM

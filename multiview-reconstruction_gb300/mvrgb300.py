@@ -46,7 +46,7 @@ EXPORTS = [
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
     "mvr_kernel_name", "mvr_convolve_static", "mvr_decon_batch", "mvr_decon_likelihood",
     "mvr_decon_set_graphs", "mvr_decon_graphs_captured", "mvr_decon_set_schedule", "mvr_decon_schedule",
-    "mvr_decon_tuning", "mvr_decon_init_psi", "mvr_fuse_group",
+    "mvr_decon_tuning", "mvr_decon_run_host", "mvr_decon_init_psi", "mvr_fuse_group",
     "mvr_fuse_last_error", "mvr_psf_extract", "mvr_psf_transformed_dims", "mvr_psf_transform_normalized",
     "mvr_psf_average", "mvr_psf_make_same_size", "mvr_psf_projection", "mvr_psf_remove_min_projections",
     "mvr_psf_last_error", "mvr_block_grid",
@@ -59,14 +59,15 @@ EXPORTS = [
 ]
 
 
-SCHED_ROWS, SCHED_PLANE, SCHED_PLANE_PERSIST, SCHED_ZPIPE = 0, 1, 2, 4
+SCHED_ROWS, SCHED_PLANE, SCHED_PLANE_PERSIST, SCHED_PAIR, SCHED_ZPIPE = 0, 1, 2, 3, 4
 
 
 def schedule_name(code: int) -> str:
     if code < 0:
         return "batch trial"
     path = {SCHED_ROWS: "row/column kernels", SCHED_PLANE: "plane kernels, one CTA per plane",
-            SCHED_PLANE_PERSIST: "plane kernels, persistent"}.get(code & 3, "?")
+            SCHED_PLANE_PERSIST: "plane kernels, persistent",
+            SCHED_PAIR: "pair plane kernels (two CTAs per plane), persistent"}[code & 3]
     return path + (" + persistent Z pass" if code & SCHED_ZPIPE else "")
 
 
@@ -139,6 +140,7 @@ def load() -> C.CDLL:
     L.mvr_decon_set_schedule.argtypes = [P, C.c_int]
     L.mvr_decon_schedule.argtypes = [P, C.c_int]
     L.mvr_decon_tuning.argtypes = [P, C.c_int, P, P, P, P]
+    L.mvr_decon_run_host.argtypes = [P, C.c_int, P, P, P]
     L.mvr_decon_prepare.argtypes = [P]
     L.mvr_decon_set_psi.argtypes = [P, P]
     L.mvr_decon_set_psi_device.argtypes = [P, P]
@@ -403,6 +405,19 @@ class Deconvolution:
     def get_psi_device(self, ptr: int):
         """Copies psi (float) into the device buffer at ptr."""
         self._check(self._lib.mvr_decon_get_psi_device(self._h, C.c_void_p(ptr)))
+
+    def run_host(self, n: int, imgs, weights, psi):
+        """mvr_decon_run_host: uploads the host images, raw weights and psi (float32 [z][y][x],
+        C-contiguous), runs n iterations and writes psi back in place."""
+        arrs = [_f32(a) for a in list(imgs) + list(weights)]
+        if any(a.shape != self.shape for a in arrs) or psi.dtype != np.float32 or psi.shape != self.shape \
+                or not psi.flags.c_contiguous:
+            raise ValueError("volumes must be C-contiguous float32 of the volume shape")
+        nv = self.num_views
+        ip = (C.c_void_p * nv)(*[a.ctypes.data for a in arrs[:nv]])
+        wp = (C.c_void_p * nv)(*[a.ctypes.data for a in arrs[nv:]])
+        self._check(self._lib.mvr_decon_run_host(self._h, int(n), ip, wp, _p(psi)))
+        return psi
 
     def run_iterations(self, n: int, stats: bool = False):
         """runIterations; returns per (iteration, view-step) [sumChange, maxChange] if asked."""

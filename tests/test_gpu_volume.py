@@ -186,3 +186,23 @@ def test_graph_replay_matches_eager_launches(vol, block, mul):
         assert d.launch_count() > n0  # replayed launches are counted
     assert np.array_equal(psi_g, psi_e)
     assert np.array_equal(st_g, st_e)
+
+
+def test_run_host_matches_device_resident_iterations(vol):
+    # mvr_decon_run_host (uploads overlapped with the first view-steps) gives the same psi as
+    # uploading the views and psi and running the iterations on the device
+    imgs = [vol["img0"], vol["img1"]]
+    raws = [vol["raw_w0"], vol["raw_w1"]]
+    with make(vol, (28, 28, 28)) as d:
+        psi0 = d.get_psi()
+        d.run_iterations(2)
+        ref = d.get_psi()
+    with make(vol, (28, 28, 28)) as d:
+        psi = psi0.copy()
+        d.run_host(1, imgs, raws, psi)
+        d.run_host(1, imgs, raws, psi)  # a second call re-uploads everything
+        assert rel(psi, ref) <= 1e-6
+        with make(vol, (28, 28, 28)) as d2:
+            psi2 = psi0.copy()
+            d2.run_host(2, imgs, raws, psi2)  # first iteration eager, the second from the graph path
+        assert rel(psi2, ref) <= 1e-6
