@@ -886,11 +886,22 @@ int Engine<T>::launch_xy_update(const Plan<T> &pl, const BlockMaps &bms, int nb,
 {
     if constexpr (sizeof(T) == sizeof(float)) {
         MVR_TRY(prof_begin(KK_XY_UPDATE, bytes));
+        // partial slots per block: one per CTA of the update grid (planes of the deepest write
+        // region when pruned; a pruned likelihood leaves the slots of shallower blocks' extra
+        // planes at zero)
+        int planes = pl.P[2];
+        if (ua.prune) {
+            planes = 0;
+            for (int i = 0; i < nb; ++i) planes = std::max(planes, bms.m[i].whi[2] - bms.m[i].wlo[2]);
+        }
+        const int slots = xy_partial_slots(pl.xy, planes);
+        if (ua.prune && epi == EPI_NLL && stats_dev)
+            MVR_CUDA(cudaMemsetAsync(partials_, 0, sizeof(double) * 2 * (size_t)slots * nb, stream_));
         MVR_CUDA(xy_update(pl.xy, epi, S, ua, bms, nb, pl.P[2], pl.Pc, pl.twx, pl.twy, stream_));
         MVR_TRY(prof_end());
         if (stats_dev && (epi == EPI_SEQ || epi == EPI_MUL_FINAL || epi == EPI_NLL)) {
-            MVR_TRY(prof_begin(KK_REDUCE, 16.0 * pl.P[2] * nb));
-            k_reduce_stats<double><<<nb, 1024, 0, stream_>>>(partials_, xy_partial_slots(pl.xy, pl.P[2]), stats_dev);
+            MVR_TRY(prof_begin(KK_REDUCE, 16.0 * slots * nb));
+            k_reduce_stats<double><<<nb, 1024, 0, stream_>>>(partials_, slots, stats_dev);
             MVR_LAUNCHED("k_reduce_stats");
             MVR_TRY(prof_end());
         }
@@ -1046,9 +1057,12 @@ int Engine<T>::likelihood(const Plan<T> &pl, const BlockPlace *bps, int nb, cons
     const long long nrows = (long long)pl.P[1] * pl.P[2];
     MVR_TRY(reserve(pl.Pc, (long long)pl.b[0] * pl.b[1] * pl.b[2], (nrows + pl.RP - 1) / pl.RP, nb));
     const BlockMaps bms = block_maps(pl, bps, nb);
+    // plane kernels: only the write regions (each volume voxel once) are transformed back
+    int zlo = 0, zhi = -1, ylo = 0, yhi = -1;
     if (pl.xy) {
+        write_region(bps, nb, zlo, zhi, ylo, yhi);
         MVR_TRY(launch_xy_fwd(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
-        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb));
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb, zlo, zhi));
     } else {
         MVR_TRY(launch_fwd_mirror(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
         MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
@@ -1056,6 +1070,7 @@ int Engine<T>::likelihood(const Plan<T> &pl, const BlockPlace *bps, int nb, cons
         MVR_TRY(launch_cols(pl, 1, 1, S0_, S0_, nullptr, nb));
     }
     UpdateArgs ua{};
+    ua.prune = pl.xy ? 1 : 0;
     ua.psi_src = bps[0].psi_src;
     ua.img = img;
     ua.weight[0] = w;

@@ -235,7 +235,7 @@ cudaError_t xy_update(int combo, int epi, float2 *S, const UpdateArgs &ua, const
     set_limits();
     int planes = Pz;
     if (ua.prune) {
-        if (epi == EPI_NLL || epi == EPI_STORE) return cudaErrorInvalidValue;
+        if (epi == EPI_STORE) return cudaErrorInvalidValue;
         planes = 0;
         for (int i = 0; i < nb; ++i) planes = std::max(planes, bms.m[i].whi[2] - bms.m[i].wlo[2]);
         if (planes < 1) return cudaSuccess;

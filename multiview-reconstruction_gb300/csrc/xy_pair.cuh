@@ -583,7 +583,8 @@ __global__ void __launch_bounds__(PairShape<VX, VH>::NT, PairShape<VX, VH>::MINB
                     update_row<float, EPI>(sm.A + yl * SH::SR, SH::m, bm, ua, y, z, lane, ksum, kcomp, kmax);
             }
     }
-    if ((EPI == EPI_SEQ || EPI == EPI_MUL_FINAL || EPI == EPI_NLL) && !ua.prune)
+    // pruned runs skip the statistics, but the likelihood is reduced over the write region
+    if ((EPI == EPI_SEQ || EPI == EPI_MUL_FINAL || EPI == EPI_NLL) && (!ua.prune || EPI == EPI_NLL))
         stats_to_partials(ksum, kcomp, kmax, red_s, red_m, ua.partials, (long long)blockIdx.y * gridDim.x + blockIdx.x);
 }
 

@@ -46,7 +46,11 @@ def run(case, code, iters=2):
         used = [d.schedule(v) for v in range(2)]
         trials = d.tuning()
         d.run_iterations(iters)
+        run.nll[code] = d.likelihood()[0]  # the plane paths reduce it over the write regions only
         return d.get_psi(), used, trials
+
+
+run.nll = {}
 
 
 def test_every_forced_schedule_gives_the_same_psi(case):
@@ -59,6 +63,7 @@ def test_every_forced_schedule_gives_the_same_psi(case):
     base = outs[M.SCHED_ROWS]
     for code, psi in outs.items():
         assert rel(psi, base) <= 1e-6, M.schedule_name(code)
+        assert run.nll[code] == pytest.approx(run.nll[M.SCHED_ROWS], rel=1e-6)
     dims, psfs, imgs, ws = case
     k1s, k2s = O.psf_init(psfs, O.PSF_OPTIMIZATION_I, 0)
     psi0, mx, _ = O.psi_init_avg(imgs)
@@ -81,6 +86,15 @@ def test_autotuner_tries_every_schedule_and_keeps_the_fastest(case):
 def test_schedule_errors():
     with M.Deconvolution((40, 36, 30), 2, (28, 28, 28)) as d:
         with pytest.raises(M.MvrError):
-            d.set_schedule(3)
+            d.set_schedule(8)
         with pytest.raises(M.MvrError):
-            d.set_schedule(99)
+            d.set_schedule(-2)
+        # a 28^3 block has no plane or pair kernels: forcing them fails at prepare
+        d.set_view(0, np.ones((30, 36, 40), np.float32), np.ones((30, 36, 40), np.float32),
+                   synthetic.make_psf((5, 5, 7), 1.0, 1.5, 0.0))
+        d.set_view(1, np.ones((30, 36, 40), np.float32), np.ones((30, 36, 40), np.float32),
+                   synthetic.make_psf((5, 5, 7), 1.0, 1.5, 90.0))
+        d.set_schedule(M.SCHED_PAIR)
+        with pytest.raises(M.MvrError) as e:
+            d.prepare()
+        assert e.value.code == M.ERR_UNSUPPORTED
