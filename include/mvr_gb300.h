@@ -345,6 +345,22 @@ MVR_API int mvr_psf_projection(const float *psf, const int dims[3], int dim, int
 MVR_API int mvr_psf_remove_min_projections(float *psf, const int dims[3], int device, void *stream);
 MVR_API const char *mvr_psf_last_error(void);
 
+/* ---- export of the deconvolved volume (Image_Deconvolution's ImgExport, MV/export) -----
+ * volume: float32 [z][y][x] of dims {x, y, z}, in host memory (on_device 0) or device memory
+ * (on_device 1, read back in slabs).  err (may be NULL) receives a message on failure.
+ * mvr_export_tiff: Save3dTIFF (MV/export/Save3dTIFF.java:86-160): an ImageJ stack of 32-bit
+ *   float slices (big-endian TIFF, one strip per slice, ImageJ description with the slice
+ *   count, unit, z spacing and the display range 0..255 of DisplayImage), calibration {x, y,
+ *   z} per pixel (NULL: 1) and unit (NULL: "px"); stacks beyond the 4 GB offsets of a TIFF
+ *   file return MVR_ERR_UNSUPPORTED.
+ * mvr_export_n5: ExportN5Api with the N5 format and no compression (MV/export/ExportN5Api.java):
+ *   dataset `dataset` under the container directory `root`, float32, raw blocks of
+ *   block_size {x, y, z} (clipped at the border), one file per grid position bx/by/bz. */
+MVR_API int mvr_export_tiff(const char *path, const float *volume, const long long dims[3], int on_device,
+                            const double calibration[3], const char *unit, char *err, int err_len);
+MVR_API int mvr_export_n5(const char *root, const char *dataset, const float *volume, const long long dims[3],
+                          int on_device, const int block_size[3], char *err, int err_len);
+
 /* ---- learned multi-iteration proposal (no counterpart in the reference) ---------------
  * A 3-level 3D U-Net (16/32/64 channels, 3x3x3 convolutions, BF16 weights and
  * activations, FP32 accumulation on the tcgen05 tensor cores) with its own forward and

@@ -12,7 +12,7 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libmvrgb300.so")
-SOURCES = ["engine.cu", "xy.cu", "capi.cu", "decon.cu", "noalloc.cu", "unet.cu", "fuse.cu", "psf.cu"]
+SOURCES = ["engine.cu", "xy.cu", "capi.cu", "decon.cu", "noalloc.cu", "unet.cu", "fuse.cu", "psf.cu", "export.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
                # host arithmetic without contraction into fused multiply-adds (x86 and Arm agree)

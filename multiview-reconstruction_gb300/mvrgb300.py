@@ -46,7 +46,7 @@ EXPORTS = [
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
     "mvr_kernel_name", "mvr_convolve_static", "mvr_decon_batch", "mvr_decon_likelihood",
     "mvr_decon_set_graphs", "mvr_decon_graphs_captured", "mvr_decon_set_schedule", "mvr_decon_schedule",
-    "mvr_decon_tuning", "mvr_decon_run_host", "mvr_decon_init_psi", "mvr_fuse_group",
+    "mvr_decon_tuning", "mvr_decon_run_host", "mvr_export_tiff", "mvr_export_n5", "mvr_decon_init_psi", "mvr_fuse_group",
     "mvr_fuse_last_error", "mvr_psf_extract", "mvr_psf_transformed_dims", "mvr_psf_transform_normalized",
     "mvr_psf_average", "mvr_psf_make_same_size", "mvr_psf_projection", "mvr_psf_remove_min_projections",
     "mvr_psf_last_error", "mvr_block_grid",
@@ -141,6 +141,8 @@ def load() -> C.CDLL:
     L.mvr_decon_schedule.argtypes = [P, C.c_int]
     L.mvr_decon_tuning.argtypes = [P, C.c_int, P, P, P, P]
     L.mvr_decon_run_host.argtypes = [P, C.c_int, P, P, P]
+    L.mvr_export_tiff.argtypes = [C.c_char_p, P, P, C.c_int, P, C.c_char_p, C.c_char_p, C.c_int]
+    L.mvr_export_n5.argtypes = [C.c_char_p, C.c_char_p, P, P, C.c_int, P, C.c_char_p, C.c_int]
     L.mvr_decon_prepare.argtypes = [P]
     L.mvr_decon_set_psi.argtypes = [P, P]
     L.mvr_decon_set_psi_device.argtypes = [P, P]
@@ -598,6 +600,38 @@ def convolve_static(img_ptr: int, img_size, kernel_ptr: int, kernel_size, out_pt
     rc = L.mvr_convolve_static(C.c_void_p(img_ptr), (C.c_int * 3)(*img_size), C.c_void_p(kernel_ptr),
                                (C.c_int * 3)(*kernel_size), C.c_void_p(out_ptr), C.c_void_p(stream) if stream else None,
                                err, len(err))
+    if rc != OK:
+        raise MvrError(rc, err.value.decode())
+
+
+def export_tiff(path, volume, calibration=(1.0, 1.0, 1.0), unit="px", dims=None):
+    """mvr_export_tiff (Save3dTIFF): volume a float32 [z][y][x] host array, or a device address
+    with dims (x, y, z)."""
+    L = load()
+    err = C.create_string_buffer(256)
+    if isinstance(volume, np.ndarray):
+        v = _f32(volume)
+        ptr, on_dev, d = _p(v), 0, (v.shape[2], v.shape[1], v.shape[0])
+    else:
+        ptr, on_dev, d = C.c_void_p(volume), 1, dims
+    rc = L.mvr_export_tiff(str(path).encode(), ptr, (C.c_longlong * 3)(*d), on_dev, (C.c_double * 3)(*calibration),
+                           unit.encode(), err, len(err))
+    if rc != OK:
+        raise MvrError(rc, err.value.decode())
+
+
+def export_n5(root, dataset, volume, block_size=(64, 64, 64), dims=None):
+    """mvr_export_n5 (ExportN5Api, N5, raw blocks): volume a float32 [z][y][x] host array, or a
+    device address with dims (x, y, z)."""
+    L = load()
+    err = C.create_string_buffer(256)
+    if isinstance(volume, np.ndarray):
+        v = _f32(volume)
+        ptr, on_dev, d = _p(v), 0, (v.shape[2], v.shape[1], v.shape[0])
+    else:
+        ptr, on_dev, d = C.c_void_p(volume), 1, dims
+    rc = L.mvr_export_n5(str(root).encode(), dataset.encode(), ptr, (C.c_longlong * 3)(*d), on_dev,
+                         (C.c_int * 3)(*block_size), err, len(err))
     if rc != OK:
         raise MvrError(rc, err.value.decode())
 
