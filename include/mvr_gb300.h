@@ -397,6 +397,15 @@ MVR_API int mvr_conv3d_tc(const void *act, int c_act, const void *weights, int n
 MVR_API int mvr_conv3d_tc_wgrad(const void *x, int c_in, const void *g, int c_out, float *dw, const int dims[4],
                                 int *err_dev, void *stream);
 MVR_API const char *mvr_conv3d_tc_last_error(void);
+/* The coarse form of the proposal: the network runs on the 2 x 2 x 2 averages of psi_k and
+ * psi_{k+1} (mvr_pool2: device float volume of even dims {x, y, z} -> dims / 2, queued on
+ * `stream`), and mvr_apply_coarse applies its prediction at full resolution:
+ * out = psi_next * exp(clamp(up(pred_low - log(next_low / psi_low)), -cap, cap)), up = trilinear
+ * interpolation of the coarse grid (cell centres), i.e. the plain step at full resolution
+ * plus the predicted further change of the coarse scales. */
+MVR_API int mvr_pool2(const float *in, const int dims[3], float *out, void *stream);
+MVR_API int mvr_apply_coarse(const float *psi_next, const int dims[3], const float *pred_low, const float *psi_low,
+                             const float *next_low, float cap, float *out, void *stream);
 
 /* ---- convolution without device allocation ------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot call

@@ -2,6 +2,8 @@
 // (declared in include/mvr_gb300.h).
 #include <cuda_runtime.h>
 
+#include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -18,7 +20,50 @@ using mvr::Plan;
 
 namespace {
 thread_local std::string g_create_error;
+
+// Host <-> device copies of the block buffers.  A block buffer of the Java driver (or any
+// caller) is ordinary pageable memory that changes from call to call; a DMA copy of it first
+// pins every page, which for freshly allocated buffers costs more than the transfer.  Where
+// the GPU reads and writes pageable host memory through the host's page tables
+// (cudaDevAttrPageableMemoryAccessUsesHostPageTables, e.g. NVLink-C2C systems), a copy kernel
+// moves the buffer instead; elsewhere cudaMemcpyAsync.  MVR_HOST_COPY=dma forces the DMA copy.
+__global__ void k_copy_words(float4 *__restrict__ dst, const float4 *__restrict__ src, long long n4)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = src[i];
 }
+__global__ void k_copy_floats(float *__restrict__ dst, const float *__restrict__ src, long long n)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+}
+
+bool kernel_host_copy(int dev)
+{
+    static int cached[64] = {0};  // 0 unknown, 1 kernel, 2 DMA
+    if (dev < 0 || dev >= 64) return false;
+    if (!cached[dev]) {
+        const char *e = std::getenv("MVR_HOST_COPY");
+        int ht = 0;
+        if (cudaDeviceGetAttribute(&ht, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) ht = 0;
+        cached[dev] = (ht == 1 && !(e && std::strcmp(e, "dma") == 0)) ? 1 : 2;
+    }
+    return cached[dev] == 1;
+}
+
+cudaError_t host_copy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, int dev, cudaStream_t s)
+{
+    if (!kernel_host_copy(dev)) return cudaMemcpyAsync(dst, src, bytes, kind, s);
+    const bool vec = ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) | bytes) & 15) == 0;
+    if (vec)
+        k_copy_words<<<608, 256, 0, s>>>(static_cast<float4 *>(dst), static_cast<const float4 *>(src),
+                                         (long long)(bytes / 16));
+    else
+        k_copy_floats<<<608, 256, 0, s>>>(static_cast<float *>(dst), static_cast<const float *>(src),
+                                          (long long)(bytes / 4));
+    return cudaGetLastError();
+}
+}  // namespace
 
 struct mvr_block {
     Engine<float> eng;
@@ -152,12 +197,13 @@ extern "C" int mvr_block_run_seq(mvr_block *h, int view, float *psi, const float
     BLK_CUDA(h, cudaSetDevice(h->eng.device()));
     cudaStream_t s = h->eng.stream();
     const size_t bytes = sizeof(float) * (size_t)h->nvox;
-    BLK_CUDA(h, cudaMemcpyAsync(h->d_psi, psi, bytes, cudaMemcpyHostToDevice, s));
-    BLK_CUDA(h, cudaMemcpyAsync(h->d_img[0], img, bytes, cudaMemcpyHostToDevice, s));
-    BLK_CUDA(h, cudaMemcpyAsync(h->d_w[0], w, bytes, cudaMemcpyHostToDevice, s));
+    const int dev = h->eng.device();
+    BLK_CUDA(h, host_copy(h->d_psi, psi, bytes, cudaMemcpyHostToDevice, dev, s));
+    BLK_CUDA(h, host_copy(h->d_img[0], img, bytes, cudaMemcpyHostToDevice, dev, s));
+    BLK_CUDA(h, host_copy(h->d_w[0], w, bytes, cudaMemcpyHostToDevice, dev, s));
     int rc = run_seq_impl(h, view, h->d_psi, h->d_psi, h->d_img[0], h->d_w[0], maxI, h->d_stats);
     if (rc != MVR_OK) return rc;
-    BLK_CUDA(h, cudaMemcpyAsync(psi, h->d_psi, bytes, cudaMemcpyDeviceToHost, s));
+    BLK_CUDA(h, host_copy(psi, h->d_psi, bytes, cudaMemcpyDeviceToHost, dev, s));
     double st[2] = {0.0, -1.0};
     BLK_CUDA(h, cudaMemcpyAsync(st, h->d_stats, sizeof(st), cudaMemcpyDeviceToHost, s));
     BLK_CUDA(h, cudaStreamSynchronize(s));
@@ -201,10 +247,11 @@ extern "C" int mvr_block_run_mul(mvr_block *h, float *psi, const float *const *i
     BLK_CUDA(h, cudaSetDevice(h->eng.device()));
     cudaStream_t s = h->eng.stream();
     const size_t bytes = sizeof(float) * (size_t)h->nvox;
-    BLK_CUDA(h, cudaMemcpyAsync(h->d_psi, psi, bytes, cudaMemcpyHostToDevice, s));
+    const int dev = h->eng.device();
+    BLK_CUDA(h, host_copy(h->d_psi, psi, bytes, cudaMemcpyHostToDevice, dev, s));
     for (int v = 0; v < h->nviews; ++v) {
-        BLK_CUDA(h, cudaMemcpyAsync(h->d_img[v], imgs[v], bytes, cudaMemcpyHostToDevice, s));
-        BLK_CUDA(h, cudaMemcpyAsync(h->d_w[v], ws[v], bytes, cudaMemcpyHostToDevice, s));
+        BLK_CUDA(h, host_copy(h->d_img[v], imgs[v], bytes, cudaMemcpyHostToDevice, dev, s));
+        BLK_CUDA(h, host_copy(h->d_w[v], ws[v], bytes, cudaMemcpyHostToDevice, dev, s));
     }
     // ComputeBlockMulThreadCPU.java:144-149: mean of the maxima in double, then float
     double miv = 0.0;
@@ -221,7 +268,7 @@ extern "C" int mvr_block_run_mul(mvr_block *h, float *psi, const float *const *i
     std::vector<const float *> di(h->d_img.begin(), h->d_img.end()), dw(h->d_w.begin(), h->d_w.end());
     int rc = h->from_engine(h->eng.run_mul(pls, &bp, 1, di.data(), dw.data(), (float)miv, h->d_stats));
     if (rc != MVR_OK) return rc;
-    BLK_CUDA(h, cudaMemcpyAsync(psi, h->d_psi, bytes, cudaMemcpyDeviceToHost, s));
+    BLK_CUDA(h, host_copy(psi, h->d_psi, bytes, cudaMemcpyDeviceToHost, dev, s));
     double st[2] = {0.0, -1.0};
     BLK_CUDA(h, cudaMemcpyAsync(st, h->d_stats, sizeof(st), cudaMemcpyDeviceToHost, s));
     BLK_CUDA(h, cudaStreamSynchronize(s));
@@ -284,10 +331,10 @@ int conv3d(float *im, const int *imDim, const float *kernel, const int *kernelDi
         c.cap = n;
     }
     cudaStream_t s = c.eng->stream();
-    if (cudaMemcpyAsync(c.d_img, im, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    if (host_copy(c.d_img, im, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, dev, s) != cudaSuccess)
         return MVR_ERR_CUDA;
     if (c.eng->convolve(*pl, c.d_img, mvr::SRC_ZERO, c.d_out) != MVR_OK) return MVR_ERR_CUDA;
-    if (cudaMemcpyAsync(out, c.d_out, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    if (host_copy(out, c.d_out, sizeof(float) * (size_t)n, cudaMemcpyDeviceToHost, dev, s) != cudaSuccess)
         return MVR_ERR_CUDA;
     return cudaStreamSynchronize(s) == cudaSuccess ? MVR_OK : MVR_ERR_CUDA;
 }

@@ -359,6 +359,57 @@ __global__ void k_propose(const float *psi, const float *pred, float *out, long 
         out[i] = psi[i] * expf(fminf(fmaxf(pred[i], -cap), cap));
 }
 
+// 2 x 2 x 2 average of a float volume [z][y][x] of even dims (the coarse grid of the proposal)
+__global__ void k_pool2_f32(const float *__restrict__ in, long long X, long long Y, long long Z, float *__restrict__ out)
+{
+    const long long x2 = X / 2, y2 = Y / 2, n = x2 * y2 * (Z / 2);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long x = i % x2, t = i / x2, y = t % y2, z = t / y2;
+        const float *p = in + ((2 * z) * Y + 2 * y) * X + 2 * x;
+        const float s = (p[0] + p[1]) + (p[X] + p[X + 1]) + ((p[X * Y] + p[X * Y + 1]) + (p[X * Y + X] + p[X * Y + X + 1]));
+        out[i] = 0.125f * s;
+    }
+}
+
+// The coarse proposal applied at full resolution: c = pred - log(next_low / psi_low) on the
+// coarse grid (the predicted log change beyond the plain step), trilinearly interpolated at
+// full-resolution voxel x (coarse coordinate x / 2 - 1 / 4, clamped at the borders), and
+// out = psi_next * exp(clamp(c, -cap, cap)).
+__device__ __forceinline__ float coarse_c(const float *pred, const float *lo_psi, const float *lo_next, long long i)
+{
+    return pred[i] - logf(fmaxf(lo_next[i], 1e-12f) / fmaxf(lo_psi[i], 1e-12f));
+}
+__global__ void k_apply_coarse(const float *__restrict__ psi_next, long long X, long long Y, long long Z,
+                               const float *__restrict__ pred, const float *__restrict__ lo_psi,
+                               const float *__restrict__ lo_next, float cap, float *__restrict__ out)
+{
+    const long long x2 = X / 2, y2 = Y / 2, z2 = Z / 2, n = X * Y * Z;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long x = i % X, t = i / X, y = t % Y, z = t / Y;
+        long long c0[3], c1[3];
+        float f[3];
+        const long long dim[3] = {x2, y2, z2}, pos[3] = {x, y, z};
+        for (int d = 0; d < 3; ++d) {
+            const float u = 0.5f * (float)pos[d] - 0.25f;
+            const float fl = floorf(u);
+            long long a = (long long)fl, b = a + 1;
+            f[d] = u - fl;
+            if (a < 0) a = 0;
+            if (b > dim[d] - 1) b = dim[d] - 1;
+            c0[d] = a;
+            c1[d] = b;
+        }
+        float acc = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const long long cx = (k & 1) ? c1[0] : c0[0], cy = (k & 2) ? c1[1] : c0[1], cz = (k & 4) ? c1[2] : c0[2];
+            const float w = ((k & 1) ? f[0] : 1.0f - f[0]) * ((k & 2) ? f[1] : 1.0f - f[1]) * ((k & 4) ? f[2] : 1.0f - f[2]);
+            acc += w * coarse_c(pred, lo_psi, lo_next, (cz * y2 + cy) * x2 + cx);
+        }
+        out[i] = psi_next[i] * expf(fminf(fmaxf(acc, -cap), cap));
+    }
+}
+
 }  // namespace
 
 // ---- the network ----------------------------------------------------------------------
@@ -711,7 +762,9 @@ extern "C" int mvr_unet_set_input(mvr_unet *h, const float *psi, const float *ps
 {
     return h ? h->net->set_input(psi, psi_next, psi_target) : MVR_ERR_ARG;
 }
-extern "C" int mvr_unet_forward(mvr_unet *h, float *pred) { return h ? h->net->forward(pred) : MVR_ERR_ARG; }
+// inference: the decoder convolutions read [up(low), skip] directly (the training step keeps the
+// concatenations for its backward pass)
+extern "C" int mvr_unet_forward(mvr_unet *h, float *pred) { return h ? h->net->forward(pred, true) : MVR_ERR_ARG; }
 extern "C" int mvr_unet_train_step(mvr_unet *h, float lr, double *loss)
 {
     return h ? h->net->train_step(lr, loss) : MVR_ERR_ARG;
@@ -753,3 +806,24 @@ extern "C" int mvr_conv3d_tc_wgrad(const void *x, int c_in, const void *g, int c
 }
 
 extern "C" const char *mvr_conv3d_tc_last_error(void) { return mvr::g_tc_error.c_str(); }
+
+extern "C" int mvr_pool2(const float *in, const int dims[3], float *out, void *stream)
+{
+    if (!in || !dims || !out || dims[0] < 2 || dims[1] < 2 || dims[2] < 2 || (dims[0] | dims[1] | dims[2]) & 1)
+        return MVR_ERR_ARG;
+    const long long n = (long long)(dims[0] / 2) * (dims[1] / 2) * (dims[2] / 2);
+    mvr::k_pool2_f32<<<mvr::gsize(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(in, dims[0], dims[1], dims[2], out);
+    return cudaGetLastError() == cudaSuccess ? MVR_OK : MVR_ERR_CUDA;
+}
+
+extern "C" int mvr_apply_coarse(const float *psi_next, const int dims[3], const float *pred_low, const float *psi_low,
+                                const float *next_low, float cap, float *out, void *stream)
+{
+    if (!psi_next || !dims || !pred_low || !psi_low || !next_low || !out || dims[0] < 2 || dims[1] < 2 ||
+        dims[2] < 2 || (dims[0] | dims[1] | dims[2]) & 1)
+        return MVR_ERR_ARG;
+    const long long n = (long long)dims[0] * dims[1] * dims[2];
+    mvr::k_apply_coarse<<<mvr::gsize(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        psi_next, dims[0], dims[1], dims[2], pred_low, psi_low, next_low, cap, out);
+    return cudaGetLastError() == cudaSuccess ? MVR_OK : MVR_ERR_CUDA;
+}

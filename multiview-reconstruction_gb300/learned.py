@@ -84,14 +84,27 @@ def synthesize(dims, seeds, psf, workers=None):
         return list(ex.map(_dataset_job, [(dims, s, psf) for s in seeds]))
 
 
+def pool2(vol, device=0):
+    """The library's 2 x 2 x 2 average of a device volume [z][y][x] (even dims)."""
+    import torch
+
+    out = torch.empty((vol.shape[0] // 2, vol.shape[1] // 2, vol.shape[2] // 2), dtype=torch.float32,
+                      device=vol.device)
+    M.pool2(vol.data_ptr(), (vol.shape[2], vol.shape[1], vol.shape[0]), out.data_ptr())
+    torch.cuda.synchronize(vol.device)
+    return out
+
+
 def generate_pairs(n_objects=50, dims=(128, 128, 128), crop=(64, 64, 64), iters=45, m=5, pairs_per_object=40,
-                   seed0=2000, psf=(31, 31, 61), device=0, datasets=None):
-    """(psi_k, psi_{k+1}, psi_{k+m}) crops from the plain method on seeded objects.
+                   seed0=2000, psf=(31, 31, 61), device=0, datasets=None, coarse=True):
+    """(psi_k, psi_{k+1}, psi_{k+m}) crops from the plain method on seeded objects (with
+    coarse, of the 2 x 2 x 2 averages of the iterates: the grid the coarse proposal runs on).
     Returns three device tensors [P][cz][cy][cx]."""
     import torch
 
     rng = np.random.default_rng(seed0)
     shape = (dims[2], dims[1], dims[0])
+    hshape = tuple(d // 2 for d in shape) if coarse else shape
     block = one_block(dims, psf)
     out = [[], [], []]
     if datasets is None:
@@ -99,15 +112,23 @@ def generate_pairs(n_objects=50, dims=(128, 128, 128), crop=(64, 64, 64), iters=
     for o in range(n_objects):
         ds = datasets[o]
         dec = make_decon(ds, dims, block, device)
-        hist = torch.empty((iters + 1,) + shape, dtype=torch.float32, device=f"cuda:{device}")
-        dec.get_psi_device(hist[0].data_ptr())
+        hist = torch.empty((iters + 1,) + hshape, dtype=torch.float32, device=f"cuda:{device}")
+        cur = torch.empty(shape, dtype=torch.float32, device=f"cuda:{device}")
+
+        def keep(k):
+            dec.get_psi_device(cur.data_ptr() if coarse else hist[k].data_ptr())
+            if coarse:
+                hist[k].copy_(pool2(cur, device))
+
+        keep(0)
         for k in range(iters):
             dec.run_iterations(1)
-            dec.get_psi_device(hist[k + 1].data_ptr())
+            keep(k + 1)
         dec.close()
+        shape_c = hshape
         for _ in range(pairs_per_object):
             k = int(rng.integers(0, iters - m))
-            z0, y0, x0 = (int(rng.integers(0, shape[i] - crop[2 - i] + 1)) for i in range(3))
+            z0, y0, x0 = (int(rng.integers(0, shape_c[i] - crop[2 - i] + 1)) for i in range(3))
             sl = (slice(z0, z0 + crop[2]), slice(y0, y0 + crop[1]), slice(x0, x0 + crop[0]))
             out[0].append(hist[k][sl].clone())
             out[1].append(hist[k + 1][sl].clone())
@@ -146,15 +167,23 @@ class GatedProposer:
     proposes (the others are plain iterations); the seconds spent in the network and in
     the gate's likelihood evaluations are accumulated in `timing`."""
 
-    def __init__(self, params, dims, cap=1.0, device=0, every=1):
+    def __init__(self, params, dims, cap=1.0, device=0, every=1, coarse=True):
         import torch
 
-        self.net = M.UNet(1, dims, seed=0, device=device)
+        self.coarse = coarse
+        self.dims = tuple(dims)
+        ndims = tuple(d // 2 for d in dims) if coarse else tuple(dims)
+        self.net = M.UNet(1, ndims, seed=0, device=device)
         self.net.set_params(params)
         shape = (1, dims[2], dims[1], dims[0])
         self.psi = torch.empty(shape, dtype=torch.float32, device=f"cuda:{device}")
         self.nxt = torch.empty_like(self.psi)
         self.prop = torch.empty_like(self.psi)
+        if coarse:
+            lshape = (ndims[2], ndims[1], ndims[0])
+            self.lo_psi = torch.empty(lshape, dtype=torch.float32, device=f"cuda:{device}")
+            self.lo_nxt = torch.empty_like(self.lo_psi)
+            self.pred = torch.empty_like(self.lo_psi)
         self.cap = cap
         self.every = max(1, int(every))
         self.count = 0
@@ -178,8 +207,19 @@ class GatedProposer:
         dec.run_iterations(1)
         dec.get_psi_device(self.nxt.data_ptr())
         t1 = time.perf_counter()
-        self.net.set_input(self.psi.data_ptr(), self.nxt.data_ptr())
-        self.net.propose(self.psi.data_ptr(), self.prop.data_ptr(), self.cap)
+        if self.coarse:
+            # the network on the coarse grid, its prediction applied to the full-resolution step
+            M.pool2(self.psi.data_ptr(), self.dims, self.lo_psi.data_ptr())
+            M.pool2(self.nxt.data_ptr(), self.dims, self.lo_nxt.data_ptr())
+            torch.cuda.synchronize()
+            self.net.set_input(self.lo_psi.data_ptr(), self.lo_nxt.data_ptr())
+            self.net.forward(self.pred.data_ptr())
+            torch.cuda.synchronize()
+            M.apply_coarse(self.nxt.data_ptr(), self.dims, self.pred.data_ptr(), self.lo_psi.data_ptr(),
+                           self.lo_nxt.data_ptr(), self.cap, self.prop.data_ptr())
+        else:
+            self.net.set_input(self.psi.data_ptr(), self.nxt.data_ptr())
+            self.net.propose(self.psi.data_ptr(), self.prop.data_ptr(), self.cap)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         l_plain = dec.likelihood()[0]
@@ -236,14 +276,16 @@ def first_time(hist, pred):
 
 def experiment(ds, dims, block, n_objects=50, train_dims=(128, 128, 128), crop=(64, 64, 64), iters=45, m=5,
                pairs_per_object=40, train_steps=1500, batch=4, lr=1e-3, eval_iters=20, tol=1e-3, device=0,
-               datasets=None, everies=(1, 3)):
+               datasets=None, everies=(1, 3), coarse=True):
     """Learned + gated vs plain GPU RL on ds: wall time to relative L2 <= tol against the
-    FP64 plain result after eval_iters iterations, and to that result's likelihood."""
+    FP64 plain result after eval_iters iterations, and to that result's likelihood.  With
+    coarse, the network sees and predicts the 2 x 2 x 2 averages (training crops of the
+    averaged iterates: the whole 64^3 average of a 128^3 object)."""
     import torch
 
     t0 = time.perf_counter()
     pairs = generate_pairs(n_objects, train_dims, crop, iters, m, pairs_per_object, psf=ds.psfs[0].shape[::-1],
-                           device=device, datasets=datasets)
+                           device=device, datasets=datasets, coarse=coarse)
     gen_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     params, losses = train(pairs, crop, train_steps, batch, lr, device=device)
@@ -266,7 +308,7 @@ def experiment(ds, dims, block, n_objects=50, train_dims=(128, 128, 128), crop=(
     runs = {}
     for every in everies:
         gated = make_decon(ds, dims, block, device)
-        prop = GatedProposer(params, dims, device=device, every=every)
+        prop = GatedProposer(params, dims, device=device, every=every, coarse=coarse)
         h = convergence(gated, eval_iters + 10, ref, prop)
         runs[every] = (h, dict(prop.timing))
         prop.close()

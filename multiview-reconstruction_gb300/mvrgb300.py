@@ -46,7 +46,8 @@ EXPORTS = [
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
     "mvr_kernel_name", "mvr_convolve_static", "mvr_decon_batch", "mvr_decon_likelihood",
     "mvr_decon_set_graphs", "mvr_decon_graphs_captured", "mvr_decon_set_schedule", "mvr_decon_schedule",
-    "mvr_decon_tuning", "mvr_decon_run_host", "mvr_export_tiff", "mvr_export_n5", "mvr_decon_init_psi", "mvr_fuse_group",
+    "mvr_decon_tuning", "mvr_decon_run_host", "mvr_export_tiff", "mvr_export_n5", "mvr_pool2",
+    "mvr_apply_coarse", "mvr_decon_init_psi", "mvr_fuse_group",
     "mvr_fuse_last_error", "mvr_psf_extract", "mvr_psf_transformed_dims", "mvr_psf_transform_normalized",
     "mvr_psf_average", "mvr_psf_make_same_size", "mvr_psf_projection", "mvr_psf_remove_min_projections",
     "mvr_psf_last_error", "mvr_block_grid",
@@ -142,6 +143,8 @@ def load() -> C.CDLL:
     L.mvr_decon_tuning.argtypes = [P, C.c_int, P, P, P, P]
     L.mvr_decon_run_host.argtypes = [P, C.c_int, P, P, P]
     L.mvr_export_tiff.argtypes = [C.c_char_p, P, P, C.c_int, P, C.c_char_p, C.c_char_p, C.c_int]
+    L.mvr_pool2.argtypes = [P, P, P, P]
+    L.mvr_apply_coarse.argtypes = [P, P, P, P, P, C.c_float, P, P]
     L.mvr_export_n5.argtypes = [C.c_char_p, C.c_char_p, P, P, C.c_int, P, C.c_char_p, C.c_int]
     L.mvr_decon_prepare.argtypes = [P]
     L.mvr_decon_set_psi.argtypes = [P, P]
@@ -560,6 +563,23 @@ class UNet:
 
     def propose(self, psi_ptr: int, out_ptr: int, cap: float = 1.0):
         self._check(self._lib.mvr_unet_propose(self._h, C.c_void_p(psi_ptr), C.c_void_p(out_ptr), cap))
+
+
+def pool2(in_ptr: int, dims, out_ptr: int, stream: int = 0):
+    """mvr_pool2: 2 x 2 x 2 average of a device float volume of even dims (x, y, z)."""
+    rc = load().mvr_pool2(C.c_void_p(in_ptr), (C.c_int * 3)(*dims), C.c_void_p(out_ptr), _sp(stream))
+    if rc != OK:
+        raise MvrError(rc, "mvr_pool2")
+
+
+def apply_coarse(psi_next_ptr: int, dims, pred_low_ptr: int, psi_low_ptr: int, next_low_ptr: int, cap: float,
+                 out_ptr: int, stream: int = 0):
+    """mvr_apply_coarse: the coarse prediction applied to the full-resolution plain step."""
+    rc = load().mvr_apply_coarse(C.c_void_p(psi_next_ptr), (C.c_int * 3)(*dims), C.c_void_p(pred_low_ptr),
+                                 C.c_void_p(psi_low_ptr), C.c_void_p(next_low_ptr), float(cap), C.c_void_p(out_ptr),
+                                 _sp(stream))
+    if rc != OK:
+        raise MvrError(rc, "mvr_apply_coarse")
 
 
 def conv3d_tc(act_ptr, c_act, w_ptr, n_out, bias_ptr, relu, transposed, out_ptr, dims_xyzb, err_ptr, stream=0):
