@@ -457,6 +457,17 @@ __global__ void __launch_bounds__(PairShape<VX, VH>::NT, PairShape<VX, VH>::MINB
 #pragma unroll
             for (int v = 0; v < VX; ++v) row[16 * v] = a[v];
         }
+        // the next item's half plane into L2 while this one is transformed forward
+        {
+            const int next = item + nclusters;
+            if (next < nitems) {
+                const int nbi = next / Pz, nz = next - nbi * Pz;
+                const char *np = reinterpret_cast<const char *>(S + (long long)nbi * Pc + (long long)nz * SH::plane +
+                                                                (long long)rank * SH::half);
+                for (int off = threadIdx.x * 128; off < SH::half * (int)sizeof(float2); off += NT * 128)
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(np + off));
+            }
+        }
         __syncthreads();
         pair_x_p2<VX, VH, false>(sm.A, sm.twx);
         pair_y_forward<VX, VH>(sm.A, sm.twy, sm.posh, rank);
