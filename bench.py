@@ -120,6 +120,13 @@ def _make_small():
     return synthetic.config_small()
 
 
+def _make_pair_case():
+    import synthetic
+
+    return synthetic.make_dataset((480, 480, 120), (0.0, 90.0), (21, 21, 15), n_beads=400, seed=1006,
+                                  side_lobes=True, weights="cosine")
+
+
 def _psf_sizes_6():
     import synthetic
 
@@ -161,6 +168,10 @@ WORKLOADS = {
                                  "6 views 512x512x256 float32, PSFs 21x21x41 ... 41x41x81 per view, "
                                  "Optimization-I, compute blocks 192x192x256 (effective 112-152 x 112-152 x 96-176, "
                                  "uneven edge blocks), Seq", fp64_iters=5),
+    "2view480": lambda: Workload("2view480", (480, 480, 120), 2, (256, 256, 64), [(21, 21, 15)] * 2, 0.006,
+                                 _make_pair_case,
+                                 "2 views 480x480x120 float32, PSF 21x21x15, compute blocks 256x256x64 (36 per view): "
+                                 "a small case of the 256-wide plane kernels, for profiling", fp64_iters=2),
     "8view1024": lambda: Workload("8view1024", (1024, 1024, 512), 8, (256, 256, 256), [(41, 41, 81)] * 8, 0.006,
                                   _make_large,
                                   "8 views 1024x1024x512 (uint16 recorded, converted to float32), 20000 nuclei-like "
@@ -463,6 +474,8 @@ def run_gb300(args, ws, rank, local):
                           lam=W.lam, boundary=boundary, precision=M.PRECISION_FP32, weight_norm=W.weight_norm,
                           batch_blocks=args.batch, device=dev)
     W.setup_blocks(dec)
+    if args.schedule >= 0:
+        dec.set_schedule(args.schedule)
     for v in range(W.views):
         dec.set_view_device(v, d_img[v].data_ptr(), d_w[v].data_ptr(), ds.psfs[v])
     dec.prepare()
@@ -786,6 +799,8 @@ def main():
                          "per-view PSF sizes and uneven edge blocks; 8view1024: 8 views 1024x1024x512, 256^3 "
                          "blocks (volumes synthesised on the device, no e2e line)")
     ap.add_argument("--boundary", choices=["circular", "reference"], default="circular")
+    ap.add_argument("--schedule", type=int, default=-1,
+                    help="force one FFT schedule code for every view (mvr_decon_set_schedule); -1 = autotuned")
     ap.add_argument("--batch", type=int, default=0,
                     help="blocks per batched launch (1..16); 0 = autotuned")
     ap.add_argument("--cpu-steps", type=int, default=2,
