@@ -112,96 +112,6 @@ __device__ __forceinline__ void tp_phase2(float2 *A)
     }
 }
 
-// ---- the y phases on lane pairs ------------------------------------------------------
-// MVR_XY_LANES=1: every DFT item of the y phases (12- or 8-point phase 1, 16-point phase 2) is
-// split over two adjacent lanes: lane h takes the inputs 2 j + h, runs the half-length DFT,
-// lane 1 multiplies by W_2M^k, one shuffle exchanges the halves, lane 0 keeps outputs k < M
-// and lane 1 outputs k + M (radix 2, decimation in time).  Twice the items at half the work
-// each: the 1152- and 1536-item phases fill 1024 threads in rounds of half the latency.
-#ifndef MVR_XY_LANES
-#define MVR_XY_LANES 0
-#endif
-
-// e: this lane's M inputs (indices 2 j + h) -> its M outputs (indices k + M h).  tw[k * step]
-// = W_2M^k (forward).  All 32 lanes of the warp take part.
-template <int M, bool INV>
-__device__ __forceinline__ void dft_lanes(float2 (&e)[M], int h, const float2 *tw, int step)
-{
-    sdft<M, INV>(e);
-    if (h) {
-#pragma unroll
-        for (int k = 1; k < M; ++k) e[k] = cmul(e[k], INV ? cconj(tw[k * step]) : tw[k * step]);
-    }
-#pragma unroll
-    for (int k = 0; k < M; ++k) {
-        float2 q;
-        q.x = __shfl_xor_sync(0xffffffffu, e[k].x, 1);
-        q.y = __shfl_xor_sync(0xffffffffu, e[k].y, 1);
-        e[k] = h ? csub(q, e[k]) : cadd(e[k], q);
-    }
-}
-
-// Phase 1 over NPEN pencils on lane pairs: half-item (pencil p, t, lane h); the V-point DFT of
-// elements t + 16 v with the W_n^(t k1) twiddle (forward after, inverse before the DFT).
-template <int V, int NPEN, int PS, int ES, bool INV, int NT>
-__device__ __forceinline__ void tp_phase1_lanes(float2 *A, const float2 *tw, int twm)
-{
-    constexpr int T = 16, M = V / 2, halves = 2 * NPEN * T;
-    static_assert(V % 2 == 0 && halves % 32 == 0 && NT % 32 == 0, "warp-uniform rounds of lane pairs");
-    for (int hi = threadIdx.x; hi < halves; hi += NT) {
-        const int h = hi & 1, it = hi >> 1, t = it / NPEN, p = it - t * NPEN;
-        float2 *a0 = A + p * PS + t * ES;
-        float2 e[M];
-        if (!INV) {
-#pragma unroll
-            for (int j = 0; j < M; ++j) e[j] = a0[T * (2 * j + h) * ES];
-            dft_lanes<M, false>(e, h, tw, T * twm);  // W_V^k = W_n^(16 k)
-#pragma unroll
-            for (int k = 0; k < M; ++k) {
-                const int k1 = k + M * h;
-                a0[T * k1 * ES] = k1 ? cmul(e[k], tw[t * k1 * twm]) : e[k];
-            }
-        } else {
-#pragma unroll
-            for (int j = 0; j < M; ++j) {
-                const int k1 = 2 * j + h;
-                const float2 b = a0[T * k1 * ES];
-                e[j] = k1 ? cmul(b, cconj(tw[t * k1 * twm])) : b;
-            }
-            dft_lanes<M, true>(e, h, tw, T * twm);
-#pragma unroll
-            for (int k = 0; k < M; ++k) a0[T * (k + M * h) * ES] = e[k];
-        }
-    }
-}
-
-// Phase 2 (16-point DFTs of elements 16 k1 + t) on lane pairs; with RECOMB the items of pencil 0
-// first recombine Y0 + i Ym from pencil 0 and the element at offset m (the inverse y
-// transform of the packed column 0).
-template <int V, int NPEN, int PS, int ES, bool INV, int NT, bool RECOMB = false>
-__device__ __forceinline__ void tp_phase2_lanes(float2 *A, const float2 *tw, int twm, int m = 0)
-{
-    constexpr int T = 16, M = 8, halves = 2 * NPEN * V;
-    static_assert(halves % 32 == 0 && NT % 32 == 0, "warp-uniform rounds of lane pairs");
-    for (int hi = threadIdx.x; hi < halves; hi += NT) {
-        const int h = hi & 1, it = hi >> 1, k1 = it / NPEN, p = it - k1 * NPEN;
-        float2 *b0 = A + p * PS + T * k1 * ES;
-        float2 e[M];
-#pragma unroll
-        for (int j = 0; j < M; ++j) {
-            float2 b = b0[(2 * j + h) * ES];
-            if (RECOMB && p == 0) {
-                const float2 c = b0[(2 * j + h) * ES + m];
-                b = make_float2(b.x - c.y, b.y + c.x);
-            }
-            e[j] = b;
-        }
-        dft_lanes<M, INV>(e, h, tw, V * twm);  // W_16^k = W_n^(V k)
-#pragma unroll
-        for (int k = 0; k < M; ++k) b0[(k + M * h) * ES] = e[k];
-    }
-}
-
 // x phase 1 of one row item (y, t) on registers: a[v] <-> positions t + 16 v of row y.
 // Forward: natural-order values in, twiddled phase-1 output out; inverse the reverse.
 template <int VX, bool INV>
@@ -353,15 +263,9 @@ __device__ __forceinline__ void xy_y(float2 *A, const float2 *twy, const int *po
     typedef XYShape<VX, VY> S;
     constexpr int m = S::m, Py = S::Py, NT = S::NT;
     if (!INV) {
-#if MVR_XY_LANES
-        tp_phase1_lanes<VY, m, 1, S::SR, false, NT>(A, twy, 1);
-        __syncthreads();
-        tp_phase2_lanes<VY, m, 1, S::SR, false, NT>(A, twy, 1);
-#else
         tp_phase1<VY, m, 1, S::SR, false, NT>(A, twy, 1);
         __syncthreads();
         tp_phase2<VY, m, 1, S::SR, false, NT>(A);
-#endif
         __syncthreads();
         for (int k = threadIdx.x; k <= Py / 2; k += NT) {
             const int g = (Py - k) % Py, pk = posy[k], pg = posy[g];
@@ -377,11 +281,6 @@ __device__ __forceinline__ void xy_y(float2 *A, const float2 *twy, const int *po
             }
         }
     } else {
-#if MVR_XY_LANES
-        tp_phase2_lanes<VY, m, 1, S::SR, true, NT, true>(A, twy, 1, m);
-        __syncthreads();
-        tp_phase1_lanes<VY, m, 1, S::SR, true, NT>(A, twy, 1);
-#else
         // phase 2 inverse; the items of column 0 first recombine Y0 + i Ym from columns 0 and m
         constexpr int T = 16, items = m * VY;
         for (int it = threadIdx.x; it < items; it += NT) {
@@ -403,7 +302,6 @@ __device__ __forceinline__ void xy_y(float2 *A, const float2 *twy, const int *po
         }
         __syncthreads();
         tp_phase1<VY, m, 1, S::SR, true, NT>(A, twy, 1);
-#endif
     }
     __syncthreads();
 }
