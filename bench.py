@@ -665,10 +665,12 @@ def run_e2e_block(args, ws, dev, ds, dec, dec_max, workers=2, iters=2):
     ComputeBlockSeqThread.java:54-61) with host buffers, one call per view-block as the
     reference's driver issues them (MultiViewDeconvolutionSeq.java:91-150), from `workers`
     host threads with one block worker each (numParallelBlocks = 2, so one worker's copies
-    overlap the other's kernels).  A call uploads the psi, image and weight block, runs
-    the iteration and returns the psi block and its statistics.  Timed: the calls of each
-    view-step; the driver's own block copies out of and into the volumes
-    (Block.copyBlock / pasteBlock, Java-side) run between them untimed."""
+    overlap the other's kernels).  Like the reference's CUDA block thread, every worker keeps
+    its own psi, image and weight arrays and the driver copies each block into them
+    (Block.copyBlock) before the call and the psi block out after it (pasteBlock); those host
+    copies are the driver's work and run untimed.  A call uploads the three arrays, runs the
+    iteration and returns the psi block and its statistics.  Timed: the calls; a view-step
+    counts the longest of the workers' summed call times (the workers run concurrently)."""
     import concurrent.futures as cf
 
     import cpu_reference as R
@@ -677,7 +679,9 @@ def run_e2e_block(args, ws, dev, ds, dec, dec_max, workers=2, iters=2):
     psi = dec.get_psi()
     wts = [dec.weights(v) for v in range(W.views)]
     boundary = M.BOUNDARY_CIRCULAR
+    shape = (W.block[2], W.block[1], W.block[0])
     wk = [M.BlockWorker(W.block, 1e-4, W.lam, W.views, boundary, dev) for _ in range(workers)]
+    hot = [[np.zeros(shape, np.float32) for _ in range(3)] for _ in range(workers)]  # psi, img, weight per worker
     try:
         for w in wk:
             for v in range(W.views):
@@ -688,46 +692,49 @@ def run_e2e_block(args, ws, dev, ds, dec, dec_max, workers=2, iters=2):
                     R.extract(wts[v], bl["offset"], W.block, "zero")) for bl in grids[v]] for v in range(W.views)]
         pool = cf.ThreadPoolExecutor(max_workers=workers)
         calls = 0
-        call_s = []
+        step_s = []
         per_call = []
         for it in range(1 + iters):
             t_it = 0.0
             for v in range(W.views):
                 pb = [R.extract(psi, bl["offset"], W.block, "mirror") for bl in grids[v]]
-                jobs = list(range(len(pb)))
 
-                def run(j, v=v, pb=pb):
-                    w = wk[j % workers]
-                    im, wt = inputs[v][j]
-                    c0 = time.perf_counter()
-                    w.run_iteration(v, pb[j], im, wt, float(dec_max[v]))
-                    per_call.append(time.perf_counter() - c0)
+                def run(r, v=v, pb=pb):
+                    hp, hi, hw = hot[r]
+                    spent = []
+                    for j in range(r, len(pb), workers):
+                        np.copyto(hp, pb[j])
+                        np.copyto(hi, inputs[v][j][0])
+                        np.copyto(hw, inputs[v][j][1])
+                        c0 = time.perf_counter()
+                        wk[r].run_iteration(v, hp, hi, hw, float(dec_max[v]))
+                        spent.append(time.perf_counter() - c0)
+                        np.copyto(pb[j], hp)
+                    return spent
 
-                t0 = time.perf_counter()
-                # worker j % workers takes block j: each worker's calls stay in order
-                list(pool.map(lambda r: [run(j) for j in jobs[r::workers]], range(workers)))
-                t_it += time.perf_counter() - t0
+                spents = list(pool.map(run, range(workers)))
+                t_it += max(sum(x) for x in spents)
                 for j, bl in enumerate(grids[v]):
                     R.paste(psi, pb[j], bl["eff_offset"], bl["eff_size"], bl["eff_local"])
                 if it:
                     calls += len(pb)
+                    per_call += [x for sp in spents for x in sp]
             if it:
-                call_s.append(t_it)
-            else:
-                per_call.clear()
+                step_s.append(t_it)
         pool.shutdown()
     finally:
         for w in wk:
             w.close()
-    t = float(np.mean(call_s))
+    t = float(np.mean(step_s))
     nb = 4 * W.block[0] * W.block[1] * W.block[2]
     return {"value": ws * W.nvox / t, "unit": UNIT, "h2d_bytes_per_step": 3 * nb * calls // iters,
             "d2h_bytes_per_step": nb * calls // iters, "calls_per_step": calls // iters, "steps": iters,
             "workers": workers, "ms_per_call": 1e3 * float(np.mean(per_call)) if per_call else None,
             "boundary": "circular (the pasted effective regions are the reference boundary's; "
-                                            "the per-block statistics differ)",
-            "note": "timed: the mvr_block_run_seq calls of each view-step with pageable host buffers; the driver's "
-                    "block copies out of / into the volumes run untimed between view-steps"}
+                        "the per-block statistics differ)",
+            "note": "timed: the mvr_block_run_seq calls (pageable host arrays kept per worker, as the reference's "
+                    "CUDA block thread keeps its float[] arrays); the driver's block copies into / out of them and "
+                    "into the volumes run untimed"}
 
 
 def run_psf(args):
