@@ -45,10 +45,13 @@ UNIT = "voxel-iterations/s"
 class Workload:
     """A named deconvolution workload: volume, views, compute block, PSF sizes per view."""
 
-    def __init__(self, name, dims, views, block, psfs, lam, make, desc, psf_type=1, weight_norm=1, fp64_iters=None):
-        # block: one compute block (x, y, z) for every view, or a list with one per view
+    def __init__(self, name, dims, views, block, psfs, lam, make, desc, psf_type=1, weight_norm=1, fp64_iters=None,
+                 effective=None):
+        # block: one compute block (x, y, z) for every view, or a list with one per view;
+        # effective: one effective block for every view (None: block - 2 (k - 1))
         per_view = isinstance(block[0], (tuple, list))
         self.vblocks = [tuple(b) for b in block] if per_view else [tuple(block)] * views
+        self.effective = tuple(effective) if effective else None
         block = self.vblocks[0]
         self.name, self.dims, self.views, self.block, self.psfs, self.lam = name, dims, views, block, psfs, lam
         self.make, self.desc = make, desc
@@ -61,16 +64,31 @@ class Workload:
         import oracle
 
         kk = tuple(2 * k - 1 for k in self.psfs[v])
+        if self.effective:
+            kk = tuple(self.vblocks[v][d] - self.effective[d] + 1 for d in range(3))
         return oracle.divide_into_blocks(self.dims, kk, self.vblocks[v])
+
+    def ref_vblocks(self):
+        """The reference's compute block per view for the same effective grid: effective + 2 (k - 1)."""
+        if not self.effective:
+            return self.vblocks
+        return [tuple(self.effective[d] + 2 * (k[d] - 1) for d in range(3)) for k in self.psfs]
+
+    def ref_blocks(self, v):
+        import oracle
+
+        return oracle.divide_into_blocks(self.dims, tuple(2 * k - 1 for k in self.psfs[v]), self.ref_vblocks()[v])
 
     def per_view_blocks(self):
         return len(set(self.vblocks)) > 1
 
     def setup_blocks(self, d):
-        """Per-view compute blocks on a Deconvolution handle (before prepare)."""
+        """Per-view compute blocks and the effective block on a Deconvolution handle (before prepare)."""
         if self.per_view_blocks():
             for v in range(self.views):
                 d.set_view_block_size(v, self.vblocks[v])
+        if self.effective:
+            d.set_effective_block_size(-1, self.effective)
 
     def view_blocks_per_iter(self):
         return sum(len(self.blocks(v)) for v in range(self.views))
@@ -88,7 +106,8 @@ class Workload:
               f"{mib:.0f} MiB)" if self.flush_l2() else
               f"inputs larger than L2 ({self.views} images + {self.views} weights + psi = {mib:.0f} MiB)")
         blk = [list(b) for b in self.vblocks] if self.per_view_blocks() else list(self.block)
-        return {"workload": self.desc, "views": self.views, "dims": list(self.dims), "block": blk,
+        extra = {"effective_block": list(self.effective)} if self.effective else {}
+        return {"workload": self.desc, "views": self.views, "dims": list(self.dims), "block": blk, **extra,
                 "psf": [list(p) for p in self.psfs] if len(set(self.psfs)) > 1 else list(self.psfs[0]),
                 "lambda": self.lam, "iterations_per_step": 1, "boundary": boundary, "l2": l2,
                 "data": "seeded synthetic beads + ellipsoid, Poisson, background 10"}
@@ -151,6 +170,16 @@ def _blocks_6():
     return [tuple(friendly(128 + 2 * (p[d] - 1), even=d == 0) for d in range(3)) for p in _psf_sizes_6()]
 
 
+def _blocks_6_plane():
+    """The smallest compute blocks at least 128 + 2 (k - 1) per axis with plane kernels:
+    x and y 192 (one CTA per plane) or 256 (a pair of CTAs), z a tile-column length."""
+    def up(n, sizes):
+        return min(s for s in sizes if s >= n)
+
+    return [(up(128 + 2 * (p[0] - 1), (192, 256)), up(128 + 2 * (p[1] - 1), (192, 256)),
+             up(128 + 2 * (p[2] - 1), (192, 256, 288))) for p in _psf_sizes_6()]
+
+
 WORKLOADS = {
     "2view128": lambda: Workload("2view128", (128, 128, 64), 2, (192, 192, 128), [(15, 15, 31)] * 2, 0.0, _make_small,
                                  "2 views 128x128x64 float32, PSF 15x15x31 at 0/90 degrees, efficient-Bayesian, "
@@ -158,11 +187,18 @@ WORKLOADS = {
                                  psf_type=2, weight_norm=0),
     "4view256": lambda: Workload("4view256", (256, 256, 256), 4, (192, 192, 192), [(31, 31, 61)] * 4, 0.006, _make256,
                                  "4 views 256^3 float32, PSF 31x31x61 Optimization-I, blocks 192^3, Seq (OSEM-like)"),
-    "6view512": lambda: Workload("6view512", (512, 512, 256), 6, _blocks_6(), _psf_sizes_6(), 0.006, _make512,
+    "6view512": lambda: Workload("6view512", (512, 512, 256), 6, _blocks_6_plane(), _psf_sizes_6(), 0.006, _make512,
                                  "6 views 512x512x256 float32, PSFs 21x21x41 ... 41x41x81 per view, "
-                                 "Optimization-I, 128^3 effective blocks plus each view's overlap: compute blocks "
-                                 "128 + 2 (k - 1) per axis (rounded up to an FFT-friendly size where needed), "
-                                 "32 blocks per view including uneven edge blocks, Seq", fp64_iters=5),
+                                 "Optimization-I, 128^3 effective blocks (4 x 4 x 2 per view, uneven edge blocks) "
+                                 "plus overlap: compute blocks 192x192x256 (views 0-3) and 256x256x288 (views 4-5), "
+                                 "the smallest plane-kernel shapes >= 128 + 2 (k - 1), Seq", fp64_iters=5,
+                                 effective=(128, 128, 128)),
+    "6view512tight": lambda: Workload("6view512tight", (512, 512, 256), 6, _blocks_6(), _psf_sizes_6(), 0.006,
+                                      _make512,
+                                      "6 views 512x512x256 float32, PSFs 21x21x41 ... 41x41x81 per view, "
+                                      "Optimization-I, 128^3 effective blocks plus exactly each view's overlap: "
+                                      "compute blocks 128 + 2 (k - 1) per axis (168x168x208 ... 208x208x288, rounded "
+                                      "up to an FFT-friendly size where needed), 32 blocks per view, Seq", fp64_iters=5),
     "6view512fixed": lambda: Workload("6view512fixed", (512, 512, 256), 6, (192, 192, 256), _psf_sizes_6(), 0.006,
                                       _make512,
                                  "6 views 512x512x256 float32, PSFs 21x21x41 ... 41x41x81 per view, "
@@ -340,14 +376,16 @@ def cpu_sampler(ds, psi, mx, prep):
     import cpu_reference as R
 
     k1s, k2s, weight_block, image_block, _, _ = prep
-    grids = [W.blocks(v) for v in range(W.views)]
-    return R.BlockSampler(psi, None, None, k1s, k2s, grids, W.vblocks, W.lam, mx, image_block=image_block,
+    # the reference's own blocks: effective + 2 (k - 1), on the same effective grid
+    grids = [W.ref_blocks(v) for v in range(W.views)]
+    return R.BlockSampler(psi, None, None, k1s, k2s, grids, W.ref_vblocks(), W.lam, mx, image_block=image_block,
                           weight_block=weight_block)
 
 
 def cpu_sample_text(steps, sampler):
     P = sampler._convolvers(0)[0].P
-    return (f"{steps} step(s) of one {W.block[0]}x{W.block[1]}x{W.block[2]} block per view (views in order, effective "
+    b = W.ref_vblocks()[0]
+    return (f"{steps} step(s) of one {b[0]}x{b[1]}x{b[2]} block per view (views in order, effective "
             f"regions pasted back into psi), float32 real-to-complex FFTs at the padded size {P[0]}x{P[1]}x{P[2]} "
             f"(util/FFTConvolution), {sampler.workers} host threads; value = voxel-iterations advanced / seconds")
 

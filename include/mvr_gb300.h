@@ -170,6 +170,15 @@ MVR_API int mvr_decon_set_view_device(mvr_decon *h, int view, const float *img, 
  * E + 2 (k_v - 1) per axis gives every view effective blocks of E (the doubled kernel
  * 2 k_v - 1).  Multiplicative mode needs one grid: equal block sizes. */
 MVR_API int mvr_decon_set_view_block_size(mvr_decon *h, int view, const int block_size[3]);
+/* Effective block size of a view (view -1: every view; NULL: back to block - 2 (k - 1)).
+ * No counterpart in the reference, whose effective block is always the block size minus
+ * the doubled kernel (DeconView.java:155-157): here a view's compute block may carry more
+ * overlap than its kernel needs, so that views with different PSF sizes split the volume on
+ * one grid of effective blocks while their compute blocks take FFT shapes with plane
+ * kernels.  block - effective + 1 must be at least 2k - 1 on every axis (checked at
+ * prepare); the effective region of every block sees only voxels within its overlap, so
+ * the result equals the reference's grid of the same effective size. */
+MVR_API int mvr_decon_set_effective_block_size(mvr_decon *h, int view, const int effective[3]);
 /* Replaces a view's image and raw weight (host) without redoing the PSF preparation. */
 MVR_API int mvr_decon_update_images(mvr_decon *h, int view, const float *img, const float *weight);
 /* DeconViews + DeconViewPSF.init, weight normalisation, block grids, PsiInitAvgPrecise. */

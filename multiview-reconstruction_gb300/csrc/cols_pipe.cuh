@@ -132,9 +132,9 @@ __global__ void __launch_bounds__(256, MVR_PIPE_MINB)
             for (int k1 = 0; k1 < V; ++k1) A[(t + T * k1) * NP + c] = a[k1];
         }
         if (MODE != 1) __syncthreads();
-        {  // phase 2: item (c, k1)
-            const int k1 = threadIdx.x / NP;
-            if (k1 < V && live) {
+        // phase 2: items (c, k1), k1 = threadIdx / NP, + 256 / NP, ... (more than one round for V > 16)
+        for (int k1 = threadIdx.x / NP; k1 < V; k1 += 256 / NP) {
+            if (live) {
                 float2 b[T];
 #pragma unroll
                 for (int t = 0; t < T; ++t) b[t] = A[(t + T * k1) * NP + c];
@@ -153,8 +153,8 @@ __global__ void __launch_bounds__(256, MVR_PIPE_MINB)
 #pragma unroll
                 for (int t = 0; t < T; ++t) A[(t + T * k1) * NP + c] = b[t];
             }
-            __syncthreads();
         }
+        __syncthreads();
         if (MODE != 0 && live) {  // phase 1 inverse: item (c, t)
             const int t = threadIdx.x / NP;
             float2 a[V];

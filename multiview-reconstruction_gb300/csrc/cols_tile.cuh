@@ -1,5 +1,5 @@
 // Column passes (y or z axis) as a two-phase register FFT over a shared-memory tile, for
-// FP32 column lengths n = V * 16 (V = 4, 6, 8, 12, 16: n = 64 ... 256).
+// FP32 column lengths n = V * 16 (V = 4, 6, 8, 12, 16, 18: n = 64 ... 288).
 //
 // With n = V * T (T = 16), column element i = t + T v (t < T, v < V):
 //   phase 1, item (column, t):  V-point DFT over v of x[t + T v], times W_n^(t k1),
@@ -91,6 +91,64 @@ __device__ __forceinline__ void dft16(float2 *v)
     }
 }
 
+// 9 = 3 x 3 (Cooley-Tukey): inner 3-point DFTs over q = 3 q1 + q2, twiddle W9^(q2 k1), outer
+// 3-point DFTs; output k = k1 + 3 k2.
+template <bool INV>
+__device__ __forceinline__ void dft9(float2 *v)
+{
+    float2 u[3][3];
+#pragma unroll
+    for (int q2 = 0; q2 < 3; ++q2) {
+#pragma unroll
+        for (int q1 = 0; q1 < 3; ++q1) u[q2][q1] = v[3 * q1 + q2];
+        dft3<INV>(u[q2]);
+    }
+    const float sg = INV ? 1.0f : -1.0f;
+    // W9^j = (cos(2 pi j / 9), -+ sin(2 pi j / 9)), j = 1, 2, 4
+    const float2 w1 = make_float2(0.76604444311897804f, sg * 0.64278760968653933f);
+    const float2 w2 = make_float2(0.17364817766693035f, sg * 0.98480775301220806f);
+    const float2 w4 = make_float2(-0.93969262078590838f, sg * 0.34202014332566873f);
+    u[1][1] = cmul(u[1][1], w1);
+    u[1][2] = cmul(u[1][2], w2);
+    u[2][1] = cmul(u[2][1], w2);
+    u[2][2] = cmul(u[2][2], w4);
+#pragma unroll
+    for (int k1 = 0; k1 < 3; ++k1) {
+        float2 w[3] = {u[0][k1], u[1][k1], u[2][k1]};
+        dft3<INV>(w);
+#pragma unroll
+        for (int k2 = 0; k2 < 3; ++k2) v[k1 + 3 * k2] = w[k2];
+    }
+}
+
+// 18 = 2 x 9: the 9-point DFTs of the even and odd inputs, X[k] = E[k] + W18^k O[k],
+// X[k + 9] = E[k] - W18^k O[k].
+template <bool INV>
+__device__ __forceinline__ void dft18(float2 *v)
+{
+    float2 e[9], o[9];
+#pragma unroll
+    for (int j = 0; j < 9; ++j) {
+        e[j] = v[2 * j];
+        o[j] = v[2 * j + 1];
+    }
+    dft9<INV>(e);
+    dft9<INV>(o);
+    const float sg = INV ? 1.0f : -1.0f;
+    // W18^k = (cos(pi k / 9), -+ sin(pi k / 9)), k = 1 .. 8
+    const float c[8] = {0.93969262078590838f, 0.76604444311897804f, 0.5f, 0.17364817766693035f,
+                        -0.17364817766693035f, -0.5f, -0.76604444311897804f, -0.93969262078590838f};
+    const float sn[8] = {0.34202014332566873f, 0.64278760968653933f, 0.86602540378443865f, 0.98480775301220806f,
+                         0.98480775301220806f, 0.86602540378443865f, 0.64278760968653933f, 0.34202014332566873f};
+#pragma unroll
+    for (int k = 1; k < 9; ++k) o[k] = cmul(o[k], make_float2(c[k - 1], sg * sn[k - 1]));
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        v[k] = cadd(e[k], o[k]);
+        v[k + 9] = csub(e[k], o[k]);
+    }
+}
+
 template <int N, bool INV>
 __device__ __forceinline__ void sdft(float2 (&a)[N])
 {
@@ -98,6 +156,7 @@ __device__ __forceinline__ void sdft(float2 (&a)[N])
     else if constexpr (N == 6) dft6<INV>(a);
     else if constexpr (N == 8) dft8<INV>(a);
     else if constexpr (N == 12) dft12<INV>(a);
+    else if constexpr (N == 18) dft18<INV>(a);
     else dft16<INV>(a);
 }
 
@@ -118,8 +177,9 @@ constexpr int kTColNP = 16;  // columns per tile
 // NP columns per tile with 16 NP threads (NP = 16: 256 threads, 3 CTAs per SM).  Measured on
 // GB300 for the 192-long Z pass: 32-column tiles (512 threads, 256-byte row segments, 2 CTAs
 // per SM) ran at 3.5 TB/s against 4.5 TB/s for 16-column tiles.
+// The 288-long columns (V = 18) take 2 CTAs per SM: at 3 the 18-point transforms spill.
 template <int V, int MODE, int NP = kTColNP>
-__global__ void __launch_bounds__(16 * NP, NP == 16 ? MVR_TCOLS_MINB : 2)
+__global__ void __launch_bounds__(16 * NP, (NP == 16 && V <= 16) ? MVR_TCOLS_MINB : 2)
     k_tcols(const float2 *src, float2 *dst, const float2 *__restrict__ Kh, int Hx, long long estride,
             long long ostride, long long Pc, const float2 *__restrict__ twg, int gather, int nother, int rlo, int rhi,
             int olo)
@@ -197,9 +257,9 @@ __global__ void __launch_bounds__(16 * NP, NP == 16 ? MVR_TCOLS_MINB : 2)
         for (int k1 = 0; k1 < V; ++k1) A[(t + T * k1) * NP + c] = a[k1];
     }
     if (MODE != 1) __syncthreads();
-    {  // phase 2: item (c, k1)
-        const int k1 = threadIdx.x / NP;
-        if (k1 < V && live) {
+    // phase 2: items (c, k1), k1 = threadIdx / NP, + NT / NP, ... (more than one round for V > 16)
+    for (int k1 = threadIdx.x / NP; k1 < V; k1 += NT / NP) {
+        if (live) {
             float2 b[T];
 #pragma unroll
             for (int t = 0; t < T; ++t) b[t] = A[(t + T * k1) * NP + c];
@@ -218,8 +278,8 @@ __global__ void __launch_bounds__(16 * NP, NP == 16 ? MVR_TCOLS_MINB : 2)
 #pragma unroll
             for (int t = 0; t < T; ++t) A[(t + T * k1) * NP + c] = b[t];
         }
-        __syncthreads();
     }
+    __syncthreads();
     if (MODE != 0 && live) {  // phase 1 inverse: item (c, t)
         const int t = threadIdx.x / NP;
         float2 a[V];

@@ -408,6 +408,7 @@ public:
     virtual int set_images(int v, const float *img, const float *w, bool on_device) = 0;
     virtual int set_psf(int v, const float *psf, const int dims[3]) = 0;
     virtual int set_view_block(int v, const int block[3]) = 0;
+    virtual int set_view_effective(int v, const int eff[3]) = 0;
     virtual int prepare() = 0;
     virtual int set_psi(const float *psi, bool on_device) = 0;
     virtual int get_psi(float *psi) = 0;
@@ -444,6 +445,7 @@ public:
     int set_images(int v, const float *img, const float *w, bool on_device) override;
     int set_psf(int v, const float *psf, const int dims[3]) override;
     int set_view_block(int v, const int block[3]) override;
+    int set_view_effective(int v, const int eff[3]) override;
     int prepare() override;
     int set_psi(const float *psi, bool on_device) override;
     int get_psi(float *psi) override;
@@ -471,6 +473,7 @@ private:
         std::vector<float> psf;
         int kd[3] = {0, 0, 0};
         int block[3] = {0, 0, 0};            // compute block size of this view (0: the handle's)
+        int eff[3] = {0, 0, 0};              // effective block size (0: block - 2 (k - 1))
         float *k1 = nullptr, *k2 = nullptr;  // device, prepared kernels
         Plan<T> plan;
         const int *bsize(const int *dflt) const { return block[0] > 0 ? block : dflt; }
@@ -695,6 +698,23 @@ int Decon<T>::set_view_block(int v, const int block[3])
 }
 
 template <typename T>
+int Decon<T>::set_view_effective(int v, const int eff[3])
+{
+    if (v < -1 || v >= p_.num_views) return fail(MVR_ERR_ARG, "view out of range");
+    for (int u = (v < 0 ? 0 : v); u < (v < 0 ? p_.num_views : v + 1); ++u) {
+        if (!eff) {
+            std::memset(views_[u].eff, 0, sizeof(views_[u].eff));
+        } else {
+            for (int d = 0; d < 3; ++d)
+                if (eff[d] < 1) return fail(MVR_ERR_ARG, "effective block sizes must be >= 1");
+            std::memcpy(views_[u].eff, eff, sizeof(views_[u].eff));
+        }
+    }
+    prepared_ = false;
+    return MVR_OK;
+}
+
+template <typename T>
 int Decon<T>::norm_to_sum1(float *k, long long n)
 {
     const long long first = p_.psf_norm_threads > 0 ? first_portion(n, p_.psf_norm_threads) : 0;
@@ -844,7 +864,8 @@ int Decon<T>::prepare()
                 return fail(MVR_ERR_ARG, "multiplicative mode needs one block grid: equal PSF sizes "
                                          "(MultiViewDeconvolutionMul.testBlockIntegrity)");
         for (int v = 1; v < nv; ++v)
-            if (std::memcmp(views_[v].bsize(p_.block_size), views_[0].bsize(p_.block_size), 3 * sizeof(int)) != 0)
+            if (std::memcmp(views_[v].bsize(p_.block_size), views_[0].bsize(p_.block_size), 3 * sizeof(int)) != 0 ||
+                std::memcmp(views_[v].eff, views_[0].eff, sizeof(views_[0].eff)) != 0)
                 return fail(MVR_ERR_ARG, "multiplicative mode needs one block grid: equal block sizes");
     }
     // weights
@@ -871,20 +892,33 @@ int Decon<T>::prepare()
     jacobi_.assign(steps, 1);
     for (int st = 0; st < steps; ++st) {
         const View &vw = views_[st];
-        int kk[3];
-        for (int d = 0; d < 3; ++d) kk[d] = 2 * vw.kd[d] - 1;
         std::vector<BlockDesc> all;
         const int *bs = vw.bsize(p_.block_size);
+        // the grid's overlap: the doubled kernel 2k-1, or block - effective + 1 when an
+        // effective block size is set (at least the doubled kernel)
+        int kk[3];
+        for (int d = 0; d < 3; ++d) {
+            kk[d] = 2 * vw.kd[d] - 1;
+            if (vw.eff[0] > 0) {
+                if (bs[d] - vw.eff[d] + 1 < kk[d])
+                    return fail(MVR_ERR_ARG, "effective block leaves less overlap than the doubled kernel (2k-1)");
+                kk[d] = bs[d] - vw.eff[d] + 1;
+            }
+        }
         if (!divide_blocks(D, kk, bs, all, sort_dim_[st]))
             return fail(MVR_ERR_ARG, "block size smaller than the doubled kernel (2k-1)");
         const float *wcheck = views_[st].w;  // Mul: view 0's grid and weight
         std::vector<int> keep(all.size(), 1);
         if (p_.filter_blocks && !all.empty()) {
-            // one launch over all blocks of the step, one copy of the flags back
+            // one launch over all blocks of the step, one copy of the flags back.  The region
+            // checked is the reference's block, effective + 2 (k - 1) around the effective
+            // region (the compute block itself unless an effective size is set)
             const int nb = (int)all.size();
+            int cs[3];
+            for (int d = 0; d < 3; ++d) cs[d] = vw.eff[0] > 0 ? vw.eff[d] + 2 * (vw.kd[d] - 1) : bs[d];
             std::vector<long long> offs(3 * (size_t)nb);
             for (int b = 0; b < nb; ++b)
-                for (int d = 0; d < 3; ++d) offs[3 * (size_t)b + d] = all[b].off[d];
+                for (int d = 0; d < 3; ++d) offs[3 * (size_t)b + d] = all[b].eoff[d] - (vw.kd[d] - 1);
             long long *d_offs = nullptr;
             int *d_flags = nullptr;
             D_CUDA(cudaMalloc(&d_offs, sizeof(long long) * offs.size()));
@@ -897,9 +931,9 @@ int Decon<T>::prepare()
                                             cudaMemcpyHostToDevice, s);
             if (e == cudaSuccess) e = cudaMemsetAsync(d_flags, 0, sizeof(int) * (size_t)nb, s);
             if (e == cudaSuccess) {
-                const long long bn = (long long)bs[0] * bs[1] * bs[2];
+                const long long bn = (long long)cs[0] * cs[1] * cs[2];
                 const int gx = (int)std::max<long long>(1, std::min<long long>((bn + 255) / 256, 64));
-                k_block_content<<<dim3(gx, nb), 256, 0, s>>>(wcheck, D[0], D[1], D[2], d_offs, bs[0], bs[1], bs[2],
+                k_block_content<<<dim3(gx, nb), 256, 0, s>>>(wcheck, D[0], D[1], D[2], d_offs, cs[0], cs[1], cs[2],
                                                             d_flags);
                 e = cudaGetLastError();
             }
@@ -1676,6 +1710,11 @@ extern "C" int mvr_decon_tuning(const mvr_decon *h, int capacity, int *step, int
 extern "C" int mvr_decon_set_view_block_size(mvr_decon *h, int view, const int block_size[3])
 {
     return h ? h->impl->set_view_block(view, block_size) : MVR_ERR_ARG;
+}
+
+extern "C" int mvr_decon_set_effective_block_size(mvr_decon *h, int view, const int effective[3])
+{
+    return h ? h->impl->set_view_effective(view, effective) : MVR_ERR_ARG;
 }
 
 extern "C" int mvr_decon_update_images(mvr_decon *h, int view, const float *img, const float *weight)

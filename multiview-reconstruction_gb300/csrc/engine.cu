@@ -172,6 +172,10 @@ int Engine<T>::cuda_check(cudaError_t e, const char *what)
             constexpr int V_ = 12;            \
             __VA_ARGS__;                      \
         } break;                              \
+        case 18: {                            \
+            constexpr int V_ = 18;            \
+            __VA_ARGS__;                      \
+        } break;                              \
         default: {                            \
             constexpr int V_ = 16;            \
             __VA_ARGS__;                      \
@@ -284,6 +288,7 @@ void set_smem_limits()
         set_smem_limits_tcols<8>(m);
         set_smem_limits_tcols<12>(m);
         set_smem_limits_tcols<16>(m);
+        set_smem_limits_tcols<18>(m);
     });
 }
 
@@ -293,7 +298,7 @@ int tile_col_v(int n)
 {
     if (sizeof(T) != sizeof(float) || n % 16) return 0;
     const int v = n / 16;
-    return (v == 4 || v == 6 || v == 8 || v == 12 || v == 16) ? v : 0;
+    return (v == 4 || v == 6 || v == 8 || v == 12 || v == 16 || v == 18) ? v : 0;
 }
 
 // Warp-shuffle column radix for an FP32 axis of length n (0: shared-memory kernels).

@@ -58,7 +58,7 @@ struct Plan {
     bool big = false;  // some axis needs radix 7, 11 or 13
     int wr = 0;        // FP32 rows of Px = 64 wr reals (wr = 2, 3, 4) take the warp-shuffle row kernels
     int wcy = 0, wcz = 0;  // FP32 columns of 32 wc (wc = 2, 3, 4, 5, 6, 8) take the warp-shuffle column kernels
-    int tcy = 0, tcz = 0;  // FP32 columns of 16 tc (tc = 4, 6, 8, 12, 16) take the two-phase tile kernels (preferred)
+    int tcy = 0, tcz = 0;  // FP32 columns of 16 tc (tc = 4, 6, 8, 12, 16, 18) take the two-phase tile kernels (preferred)
     int xy = 0;            // plane kernels (x and y fused per z-plane): shape code, 0 = row / column kernels
     size_t smem_row = 0, smem_coly = 0, smem_colz = 0;
     // FFT schedule (chosen by the autotuner of the whole-volume driver, or forced):

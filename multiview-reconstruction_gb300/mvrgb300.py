@@ -40,7 +40,8 @@ EXPORTS = [
     "mvr_block_create", "mvr_block_destroy", "mvr_block_last_error", "mvr_block_set_kernels",
     "mvr_block_run_seq", "mvr_block_run_mul", "mvr_block_run_seq_device", "mvr_block_synchronize",
     "mvr_decon_create", "mvr_decon_destroy", "mvr_decon_last_error", "mvr_decon_set_view",
-    "mvr_decon_set_view_device", "mvr_decon_set_view_block_size", "mvr_decon_update_images", "mvr_decon_prepare", "mvr_decon_set_psi",
+    "mvr_decon_set_view_device", "mvr_decon_set_view_block_size", "mvr_decon_set_effective_block_size",
+    "mvr_decon_update_images", "mvr_decon_prepare", "mvr_decon_set_psi",
     "mvr_decon_set_psi_device", "mvr_decon_get_psi", "mvr_decon_get_psi_device", "mvr_decon_run", "mvr_decon_get_kernels",
     "mvr_decon_get_max", "mvr_decon_get_weights", "mvr_decon_psi_device", "mvr_decon_synchronize",
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
@@ -138,6 +139,7 @@ def load() -> C.CDLL:
     L.mvr_decon_set_view_device.argtypes = [P, C.c_int, P, P, P, P]
     L.mvr_decon_update_images.argtypes = [P, C.c_int, P, P]
     L.mvr_decon_set_view_block_size.argtypes = [P, C.c_int, P]
+    L.mvr_decon_set_effective_block_size.argtypes = [P, C.c_int, P]
     L.mvr_decon_set_schedule.argtypes = [P, C.c_int]
     L.mvr_decon_schedule.argtypes = [P, C.c_int]
     L.mvr_decon_tuning.argtypes = [P, C.c_int, P, P, P, P]
@@ -386,6 +388,12 @@ class Deconvolution:
         """Compute block size (x, y, z) of one view (None: the handle's), before prepare()."""
         self._check(self._lib.mvr_decon_set_view_block_size(self._h, view,
                                                             (C.c_int * 3)(*block_size) if block_size else None))
+
+    def set_effective_block_size(self, view, effective):
+        """Effective block size (x, y, z) of one view (view -1: every view; None: block - 2 (k - 1)),
+        before prepare(): the compute block then carries block - effective of overlap."""
+        self._check(self._lib.mvr_decon_set_effective_block_size(self._h, view,
+                                                                (C.c_int * 3)(*effective) if effective else None))
 
     def update_images(self, view, img, weight):
         img, w = _f32(img), _f32(weight)

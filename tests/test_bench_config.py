@@ -18,12 +18,26 @@ def test_workload_block_grids():
     # effective sizes 192 - 2(k-1): 152 ... 112 in x/y, 256 - 2(k-1): 176 ... 96 in z
     assert [len(w.blocks(v)) for v in range(6)] == [32, 32, 32, 32, 75, 75]
     # 128^3 effective blocks plus each view's overlap: 4 x 4 x 2 blocks in every view
-    w = bench.WORKLOADS["6view512"]()
+    w = bench.WORKLOADS["6view512tight"]()
     assert w.per_view_blocks() and [len(w.blocks(v)) for v in range(6)] == [32] * 6
     for v, k in enumerate(w.psfs):
         b = w.vblocks[v]
         assert all(b[d] >= 128 + 2 * (k[d] - 1) for d in range(3))
         assert all(w.blocks(v)[0]["eff_size"][d] >= 128 for d in range(3))  # the last block may be clipped
+    # the same effective grid with plane-kernel compute blocks: every block's effective
+    # region where the reference's blocks (effective + 2 (k - 1)) put it, centred in a
+    # compute block with at least k - 1 of overlap on each side
+    w = bench.WORKLOADS["6view512"]()
+    assert w.vblocks == [(192, 192, 256)] * 4 + [(256, 256, 288)] * 2 and w.effective == (128, 128, 128)
+    for v, k in enumerate(w.psfs):
+        g, r = w.blocks(v), w.ref_blocks(v)
+        assert len(g) == 32 and w.ref_vblocks()[v] == tuple(128 + 2 * (k[d] - 1) for d in range(3))
+        assert [(b["eff_offset"], b["eff_size"]) for b in g] == [(b["eff_offset"], b["eff_size"]) for b in r]
+        for b in g:
+            for d in range(3):
+                lo = b["eff_offset"][d] - b["offset"][d]
+                hi = w.vblocks[v][d] - lo - b["eff_size"][d]
+                assert lo >= k[d] - 1 and hi >= k[d] - 1
     w = bench.WORKLOADS["8view1024"]()
     assert [len(w.blocks(v)) for v in range(8)] == [216] * 8
 
