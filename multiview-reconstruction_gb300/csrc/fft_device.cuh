@@ -52,6 +52,45 @@ __device__ __forceinline__ V cmul(V a, V b) { return cx<V>(a.x * b.x - a.y * b.y
 template <bool INV, typename V>
 __device__ __forceinline__ V mul_j(V a) { return INV ? cx<V>(-a.y, a.x) : cx<V>(a.y, -a.x); }
 
+// FP32 complex additions and real scalings on the paired FP32 instructions of sm_100 and
+// later (one instruction for both components, rounded to nearest like the scalar ones).
+// MVR_PAIRED_FP=0 keeps the scalar forms.
+#ifndef MVR_PAIRED_FP
+#define MVR_PAIRED_FP 1
+#endif
+#if MVR_PAIRED_FP && defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+template <> __device__ __forceinline__ float2 cadd<float2>(float2 a, float2 b) { return __fadd2_rn(a, b); }
+template <> __device__ __forceinline__ float2 csub<float2>(float2 a, float2 b)
+{
+    return __fadd2_rn(a, make_float2(-b.x, -b.y));
+}
+template <> __device__ __forceinline__ float2 cscale<float2>(float2 a, float s)
+{
+    return __fmul2_rn(a, make_float2(s, s));
+}
+// a - s b with one fused paired instruction
+__device__ __forceinline__ float2 csub_scaled(float2 a, float2 b, float s)
+{
+    return __ffma2_rn(b, make_float2(-s, -s), a);
+}
+#endif
+template <typename V>
+__device__ __forceinline__ V csub_scaled(V a, V b, typename Re<V>::t s) { return csub(a, cscale(b, s)); }
+
+// t +- (-+i) d component-wise (the rotated operand never forms a swizzled pair):
+// returns t + mul_j(d) in p and t - mul_j(d) in q
+template <bool INV, typename V>
+__device__ __forceinline__ void add_sub_j(V t, V d, V &p, V &q)
+{
+    if (INV) {
+        p = cx<V>(t.x - d.y, t.y + d.x);
+        q = cx<V>(t.x + d.y, t.y - d.x);
+    } else {
+        p = cx<V>(t.x + d.y, t.y - d.x);
+        q = cx<V>(t.x - d.y, t.y + d.x);
+    }
+}
+
 // ---- small DFTs (constants are the exact roots of unity of each radix) -------------
 template <bool INV, typename V> __device__ __forceinline__ void dft2(V *v)
 {
@@ -65,21 +104,26 @@ template <bool INV, typename V> __device__ __forceinline__ void dft3(V *v)
     typedef typename Re<V>::t T;
     const T s3 = (T)0.86602540378443864676;  // sin(2 pi / 3)
     V t1 = cadd(v[1], v[2]);
-    V m = csub(v[0], cscale(t1, (T)0.5));
-    V d = cscale(mul_j<INV>(csub(v[1], v[2])), s3);
+    V m = csub_scaled(v[0], t1, (T)0.5);
+    V e = csub(v[1], v[2]);
     v[0] = cadd(v[0], t1);
-    v[1] = cadd(m, d);
-    v[2] = csub(m, d);
+    // m +- s3 mul_j(e), component-wise
+    if (INV) {
+        v[1] = cx<V>(m.x - s3 * e.y, m.y + s3 * e.x);
+        v[2] = cx<V>(m.x + s3 * e.y, m.y - s3 * e.x);
+    } else {
+        v[1] = cx<V>(m.x + s3 * e.y, m.y - s3 * e.x);
+        v[2] = cx<V>(m.x - s3 * e.y, m.y + s3 * e.x);
+    }
 }
 
 template <bool INV, typename V> __device__ __forceinline__ void dft4(V *v)
 {
     V t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
-    V t2 = cadd(v[1], v[3]), t3 = mul_j<INV>(csub(v[1], v[3]));
+    V t2 = cadd(v[1], v[3]), d = csub(v[1], v[3]);
     v[0] = cadd(t0, t2);
-    v[1] = cadd(t1, t3);
     v[2] = csub(t0, t2);
-    v[3] = csub(t1, t3);
+    add_sub_j<INV>(t1, d, v[1], v[3]);
 }
 
 template <bool INV, typename V> __device__ __forceinline__ void dft5(V *v)

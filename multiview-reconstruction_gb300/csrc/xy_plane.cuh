@@ -151,87 +151,109 @@ __device__ __forceinline__ float2 xy_split_one(float2 zf, float2 zg, int f, cons
     return make_float2(e.x - q.y, e.y + q.x);
 }
 
+// One item (y, k1) of x phase 2 with the split / merge: b holds its 16 values, read from b0;
+// the results go back to b0.  All 32 lanes of the warp take part (the partner item's values
+// come over shuffles).
 template <int VX, int VY, bool INV>
-__device__ __forceinline__ void xy_x_p2_split(float2 *A, const float2 *twx)
+__device__ __forceinline__ void xy_x_p2_item(float2 (&b)[16], float2 *b0, int k1, int h, bool selfgrp,
+                                             const float2 *twx)
+{
+    constexpr int T = 16;
+    if (!INV) sdft<T, false>(b);  // b[k2] = Z[k1 + V k2]
+    if (!selfgrp) {
+        // partner item V - k1 in lane ^ 16: frequency m - f sits at its slot 15 - k2
+#pragma unroll
+        for (int k2 = 0; k2 < T / 2; ++k2) {
+            const int k3 = T - 1 - k2;
+            float2 ga, gb;
+            ga.x = __shfl_xor_sync(0xffffffffu, b[k3].x, 16);
+            ga.y = __shfl_xor_sync(0xffffffffu, b[k3].y, 16);
+            gb.x = __shfl_xor_sync(0xffffffffu, b[k2].x, 16);
+            gb.y = __shfl_xor_sync(0xffffffffu, b[k2].y, 16);
+            const float2 oa = xy_split_one<VX, VY, INV>(b[k2], ga, k1 + VX * k2, twx);
+            const float2 ob = xy_split_one<VX, VY, INV>(b[k3], gb, k1 + VX * k3, twx);
+            if (INV) {
+                b[k2] = oa;
+                b[k3] = ob;
+            } else {  // forward: straight back to shared memory
+                b0[k2] = oa;
+                b0[k3] = ob;
+            }
+        }
+    } else if (h == 0) {  // k1 = 0: f = V k2 pairs with slot 16 - k2; slot 8 is m / 2
+        const float2 o0 = xy_split_one<VX, VY, INV>(b[0], b[0], 0, twx);
+        const float2 o8 = xy_split_one<VX, VY, INV>(b[8], b[8], VX * 8, twx);
+        if (INV) {
+            b[0] = o0;
+            b[8] = o8;
+        } else {
+            b0[0] = o0;
+            b0[8] = o8;
+        }
+#pragma unroll
+        for (int k2 = 1; k2 < T / 2; ++k2) {
+            const int k3 = T - k2;
+            const float2 oa = xy_split_one<VX, VY, INV>(b[k2], b[k3], VX * k2, twx);
+            const float2 ob = xy_split_one<VX, VY, INV>(b[k3], b[k2], VX * k3, twx);
+            if (INV) {
+                b[k2] = oa;
+                b[k3] = ob;
+            } else {  // forward: straight back to shared memory
+                b0[k2] = oa;
+                b0[k3] = ob;
+            }
+        }
+    } else {  // k1 = V / 2: slot k2 pairs with slot 15 - k2
+#pragma unroll
+        for (int k2 = 0; k2 < T / 2; ++k2) {
+            const int k3 = T - 1 - k2;
+            const float2 oa = xy_split_one<VX, VY, INV>(b[k2], b[k3], VX / 2 + VX * k2, twx);
+            const float2 ob = xy_split_one<VX, VY, INV>(b[k3], b[k2], VX / 2 + VX * k3, twx);
+            if (INV) {
+                b[k2] = oa;
+                b[k3] = ob;
+            } else {  // forward: straight back to shared memory
+                b0[k2] = oa;
+                b0[k3] = ob;
+            }
+        }
+    }
+    if (INV) {
+        sdft<T, true>(b);
+#pragma unroll
+        for (int t = 0; t < T; ++t) b0[t] = b[t];
+    }
+}
+
+// x phase 2 items of the rows [y0, y0 + NR): item it (warp-aligned) is row y of a block of 16
+// rows; half-warp h holds k1, the other half its partner V - k1 (or the self-paired k1 = 0 and
+// V / 2 in the last group), for threads i0, i0 + step, ... of the items.
+template <int VX, int VY, bool INV, int NR>
+__device__ __forceinline__ void xy_x_p2_rows(float2 *A, const float2 *twx, int y0, int i0, int step)
 {
     typedef XYShape<VX, VY> S;
-    constexpr int T = 16, Py = S::Py, NT = S::NT, RB = Py / 16, items = Py * VX;
-    static_assert(Py % 16 == 0 && VX % 2 == 0 && items % 32 == 0 && NT % 32 == 0, "whole warps of row pairs");
-    for (int it = threadIdx.x; it < items; it += NT) {
+    constexpr int T = 16, RB = NR / 16, items = NR * VX;
+    static_assert(NR % 16 == 0 && VX % 2 == 0 && items % 32 == 0, "whole warps of row pairs");
+    for (int it = i0; it < items; it += step) {
         const int l = it & 31, grp = it >> 5;
         const int h = l >> 4, jp = grp / RB;
-        const int y = (grp - jp * RB) * 16 + (l & 15);
+        const int y = y0 + (grp - jp * RB) * 16 + (l & 15);
         const bool selfgrp = jp == VX / 2 - 1;  // the same for the whole warp
         const int k1 = selfgrp ? (h ? VX / 2 : 0) : (h ? VX - 1 - jp : 1 + jp);
         float2 *b0 = A + y * S::SR + T * k1;
         float2 b[T];
 #pragma unroll
         for (int t = 0; t < T; ++t) b[t] = b0[t];
-        if (!INV) sdft<T, false>(b);  // b[k2] = Z[k1 + V k2]
-        if (!selfgrp) {
-            // partner item V - k1 in lane ^ 16: frequency m - f sits at its slot 15 - k2
-#pragma unroll
-            for (int k2 = 0; k2 < T / 2; ++k2) {
-                const int k3 = T - 1 - k2;
-                float2 ga, gb;
-                ga.x = __shfl_xor_sync(0xffffffffu, b[k3].x, 16);
-                ga.y = __shfl_xor_sync(0xffffffffu, b[k3].y, 16);
-                gb.x = __shfl_xor_sync(0xffffffffu, b[k2].x, 16);
-                gb.y = __shfl_xor_sync(0xffffffffu, b[k2].y, 16);
-                const float2 oa = xy_split_one<VX, VY, INV>(b[k2], ga, k1 + VX * k2, twx);
-                const float2 ob = xy_split_one<VX, VY, INV>(b[k3], gb, k1 + VX * k3, twx);
-                if (INV) {
-                    b[k2] = oa;
-                    b[k3] = ob;
-                } else {  // forward: straight back to shared memory
-                    b0[k2] = oa;
-                    b0[k3] = ob;
-                }
-            }
-        } else if (h == 0) {  // k1 = 0: f = V k2 pairs with slot 16 - k2; slot 8 is m / 2
-            const float2 o0 = xy_split_one<VX, VY, INV>(b[0], b[0], 0, twx);
-            const float2 o8 = xy_split_one<VX, VY, INV>(b[8], b[8], VX * 8, twx);
-            if (INV) {
-                b[0] = o0;
-                b[8] = o8;
-            } else {
-                b0[0] = o0;
-                b0[8] = o8;
-            }
-#pragma unroll
-            for (int k2 = 1; k2 < T / 2; ++k2) {
-                const int k3 = T - k2;
-                const float2 oa = xy_split_one<VX, VY, INV>(b[k2], b[k3], VX * k2, twx);
-                const float2 ob = xy_split_one<VX, VY, INV>(b[k3], b[k2], VX * k3, twx);
-                if (INV) {
-                    b[k2] = oa;
-                    b[k3] = ob;
-                } else {  // forward: straight back to shared memory
-                    b0[k2] = oa;
-                    b0[k3] = ob;
-                }
-            }
-        } else {  // k1 = V / 2: slot k2 pairs with slot 15 - k2
-#pragma unroll
-            for (int k2 = 0; k2 < T / 2; ++k2) {
-                const int k3 = T - 1 - k2;
-                const float2 oa = xy_split_one<VX, VY, INV>(b[k2], b[k3], VX / 2 + VX * k2, twx);
-                const float2 ob = xy_split_one<VX, VY, INV>(b[k3], b[k2], VX / 2 + VX * k3, twx);
-                if (INV) {
-                    b[k2] = oa;
-                    b[k3] = ob;
-                } else {  // forward: straight back to shared memory
-                    b0[k2] = oa;
-                    b0[k3] = ob;
-                }
-            }
-        }
-        if (INV) {
-            sdft<T, true>(b);
-#pragma unroll
-            for (int t = 0; t < T; ++t) b0[t] = b[t];
-        }
+        xy_x_p2_item<VX, VY, INV>(b, b0, k1, h, selfgrp, twx);
     }
+}
+
+template <int VX, int VY, bool INV>
+__device__ __forceinline__ void xy_x_p2_split(float2 *A, const float2 *twx)
+{
+    typedef XYShape<VX, VY> S;
+    static_assert(S::NT % 32 == 0, "whole warps");
+    xy_x_p2_rows<VX, VY, INV, S::Py>(A, twx, 0, threadIdx.x, S::NT);
 }
 
 // x phase 2 (forward), then the packed-real split in tile order.  The DC and Nyquist
