@@ -660,8 +660,10 @@ def run_gb300(args, ws, rank, local):
 
 
 def run_e2e(args, ws, dev, ds, dec, shape, boundary):
-    """The public C ABI with pinned host buffers: every step uploads the images, the raw
-    weights and psi, runs one iteration and reads psi back (mvr_decon_run_host)."""
+    """The public C ABI with pinned host buffers: every step uploads psi, runs one iteration
+    and reads psi back, and uploads the images and raw weights of the next step while its
+    iteration runs (mvr_decon_run_host_next; the first timed step's set came up during the
+    last warm-up step, the last timed step's set is uploaded inside the timed region)."""
     import torch
 
     import mvrgb300 as M
@@ -682,13 +684,14 @@ def run_e2e(args, ws, dev, ds, dec, shape, boundary):
     imgs = [a.numpy() for a in h_img]
     wts = [a.numpy() for a in h_w]
     for _ in range(min(2, args.warmup)):
-        e2e_dec.run_host(1, imgs, wts, out)
+        e2e_dec.run_host(1, imgs, wts, out, imgs, wts)
     barrier(ws)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        # mvr_decon_run_host: uploads (weights and psi, then the images overlapping the first
-        # view-steps), one iteration, psi back
-        e2e_dec.run_host(1, imgs, wts, out)
+        # mvr_decon_run_host_next: psi up, one iteration, psi back; the next step's images and
+        # raw weights upload during this step's iteration (every step uploads one full set)
+        e2e_dec.run_host(1, imgs, wts, out, imgs, wts)
+    e2e_dec.synchronize()  # the last step's uploads are inside the timed region
     e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
     e2e_value = ws * W.nvox * e2e_steps / e2e_s
     h2d = W.views * 2 * W.nvox * 4 + W.nvox * 4

@@ -213,6 +213,18 @@ MVR_API int mvr_decon_run(mvr_decon *h, int iterations, double *stats);
  * uploads overlap the computation; page-locked host buffers keep the copies asynchronous. */
 MVR_API int mvr_decon_run_host(mvr_decon *h, int iterations, const float *const *imgs, const float *const *weights,
                                float *psi);
+/* mvr_decon_run_host that also starts uploading the NEXT call's images and raw weights
+ * (next_images / next_weights, one host array per view) into a second set of device buffers
+ * while this call's iterations run; a later call given those same host arrays as its images
+ * and weights then uploads only psi before its first view-step (a time series of views, or
+ * repeated steps on the same arrays).  The next arrays are read asynchronously until the next
+ * call on the handle (or mvr_decon_synchronize) returns: keep them alive and unchanged until
+ * then.  NULL next arrays: the same as mvr_decon_run_host.  No counterpart in the reference,
+ * whose driver holds its images in host memory for the whole run
+ * (MultiViewDeconvolution.java:144-200). */
+MVR_API int mvr_decon_run_host_next(mvr_decon *h, int iterations, const float *const *images,
+                                    const float *const *weights, float *psi, const float *const *next_images,
+                                    const float *const *next_weights);
 /* Prepared kernel1 / kernel2 of a view (DeconViewPSF.getKernel1/getKernel2). */
 MVR_API int mvr_decon_get_kernels(mvr_decon *h, int view, float *kernel1, float *kernel2);
 /* Maximum intensity per view (PsiInit.getMax). */

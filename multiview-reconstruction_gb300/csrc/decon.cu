@@ -10,6 +10,7 @@
 //   cuda/BlockSorter.java:55-143, deconvolution/DeconView.java:118-274,
 //   deconvolution/normalization/NormalizingRandomAccess.java:76-214,
 //   deconvolution/init/PsiInitAvgPrecise.java:52-110
+#include "wdiv.h"
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -102,16 +103,18 @@ struct WeightPtrs {
 __global__ void k_normalize_weights(WeightPtrs wp, int nv, long long n, double osem, int smooth, float maxDiffRange,
                                     float scalingRange)
 {
-    // the double operations of the reference are kept where they round (the sum and the
-    // division); min(1, w) is exact in float, and the OSEM factor 1 needs no product
+    // the double sum of the reference is kept, and its division rounds as the reference's
+    // (mvr_weight_div: float operations, the double division only next to a float rounding
+    // boundary); min(1, w) is exact in float, and the OSEM factor 1 needs no product
     const bool osem_one = osem == 1.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         double sumW = 0.0;
         for (int v = 0; v < nv; ++v) sumW += (double)fminf(1.0f, wp.raw[v][i]);
+        const MvrWdSum ws = mvr_wd_sum(sumW);
         for (int v = 0; v < nv; ++v) {
             const float my = fminf(1.0f, wp.raw[v][i]);
             if (!smooth && osem_one) {
-                wp.out[v][i] = sumW > 1 ? (float)((double)my / sumW) : my;
+                wp.out[v][i] = sumW > 1 ? mvr_weight_div(my, &ws) : my;
                 continue;
             }
             double r;
@@ -119,7 +122,7 @@ __global__ void k_normalize_weights(WeightPtrs wp, int nv, long long n, double o
                 float s;
                 if (sumW <= 0) s = 0.0f;
                 else {
-                    const float ideal = (float)((double)my / sumW);
+                    const float ideal = mvr_weight_div(my, &ws);
                     const float diff = __fsub_rn(my, ideal);
                     float y = __fmul_rn(__fsub_rn(maxDiffRange, fabsf(diff)), __fdiv_rn(1.0f, maxDiffRange));
                     y = y > 0.0f ? y : 0.0f;
@@ -127,7 +130,7 @@ __global__ void k_normalize_weights(WeightPtrs wp, int nv, long long n, double o
                     s = __fsub_rn(fminf(my, ideal), scale);
                 }
                 r = s;
-            } else if (sumW > 1) r = (float)((double)my / sumW);
+            } else if (sumW > 1) r = mvr_weight_div(my, &ws);
             else r = my;
             const double m = r * osem;
             wp.out[v][i] = (float)(m < 1.0 ? m : 1.0);
@@ -414,7 +417,8 @@ public:
     virtual int get_psi(float *psi) = 0;
     virtual int get_psi_device(float *psi) = 0;
     virtual int run(int iterations, double *stats) = 0;
-    virtual int run_host(int iterations, const float *const *imgs, const float *const *ws, float *psi) = 0;
+    virtual int run_host(int iterations, const float *const *imgs, const float *const *ws, float *psi,
+                         const float *const *next_imgs, const float *const *next_ws) = 0;
     virtual int get_kernels(int v, float *k1, float *k2) = 0;
     virtual int get_max(float *mx) = 0;
     virtual int get_weights(int v, float *w) = 0;
@@ -451,7 +455,8 @@ public:
     int get_psi(float *psi) override;
     int get_psi_device(float *psi) override;
     int run(int iterations, double *stats) override;
-    int run_host(int iterations, const float *const *imgs, const float *const *ws, float *psi) override;
+    int run_host(int iterations, const float *const *imgs, const float *const *ws, float *psi,
+                 const float *const *next_imgs, const float *const *next_ws) override;
     int get_kernels(int v, float *k1, float *k2) override;
     int get_max(float *mx) override;
     int get_weights(int v, float *w) override;
@@ -513,13 +518,14 @@ private:
         int batch = 0;
         long long epoch = -1;
         long long inputs = -1;
+        int set = 0;  // which of the two input buffer sets of mvr_decon_run_host_next is in use
         cudaGraphExec_t exec = nullptr;
         T *psi_end = nullptr, *stage_end = nullptr;
         long long launches = 0;
         bool same(const IterGraph &o) const
         {
             return psi_start == o.psi_start && stats == o.stats && batch == o.batch && epoch == o.epoch &&
-                   inputs == o.inputs;
+                   inputs == o.inputs && set == o.set;
         }
     };
     std::vector<IterGraph> graphs_;
@@ -570,6 +576,13 @@ private:
     cudaStream_t copy_ = nullptr;              // uploads of mvr_decon_run_host
     cudaEvent_t ev_w_ = nullptr;               // weights and psi uploaded
     std::vector<cudaEvent_t> ev_img_;          // image of view v uploaded
+    // the next call's images and raw weights, uploaded during this call's iterations into a
+    // second set of device buffers (mvr_decon_run_host_next)
+    std::vector<float *> alt_img_, alt_w_;
+    std::vector<const float *> pre_img_, pre_w_;  // the host arrays the second set holds
+    bool pre_valid_ = false;
+    int cur_set_ = 0;               // flips with every swap of the two sets
+    cudaEvent_t ev_pre_ = nullptr;  // the second set uploaded
     bool prepared_ = false;
     std::string err_;
 };
@@ -598,8 +611,12 @@ Decon<T>::~Decon()
     cudaFree(d_scratch_);
     cudaFree(d_perm_);
     cudaFree(d_stats_);
+    if (copy_) cudaStreamSynchronize(copy_);  // a prefetch may still read host arrays
+    for (float *a : alt_img_) cudaFree(a);
+    for (float *a : alt_w_) cudaFree(a);
     for (cudaEvent_t e : ev_img_) cudaEventDestroy(e);
     if (ev_w_) cudaEventDestroy(ev_w_);
+    if (ev_pre_) cudaEventDestroy(ev_pre_);
     if (copy_) cudaStreamDestroy(copy_);
     drop_graphs();
 }
@@ -1182,6 +1199,7 @@ int Decon<T>::synchronize()
 {
     D_CUDA(cudaSetDevice(p_.device));
     D_CUDA(cudaStreamSynchronize(engine_.stream()));
+    if (copy_) D_CUDA(cudaStreamSynchronize(copy_));
     return MVR_OK;
 }
 
@@ -1284,6 +1302,7 @@ int Decon<T>::run_iteration(double *stats_base, size_t stats_stride)
     key.batch = batch_;
     key.epoch = engine_.alloc_epoch();
     key.inputs = inputs_epoch_;
+    key.set = cur_set_;
     for (const auto &g : graphs_) {
         if (!g.same(key)) continue;
         D_CUDA(cudaGraphLaunch(g.exec, s));
@@ -1465,13 +1484,18 @@ int Decon<T>::tuning(int capacity, int *step, int *code, int *batch, float *ms) 
 // view-steps.  psi comes back at the end.  With page-locked host buffers the copies run
 // asynchronously to the host; pageable buffers work but may serialise them.
 template <typename T>
-int Decon<T>::run_host(int iterations, const float *const *imgs, const float *const *ws, float *psi)
+int Decon<T>::run_host(int iterations, const float *const *imgs, const float *const *ws, float *psi,
+                       const float *const *next_imgs, const float *const *next_ws)
 {
     if (!prepared_) return fail(MVR_ERR_STATE, "mvr_decon_prepare was not called");
     if (!imgs || !ws || !psi || iterations < 1) return fail(MVR_ERR_ARG, "inputs must not be NULL, iterations >= 1");
+    if ((next_imgs == nullptr) != (next_ws == nullptr))
+        return fail(MVR_ERR_ARG, "next images and next weights: both or neither");
     const int nv = p_.num_views;
     for (int v = 0; v < nv; ++v) {
         if (!imgs[v] || !ws[v]) return fail(MVR_ERR_ARG, "image and weight pointers must not be NULL");
+        if (next_imgs && (!next_imgs[v] || !next_ws[v]))
+            return fail(MVR_ERR_ARG, "next image and weight pointers must not be NULL");
         if (!views_[v].own_img || !views_[v].own_w)
             return fail(MVR_ERR_STATE, "mvr_decon_run_host needs views set with mvr_decon_set_view (host arrays)");
     }
@@ -1479,23 +1503,63 @@ int Decon<T>::run_host(int iterations, const float *const *imgs, const float *co
     cudaStream_t s = engine_.stream();
     if (!copy_) D_CUDA(cudaStreamCreateWithFlags(&copy_, cudaStreamNonBlocking));
     if (!ev_w_) D_CUDA(cudaEventCreateWithFlags(&ev_w_, cudaEventDisableTiming));
+    if (!ev_pre_) D_CUDA(cudaEventCreateWithFlags(&ev_pre_, cudaEventDisableTiming));
     while ((int)ev_img_.size() < nv) {
         cudaEvent_t e = nullptr;
         D_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         ev_img_.push_back(e);
     }
     const size_t bytes = sizeof(float) * (size_t)n_;
+    // this call's images and weights were uploaded by the previous call when it was given
+    // the same host arrays as its next ones
+    bool pre = pre_valid_;
+    for (int v = 0; pre && v < nv; ++v) pre = imgs[v] == pre_img_[v] && ws[v] == pre_w_[v];
+    pre_valid_ = false;
     // the copy stream starts after the work already queued on the compute stream (earlier
     // iterations still read the buffers it overwrites)
     D_CUDA(cudaEventRecord(ev_w_, s));
     D_CUDA(cudaStreamWaitEvent(copy_, ev_w_, 0));
-    for (int v = 0; v < nv; ++v) D_CUDA(cudaMemcpyAsync(views_[v].w_raw, ws[v], bytes, cudaMemcpyHostToDevice, copy_));
+    if (pre) {
+        for (int v = 0; v < nv; ++v) {
+            std::swap(views_[v].img, alt_img_[v]);
+            std::swap(views_[v].w_raw, alt_w_[v]);
+            if (p_.weight_norm == MVR_WEIGHTS_AS_GIVEN) views_[v].w = views_[v].w_raw;
+        }
+        cur_set_ ^= 1;  // captured iterations are kept per set
+        D_CUDA(cudaStreamWaitEvent(s, ev_pre_, 0));
+    } else {
+        for (int v = 0; v < nv; ++v)
+            D_CUDA(cudaMemcpyAsync(views_[v].w_raw, ws[v], bytes, cudaMemcpyHostToDevice, copy_));
+    }
     float *psi_up = sizeof(T) == sizeof(float) ? reinterpret_cast<float *>(psi_) : reinterpret_cast<float *>(stage_);
     D_CUDA(cudaMemcpyAsync(psi_up, psi, bytes, cudaMemcpyHostToDevice, copy_));
     D_CUDA(cudaEventRecord(ev_w_, copy_));
-    for (int v = 0; v < nv; ++v) {
-        D_CUDA(cudaMemcpyAsync(views_[v].img, imgs[v], bytes, cudaMemcpyHostToDevice, copy_));
-        D_CUDA(cudaEventRecord(ev_img_[v], copy_));
+    if (!pre) {
+        for (int v = 0; v < nv; ++v) {
+            D_CUDA(cudaMemcpyAsync(views_[v].img, imgs[v], bytes, cudaMemcpyHostToDevice, copy_));
+            D_CUDA(cudaEventRecord(ev_img_[v], copy_));
+        }
+    }
+    if (next_imgs) {
+        // the next call's inputs into the second set, behind this call's uploads on the copy
+        // stream and concurrent with this call's iterations (the second set's last reader was
+        // the previous call, which has returned)
+        if (alt_img_.empty()) {
+            alt_img_.assign(nv, nullptr);
+            alt_w_.assign(nv, nullptr);
+            for (int v = 0; v < nv; ++v) {
+                D_CUDA(cudaMalloc(&alt_img_[v], bytes));
+                D_CUDA(cudaMalloc(&alt_w_[v], bytes));
+            }
+        }
+        for (int v = 0; v < nv; ++v) {
+            D_CUDA(cudaMemcpyAsync(alt_w_[v], next_ws[v], bytes, cudaMemcpyHostToDevice, copy_));
+            D_CUDA(cudaMemcpyAsync(alt_img_[v], next_imgs[v], bytes, cudaMemcpyHostToDevice, copy_));
+        }
+        D_CUDA(cudaEventRecord(ev_pre_, copy_));
+        pre_img_.assign(next_imgs, next_imgs + nv);
+        pre_w_.assign(next_ws, next_ws + nv);
+        pre_valid_ = true;
     }
     D_CUDA(cudaStreamWaitEvent(s, ev_w_, 0));
     if (sizeof(T) != sizeof(float)) {
@@ -1509,15 +1573,20 @@ int Decon<T>::run_host(int iterations, const float *const *imgs, const float *co
         cudaFree(hold);
     }
     if (p_.weight_norm != MVR_WEIGHTS_AS_GIVEN) D_TRY(normalize_weights());
-    // the first iteration eagerly, each view-step after its image
-    const int steps = num_steps();
-    for (int st = 0; st < steps; ++st) {
-        if (p_.mul)
-            for (int v = 0; v < nv; ++v) D_CUDA(cudaStreamWaitEvent(s, ev_img_[v], 0));
-        else D_CUDA(cudaStreamWaitEvent(s, ev_img_[st], 0));
-        D_TRY(run_step(st, nullptr, false, batch_));
+    int it = 0;
+    if (!pre) {
+        // the first iteration eagerly, each view-step after its image
+        const int steps = num_steps();
+        for (int st = 0; st < steps; ++st) {
+            if (p_.mul)
+                for (int v = 0; v < nv; ++v) D_CUDA(cudaStreamWaitEvent(s, ev_img_[v], 0));
+            else D_CUDA(cudaStreamWaitEvent(s, ev_img_[st], 0));
+            D_TRY(run_step(st, nullptr, false, batch_));
+        }
+        it = 1;
     }
-    for (int it = 1; it < iterations; ++it) D_TRY(run_iteration(nullptr, 0));
+    // (with every input already on the device, all iterations take the captured-graph path)
+    for (; it < iterations; ++it) D_TRY(run_iteration(nullptr, 0));
     return get_psi(psi);
 }
 
@@ -1685,10 +1754,17 @@ extern "C" int mvr_decon_set_view_device(mvr_decon *h, int view, const float *im
     return rc != MVR_OK ? rc : h->impl->set_psf(view, psf, psf_size);
 }
 
+extern "C" int mvr_decon_run_host_next(mvr_decon *h, int iterations, const float *const *images,
+                                       const float *const *weights, float *psi, const float *const *next_images,
+                                       const float *const *next_weights)
+{
+    return h ? h->impl->run_host(iterations, images, weights, psi, next_images, next_weights) : MVR_ERR_ARG;
+}
+
 extern "C" int mvr_decon_run_host(mvr_decon *h, int iterations, const float *const *imgs, const float *const *weights,
                                   float *psi)
 {
-    return h ? h->impl->run_host(iterations, imgs, weights, psi) : MVR_ERR_ARG;
+    return h ? h->impl->run_host(iterations, imgs, weights, psi, nullptr, nullptr) : MVR_ERR_ARG;
 }
 
 extern "C" int mvr_decon_set_schedule(mvr_decon *h, int code)

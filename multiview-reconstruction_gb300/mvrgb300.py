@@ -47,7 +47,7 @@ EXPORTS = [
     "mvr_decon_stream", "mvr_decon_launch_count", "mvr_decon_set_profiling", "mvr_decon_get_profile",
     "mvr_kernel_name", "mvr_convolve_static", "mvr_decon_batch", "mvr_decon_likelihood",
     "mvr_decon_set_graphs", "mvr_decon_graphs_captured", "mvr_decon_set_schedule", "mvr_decon_schedule",
-    "mvr_decon_tuning", "mvr_decon_run_host", "mvr_export_tiff", "mvr_export_n5", "mvr_pool2",
+    "mvr_decon_tuning", "mvr_decon_run_host", "mvr_decon_run_host_next", "mvr_export_tiff", "mvr_export_n5", "mvr_pool2",
     "mvr_apply_coarse", "mvr_decon_init_psi", "mvr_fuse_group",
     "mvr_fuse_last_error", "mvr_psf_extract", "mvr_psf_transformed_dims", "mvr_psf_transform_normalized",
     "mvr_psf_average", "mvr_psf_make_same_size", "mvr_psf_projection", "mvr_psf_remove_min_projections",
@@ -144,6 +144,7 @@ def load() -> C.CDLL:
     L.mvr_decon_schedule.argtypes = [P, C.c_int]
     L.mvr_decon_tuning.argtypes = [P, C.c_int, P, P, P, P]
     L.mvr_decon_run_host.argtypes = [P, C.c_int, P, P, P]
+    L.mvr_decon_run_host_next.argtypes = [P, C.c_int, P, P, P, P, P]
     L.mvr_export_tiff.argtypes = [C.c_char_p, P, P, C.c_int, P, C.c_char_p, C.c_char_p, C.c_int]
     L.mvr_pool2.argtypes = [P, P, P, P]
     L.mvr_apply_coarse.argtypes = [P, P, P, P, P, C.c_float, P, P]
@@ -419,9 +420,12 @@ class Deconvolution:
         """Copies psi (float) into the device buffer at ptr."""
         self._check(self._lib.mvr_decon_get_psi_device(self._h, C.c_void_p(ptr)))
 
-    def run_host(self, n: int, imgs, weights, psi):
+    def run_host(self, n: int, imgs, weights, psi, next_imgs=None, next_weights=None):
         """mvr_decon_run_host: uploads the host images, raw weights and psi (float32 [z][y][x],
-        C-contiguous), runs n iterations and writes psi back in place."""
+        C-contiguous), runs n iterations and writes psi back in place.  With next_imgs /
+        next_weights (mvr_decon_run_host_next) the next call's images and weights upload during
+        these iterations; they must be C-contiguous float32 arrays of the volume shape and stay
+        unchanged until the next call returns (the handle keeps references to them)."""
         arrs = [_f32(a) for a in list(imgs) + list(weights)]
         if any(a.shape != self.shape for a in arrs) or psi.dtype != np.float32 or psi.shape != self.shape \
                 or not psi.flags.c_contiguous:
@@ -429,7 +433,18 @@ class Deconvolution:
         nv = self.num_views
         ip = (C.c_void_p * nv)(*[a.ctypes.data for a in arrs[:nv]])
         wp = (C.c_void_p * nv)(*[a.ctypes.data for a in arrs[nv:]])
-        self._check(self._lib.mvr_decon_run_host(self._h, int(n), ip, wp, _p(psi)))
+        if next_imgs is None and next_weights is None:
+            self._check(self._lib.mvr_decon_run_host(self._h, int(n), ip, wp, _p(psi)))
+            self._next_keep = None
+            return psi
+        nxt = list(next_imgs) + list(next_weights)
+        if len(nxt) != 2 * nv or any(not isinstance(a, np.ndarray) or a.dtype != np.float32 or a.shape != self.shape
+                                     or not a.flags.c_contiguous for a in nxt):
+            raise ValueError("next images and weights: one C-contiguous float32 volume per view each")
+        nip = (C.c_void_p * nv)(*[a.ctypes.data for a in nxt[:nv]])
+        nwp = (C.c_void_p * nv)(*[a.ctypes.data for a in nxt[nv:]])
+        self._check(self._lib.mvr_decon_run_host_next(self._h, int(n), ip, wp, _p(psi), nip, nwp))
+        self._next_keep = nxt  # read by the copies in flight until the next call returns
         return psi
 
     def run_iterations(self, n: int, stats: bool = False):

@@ -188,6 +188,37 @@ def test_graph_replay_matches_eager_launches(vol, block, mul):
     assert np.array_equal(st_g, st_e)
 
 
+def test_run_host_next_prefetches_the_next_inputs(vol):
+    # mvr_decon_run_host_next: the next call's images and weights upload during this call.  A
+    # sequence over two input sets (A, B = A with brighter images and other weights) gives the
+    # psi of the same sequence of plain mvr_decon_run_host calls, whether the next call's arrays
+    # match the prefetched ones (B after A, A after B) or not (the last call)
+    a_i = [np.ascontiguousarray(vol["img0"], np.float32), np.ascontiguousarray(vol["img1"], np.float32)]
+    a_w = [np.ascontiguousarray(vol["raw_w0"], np.float32), np.ascontiguousarray(vol["raw_w1"], np.float32)]
+    b_i = [a * np.float32(1.25) for a in a_i]
+    b_w = [np.ascontiguousarray(a_w[1]), np.ascontiguousarray(a_w[0])]
+    c_i = [a * np.float32(0.8) for a in a_i]
+    seq = [(a_i, a_w, b_i, b_w), (b_i, b_w, a_i, a_w), (a_i, a_w, b_i, b_w), (c_i, a_w, None, None)]
+    with make(vol, (28, 28, 28)) as d:
+        psi0 = d.get_psi()
+    ref = psi0.copy()
+    with make(vol, (28, 28, 28)) as d:
+        refs = []
+        for im, w, _, _ in seq:
+            d.run_host(1, im, w, ref)
+            refs.append(ref.copy())
+    psi = psi0.copy()
+    with make(vol, (28, 28, 28)) as d:
+        for (im, w, ni, nw), r in zip(seq, refs):
+            d.run_host(1, im, w, psi, ni, nw)
+            assert rel(psi, r) <= 1e-6
+        d.run_host(2, a_i, a_w, psi, a_i, a_w)  # two iterations: the second from the graph path
+        d.synchronize()
+    with make(vol, (28, 28, 28)) as d:
+        d.run_host(2, a_i, a_w, ref)
+    assert rel(psi, ref) <= 1e-6
+
+
 def test_run_host_matches_device_resident_iterations(vol):
     # mvr_decon_run_host (uploads overlapped with the first view-steps) gives the same psi as
     # uploading the views and psi and running the iterations on the device
