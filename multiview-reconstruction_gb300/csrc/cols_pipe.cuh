@@ -60,7 +60,7 @@ template <int V, int MODE>
 __global__ void __launch_bounds__(256, MVR_PIPE_MINB)
     k_tcols_pipe(const float2 *src, float2 *dst, const float2 *__restrict__ Kh, int Hx, long long estride,
                  long long ostride, long long Pc, const float2 *__restrict__ twg, int gather, int nother, int rlo,
-                 int rhi, int olo, PipeGeom pg)
+                 int rhi, int olo, PipeGeom pg, int zfill)
 {
     constexpr int T = kTColT, NP = kTColNP, n = V * T, tot = n * NP;
     constexpr bool KS = pipe_kstage<V, MODE>();
@@ -167,10 +167,17 @@ __global__ void __launch_bounds__(256, MVR_PIPE_MINB)
             for (int v = 0; v < V; ++v) A[(t + T * v) * NP + c] = a[v];
         }
         if (MODE != 0) __syncthreads();
-        // rows [rlo, rhi) of the transformed axis go back to HBM
+        // rows [rlo, rhi) of the transformed axis go back to HBM (with zfill, zeros the others)
         if (pc < np) {
             float2 *cb = dst + boff + base + (long long)pc * pstride;
-            for (int e = threadIdx.x + rlo * NP; e < rhi * NP; e += 256) cb[(long long)(e / NP) * estride] = A[e];
+            if (!zfill) {
+                for (int e = threadIdx.x + rlo * NP; e < rhi * NP; e += 256) cb[(long long)(e / NP) * estride] = A[e];
+            } else {
+                for (int e = threadIdx.x; e < n * NP; e += 256) {
+                    const int row = e / NP;
+                    cb[(long long)row * estride] = (row >= rlo && row < rhi) ? A[e] : make_float2(0.0f, 0.0f);
+                }
+            }
         }
         __syncthreads();  // the next iteration refills this stage
     }

@@ -182,7 +182,7 @@ template <int V, int MODE, int NP = kTColNP>
 __global__ void __launch_bounds__(16 * NP, (NP == 16 && V <= 16) ? MVR_TCOLS_MINB : 2)
     k_tcols(const float2 *src, float2 *dst, const float2 *__restrict__ Kh, int Hx, long long estride,
             long long ostride, long long Pc, const float2 *__restrict__ twg, int gather, int nother, int rlo, int rhi,
-            int olo)
+            int olo, int zfill)
 {
     constexpr int T = kTColT, n = V * T, NT = 16 * NP;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(16 * NP, (NP == 16 && V <= 16) ? MVR_TCOLS_MIN
     }
     if (MODE != 0) __syncthreads();
     // rows [rlo, rhi) of the transformed axis are stored (all of them unless the caller
-    // reads only a sub-range)
+    // reads only a sub-range); with zfill the other rows are stored as zeros
     if (plive) {
         float2 *dp = dst + coff;
         const int prow = threadIdx.x / NP;
@@ -301,6 +301,7 @@ __global__ void __launch_bounds__(16 * NP, (NP == 16 && V <= 16) ? MVR_TCOLS_MIN
         for (int j = 0; j < R; ++j) {
             const int row = prow + (NT / NP) * j;
             if (row >= rlo && row < rhi) dp[j * rstep] = A[threadIdx.x + j * NT];
+            else if (zfill) dp[j * rstep] = make_float2(0.0f, 0.0f);
         }
     }
 }

@@ -626,7 +626,7 @@ int Engine<T>::kernel_spectra(Plan<T> &pl, const float *k1, const float *k2, boo
 
 template <typename T>
 int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh, int nb, int rlo,
-                           int rhi, int olo, int ohi)
+                           int rhi, int olo, int ohi, bool zfill)
 {
     const int Hx = pl.Hx;
     long long estride, ostride;
@@ -654,11 +654,14 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
     const int kind = mode == 2 ? KK_COLS_ZMUL : (mode == 1 ? KK_COLS_INV : KK_COLS_FWD);
     const int nax = pl.P[axis];
     const bool tiled = sizeof(T) == sizeof(float) && (axis == 1 ? pl.tcy : pl.tcz);
-    if (rhi < 0 || rhi > nax || !tiled) rhi = nax;
-    if (rlo < 0 || rlo > rhi || rhi == nax) rlo = 0;
+    if (zfill && !(tiled && rlo >= 0 && rlo <= rhi && rhi <= nax)) return fail(ERR_STATE, "zero fill needs a tile pass");
+    if (!zfill) {
+        if (rhi < 0 || rhi > nax || !tiled) rhi = nax;
+        if (rlo < 0 || rlo > rhi || rhi == nax) rlo = 0;
+    }
     if (ohi < 0 || ohi > nother || !tiled) ohi = nother;
     if (olo < 0 || olo >= ohi) olo = 0;
-    const double stored = (double)(rhi - rlo) / nax, part = (double)(ohi - olo) / nother;
+    const double stored = zfill ? 1.0 : (double)(rhi - rlo) / nax, part = (double)(ohi - olo) / nother;
     MVR_TRY(prof_begin(kind, part * (mode == 2 ? (2.0 + stored) * cb : (1.0 + stored) * cb)));
     const long long Pc = pl.Pc;
     const int wc = axis == 1 ? pl.wcy : pl.wcz;
@@ -682,14 +685,14 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
                     const size_t ps = pipe_smem<V_, 0>();
                     if (mode == 0)
                         k_tcols_pipe<V_, 0><<<std::min(pg.ntiles, pipe_resident<V_, 0>()), kThreads, ps, stream_>>>(
-                            src, dst, Kh, Hx, estride, ostride, Pc, tw, gather, ohi, rlo, rhi, olo, pg);
+                            src, dst, Kh, Hx, estride, ostride, Pc, tw, gather, ohi, rlo, rhi, olo, pg, zfill ? 1 : 0);
                     else if (mode == 1)
                         k_tcols_pipe<V_, 1><<<std::min(pg.ntiles, pipe_resident<V_, 1>()), kThreads, ps, stream_>>>(
-                            src, dst, Kh, Hx, estride, ostride, Pc, tw, gather, ohi, rlo, rhi, olo, pg);
+                            src, dst, Kh, Hx, estride, ostride, Pc, tw, gather, ohi, rlo, rhi, olo, pg, zfill ? 1 : 0);
                     else
                         MVR_CUDA(launch_pdl(k_tcols_pipe<V_, 2>, std::min(pg.ntiles, pipe_resident<V_, 2>()), kThreads,
                                             pipe_smem<V_, 2>(), stream_, src, dst, Kh, Hx, estride, ostride, Pc, tw,
-                                            gather, ohi, rlo, rhi, olo, pg));
+                                            gather, ohi, rlo, rhi, olo, pg, zfill ? 1 : 0));
                 });
                 MVR_LAUNCHED("k_tcols_pipe");
                 return prof_end();
@@ -699,13 +702,13 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
             TILE_COLS(tc, {
                 if (mode == 0)
                     MVR_CUDA(launch_pdl(k_tcols<V_, 0>, tgrid, kThreads, ts, stream_, src, dst, Kh, Hx, estride, ostride, Pc, tw,
-                                       gather, ohi, rlo, rhi, olo));
+                                       gather, ohi, rlo, rhi, olo, zfill ? 1 : 0));
                 else if (mode == 1)
                     MVR_CUDA(launch_pdl(k_tcols<V_, 1>, tgrid, kThreads, ts, stream_, src, dst, Kh, Hx, estride, ostride, Pc, tw,
-                                       gather, ohi, rlo, rhi, olo));
+                                       gather, ohi, rlo, rhi, olo, zfill ? 1 : 0));
                 else
                     MVR_CUDA(launch_pdl(k_tcols<V_, 2>, tgrid, kThreads, ts, stream_, src, dst, Kh, Hx, estride, ostride, Pc, tw,
-                                       gather, ohi, rlo, rhi, olo));
+                                       gather, ohi, rlo, rhi, olo, zfill ? 1 : 0));
             });
             MVR_LAUNCHED("k_tcols");
             return prof_end();
@@ -873,13 +876,42 @@ int Engine<T>::launch_xy_fwd(const Plan<T> &pl, const BlockMaps &bms, int nb, co
     return fail(ERR_STATE, "plane kernels are FP32 only");
 }
 
+// The second convolution's output on the planes [zlo, zhi) reads its input on
+// [zlo - r, zhi + r) only, r = kd / 2 + 1 covering the kernel's reach on either side of its
+// centre.  When that band lies inside the domain (no circular wrap) and is shorter than it, the
+// first convolution's Z pass stores zeros outside the band and the quotient pass works on the
+// band alone: the skipped planes carry no weight in the outputs that are kept.
+// MVR_RATIO_BAND=0 keeps the quotient pass on every plane
+static bool ratio_band_off()
+{
+    const char *e = std::getenv("MVR_RATIO_BAND");
+    return e && e[0] == '0';
+}
+
 template <typename T>
-int Engine<T>::launch_xy_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img)
+bool Engine<T>::ratio_band(const Plan<T> &pl, int zlo, int zhi, int &lo, int &hi) const
+{
+    lo = 0;
+    hi = pl.P[2];
+    if (sizeof(T) != sizeof(float) || !pl.tcz || zhi <= zlo || ratio_band_off()) return false;
+    const int r = pl.kd[2] / 2 + 1;
+    if (zlo - r < 0 || zhi + r > pl.P[2] || zhi - zlo + 2 * r >= pl.P[2]) return false;
+    lo = zlo - r;
+    hi = zhi + r;
+    return true;
+}
+
+template <typename T>
+int Engine<T>::launch_xy_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img, int zlo,
+                               int zhi)
 {
     if constexpr (sizeof(T) == sizeof(float)) {
+        if (zhi < 0 || zhi > pl.P[2]) zhi = pl.P[2];
+        if (zlo < 0 || zlo >= zhi) zlo = 0;
+        const double part = (double)(zhi - zlo) / pl.P[2];
         const double nv = (double)pl.b[0] * pl.b[1] * pl.b[2];
-        MVR_TRY(prof_begin(KK_XY_RATIO, nb * (2.0 * sizeof(V) * (double)pl.Pc + 4.0 * nv)));
-        MVR_CUDA(xy_ratio(pl.xy, S, img, bms, nb, pl.P[2], pl.Pc, pl.twx, pl.twy, stream_, pl.persist != 0));
+        MVR_TRY(prof_begin(KK_XY_RATIO, part * nb * (2.0 * sizeof(V) * (double)pl.Pc + 4.0 * nv)));
+        MVR_CUDA(xy_ratio(pl.xy, S, img, bms, nb, zlo, zhi - zlo, pl.Pc, pl.twx, pl.twy, stream_, pl.persist != 0));
         return prof_end();
     }
     return fail(ERR_STATE, "plane kernels are FP32 only");
@@ -945,9 +977,11 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const f
     int zlo = 0, zhi = -1, ylo = 0, yhi = -1;
     if (prune) write_region(bps, nb, zlo, zhi, ylo, yhi);
     if (pl.xy) {
+        int blo = 0, bhi = -1;
+        const bool band = prune && ratio_band(pl, zlo, zhi, blo, bhi);
         MVR_TRY(launch_xy_fwd(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
-        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb));
-        MVR_TRY(launch_xy_ratio(pl, bms, nb, S0_, img));
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb, blo, bhi, 0, -1, band));
+        MVR_TRY(launch_xy_ratio(pl, bms, nb, S0_, img, blo, bhi));
         MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k2h, nb, zlo, zhi));
     } else {
         MVR_TRY(launch_fwd_mirror(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
@@ -1030,11 +1064,12 @@ int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace
             }
         }
         prev = &pl;
-        MVR_TRY(launch_cols(pl, 2, 2, S0_, S1_, pl.k1h, nb));
+        int zlo = 0, zhi = -1, ylo, yhi, blo = 0, bhi = -1;
+        if (pl.xy && !stats_dev) write_region(bps, nb, zlo, zhi, ylo, yhi);
+        const bool band = pl.xy && !stats_dev && ratio_band(pl, zlo, zhi, blo, bhi);
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S1_, pl.k1h, nb, band ? blo : 0, band ? bhi : -1, 0, -1, band));
         if (pl.xy) {
-            int zlo = 0, zhi = -1, ylo, yhi;
-            if (!stats_dev) write_region(bps, nb, zlo, zhi, ylo, yhi);
-            MVR_TRY(launch_xy_ratio(pl, bms, nb, S1_, imgs[v]));
+            MVR_TRY(launch_xy_ratio(pl, bms, nb, S1_, imgs[v], band ? blo : 0, band ? bhi : -1));
             MVR_TRY(launch_cols(pl, 2, 2, S1_, S1_, pl.k2h, nb, zlo, zhi));
         } else {
             MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr, nb));

@@ -152,13 +152,19 @@ public:
 private:
     int launch_fwd_mirror(const Plan<T> &pl, const BlockMaps &bms, int nb, const T *src, V *S);
     int launch_xy_fwd(const Plan<T> &pl, const BlockMaps &bms, int nb, const T *src, V *S);
-    int launch_xy_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img);
+    // the quotient pass over the planes [zlo, zhi) of each block (zhi < 0: all)
+    int launch_xy_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img, int zlo = 0,
+                        int zhi = -1);
     int launch_xy_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const UpdateArgs &ua, int epi,
                          double bytes, double *stats_dev);
     // rows [rlo, rhi) of the transformed axis are stored, and only the other-axis indices
-    // [olo, ohi) are transformed (negative hi: all; tile kernels only, the others do all)
+    // [olo, ohi) are transformed (negative hi: all; tile kernels only, the others do all);
+    // zfill (tile kernels only): the rows outside [rlo, rhi) are stored as zeros
     int launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh, int nb, int rlo = 0,
-                    int rhi = -1, int olo = 0, int ohi = -1);
+                    int rhi = -1, int olo = 0, int ohi = -1, bool zfill = false);
+    // the planes [lo, hi) that the second convolution reads for a write region [zlo, zhi) (its
+    // kernel's reach either side); false when pruning does not apply
+    bool ratio_band(const Plan<T> &pl, int zlo, int zhi, int &lo, int &hi) const;
     int launch_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img);
     int launch_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const UpdateArgs &ua, int epi,
                       double bytes, double *stats_dev);

@@ -211,21 +211,21 @@ cudaError_t xy_fwd_kernel(int combo, const SrcKernel &src, float2 *S, const Bloc
     return fwd(combo, src, S, bms, nb, Pz, Pc, twx, twy, s, persist);
 }
 
-cudaError_t xy_ratio(int combo, float2 *S, const float *img, const BlockMaps &bms, int nb, int Pz, long long Pc,
-                     const float2 *twx, const float2 *twy, cudaStream_t s, bool persist)
+cudaError_t xy_ratio(int combo, float2 *S, const float *img, const BlockMaps &bms, int nb, int z0, int nzb,
+                     long long Pc, const float2 *twx, const float2 *twy, cudaStream_t s, bool persist)
 {
     set_limits();
-    const int nitems = Pz * nb;
+    const int nitems = nzb * nb;
     if (combo >= 10000) {
         PAIR_DISPATCH(combo, return launch_pair(k_xy2_ratio<VX_, VH_>,
                                                 dim3(2 * (unsigned)std::min(nitems, pair_clusters<VX_, VH_>())),
                                                 PairShape<VX_, VH_>::NT, pair_smem_bytes<VX_, VH_>(), s, S, img, bms,
-                                                Pc, twx, twy, Pz, nitems));
+                                                Pc, twx, twy, z0, nzb, nitems));
         return cudaGetLastError();
     }
     const dim3 grid((unsigned)(persist ? std::min(nitems, persist_ctas()) : nitems));
     XY_DISPATCH(combo, return launch_pdl(k_xy_ratio<VX_, VY_>, grid, XYShape<VX_, VY_>::NT, xy_smem_bytes<VX_, VY_>(),
-                                         s, S, img, bms, Pc, twx, twy, Pz, nitems));
+                                         s, S, img, bms, Pc, twx, twy, z0, nzb, nitems));
     return cudaGetLastError();
 }
 

@@ -25,8 +25,9 @@ cudaError_t xy_fwd_zero(int combo, const float *blk, float2 *S, const BlockMaps 
                         const float2 *twx, const float2 *twy, cudaStream_t s, bool persist = true);
 cudaError_t xy_fwd_kernel(int combo, const SrcKernel &src, float2 *S, const BlockMaps &bms, int nb, int Pz,
                           long long Pc, const float2 *twx, const float2 *twy, cudaStream_t s, bool persist = true);
-cudaError_t xy_ratio(int combo, float2 *S, const float *img, const BlockMaps &bms, int nb, int Pz, long long Pc,
-                     const float2 *twx, const float2 *twy, cudaStream_t s, bool persist = true);
+// the quotient pass over the planes [z0, z0 + nzb) of each block
+cudaError_t xy_ratio(int combo, float2 *S, const float *img, const BlockMaps &bms, int nb, int z0, int nzb,
+                     long long Pc, const float2 *twx, const float2 *twy, cudaStream_t s, bool persist = true);
 cudaError_t xy_update(int combo, int epi, float2 *S, const UpdateArgs &ua, const BlockMaps &bms, int nb, int Pz,
                       long long Pc, const float2 *twx, const float2 *twy, cudaStream_t s);
 

@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(PairShape<VX, VH>::NT, PairShape<VX, VH>::MINB
 template <int VX, int VH>
 __global__ void __launch_bounds__(PairShape<VX, VH>::NT, PairShape<VX, VH>::MINB)
     k_xy2_ratio(float2 *__restrict__ S, const float *__restrict__ img, const BlockMaps bms, long long Pc,
-                const float2 *__restrict__ gtwx, const float2 *__restrict__ gtwy, int Pz, int nitems)
+                const float2 *__restrict__ gtwx, const float2 *__restrict__ gtwy, int z0, int nzb, int nitems)
 {
     typedef PairShape<VX, VH> SH;
     constexpr int NT = SH::NT, RX = SH::RX, H = SH::H;
@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(PairShape<VX, VH>::NT, PairShape<VX, VH>::MINB
     pdl_wait();
     const int nclusters = gridDim.x >> 1;
     for (int item = blockIdx.x >> 1; item < nitems; item += nclusters) {
-        const int bi = item / Pz, z = item - bi * Pz;
+        const int bi = item / nzb, z = z0 + (item - bi * nzb);
         const BlockMap &bm = bms.m[bi];
         float2 *Sp = S + (long long)bi * Pc + (long long)z * SH::plane + (long long)rank * SH::half;
         const int ez = ext_e(z, bm.P[2], bm.L[2]);
@@ -461,7 +461,7 @@ __global__ void __launch_bounds__(PairShape<VX, VH>::NT, PairShape<VX, VH>::MINB
         {
             const int next = item + nclusters;
             if (next < nitems) {
-                const int nbi = next / Pz, nz = next - nbi * Pz;
+                const int nbi = next / nzb, nz = z0 + (next - nbi * nzb);
                 const char *np = reinterpret_cast<const char *>(S + (long long)nbi * Pc + (long long)nz * SH::plane +
                                                                 (long long)rank * SH::half);
                 for (int off = threadIdx.x * 128; off < SH::half * (int)sizeof(float2); off += NT * 128)

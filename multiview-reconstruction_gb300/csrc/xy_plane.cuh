@@ -397,11 +397,12 @@ __device__ __forceinline__ void xy_store_plane(float2 *__restrict__ Sp, const fl
 // L2 prefetch of item `next`'s plane (persistent plane kernels): one 128-byte line per
 // thread and step, issued before the current plane is transformed.
 template <int VX, int VY>
-__device__ __forceinline__ void xy_prefetch_next(const float2 *S, long long Pc, int Pz, int next, int nitems)
+__device__ __forceinline__ void xy_prefetch_next(const float2 *S, long long Pc, int z0, int nzb, int next,
+                                                 int nitems)
 {
     if (next >= nitems) return;
     constexpr int bytes = XYShape<VX, VY>::plane * (int)sizeof(float2), NT = XYShape<VX, VY>::NT;
-    const int nb = next / Pz, nz = next - nb * Pz;
+    const int nb = next / nzb, nz = z0 + (next - nb * nzb);
     const char *p = reinterpret_cast<const char *>(S + (long long)nb * Pc + (long long)nz * XYShape<VX, VY>::plane);
     for (int off = threadIdx.x * 128; off < bytes; off += NT * 128)
         asm volatile("prefetch.global.L2 [%0];" ::"l"(p + off));
@@ -475,13 +476,14 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
 }
 
 // ---- C2R -> quotient -> R2C ----------------------------------------------------------
+// The CTAs walk the planes [z0, z0 + nzb) of every block of the batch (items nb * nzb).
 // DeconvolutionMethods.java:71-74: img > 0 ? img / conv1 : 1.  Domain voxels outside the
 // block (the value-1 extension) and outside the volume (img zero-extended) read img = 0.
 // x phase 1 inverse, the quotient and x phase 1 forward run on registers per row item.
 template <int VX, int VY>
 __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
     k_xy_ratio(float2 *__restrict__ S, const float *__restrict__ img, const BlockMaps bms, long long Pc,
-               const float2 *__restrict__ gtwx, const float2 *__restrict__ gtwy, int Pz, int nitems)
+               const float2 *__restrict__ gtwx, const float2 *__restrict__ gtwy, int z0, int nzb, int nitems)
 {
     typedef XYShape<VX, VY> SH;
     constexpr int NT = SH::NT, RX = SH::RX;
@@ -492,7 +494,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
     pdl_wait();
     // persistent: the CTA walks the (block, plane) items blockIdx.x, + gridDim.x, ...
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int bi = item / Pz, z = item - bi * Pz;
+        const int bi = item / nzb, z = z0 + (item - bi * nzb);
         const BlockMap &bm = bms.m[bi];
         float2 *Sp = S + (long long)bi * Pc + (long long)z * SH::plane;
         const int ez = ext_e(z, bm.P[2], bm.L[2]);
@@ -534,7 +536,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
             for (int v = 0; v < VX; ++v) row[16 * v] = a[v];
         }
         // the next item's plane into L2 while this one is transformed forward
-        xy_prefetch_next<VX, VY>(S, Pc, Pz, item + gridDim.x, nitems);
+        xy_prefetch_next<VX, VY>(S, Pc, z0, nzb, item + gridDim.x, nitems);
         __syncthreads();
         xy_x_forward_p2<VX, VY>(sm.A, sm.twx, sm.posx);
         xy_y<VX, VY, false>(sm.A, sm.twy, sm.posy);
