@@ -60,7 +60,7 @@ template <int V, int MODE>
 __global__ void __launch_bounds__(256, MVR_PIPE_MINB)
     k_tcols_pipe(const float2 *src, float2 *dst, const float2 *__restrict__ Kh, int Hx, long long estride,
                  long long ostride, long long Pc, const float2 *__restrict__ twg, int gather, int nother, int rlo,
-                 int rhi, int olo, PipeGeom pg, int zfill)
+                 int rhi, int olo, PipeGeom pg, int llo, int lhi)
 {
     constexpr int T = kTColT, NP = kTColNP, n = V * T, tot = n * NP;
     constexpr bool KS = pipe_kstage<V, MODE>();
@@ -100,7 +100,9 @@ __global__ void __launch_bounds__(256, MVR_PIPE_MINB)
 #pragma unroll
         for (int u = 0; u < tot / 256; ++u) {
             const long long o = c0 + u * rs;
-            cp_async8(st + threadIdx.x + 256 * u, src + boff + o, live);
+            // rows outside [llo, lhi) are zero-filled (the caller's input is zero there)
+            const int row = prow + (256 / NP) * u;
+            cp_async8(st + threadIdx.x + 256 * u, src + boff + o, live && row >= llo && row < lhi);
             if (KS) cp_async8(st + tot + threadIdx.x + 256 * u, Kh + o, live);
         }
     };
@@ -167,17 +169,10 @@ __global__ void __launch_bounds__(256, MVR_PIPE_MINB)
             for (int v = 0; v < V; ++v) A[(t + T * v) * NP + c] = a[v];
         }
         if (MODE != 0) __syncthreads();
-        // rows [rlo, rhi) of the transformed axis go back to HBM (with zfill, zeros the others)
+        // rows [rlo, rhi) of the transformed axis go back to HBM
         if (pc < np) {
             float2 *cb = dst + boff + base + (long long)pc * pstride;
-            if (!zfill) {
-                for (int e = threadIdx.x + rlo * NP; e < rhi * NP; e += 256) cb[(long long)(e / NP) * estride] = A[e];
-            } else {
-                for (int e = threadIdx.x; e < n * NP; e += 256) {
-                    const int row = e / NP;
-                    cb[(long long)row * estride] = (row >= rlo && row < rhi) ? A[e] : make_float2(0.0f, 0.0f);
-                }
-            }
+            for (int e = threadIdx.x + rlo * NP; e < rhi * NP; e += 256) cb[(long long)(e / NP) * estride] = A[e];
         }
         __syncthreads();  // the next iteration refills this stage
     }

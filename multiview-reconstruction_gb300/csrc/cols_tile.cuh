@@ -182,7 +182,7 @@ template <int V, int MODE, int NP = kTColNP>
 __global__ void __launch_bounds__(16 * NP, (NP == 16 && V <= 16) ? MVR_TCOLS_MINB : 2)
     k_tcols(const float2 *src, float2 *dst, const float2 *__restrict__ Kh, int Hx, long long estride,
             long long ostride, long long Pc, const float2 *__restrict__ twg, int gather, int nother, int rlo, int rhi,
-            int olo, int zfill)
+            int olo, int llo, int lhi)
 {
     constexpr int T = kTColT, n = V * T, NT = 16 * NP;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -230,7 +230,9 @@ __global__ void __launch_bounds__(16 * NP, (NP == 16 && V <= 16) ? MVR_TCOLS_MIN
             float2 r[LB], q[LB];
 #pragma unroll
             for (int u = 0; u < LB; ++u) {
-                r[u] = plive ? sp[(j0 + u) * rstep] : make_float2(0.0f, 0.0f);
+                // rows outside [llo, lhi) are read as zeros (the caller's input is zero there)
+                const int row = (int)(threadIdx.x / NP) + (NT / NP) * (j0 + u);
+                r[u] = (plive && row >= llo && row < lhi) ? sp[(j0 + u) * rstep] : make_float2(0.0f, 0.0f);
                 if (MODE == 2 && MVR_TCOLS_KS) q[u] = plive ? __ldg(kp + (j0 + u) * rstep) : make_float2(0.0f, 0.0f);
             }
 #pragma unroll
@@ -293,7 +295,7 @@ __global__ void __launch_bounds__(16 * NP, (NP == 16 && V <= 16) ? MVR_TCOLS_MIN
     }
     if (MODE != 0) __syncthreads();
     // rows [rlo, rhi) of the transformed axis are stored (all of them unless the caller
-    // reads only a sub-range); with zfill the other rows are stored as zeros
+    // reads only a sub-range)
     if (plive) {
         float2 *dp = dst + coff;
         const int prow = threadIdx.x / NP;
@@ -301,7 +303,6 @@ __global__ void __launch_bounds__(16 * NP, (NP == 16 && V <= 16) ? MVR_TCOLS_MIN
         for (int j = 0; j < R; ++j) {
             const int row = prow + (NT / NP) * j;
             if (row >= rlo && row < rhi) dp[j * rstep] = A[threadIdx.x + j * NT];
-            else if (zfill) dp[j * rstep] = make_float2(0.0f, 0.0f);
         }
     }
 }

@@ -626,7 +626,7 @@ int Engine<T>::kernel_spectra(Plan<T> &pl, const float *k1, const float *k2, boo
 
 template <typename T>
 int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh, int nb, int rlo,
-                           int rhi, int olo, int ohi, bool zfill)
+                           int rhi, int olo, int ohi, int llo, int lhi)
 {
     const int Hx = pl.Hx;
     long long estride, ostride;
@@ -654,15 +654,16 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
     const int kind = mode == 2 ? KK_COLS_ZMUL : (mode == 1 ? KK_COLS_INV : KK_COLS_FWD);
     const int nax = pl.P[axis];
     const bool tiled = sizeof(T) == sizeof(float) && (axis == 1 ? pl.tcy : pl.tcz);
-    if (zfill && !(tiled && rlo >= 0 && rlo <= rhi && rhi <= nax)) return fail(ERR_STATE, "zero fill needs a tile pass");
-    if (!zfill) {
-        if (rhi < 0 || rhi > nax || !tiled) rhi = nax;
-        if (rlo < 0 || rlo > rhi || rhi == nax) rlo = 0;
-    }
+    if (rhi < 0 || rhi > nax || !tiled) rhi = nax;
+    if (rlo < 0 || rlo > rhi || rhi == nax) rlo = 0;
+    if (lhi < 0 || lhi > nax) lhi = nax;
+    if (llo < 0 || llo > lhi) llo = 0;
+    if ((llo > 0 || lhi < nax) && !tiled) return fail(ERR_STATE, "a partial input band needs a tile pass");
     if (ohi < 0 || ohi > nother || !tiled) ohi = nother;
     if (olo < 0 || olo >= ohi) olo = 0;
-    const double stored = zfill ? 1.0 : (double)(rhi - rlo) / nax, part = (double)(ohi - olo) / nother;
-    MVR_TRY(prof_begin(kind, part * (mode == 2 ? (2.0 + stored) * cb : (1.0 + stored) * cb)));
+    const double stored = (double)(rhi - rlo) / nax, loaded = (double)(lhi - llo) / nax;
+    const double part = (double)(ohi - olo) / nother;
+    MVR_TRY(prof_begin(kind, part * (mode == 2 ? (1.0 + loaded + stored) * cb : (loaded + stored) * cb)));
     const long long Pc = pl.Pc;
     const int wc = axis == 1 ? pl.wcy : pl.wcz;
     const int tc = axis == 1 ? pl.tcy : pl.tcz;
@@ -685,14 +686,14 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
                     const size_t ps = pipe_smem<V_, 0>();
                     if (mode == 0)
                         k_tcols_pipe<V_, 0><<<std::min(pg.ntiles, pipe_resident<V_, 0>()), kThreads, ps, stream_>>>(
-                            src, dst, Kh, Hx, estride, ostride, Pc, tw, gather, ohi, rlo, rhi, olo, pg, zfill ? 1 : 0);
+                            src, dst, Kh, Hx, estride, ostride, Pc, tw, gather, ohi, rlo, rhi, olo, pg, llo, lhi);
                     else if (mode == 1)
                         k_tcols_pipe<V_, 1><<<std::min(pg.ntiles, pipe_resident<V_, 1>()), kThreads, ps, stream_>>>(
-                            src, dst, Kh, Hx, estride, ostride, Pc, tw, gather, ohi, rlo, rhi, olo, pg, zfill ? 1 : 0);
+                            src, dst, Kh, Hx, estride, ostride, Pc, tw, gather, ohi, rlo, rhi, olo, pg, llo, lhi);
                     else
                         MVR_CUDA(launch_pdl(k_tcols_pipe<V_, 2>, std::min(pg.ntiles, pipe_resident<V_, 2>()), kThreads,
                                             pipe_smem<V_, 2>(), stream_, src, dst, Kh, Hx, estride, ostride, Pc, tw,
-                                            gather, ohi, rlo, rhi, olo, pg, zfill ? 1 : 0));
+                                            gather, ohi, rlo, rhi, olo, pg, llo, lhi));
                 });
                 MVR_LAUNCHED("k_tcols_pipe");
                 return prof_end();
@@ -702,13 +703,13 @@ int Engine<T>::launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, 
             TILE_COLS(tc, {
                 if (mode == 0)
                     MVR_CUDA(launch_pdl(k_tcols<V_, 0>, tgrid, kThreads, ts, stream_, src, dst, Kh, Hx, estride, ostride, Pc, tw,
-                                       gather, ohi, rlo, rhi, olo, zfill ? 1 : 0));
+                                       gather, ohi, rlo, rhi, olo, llo, lhi));
                 else if (mode == 1)
                     MVR_CUDA(launch_pdl(k_tcols<V_, 1>, tgrid, kThreads, ts, stream_, src, dst, Kh, Hx, estride, ostride, Pc, tw,
-                                       gather, ohi, rlo, rhi, olo, zfill ? 1 : 0));
+                                       gather, ohi, rlo, rhi, olo, llo, lhi));
                 else
                     MVR_CUDA(launch_pdl(k_tcols<V_, 2>, tgrid, kThreads, ts, stream_, src, dst, Kh, Hx, estride, ostride, Pc, tw,
-                                       gather, ohi, rlo, rhi, olo, zfill ? 1 : 0));
+                                       gather, ohi, rlo, rhi, olo, llo, lhi));
             });
             MVR_LAUNCHED("k_tcols");
             return prof_end();
@@ -879,8 +880,9 @@ int Engine<T>::launch_xy_fwd(const Plan<T> &pl, const BlockMaps &bms, int nb, co
 // The second convolution's output on the planes [zlo, zhi) reads its input on
 // [zlo - r, zhi + r) only, r = kd / 2 + 1 covering the kernel's reach on either side of its
 // centre.  When that band lies inside the domain (no circular wrap) and is shorter than it, the
-// first convolution's Z pass stores zeros outside the band and the quotient pass works on the
-// band alone: the skipped planes carry no weight in the outputs that are kept.
+// first convolution's Z pass stores the band alone, the quotient pass works on it, and the
+// second convolution's Z pass reads it with zeros for the other planes: those carry no weight
+// in the outputs that are kept.
 // MVR_RATIO_BAND=0 keeps the quotient pass on every plane
 static bool ratio_band_off()
 {
@@ -978,11 +980,13 @@ int Engine<T>::run_seq(const Plan<T> &pl, const BlockPlace *bps, int nb, const f
     if (prune) write_region(bps, nb, zlo, zhi, ylo, yhi);
     if (pl.xy) {
         int blo = 0, bhi = -1;
-        const bool band = prune && ratio_band(pl, zlo, zhi, blo, bhi);
+        if (prune) ratio_band(pl, zlo, zhi, blo, bhi);
         MVR_TRY(launch_xy_fwd(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
-        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb, blo, bhi, 0, -1, band));
+        // the first convolution stores the band, the quotient pass works on it, and the second
+        // convolution reads it (the planes outside it are zeros to the transform)
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k1h, nb, blo, bhi));
         MVR_TRY(launch_xy_ratio(pl, bms, nb, S0_, img, blo, bhi));
-        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k2h, nb, zlo, zhi));
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S0_, pl.k2h, nb, zlo, zhi, 0, -1, blo, bhi));
     } else {
         MVR_TRY(launch_fwd_mirror(pl, bms, nb, reinterpret_cast<const T *>(bps[0].psi_src), S0_));
         MVR_TRY(launch_cols(pl, 1, 0, S0_, S0_, nullptr, nb));
@@ -1067,10 +1071,10 @@ int Engine<T>::run_mul(const std::vector<const Plan<T> *> &pls, const BlockPlace
         int zlo = 0, zhi = -1, ylo, yhi, blo = 0, bhi = -1;
         if (pl.xy && !stats_dev) write_region(bps, nb, zlo, zhi, ylo, yhi);
         const bool band = pl.xy && !stats_dev && ratio_band(pl, zlo, zhi, blo, bhi);
-        MVR_TRY(launch_cols(pl, 2, 2, S0_, S1_, pl.k1h, nb, band ? blo : 0, band ? bhi : -1, 0, -1, band));
+        MVR_TRY(launch_cols(pl, 2, 2, S0_, S1_, pl.k1h, nb, band ? blo : 0, band ? bhi : -1));
         if (pl.xy) {
             MVR_TRY(launch_xy_ratio(pl, bms, nb, S1_, imgs[v], band ? blo : 0, band ? bhi : -1));
-            MVR_TRY(launch_cols(pl, 2, 2, S1_, S1_, pl.k2h, nb, zlo, zhi));
+            MVR_TRY(launch_cols(pl, 2, 2, S1_, S1_, pl.k2h, nb, zlo, zhi, 0, -1, band ? blo : 0, band ? bhi : -1));
         } else {
             MVR_TRY(launch_cols(pl, 1, 1, S1_, S1_, nullptr, nb));
             MVR_TRY(launch_ratio(pl, bms, nb, S1_, imgs[v]));

@@ -159,11 +159,11 @@ private:
                          double bytes, double *stats_dev);
     // rows [rlo, rhi) of the transformed axis are stored, and only the other-axis indices
     // [olo, ohi) are transformed (negative hi: all; tile kernels only, the others do all);
-    // zfill (tile kernels only): the rows outside [rlo, rhi) are stored as zeros
+    // the input rows outside [llo, lhi) are taken as zeros without being read (tile kernels)
     int launch_cols(const Plan<T> &pl, int axis, int mode, const V *src, V *dst, const V *Kh, int nb, int rlo = 0,
-                    int rhi = -1, int olo = 0, int ohi = -1, bool zfill = false);
+                    int rhi = -1, int olo = 0, int ohi = -1, int llo = 0, int lhi = -1);
     // the planes [lo, hi) that the second convolution reads for a write region [zlo, zhi) (its
-    // kernel's reach either side); false when pruning does not apply
+    // kernel's reach either side); false when pruning does not apply (lo = 0, hi = P)
     bool ratio_band(const Plan<T> &pl, int zlo, int zhi, int &lo, int &hi) const;
     int launch_ratio(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const float *img);
     int launch_update(const Plan<T> &pl, const BlockMaps &bms, int nb, V *S, const UpdateArgs &ua, int epi,
