@@ -97,43 +97,33 @@ struct WeightPtrs {
     float *out[kMaxViews];
 };
 
-// NormalizingRandomAccess.get 76-109 (hardWeights 211-214, smoothWeights 183-200).
-// The raw weights are read twice (sum, then per view) instead of being held in a
-// per-thread array, which would live in local memory.
+// NormalizingRandomAccess.get 76-109 (hardWeights 211-214, smoothWeights 183-200), one voxel
+// at a time through mvr_wd_normalize: float operations that round as the reference's double
+// sum and division do (the double operations only next to a float rounding boundary).  The
+// views' weights sit in registers (loops over MAXV >= nv views, unrolled), and every thread
+// loads U voxels before normalising any, so that more loads are in flight.
+template <int MAXV, int U = (MAXV <= 8 ? 2 : 1)>
 __global__ void k_normalize_weights(WeightPtrs wp, int nv, long long n, double osem, int smooth, float maxDiffRange,
                                     float scalingRange)
 {
-    // the double sum of the reference is kept, and its division rounds as the reference's
-    // (mvr_weight_div: float operations, the double division only next to a float rounding
-    // boundary); min(1, w) is exact in float, and the OSEM factor 1 needs no product
-    const bool osem_one = osem == 1.0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        double sumW = 0.0;
-        for (int v = 0; v < nv; ++v) sumW += (double)fminf(1.0f, wp.raw[v][i]);
-        const MvrWdSum ws = mvr_wd_sum(sumW);
-        for (int v = 0; v < nv; ++v) {
-            const float my = fminf(1.0f, wp.raw[v][i]);
-            if (!smooth && osem_one) {
-                wp.out[v][i] = sumW > 1 ? mvr_weight_div(my, &ws) : my;
-                continue;
-            }
-            double r;
-            if (smooth) {
-                float s;
-                if (sumW <= 0) s = 0.0f;
-                else {
-                    const float ideal = mvr_weight_div(my, &ws);
-                    const float diff = __fsub_rn(my, ideal);
-                    float y = __fmul_rn(__fsub_rn(maxDiffRange, fabsf(diff)), __fdiv_rn(1.0f, maxDiffRange));
-                    y = y > 0.0f ? y : 0.0f;
-                    const float scale = __fmul_rn(__fmul_rn(y, my), scalingRange);
-                    s = __fsub_rn(fminf(my, ideal), scale);
-                }
-                r = s;
-            } else if (sumW > 1) r = mvr_weight_div(my, &ws);
-            else r = my;
-            const double m = r * osem;
-            wp.out[v][i] = (float)(m < 1.0 ? m : 1.0);
+    const int osem_one = osem == 1.0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n; i0 += U * stride) {
+        float w[U][MAXV], o[MAXV];
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+            const long long i = i0 + k * stride;
+#pragma unroll
+            for (int v = 0; v < MAXV; ++v) w[k][v] = (v < nv && i < n) ? fminf(1.0f, wp.raw[v][i]) : 0.0f;
+        }
+#pragma unroll
+        for (int k = 0; k < U; ++k) {
+            const long long i = i0 + k * stride;
+            if (i >= n) break;
+            mvr_wd_normalize(w[k], nv, MAXV, osem_one, osem, smooth, maxDiffRange, scalingRange, o);
+#pragma unroll
+            for (int v = 0; v < MAXV; ++v)
+                if (v < nv) wp.out[v][i] = o[v];
         }
     }
 }
@@ -1091,9 +1081,16 @@ int Decon<T>::normalize_weights()
         wp.raw[v] = views_[v].w_raw;
         wp.out[v] = views_[v].w;
     }
-    k_normalize_weights<<<grid_for(n_), 256, 0, engine_.stream()>>>(wp, p_.num_views, n_, (double)p_.osem_speedup,
-                                                                   p_.weight_norm == MVR_WEIGHTS_SMOOTH,
-                                                                   p_.max_diff_range, p_.scaling_range);
+    const int nv = p_.num_views, sm = p_.weight_norm == MVR_WEIGHTS_SMOOTH;
+    const double osem = (double)p_.osem_speedup;
+    cudaStream_t s = engine_.stream();
+    if (nv <= 4)
+        k_normalize_weights<4><<<grid_for(n_), 256, 0, s>>>(wp, nv, n_, osem, sm, p_.max_diff_range, p_.scaling_range);
+    else if (nv <= 8)
+        k_normalize_weights<8><<<grid_for(n_), 256, 0, s>>>(wp, nv, n_, osem, sm, p_.max_diff_range, p_.scaling_range);
+    else
+        k_normalize_weights<16><<<grid_for(n_), 256, 0, s>>>(wp, nv, n_, osem, sm, p_.max_diff_range,
+                                                             p_.scaling_range);
     D_CUDA(cudaGetLastError());
     weights_dirty_ = false;
     return MVR_OK;
