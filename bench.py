@@ -61,12 +61,16 @@ class Workload:
         self.metric = f"voxel-iterations/s ({views} views)"
 
     def blocks(self, v):
-        import oracle
+        """The library's block grid of view v (mvr_block_grid, the whole-volume driver's)."""
+        import mvrgb300 as M
 
-        kk = tuple(2 * k - 1 for k in self.psfs[v])
+        k = self.psfs[v]
         if self.effective:
-            kk = tuple(self.vblocks[v][d] - self.effective[d] + 1 for d in range(3))
-        return oracle.divide_into_blocks(self.dims, kk, self.vblocks[v])
+            # the overlap block - effective + 1 as the doubled kernel 2k' - 1 of a kernel k'
+            kk = [self.vblocks[v][d] - self.effective[d] + 1 for d in range(3)]
+            assert all(x % 2 == 1 for x in kk), "block - effective must be even"
+            k = tuple((x + 1) // 2 for x in kk)
+        return M.block_grid(self.dims, k, self.vblocks[v])[0]
 
     def ref_vblocks(self):
         """The reference's compute block per view for the same effective grid: effective + 2 (k - 1)."""
