@@ -45,6 +45,18 @@ __device__ __forceinline__ long long neighbour(const ConvGeom &g, int x, int y, 
     return (((long long)b * g.D + zz) * g.H + yy) * g.W + xx;
 }
 
+// 16-byte asynchronous copy global -> shared (L2 only); ok == false writes 16 zero bytes
+// (source size 0, the source address not read)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, bool ok)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(ok ? 16 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
 template <int N>
 struct TmemCols {
     static constexpr uint32_t value = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
@@ -383,32 +395,35 @@ __global__ void __launch_bounds__(128) k_conv3d_shift(const __nv_bfloat16 *__res
     const int z0 = (int)(q % g.D);
     const int b = (int)(q / g.D);
     const int x0 = ibx * kShX, y0 = iby * kShY;
-    // halo, channel chunk fastest (coalesced reads), zero outside the volume
+    // halo, channel chunk fastest (coalesced reads), zero outside the volume; every copy is
+    // asynchronous, so a thread's copies are all in flight together
     for (int k = tid; k < kShRows * CH; k += 128) {
         const int h = k / CH, j = k - h * CH;
         const int hx = h % kShHX, hy = (h / kShHX) % kShHY, hz = h / (kShHX * kShHY);
         const int xx = x0 - 1 + hx, yy = y0 - 1 + hy, zz = z0 - 1 + hz;
-        uint4 v = make_uint4(0, 0, 0, 0);
-        if (xx >= 0 && yy >= 0 && zz >= 0 && xx < g.W && yy < g.H && zz < g.D) {
+        const bool in = xx >= 0 && yy >= 0 && zz >= 0 && xx < g.W && yy < g.H && zz < g.D;
+        const uint4 *src = reinterpret_cast<const uint4 *>(act);
+        if (in) {
             if constexpr (CU == 0) {
-                v = __ldg(reinterpret_cast<const uint4 *>(act + ((((long long)b * g.D + zz) * g.H + yy) * g.W + xx) * C) + j);
+                src = reinterpret_cast<const uint4 *>(act + ((((long long)b * g.D + zz) * g.H + yy) * g.W + xx) * C) + j;
             } else if (j < CU / 8) {
                 const long long lv = (((long long)b * (g.D / 2) + zz / 2) * (g.H / 2) + yy / 2) * (g.W / 2) + xx / 2;
-                v = __ldg(reinterpret_cast<const uint4 *>(act + lv * CU) + j);
+                src = reinterpret_cast<const uint4 *>(act + lv * CU) + j;
             } else {
                 const long long hv2 = (((long long)b * g.D + zz) * g.H + yy) * g.W + xx;
-                v = __ldg(reinterpret_cast<const uint4 *>(act2 + hv2 * (C - CU)) + (j - CU / 8));
+                src = reinterpret_cast<const uint4 *>(act2 + hv2 * (C - CU)) + (j - CU / 8);
             }
         }
-        *reinterpret_cast<uint4 *>(halo + (size_t)j * kShLbo + 16 * h) = v;
+        cp_async16(halo + (size_t)j * kShLbo + 16 * h, src, in);
     }
     // B chunk c (taps G c .. G c + G - 1) into buffer `buf`, canonical K-major per tap
     auto load_b = [&](int c, int buf) {
         for (int s = tid; s < G * N * CH; s += 128) {
             const int tt = s / (N * CH), rem = s - tt * (N * CH), r = rem / CH, j = rem - r * CH;
-            const uint4 v = __ldg(reinterpret_cast<const uint4 *>(wk + ((long long)r * 27 + G * c + tt) * C) + j);
-            *reinterpret_cast<uint4 *>(sB[buf] + tt * B_TAP + tc::core_offset(r, 8 * j, C)) = v;
+            cp_async16(sB[buf] + tt * B_TAP + tc::core_offset(r, 8 * j, C),
+                       reinterpret_cast<const uint4 *>(wk + ((long long)r * 27 + G * c + tt) * C) + j, true);
         }
+        cp_async_wait_all();
     };
     load_b(0, 0);
     tc::fence_proxy_async();
