@@ -95,7 +95,8 @@ def test_forced_schedules_on_288_columns():
         assert rel(out[code], out[M.SCHED_ROWS]) <= 1e-6, M.schedule_name(code)
 
 
-def test_effective_block_grid_matches_the_reference_grid():
+@pytest.mark.parametrize("mul", [False, True])
+def test_effective_block_grid_matches_the_reference_grid(mul):
     # effective blocks 48 x 40 x 36 with 9 x 9 x 15 PSFs: the reference's blocks are
     # 64 x 56 x 64 (effective + 2 (k - 1)); here 128 x 128 x 96 compute blocks (plane kernels)
     # on the same grid of effective blocks, and the same effective size with the reference's
@@ -114,7 +115,7 @@ def test_effective_block_grid_matches_the_reference_grid():
     eff, ref_block = (48, 40, 36), (64, 56, 64)
     out = {}
     for block, e in (((128, 128, 96), eff), (ref_block, None)):
-        with M.Deconvolution(dims, 2, block, psf_type=M.PSF_OPTIMIZATION_I, lam=0.006,
+        with M.Deconvolution(dims, 2, block, mul=mul, psf_type=M.PSF_OPTIMIZATION_I, lam=0.006,
                              boundary=M.BOUNDARY_CIRCULAR, weight_norm=M.WEIGHTS_AS_GIVEN) as d:
             for v in range(2):
                 d.set_view(v, imgs[v], ws[v], psfs[v])
@@ -128,7 +129,7 @@ def test_effective_block_grid_matches_the_reference_grid():
     assert rel(big, out[ref_block]) <= 1e-5
     k1s, k2s = O.psf_init(psfs, O.PSF_OPTIMIZATION_I, 0)
     psi0, mx, _ = O.psi_init_avg(imgs)
-    ref, _ = O.decon_run(psi0, imgs, ws, k1s, k2s, ref_block, 2, lam=0.006, max_intensities=mx)
+    ref, _ = O.decon_run(psi0, imgs, ws, k1s, k2s, ref_block, 2, mul=mul, lam=0.006, max_intensities=mx)
     assert rel(big, ref) <= 1e-4
 
 

@@ -188,7 +188,9 @@ def test_graph_replay_matches_eager_launches(vol, block, mul):
     assert np.array_equal(st_g, st_e)
 
 
-def test_run_host_next_prefetches_the_next_inputs(vol):
+@pytest.mark.parametrize("mul,precision", [(False, M.PRECISION_FP32), (True, M.PRECISION_FP32),
+                                           (False, M.PRECISION_FP64)])
+def test_run_host_next_prefetches_the_next_inputs(vol, mul, precision):
     # mvr_decon_run_host_next: the next call's images and weights upload during this call.  A
     # sequence over two input sets (A, B = A with brighter images and other weights) gives the
     # psi of the same sequence of plain mvr_decon_run_host calls, whether the next call's arrays
@@ -199,22 +201,22 @@ def test_run_host_next_prefetches_the_next_inputs(vol):
     b_w = [np.ascontiguousarray(a_w[1]), np.ascontiguousarray(a_w[0])]
     c_i = [a * np.float32(0.8) for a in a_i]
     seq = [(a_i, a_w, b_i, b_w), (b_i, b_w, a_i, a_w), (a_i, a_w, b_i, b_w), (c_i, a_w, None, None)]
-    with make(vol, (28, 28, 28)) as d:
+    with make(vol, (28, 28, 28), mul=mul, precision=precision) as d:
         psi0 = d.get_psi()
     ref = psi0.copy()
-    with make(vol, (28, 28, 28)) as d:
+    with make(vol, (28, 28, 28), mul=mul, precision=precision) as d:
         refs = []
         for im, w, _, _ in seq:
             d.run_host(1, im, w, ref)
             refs.append(ref.copy())
     psi = psi0.copy()
-    with make(vol, (28, 28, 28)) as d:
+    with make(vol, (28, 28, 28), mul=mul, precision=precision) as d:
         for (im, w, ni, nw), r in zip(seq, refs):
             d.run_host(1, im, w, psi, ni, nw)
             assert rel(psi, r) <= 1e-6
         d.run_host(2, a_i, a_w, psi, a_i, a_w)  # two iterations: the second from the graph path
         d.synchronize()
-    with make(vol, (28, 28, 28)) as d:
+    with make(vol, (28, 28, 28), mul=mul, precision=precision) as d:
         d.run_host(2, a_i, a_w, ref)
     assert rel(psi, ref) <= 1e-6
 
