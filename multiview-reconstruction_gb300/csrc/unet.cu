@@ -25,8 +25,11 @@
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "../../include/mvr_gb300.h"
 #include "conv3d_tc.cuh"
+#include "conv3d_tma.cuh"
 #include "fsum.cuh"
 
 namespace mvr {
@@ -42,14 +45,85 @@ size_t conv_smem() { return 2 * (128 * C * 2 + N * C * 2); }
 template <int N>
 size_t wgrad_smem() { return 2 * (128 * 64 * 2 + N * 64 * 2); }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// MVR_CONV_TMA=0 keeps every convolution on k_conv3d_shift
+bool conv_tma_enabled()
+{
+    const char *e = std::getenv("MVR_CONV_TMA");
+    return !(e && e[0] == '0');
+}
+
+// The persistent TMA convolution (k_conv3d_tma) of a shape that fits: the tensor map of the
+// [B][D][H][W][C] input with a box of 8 channels x 10 x 18 x 3 voxels, one CTA per SM slot.
+// cudaErrorNotSupported when no encoder is available (the caller falls back).
+template <int N, int C, int OUT>
+cudaError_t launch_conv_tma(const bf16 *act, const bf16 *w, const float *bias, void *out, const ConvGeom &g, int sign,
+                            int relu, int *err, cudaStream_t s)
+{
+    const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return cudaErrorNotSupported;
+    CUtensorMap map;
+    const cuuint64_t dims[5] = {(cuuint64_t)C, (cuuint64_t)g.W, (cuuint64_t)g.H, (cuuint64_t)g.D, (cuuint64_t)g.B};
+    const cuuint64_t strides[4] = {(cuuint64_t)C * 2, (cuuint64_t)g.W * C * 2, (cuuint64_t)g.H * g.W * C * 2,
+                                   (cuuint64_t)g.D * g.H * g.W * C * 2};
+    const cuuint32_t box[5] = {8, (cuuint32_t)kShHX, (cuuint32_t)kShHY, (cuuint32_t)kShHZ, 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(act), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    const size_t sm = conv_tma_smem<N, C>();
+    cudaError_t e =
+        cudaFuncSetAttribute(k_conv3d_tma<N, C, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_conv3d_tma<N, C, OUT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 (int)cudaSharedmemCarveoutMaxShared);
+    if (e != cudaSuccess) return e;
+    int per = 0, dev = 0, nsm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_conv3d_tma<N, C, OUT>, 128, sm)) != cudaSuccess)
+        return e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    const long long bricks =
+        (long long)((g.W + kShX - 1) / kShX) * ((g.H + kShY - 1) / kShY) * g.D * g.B;
+    const long long grid = std::min<long long>(bricks, (long long)nsm * std::max(1, per));
+    k_conv3d_tma<N, C, OUT><<<(unsigned)grid, 128, sm, s>>>(map, w, bias, out, g, sign, relu, err);
+    return cudaGetLastError();
+}
+
 // Forward and data-gradient convolutions run on 8 x 16 x 1 output bricks with the input
-// halo staged once in shared memory and one descriptor per tap (k_conv3d_shift);
-// k_conv3d_brick (halo, per-tap copies) and k_conv3d_tc (gathered per tap) are earlier
-// forms of the same product.
+// halo staged once in shared memory and one descriptor per tap: the persistent TMA kernel
+// where its buffers fit and N + C >= 48 (k_conv3d_tma), else k_conv3d_shift; k_conv3d_brick
+// (halo, per-tap copies) and k_conv3d_tc (gathered per tap) are earlier forms of the same
+// product.  Measured on the 128^3 grid (ncu, serialised): 16 <- 48 channels 632 against
+// 680 us, 32 <- 16 (64^3) 40 against 49 us, 64 <- 32 (32^3) 20 against 28 us, but 16 <- 16
+// 251 against 193 us: the halo's tiles have a 16-byte inner extent (one K group of one voxel),
+// which the copy engine moves as that many small rows, and the threads' 16-byte
+// asynchronous copies of k_conv3d_shift keep up with it when the tile is small.
 template <int N, int C, int OUT>
 cudaError_t launch_conv(const bf16 *act, const bf16 *w, const float *bias, void *out, const ConvGeom &g, int sign,
                         int relu, int *err, cudaStream_t s)
 {
+    if constexpr (conv_tma_fits<N, C>() && N + C >= 48) {
+        if (conv_tma_enabled()) {
+            const cudaError_t e = launch_conv_tma<N, C, OUT>(act, w, bias, out, g, sign, relu, err, s);
+            if (e != cudaErrorNotSupported) return e;
+        }
+    }
     const size_t sm = conv_shift_smem<N, C>();
     cudaError_t e =
         cudaFuncSetAttribute(k_conv3d_shift<N, C, OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -594,6 +668,8 @@ int UNet::forward(float *pred, bool fused)
     k_pool<<<gsize(g3_.nvox * 32), 256, 0, s_>>>(e2_, p2_, g3_, 32);
     C_(conv_any(64, 32, 0, p2_, wt_[2], params_ + boff_[2], b3_, g3_, 1, 1, err_dev_, s_))
     if (fused) {  // inference: the decoder convolutions read [up(low), skip] directly
+        // (materialising [up(d2), e1] for the TMA kernel costs more than that kernel saves:
+        // 82 + 632 against 680 us on the 128^3 grid)
         C_((launch_conv_concat<32, 96, 64>(b3_, e2_, wt_[3], params_ + boff_[3], d2_, g2_, err_dev_, s_)))
         C_((launch_conv_concat<16, 48, 32>(d2_, e1_, wt_[4], params_ + boff_[4], d1_, g1_, err_dev_, s_)))
     } else {  // training: the concatenations are kept for the backward pass
