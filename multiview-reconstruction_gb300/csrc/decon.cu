@@ -1558,6 +1558,10 @@ int Decon<T>::run_host(int iterations, const float *const *imgs, const float *co
         pre_w_.assign(next_ws, next_ws + nv);
         pre_valid_ = true;
     }
+    // prefetched raw weights are already on the device (the compute stream waited for the
+    // second set above): normalise them while psi is still uploading
+    const bool norm = p_.weight_norm != MVR_WEIGHTS_AS_GIVEN;
+    if (pre && norm) D_TRY(normalize_weights());
     D_CUDA(cudaStreamWaitEvent(s, ev_w_, 0));
     if (sizeof(T) != sizeof(float)) {
         // FP64 run: the uploaded float psi (in the staging volume) converted into psi
@@ -1569,7 +1573,7 @@ int Decon<T>::run_host(int iterations, const float *const *imgs, const float *co
         D_CUDA(cudaStreamSynchronize(s));
         cudaFree(hold);
     }
-    if (p_.weight_norm != MVR_WEIGHTS_AS_GIVEN) D_TRY(normalize_weights());
+    if (!pre && norm) D_TRY(normalize_weights());
     int it = 0;
     if (!pre) {
         // the first iteration eagerly, each view-step after its image
