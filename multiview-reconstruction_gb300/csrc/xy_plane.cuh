@@ -30,6 +30,8 @@
 // layout of the plane in S ([z][y][c], c < m + 1), so the plane moves between HBM and
 // shared memory as one contiguous 16-byte-vectorised copy.
 #pragma once
+#include <type_traits>
+
 #include "rows_warp.cuh"
 #include "cols_tile.cuh"
 #include "pdl.cuh"
@@ -225,15 +227,16 @@ __device__ __forceinline__ void xy_x_p2_item(float2 (&b)[16], float2 *b0, int k1
     }
 }
 
-// x phase 2 items of the rows [y0, y0 + NR): item it (warp-aligned) is row y of a block of 16
-// rows; half-warp h holds k1, the other half its partner V - k1 (or the self-paired k1 = 0 and
-// V / 2 in the last group), for threads i0, i0 + step, ... of the items.
-template <int VX, int VY, bool INV, int NR>
-__device__ __forceinline__ void xy_x_p2_rows(float2 *A, const float2 *twx, int y0, int i0, int step)
+// x phase 2 items of the rows [y0, y0 + 16 RB): item it (warp-aligned) is row y of a block of
+// 16 rows; half-warp h holds k1, the other half its partner V - k1 (or the self-paired k1 = 0
+// and V / 2 in the last group), for threads i0, i0 + step, ... of the items.
+template <int VX, int VY, bool INV>
+__device__ __forceinline__ void xy_x_p2_rows_n(float2 *A, const float2 *twx, int y0, int RB, int i0, int step)
 {
     typedef XYShape<VX, VY> S;
-    constexpr int T = 16, RB = NR / 16, items = NR * VX;
-    static_assert(NR % 16 == 0 && VX % 2 == 0 && items % 32 == 0, "whole warps of row pairs");
+    constexpr int T = 16;
+    static_assert(VX % 2 == 0 && (16 * VX) % 32 == 0, "whole warps of row pairs");
+    const int items = 16 * RB * VX;
     for (int it = i0; it < items; it += step) {
         const int l = it & 31, grp = it >> 5;
         const int h = l >> 4, jp = grp / RB;
@@ -246,6 +249,14 @@ __device__ __forceinline__ void xy_x_p2_rows(float2 *A, const float2 *twx, int y
         for (int t = 0; t < T; ++t) b[t] = b0[t];
         xy_x_p2_item<VX, VY, INV>(b, b0, k1, h, selfgrp, twx);
     }
+}
+
+// the same for a compile-time row count NR
+template <int VX, int VY, bool INV, int NR>
+__device__ __forceinline__ void xy_x_p2_rows(float2 *A, const float2 *twx, int y0, int i0, int step)
+{
+    static_assert(NR % 16 == 0, "whole blocks of 16 rows");
+    xy_x_p2_rows_n<VX, VY, INV>(A, twx, y0, NR / 16, i0, step);
 }
 
 template <int VX, int VY, bool INV>
@@ -595,7 +606,15 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
         xy_load_plane<VX, VY>(sm.A, Sp);
         __syncthreads();
         xy_y<VX, VY, true>(sm.A, sm.twy, sm.posy);
-        xy_x_inverse_p2<VX, VY>(sm.A, sm.twx, sm.posx);
+        if (ua.prune) {
+            // only the rows of the write region go on through the x transform (in whole
+            // blocks of 16 rows)
+            const int y0 = bm.wlo[1] & ~15, y1 = min(SH::Py, (bm.whi[1] + 15) & ~15);
+            if (y1 > y0) xy_x_p2_rows_n<VX, VY, true>(sm.A, sm.twx, y0, (y1 - y0) >> 4, threadIdx.x, NT);
+            __syncthreads();
+        } else {
+            xy_x_inverse_p2<VX, VY>(sm.A, sm.twx, sm.posx);
+        }
         const float *psrc = reinterpret_cast<const float *>(ua.psi_src);
         float *pdst = reinterpret_cast<float *>(ua.psi_dst);
         const float *wgt = ua.weight[0];
@@ -605,48 +624,61 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
         uc.inv_maxI = 1.0f / ua.maxI;
         uc.two_lambda = ua.two_lambda;
         uc.tik = ua.tik != 0;
+        // ST: with the statistics every block voxel is updated and summed; without them (a
+        // pruned run) only the written voxels are, and only their psi and weight are read
+        auto rows = [&](auto stats) {
+            constexpr bool ST = decltype(stats)::value;
 #pragma unroll 1
-        for (int r = 0; r < RX; ++r) {
-            const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;
-            const long long pb = sm.rowb[y], wb = sm.rowb2[y], ob = sm.rowb3[y];
-            if (pb < 0 || (ua.prune && ob == kNoRow)) continue;  // not a block row / not written
-            float pv[VX][2], wv[VX][2];
+            for (int r = 0; r < RX; ++r) {
+                const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;
+                const long long pb = sm.rowb[y], wb = sm.rowb2[y], ob = sm.rowb3[y];
+                if (pb < 0 || (!ST && ob == kNoRow)) continue;  // not a block row / not written
+                float pv[VX][2], wv[VX][2];
 #pragma unroll
-            for (int v = 0; v < VX; ++v) {
-                const int x = 2 * (t + 16 * v);  // even: the pair of table entries is one 8-byte read
-                const int2 mx = *reinterpret_cast<const int2 *>(sm.colx + x);
-                const int2 gx = *reinterpret_cast<const int2 *>(sm.colx2 + x);
-                pv[v][0] = mx.x >= 0 ? __ldg(psrc + pb + mx.x) : 0.0f;
-                pv[v][1] = mx.y >= 0 ? __ldg(psrc + pb + mx.y) : 0.0f;
-                wv[v][0] = (wb >= 0 && gx.x >= 0) ? __ldg(wgt + wb + gx.x) : 0.0f;
-                wv[v][1] = (wb >= 0 && gx.y >= 0) ? __ldg(wgt + wb + gx.y) : 0.0f;
-            }
-            float2 a[VX];
-            const float2 *row = sm.A + y * SH::SR + t;
+                for (int v = 0; v < VX; ++v) {
+                    const int x = 2 * (t + 16 * v);  // even: the pair of table entries is one 8-byte read
+                    const int2 mx = *reinterpret_cast<const int2 *>(sm.colx + x);
+                    const int2 gx = *reinterpret_cast<const int2 *>(sm.colx2 + x);
+                    const int2 c3 = *reinterpret_cast<const int2 *>(sm.colx3 + x);
+                    const bool u0 = mx.x >= 0 && (ST || c3.x >= 0), u1 = mx.y >= 0 && (ST || c3.y >= 0);
+                    pv[v][0] = u0 ? __ldg(psrc + pb + mx.x) : 0.0f;
+                    pv[v][1] = u1 ? __ldg(psrc + pb + mx.y) : 0.0f;
+                    wv[v][0] = (u0 && wb >= 0 && gx.x >= 0) ? __ldg(wgt + wb + gx.x) : 0.0f;
+                    wv[v][1] = (u1 && wb >= 0 && gx.y >= 0) ? __ldg(wgt + wb + gx.y) : 0.0f;
+                }
+                float2 a[VX];
+                const float2 *row = sm.A + y * SH::SR + t;
 #pragma unroll
-            for (int v = 0; v < VX; ++v) a[v] = row[16 * v];
-            xrow_p1<VX, true>(a, sm.twx, t);  // natural order: conv2 at x = 2 (t + 16 v) + {0, 1}
+                for (int v = 0; v < VX; ++v) a[v] = row[16 * v];
+                xrow_p1<VX, true>(a, sm.twx, t);  // natural order: conv2 at x = 2 (t + 16 v) + {0, 1}
 #pragma unroll
-            for (int v = 0; v < VX; ++v) {
-                const float cv[2] = {a[v].x, a[v].y};
-                const int2 cx = *reinterpret_cast<const int2 *>(sm.colx + 2 * (t + 16 * v));
-                const int2 c3 = *reinterpret_cast<const int2 *>(sm.colx3 + 2 * (t + 16 * v));
+                for (int v = 0; v < VX; ++v) {
+                    const float cv[2] = {a[v].x, a[v].y};
+                    const int2 cx = *reinterpret_cast<const int2 *>(sm.colx + 2 * (t + 16 * v));
+                    const int2 c3 = *reinterpret_cast<const int2 *>(sm.colx3 + 2 * (t + 16 * v));
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int x = 2 * (t + 16 * v) + h;
-                    if ((h ? cx.y : cx.x) < 0) continue;  // beyond the block
-                    const float last = pv[v][h];
-                    const float next = next_value_fast(last, cv[h], wv[v][h], uc);
-                    const float ch = next - last;  // signed change (DeconvolutionMethods.java:308)
-                    const float ky = ch - kcomp;
-                    const float kt = ksum + ky;
-                    kcomp = (kt - ksum) - ky;
-                    ksum = kt;
-                    kmax = kmax > ch ? kmax : ch;
-                    if (ob != kNoRow && (h ? c3.y : c3.x) >= 0) pdst[ob + x] = next;
+                    for (int h = 0; h < 2; ++h) {
+                        const int x = 2 * (t + 16 * v) + h;
+                        if ((h ? cx.y : cx.x) < 0) continue;  // beyond the block
+                        const bool w = ob != kNoRow && (h ? c3.y : c3.x) >= 0;
+                        if (!ST && !w) continue;
+                        const float last = pv[v][h];
+                        const float next = next_value_fast(last, cv[h], wv[v][h], uc);
+                        if constexpr (ST) {
+                            const float ch = next - last;  // signed change (DeconvolutionMethods.java:308)
+                            const float ky = ch - kcomp;
+                            const float kt = ksum + ky;
+                            kcomp = (kt - ksum) - ky;
+                            ksum = kt;
+                            kmax = kmax > ch ? kmax : ch;
+                        }
+                        if (w) pdst[ob + x] = next;
+                    }
                 }
             }
-        }
+        };
+        if (ua.prune) rows(std::false_type{});
+        else rows(std::true_type{});
     } else {
         pdl_wait();
         xy_load_plane<VX, VY>(sm.A, Sp);

@@ -135,11 +135,16 @@ def test_volume_run_and_likelihood_plane_kernels():
     assert res[True][2] == pytest.approx(res[False][2], rel=1e-6)
 
 
-@pytest.mark.parametrize("mul,plane,block,dims", [(False, True, (128, 128, 64), (200, 180, 150)),
-                                                  (True, True, (128, 128, 64), (200, 180, 150)),
-                                                  (False, False, (128, 128, 64), (200, 180, 150)),
-                                                  (False, False, (256, 256, 256), (300, 280, 270))])
-def test_runs_without_statistics_write_the_same_volume(mul, plane, block, dims):
+@pytest.mark.parametrize("mul,plane,block,dims,boundary", [
+    (False, True, (128, 128, 64), (200, 180, 150), M.BOUNDARY_REFERENCE),
+    (True, True, (128, 128, 64), (200, 180, 150), M.BOUNDARY_REFERENCE),
+    (False, False, (128, 128, 64), (200, 180, 150), M.BOUNDARY_REFERENCE),
+    (False, False, (256, 256, 256), (300, 280, 270), M.BOUNDARY_REFERENCE),
+    # FFT domains of the blocks themselves: the 128 x 128 and 192 x 192 plane kernels
+    (False, True, (128, 128, 64), (200, 180, 150), M.BOUNDARY_CIRCULAR),
+    (False, True, (192, 192, 64), (300, 280, 150), M.BOUNDARY_CIRCULAR),
+    (True, True, (192, 192, 64), (300, 280, 150), M.BOUNDARY_CIRCULAR)])
+def test_runs_without_statistics_write_the_same_volume(mul, plane, block, dims, boundary):
     # without statistics the plane kernels (and the row / column path's second Z pass, Y
     # inverse and update) work only on the planes and rows of each block's write region;
     # the volume they leave is bit-identical to the run that updates (and reduces) every
@@ -156,7 +161,7 @@ def test_runs_without_statistics_write_the_same_volume(mul, plane, block, dims):
         try:
             with plane_kernels(plane):
                 d = M.Deconvolution(dims, 2, block, mul=mul, psf_type=M.PSF_OPTIMIZATION_I, lam=0.006,
-                                    weight_norm=M.WEIGHTS_HARD)
+                                    boundary=boundary, weight_norm=M.WEIGHTS_HARD)
                 for v in range(2):
                     d.set_view(v, ds.images[v], ds.weights[v], ds.psfs[v])
                 d.prepare()
