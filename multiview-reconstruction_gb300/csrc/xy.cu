@@ -86,6 +86,7 @@ void set_limits_one()
     cudaFuncSetAttribute(k_xy_fwd<VX, VY, SrcKernel>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     cudaFuncSetAttribute(k_xy_ratio<VX, VY>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     cudaFuncSetAttribute(k_xy_update<VX, VY, EPI_SEQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
+    cudaFuncSetAttribute(k_xy_update<VX, VY, EPI_SEQ, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     cudaFuncSetAttribute(k_xy_update<VX, VY, EPI_MUL_FIRST>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     cudaFuncSetAttribute(k_xy_update<VX, VY, EPI_MUL_ACC>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
     cudaFuncSetAttribute(k_xy_update<VX, VY, EPI_MUL_FINAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, m);
@@ -258,11 +259,17 @@ cudaError_t xy_update(int combo, int epi, float2 *S, const UpdateArgs &ua, const
         return cudaGetLastError();
     }
     const dim3 grid((unsigned)planes, (unsigned)nb);
-#define XY_UPD(E)                                                                                           \
-    XY_DISPATCH(combo, return launch_pdl(k_xy_update<VX_, VY_, E>, grid, XYShape<VX_, VY_>::NT,              \
+#define XY_UPD(...)                                                                                         \
+    XY_DISPATCH(combo, return launch_pdl(k_xy_update<VX_, VY_, __VA_ARGS__>, grid, XYShape<VX_, VY_>::NT,    \
                                          xy_smem_bytes<VX_, VY_>(), s, S, ua, bms, Pc, twx, twy))
     switch (epi) {
-    case EPI_SEQ: XY_UPD(EPI_SEQ); break;
+    case EPI_SEQ:
+        if (ua.prune) {
+            XY_UPD(EPI_SEQ, true);  // the write regions alone
+        } else {
+            XY_UPD(EPI_SEQ);
+        }
+        break;
     case EPI_MUL_FIRST: XY_UPD(EPI_MUL_FIRST); break;
     case EPI_MUL_ACC: XY_UPD(EPI_MUL_ACC); break;
     case EPI_MUL_FINAL: XY_UPD(EPI_MUL_FINAL); break;

@@ -30,8 +30,6 @@
 // layout of the plane in S ([z][y][c], c < m + 1), so the plane moves between HBM and
 // shared memory as one contiguous 16-byte-vectorised copy.
 #pragma once
-#include <type_traits>
-
 #include "rows_warp.cuh"
 #include "cols_tile.cuh"
 #include "pdl.cuh"
@@ -557,7 +555,10 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
 }
 
 // ---- C2R -> update epilogue --------------------------------------------------------------
-template <int VX, int VY, int EPI>
+// WR (with EPI_SEQ, for runs without statistics, ua.prune): only the write region's voxels are
+// updated, through the x transform of its rows alone, and only their psi and weight are read;
+// a separate instantiation, so that the form with statistics keeps its own register budget.
+template <int VX, int VY, int EPI, bool WR = false>
 __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
     k_xy_update(float2 *__restrict__ S, UpdateArgs ua, const BlockMaps bms, long long Pc,
                 const float2 *__restrict__ gtwx, const float2 *__restrict__ gtwy)
@@ -606,7 +607,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
         xy_load_plane<VX, VY>(sm.A, Sp);
         __syncthreads();
         xy_y<VX, VY, true>(sm.A, sm.twy, sm.posy);
-        if (ua.prune) {
+        if constexpr (WR) {
             // only the rows of the write region go on through the x transform (in whole
             // blocks of 16 rows)
             const int y0 = bm.wlo[1] & ~15, y1 = min(SH::Py, (bm.whi[1] + 15) & ~15);
@@ -624,15 +625,15 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
         uc.inv_maxI = 1.0f / ua.maxI;
         uc.two_lambda = ua.two_lambda;
         uc.tik = ua.tik != 0;
-        // ST: with the statistics every block voxel is updated and summed; without them (a
-        // pruned run) only the written voxels are, and only their psi and weight are read
-        auto rows = [&](auto stats) {
-            constexpr bool ST = decltype(stats)::value;
+        // ST: every block voxel is updated and its change summed (the statistics)
+        constexpr bool ST = !WR;
+        {
 #pragma unroll 1
             for (int r = 0; r < RX; ++r) {
                 const int it = threadIdx.x + r * NT, t = it & 15, y = it >> 4;
                 const long long pb = sm.rowb[y], wb = sm.rowb2[y], ob = sm.rowb3[y];
-                if (pb < 0 || (!ST && ob == kNoRow)) continue;  // not a block row / not written
+                // not a block row / not written
+                if (pb < 0 || ((!ST || ua.prune) && ob == kNoRow)) continue;
                 float pv[VX][2], wv[VX][2];
 #pragma unroll
                 for (int v = 0; v < VX; ++v) {
@@ -676,9 +677,7 @@ __global__ void __launch_bounds__(XYShape<VX, VY>::NT, XYShape<VX, VY>::MINB)
                     }
                 }
             }
-        };
-        if (ua.prune) rows(std::false_type{});
-        else rows(std::true_type{});
+        }
     } else {
         pdl_wait();
         xy_load_plane<VX, VY>(sm.A, Sp);
